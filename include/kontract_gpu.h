@@ -1,0 +1,259 @@
+/*
+ * kontract_gpu.h — C ABI of the GB300 (sm_103a) Monte-Carlo engine for the
+ * compiled-contract pricing path of the `kontract` contract algebra.
+ *
+ * This is the drop-in boundary. A Rust crate (or any FFI) that today calls the
+ * reference's pricer binds these symbols instead; every entry point below names
+ * the reference interface it replaces (file:line in LePhilippeDucTai/kontracts).
+ *
+ * Conventions
+ *  - Plain C types only: pointers, sizes, POD structs. No torch or CUDA types.
+ *  - The caller owns every input and output buffer. `kx_program` is an opaque
+ *    handle created by kx_compile and released by kx_program_free.
+ *  - Device memory, streams and kernels belong to one lazily created
+ *    per-process context (first GPU call). Calls are serialised on it by a
+ *    mutex, so the API is thread-safe; it is not re-entrant from callbacks.
+ *  - Every function returns kx_status. Nothing aborts. On failure the message
+ *    of the calling thread is available from kx_last_error_message().
+ *  - There is no CPU fallback: without a usable CUDA device the pricing entry
+ *    points return KX_NO_DEVICE.
+ */
+#ifndef KONTRACT_GPU_H
+#define KONTRACT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KX_ABI_VERSION 1
+
+/* Status codes. 1..7 mirror the seven variants of KontractError
+ * (src/error.rs:6-28) one to one; Python raises ValueError for all of them,
+ * as the reference binding does (src/bindings.rs:50-52). */
+typedef enum kx_status {
+    KX_OK = 0,
+    KX_UNKNOWN_ASSET = 1,       /* KontractError::UnknownAsset      error.rs:8  */
+    KX_TIME_OUT_OF_RANGE = 2,   /* KontractError::TimeOutOfRange    error.rs:11 */
+    KX_STEP_OUT_OF_RANGE = 3,   /* KontractError::StepOutOfRange    error.rs:14 */
+    KX_INCONSISTENT_PATH = 4,   /* KontractError::InconsistentPath  error.rs:17 */
+    KX_SERDE = 5,               /* KontractError::Serde             error.rs:20 */
+    KX_MALFORMED_CONTRACT = 6,  /* KontractError::MalformedContract error.rs:23 */
+    KX_UNSUPPORTED = 7,         /* KontractError::Unsupported       error.rs:26 */
+    KX_INVALID_ARGUMENT = 8,    /* null pointer, size or option out of range */
+    KX_CUDA_ERROR = 9,          /* a CUDA runtime call failed */
+    KX_DEVICE_TIMEOUT = 10,     /* a bounded device-side wait gave up */
+    KX_NO_DEVICE = 11           /* no CUDA device could be used */
+} kx_status;
+
+typedef struct kx_program kx_program; /* compiled + lowered contract (opaque) */
+
+/* ---- models --------------------------------------------------------------
+ * Mirrors Gbm (src/simulator.rs:188-199) and HestonSimulator
+ * (src/simulator.rs:453-471). `asset` is the name the contract's Spot(...)
+ * observables must use (Simulator::asset_name, simulator.rs:98). */
+enum { KX_MODEL_GBM = 0, KX_MODEL_HESTON = 1 };
+
+/* Heston discretisation. REFERENCE_FLOOR is the reference's scheme
+ * (Euler step, then v = max(v, 0); simulator.rs:517-534) and is the default.
+ * FULL_TRUNCATION is Lord et al. (2010): drift and diffusion use max(v, 0)
+ * and v itself is not floored. */
+enum { KX_HESTON_REFERENCE_FLOOR = 0, KX_HESTON_FULL_TRUNCATION = 1 };
+
+typedef struct kx_model {
+    int32_t kind;          /* KX_MODEL_* */
+    int32_t heston_scheme; /* KX_HESTON_*; ignored for GBM */
+    double s0;             /* initial spot */
+    double mu;             /* GBM drift (risk neutral: r - q) */
+    double sigma;          /* GBM volatility */
+    double v0, kappa, theta, sigma_v, rho; /* Heston parameters */
+    double r;              /* Heston drift (risk-neutral rate) */
+    const char *asset;     /* NUL-terminated asset name; NULL means "ASSET" */
+} kx_model;
+
+/* ---- Monte-Carlo configuration -------------------------------------------
+ * Mirrors McConfig (src/pricer.rs:30-54): n_paths, seed, steps_per_year,
+ * rate. The remaining fields select engine options the reference does not
+ * have. */
+enum { KX_RNG_PHILOX = 0, KX_RNG_SHARED_DRAWS = 1 };
+enum { KX_PREC_FP32 = 0, KX_PREC_FP64 = 1 };
+
+typedef struct kx_mc_config {
+    uint64_t n_paths;        /* number of paths (0 gives a zero result) */
+    uint64_t seed;           /* Philox key */
+    uint32_t steps_per_year; /* fine-grid resolution (compiler.rs:54-65) */
+    int32_t rng;             /* KX_RNG_*: Philox in registers, or the host normals
+                                registered with kx_set_shared_draws */
+    int32_t precision;       /* KX_PREC_*: path arithmetic type; payoff sums are
+                                always FP64 */
+    int32_t flags;           /* reserved, must be 0 */
+    double rate;             /* deterministic discount rate */
+} kx_mc_config;
+
+/* Mirrors PriceResult (src/pricer.rs:58-71). */
+typedef struct kx_price_result {
+    double price;      /* mean discounted payoff */
+    double sample_std; /* unbiased sample standard deviation of per-path PVs */
+    double std_error;  /* sample_std / sqrt(n) */
+    double ci95_low;   /* price - 1.959963984540054 * std_error */
+    double ci95_high;  /* price + 1.959963984540054 * std_error */
+    uint64_t n_paths;
+} kx_price_result;
+
+/* Mirrors BumpSizes (src/greeks.rs:22-39). With `relative` = 0 the bumps are
+ * absolute (reference defaults spot 1e-2, vol 1e-2, rate 1e-4); with
+ * `relative` = 1 each bump is multiplied by the bumped parameter's value. */
+typedef struct kx_bumps {
+    double spot, vol, rate;
+    int32_t relative;
+    int32_t smooth;        /* 1: reprice the barrier-smoothed payoff (see kx_adjoint_cfg) */
+    double smoothing_width;/* log-space logistic width when smooth = 1 */
+} kx_bumps;
+
+/* Mirrors Greeks (src/greeks.rs:43-54), plus the standard error of each CRN
+ * estimator (per-path finite differences). */
+typedef struct kx_greeks {
+    double price, delta, gamma, vega, rho;
+    double price_se, delta_se, gamma_se, vega_se, rho_se;
+} kx_greeks;
+
+/* Pathwise-adjoint configuration (no reference counterpart). */
+typedef struct kx_adjoint_cfg {
+    uint32_t checkpoint_every; /* reverse sweep recomputes segments of this many steps */
+    int32_t reserved;
+    double smoothing_width;    /* log-space width w of the logistic barrier indicator;
+                                  <= 0 selects 0.5 * sigma_eff * sqrt(dt) */
+} kx_adjoint_cfg;
+
+/* Sensitivities of the (smoothed) price. For GBM: d/ds0, d/dsigma, d/dr
+ * (r moves drift and discount together, as greeks.rs:70 does). For Heston the
+ * model parameters are filled as well. Each value has its standard error. */
+typedef struct kx_sens {
+    double price, price_se;
+    double d_s0, d_sigma, d_r;
+    double d_v0, d_kappa, d_theta, d_sigma_v, d_rho;
+    double se_s0, se_sigma, se_r;
+    double se_v0, se_kappa, se_theta, se_sigma_v, se_rho;
+    double smoothing_width; /* the width actually used */
+} kx_sens;
+
+/* Timing and counters of the last pricing call on the calling process. */
+typedef struct kx_launch_stats {
+    double kernel_ms;          /* CUDA-event time of the main kernel(s) */
+    double total_ms;           /* wall time of the whole call */
+    uint64_t path_steps;       /* nominal path-steps (n_paths * grid steps) */
+    uint64_t steps_simulated;  /* steps actually simulated (early exit skips) */
+    uint32_t kernel_launches;  /* kernels launched by the call */
+    uint32_t grid_blocks;
+    uint32_t block_threads;
+    uint32_t reserved;
+    uint64_t h2d_bytes, d2h_bytes;
+} kx_launch_stats;
+
+/* Static plan of a contract: Plan (src/compiler.rs:25-34). */
+typedef struct kx_plan_info {
+    uint32_t n_assets;
+    uint32_t n_fixed_dates;
+    double horizon;
+    int32_t needs_fine_grid;
+    int32_t n_triggers;   /* lowered when/anytime/until slots */
+    int32_t n_flows;      /* lowered one(...) leaves */
+    int32_t n_accumulators;
+} kx_plan_info;
+
+/* ---- entry points ----------------------------------------------------------*/
+
+/* ABI version of the loaded library (KX_ABI_VERSION). */
+int32_t kx_abi_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *kx_last_error_message(void);
+
+/* Parse the serde JSON of a Contract (Contract::from_json, src/ast.rs:215),
+ * run the compiler (compile, src/compiler.rs:69) and lower the AST to the
+ * flat trigger/flow/accumulator table the kernels interpret. Replaces the
+ * per-call compile() inside price_gbm (src/pricer.rs:102). Host only. */
+kx_status kx_compile(const char *contract_json, kx_program **out);
+void kx_program_free(kx_program *prog);
+
+/* Plan::assets / fixed_dates / horizon / needs_fine_grid (compiler.rs:25-34).
+ * `assets_buf` receives the sorted asset names separated by '\n'. Host only. */
+kx_status kx_program_plan(const kx_program *prog, kx_plan_info *info,
+                          double *fixed_dates, size_t dates_cap,
+                          char *assets_buf, size_t assets_cap);
+
+/* Plan::time_grid_forced (src/compiler.rs:54-65). Writes at most `cap`
+ * points, stores the full count in *n. Host only. */
+kx_status kx_time_grid(const kx_program *prog, uint32_t steps_per_year,
+                       int32_t force_fine, double *out, size_t cap, size_t *n);
+
+/* Register host normals for KX_RNG_SHARED_DRAWS (path-major:
+ * z[path * draws_per_path + d]; GBM uses draw k-1 at grid step k, Heston
+ * draws 2(k-1) and 2(k-1)+1). The data is copied to the device. Exactly one
+ * of z64 / z32 must be non-NULL. No reference counterpart (the reference
+ * draws ChaCha8 normals inside Gbm::simulate, simulator.rs:233-241). */
+kx_status kx_set_shared_draws(const double *z64, const float *z32,
+                              uint64_t n_paths, uint64_t draws_per_path);
+kx_status kx_clear_shared_draws(void);
+
+/* price_gbm (src/pricer.rs:97-115): compile-time plan + grid, simulate, value
+ * every path, summarise. `per_path_pv` (nullable, n_paths doubles) receives
+ * the discounted value of every path (present_value, pricer.rs:344-355). */
+kx_status kx_price(const kx_program *prog, const kx_model *model,
+                   const kx_mc_config *cfg, kx_price_result *out,
+                   double *per_path_pv);
+
+/* price_batch_gbm (src/pricer.rs:250-294): one shared simulation on the
+ * merged grid of all contracts, each contract valued on the same paths. */
+kx_status kx_price_batch_shared(size_t n, const kx_program *const *progs,
+                                const kx_model *model, const kx_mc_config *cfg,
+                                kx_price_result *out);
+
+/* Uneven portfolio in one persistent launch over a (contract, path-block)
+ * work queue: each contract has its own model and config (its own grid,
+ * n_paths and seed). Optional per-contract pathwise delta / vega (`sens`,
+ * nullable: price, d_s0 and d_sigma filled). No reference counterpart: the
+ * reference prices such a book with one price_gbm call per contract. */
+kx_status kx_price_portfolio(size_t n, const kx_program *const *progs,
+                             const kx_model *models, const kx_mc_config *cfgs,
+                             kx_price_result *out, kx_sens *sens);
+
+/* greeks_gbm (src/greeks.rs:60-98): CRN bump-and-reprice. All bumped
+ * scenarios reuse each path's normals inside one launch. GBM only (model->kind
+ * must be KX_MODEL_GBM); drift = rate, as the reference rebuilds the model
+ * with Gbm::new(asset, s0, rate, sigma) (greeks.rs:70). */
+kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model,
+                         const kx_mc_config *cfg, const kx_bumps *bumps,
+                         kx_greeks *out);
+
+/* Pathwise adjoint: one reverse sweep per path recomputing the path from its
+ * Philox counters with a checkpoint every `checkpoint_every` steps; the
+ * barrier indicator of until-conditions is a logistic of the stated width.
+ * No reference counterpart (the reference only bumps). */
+kx_status kx_greeks_adjoint(const kx_program *prog, const kx_model *model,
+                            const kx_mc_config *cfg, const kx_adjoint_cfg *acfg,
+                            kx_sens *out);
+
+/* price_american_lsm (src/lsm.rs:80-124): Longstaff-Schwartz on the grid
+ * [0, dates...] with the monomial basis {1, S, ..., S^(n_basis-1)}
+ * (lsm.rs:259-288) and Gauss elimination with partial pivoting
+ * (numerics.rs:190-236). Paths are stored in HBM (FP32 or FP64 per
+ * cfg->precision), the Gram matrix is block-reduced in FP64. */
+kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model,
+                                const kx_mc_config *cfg, const double *dates,
+                                size_t n_dates, int32_t n_basis,
+                                kx_price_result *out);
+
+/* Counters of the last pricing call (see kx_launch_stats). */
+kx_status kx_last_launch_stats(kx_launch_stats *out);
+
+/* Device name, SM count and the compute capability of device 0. */
+kx_status kx_device_info(char *name, size_t cap, int32_t *sm_count,
+                         int32_t *cc_major, int32_t *cc_minor);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KONTRACT_GPU_H */

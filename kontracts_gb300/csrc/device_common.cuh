@@ -1,0 +1,155 @@
+// device_common.cuh — device building blocks shared by the path kernels:
+// counter-based normals, the postfix expression interpreter and the
+// accumulator (Average / RunningMax / RunningMin) semantics.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "devprog.hpp"
+
+namespace kx {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): 10 rounds of two 32x32->64 multiplies with a
+// Weyl-sequence key schedule. Counter = (block, path_lo, path_hi, stream),
+// key = (seed_lo, seed_hi).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Box-Muller on two 32-bit words: u = (w + 1/2) 2^-32 in (0, 1),
+// z0 = r cos(2 pi u2), z1 = r sin(2 pi u2), r = sqrt(-2 ln u1).
+// FP32: the angle is taken as 2 pi (u2 - 1/2) in (-pi, pi), the range where
+// the hardware sine/cosine are accurate, and the sign is folded back.
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float &z0, float &z1) {
+    const float u1 = fmaf(__uint2float_rn(a), 0x1p-32f, 0x1p-33f);
+    const float h = fmaf(__uint2float_rn(b), 0x1p-32f, 0x1p-33f - 0.5f);
+    const float r = sqrt_approx(-2.0f * __logf(u1));
+    float s, c;
+    __sincosf(6.283185307179586f * h, &s, &c);
+    z0 = -r * c;
+    z1 = -r * s;
+}
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double &z0, double &z1) {
+    const double u1 = ((double)a + 0.5) * 0x1p-32;
+    const double u2 = ((double)b + 0.5) * 0x1p-32;
+    const double r = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+template <class Real>
+__device__ __forceinline__ Real fast_exp(Real x);
+template <>
+__device__ __forceinline__ float fast_exp<float>(float x) { return __expf(x); }
+template <>
+__device__ __forceinline__ double fast_exp<double>(double x) { return exp(x); }
+
+// ---------------------------------------------------------------------------
+// Accumulators live in shared memory, one column per thread:
+// slot j of this thread is base[j * stride].
+// ---------------------------------------------------------------------------
+template <class Real>
+struct AccView {
+    Real *base;
+    int stride;
+    __device__ __forceinline__ Real &operator[](int j) const { return base[j * stride]; }
+};
+
+// Value of accumulator `a` read at step k (observable.rs:103-140).
+// err gets KX_ERR_* bits when the reference would fail there.
+template <class Real>
+__device__ __forceinline__ Real acc_value(const KxProgram &P, int a, AccView<Real> acc, uint32_t poisoned, int k,
+                                          uint32_t &err) {
+    const KxAcc &A = P.acc[a];
+    if (poisoned >> a & 1u) err |= KX_ERR_MALFORMED;
+    const Real v = acc[a];
+    if (A.kind != ACC_SUM) return v;
+    if (A.fixed) {
+        if (A.static_err) { err |= KX_ERR_MALFORMED; return Real(0); }
+        if (k < A.e_min) { err |= KX_ERR_LOOKAHEAD; return Real(0); }
+        return v / (Real)A.inv_count;
+    }
+    if (k < A.e_min) { err |= KX_ERR_MALFORMED; return Real(0); }
+    return v / (Real)(k - A.i_from + 1);
+}
+
+// Postfix interpreter. Reals and booleans share one stack (booleans as 0/1);
+// `em` keeps one error bit per stack slot so that errors propagate the way
+// the reference's `?` operators do, including the short-circuit of
+// `a && b` / `a || b` (observable.rs:164-165).
+template <class Real>
+__device__ Real eval_code(const KxProgram &P, int off, int len, AccView<Real> acc, uint32_t poisoned, int k,
+                          Real S, uint32_t &err) {
+    Real st[KX_MAX_STACK];
+    uint32_t eb[KX_MAX_STACK];
+    int sp = 0;
+    for (int pc = off; pc < off + len; ++pc) {
+        const KxIns ins = P.code[pc];
+        switch (ins.op) {
+        case OP_CONST: st[sp] = (Real)P.cpool[ins.arg]; eb[sp++] = 0; break;
+        case OP_SPOT: st[sp] = S; eb[sp++] = 0; break;
+        case OP_ACC: {
+            uint32_t e = 0;
+            st[sp] = acc_value<Real>(P, ins.arg, acc, poisoned, k, e);
+            eb[sp++] = e;
+            break;
+        }
+        case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+        case OP_TRUE: st[sp] = Real(1); eb[sp++] = 0; break;
+        case OP_FALSE: st[sp] = Real(0); eb[sp++] = 0; break;
+        case OP_AT: st[sp] = k >= P.at_index[ins.arg] ? Real(1) : Real(0); eb[sp++] = 0; break;
+        case OP_NOT: st[sp - 1] = st[sp - 1] != Real(0) ? Real(0) : Real(1); break;
+        default: {
+            --sp;
+            const Real a = st[sp - 1], b = st[sp];
+            const uint32_t ea = eb[sp - 1], ebb = eb[sp];
+            Real r;
+            uint32_t e = ea | ebb;
+            switch (ins.op) {
+            case OP_ADD: r = a + b; break;
+            case OP_SUB: r = a - b; break;
+            case OP_MUL: r = a * b; break;
+            case OP_DIV: r = a / b; break;
+            case OP_MAX: r = fmax(a, b); break;
+            case OP_MIN: r = fmin(a, b); break;
+            case OP_GE: r = a >= b ? Real(1) : Real(0); break;
+            case OP_GT: r = a > b ? Real(1) : Real(0); break;
+            case OP_LE: r = a <= b ? Real(1) : Real(0); break;
+            case OP_LT: r = a < b ? Real(1) : Real(0); break;
+            case OP_AND: r = (a != Real(0) && b != Real(0)) ? Real(1) : Real(0); e = ea | (a != Real(0) ? ebb : 0u); break;
+            case OP_OR: r = (a != Real(0) || b != Real(0)) ? Real(1) : Real(0); e = ea | (a == Real(0) ? ebb : 0u); break;
+            default: r = Real(0); break;
+            }
+            st[sp - 1] = r;
+            eb[sp - 1] = e;
+            break;
+        }
+        }
+    }
+    err |= eb[0];
+    return st[0];
+}
+
+}  // namespace kx

@@ -1,0 +1,1153 @@
+// engine.cu — the fused path kernel and the GPU entry points of the C ABI.
+//
+// One kernel (k_paths) replaces Gbm::simulate / HestonSimulator::simulate
+// (src/simulator.rs:215-253, 506-541) + price_on_paths / cashflows
+// (src/pricer.rs:230-433): each thread draws its normals from Philox in
+// registers, advances the path state (log-spot, variance) one grid step at a
+// time and interprets the lowered contract table at every step, so the path is
+// never stored. Only the discounted value of each path leaves the kernel; a
+// second kernel reduces those in a fixed order (bitwise reproducible).
+//
+// Scheduling: a persistent grid; each warp takes (contract, path-range) work
+// items from an atomic counter and its 32 lanes take paths one by one from
+// the item. A lane whose path is finished early (every flow emitted or knocked
+// out) starts a new path at once, so knocked-out barrier paths do not hold a
+// lane idle. Path-to-lane assignment depends only on the data, and per-path
+// values are written to fixed slots, so results do not depend on timing.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "device_common.cuh"
+#include "engine.hpp"
+
+namespace kx {
+
+constexpr int KX_MAX_NS = 7;
+constexpr int KX_BLOCK = 256;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        raise(KX_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+void DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    KX_CUDA(cudaMalloc(&p, want));
+    cap = want;
+}
+
+Ctx &ctx() {
+    static Ctx c;
+    if (c.ready) return c;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        raise(KX_NO_DEVICE, std::string("no CUDA device: ") + (e == cudaSuccess ? "count is 0" : cudaGetErrorString(e)));
+    }
+    KX_CUDA(cudaSetDevice(c.device));
+    cudaDeviceProp prop;
+    KX_CUDA(cudaGetDeviceProperties(&prop, c.device));
+    c.sm_count = prop.multiProcessorCount;
+    c.cc_major = prop.major;
+    c.cc_minor = prop.minor;
+    c.name = prop.name;
+    KX_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    KX_CUDA(cudaEventCreate(&c.ev0));
+    KX_CUDA(cudaEventCreate(&c.ev1));
+    c.ready = true;
+    return c;
+}
+
+int persistent_blocks(const void *kernel, int block, size_t smem) {
+    Ctx &c = ctx();
+    int per_sm = 0;
+    KX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem));
+    if (per_sm < 1) raise(KX_CUDA_ERROR, "kernel does not fit on an SM");
+    return per_sm * c.sm_count;
+}
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------------------
+// device data layout
+// ---------------------------------------------------------------------------
+template <class Real>
+struct StepRec {  // grid step k (k = 0 carries only the time bits)
+    Real c0, c1;  // GBM single scenario: drift*dt, sigma*sqrt(dt); otherwise dt, sqrt(dt)
+    uint32_t tt;  // CK_TIME trigger bits true at step k
+    uint32_t pad;
+};
+
+constexpr int KX_MAX_SPOT = KX_MAX_TRIG;
+
+struct ContractDev {
+    int32_t n_times;
+    int32_t step_off;   // first StepRec of this contract
+    int32_t disc_off;   // first discount factor (scenario s: + s * n_times)
+    int32_t prog;       // index into the program array
+    uint64_t n_paths;
+    uint64_t pv_off;    // first output slot (scenario s: + s * pv_stride)
+    uint64_t seed;
+    uint32_t stream;    // Philox stream id
+    int32_t smooth;     // 1: until(Spot cmp Const) is a logistic survival weight
+    int32_t heston_scheme;
+    int32_t pad;
+    // per-scenario values, in both precisions so the FP32 kernel never converts
+    double s0[KX_MAX_NS], drift[KX_MAX_NS], sigma[KX_MAX_NS];
+    float s0f[KX_MAX_NS], driftf[KX_MAX_NS], sigmaf[KX_MAX_NS];
+    double v0, kappa, theta, sigma_v, rho, rho_perp, r, inv_w;
+    float v0f, kappaf, thetaf, sigma_vf, rhof, rho_perpf, rf, inv_wf;
+};
+
+struct WorkItem {
+    int32_t contract;
+    int32_t pad;
+    uint64_t first;
+    uint64_t count;
+};
+
+struct PathArgs {
+    const KxProgram *progs;
+    const void *steps;
+    const double *disc;
+    const ContractDev *cons;
+    const void *thr;     // Real[contract][KX_MAX_NS][KX_MAX_SPOT] log-spot thresholds
+    const WorkItem *items;
+    uint32_t n_items;
+    uint32_t slots;      // shared-memory slots per thread per scenario
+    uint32_t surv_base;  // first survival slot (after 2 slots per accumulator)
+    uint32_t pad;
+    uint32_t *item_counter;
+    uint32_t *err_word;
+    unsigned long long *steps_done;
+    double *pv;
+    uint64_t pv_stride;
+    const double *z64;   // shared draws (path-major) or null
+    const float *z32;
+    uint64_t z_dpp;
+};
+
+enum { M_GBM = 0, M_HESTON = 1 };
+
+template <class Real> __device__ __forceinline__ Real pick(double d, float f);
+template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
+
+template <class Real> __device__ __forceinline__ Real fsqrt(Real x);
+template <> __device__ __forceinline__ float fsqrt<float>(float x) { return sqrt_approx(x); }
+template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(x); }
+
+// Per-contract values a warp keeps in registers while it works on a contract.
+template <class Real, int NS>
+struct Hot {
+    const KxProgram *P;
+    const ContractDev *C;
+    const StepRec<Real> *R;
+    const double *D;
+    const Real *thr;  // [NS][KX_MAX_SPOT]
+    Real s0[NS], drift[NS], sig[NS];
+    Real kap, th, sv, rho, rp, r, v0, inv_w;
+    int n_times, n_acc;
+    uint32_t spot_each, time_mask, price_mask, until_mask, when_mask, all_leaves, err_capable, root_arm, root_leaves;
+    int smooth, scheme;
+};
+
+template <class Real, int NS>
+struct Lane {
+    Real y[NS];  // log(S / s0) of each scenario
+    Real v[NS];  // Heston variance
+    uint32_t armed[NS], resolved[NS], dead[NS], emitted[NS], poisoned[NS];
+    double pv[NS];
+    uint32_t err;
+};
+
+template <class Real>
+__device__ __forceinline__ bool cmp_y(uint8_t cmp, Real y, Real thr) {
+    switch (cmp) {
+    case CMP_GE: return y >= thr;
+    case CMP_GT: return y > thr;
+    case CMP_LE: return y <= thr;
+    default: return y < thr;
+    }
+}
+
+// Survival weight of one step under a smoothed until(S cmp B): the breach
+// indicator 1{y cmp b} is replaced by the logistic sigma(+-(y - b) / w).
+template <class Real>
+__device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, Real inv_w) {
+    Real x = (y - thr) * inv_w;  // > 0 beyond the barrier for >=, >
+    if (cmp == CMP_LE || cmp == CMP_LT) x = -x;
+    return Real(1) / (Real(1) + fast_exp<Real>(x));
+}
+
+template <class Real, int NS>
+__device__ __forceinline__ Real spot_of(const Hot<Real, NS> &H, const Lane<Real, NS> &L, int s) {
+    return H.s0[s] * fast_exp<Real>(L.y[s]);
+}
+
+// Conditions of the trigger slots in `mask` at step k for scenario s.
+template <class Real, int NS>
+__device__ __forceinline__ uint32_t cond_bits(const Hot<Real, NS> &H, Lane<Real, NS> &L, int s, uint32_t mask, int k,
+                                              uint32_t tt, AccView<Real> acc, Real &S, bool &haveS) {
+    const KxProgram &P = *H.P;
+    uint32_t bits = mask & H.time_mask & tt;
+    uint32_t pm = mask & H.price_mask;
+    while (pm) {
+        const int i = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const KxTrig &T = P.trig[i];
+        bool b;
+        if (T.cond_kind == CK_SPOT_CMP) {
+            if (H.smooth && T.kind == TK_UNTIL) continue;  // weighted instead of knocked
+            b = cmp_y<Real>(T.cmp, L.y[s], H.thr[s * KX_MAX_SPOT + T.spot_slot]);
+        } else {
+            if (!haveS) { S = spot_of(H, L, s); haveS = true; }
+            uint32_t e = 0;
+            b = eval_code<Real>(P, T.code_off, T.code_len, acc, L.poisoned[s], k, S, e) != Real(0);
+            L.err |= e;
+        }
+        if (b) bits |= 1u << i;
+    }
+    return bits;
+}
+
+// Everything the contract does at grid step k for scenario s, after the
+// model moved to step k. Returns true when no flow can change any more.
+template <class Real, int NS>
+__device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, Lane<Real, NS> &L, int s, int k, uint32_t tt,
+                                              AccView<Real> acc, AccView<Real> surv) {
+    const KxProgram &P = *H.P;
+    Real S = Real(0);
+    bool haveS = false;
+    if (H.spot_each) { S = spot_of(H, L, s); haveS = true; }
+    // accumulators (observable.rs:120-140), inner ones first (slot order)
+    for (int a = 0; a < H.n_acc; ++a) {
+        const KxAcc &A = P.acc[a];
+        if (k < A.i_from || k > A.i_to) continue;
+        Real x;
+        if (A.inner == IK_SPOT) {
+            x = S;
+        } else {
+            uint32_t e = 0;
+            x = eval_code<Real>(P, A.code_off, A.code_len, acc, L.poisoned[s], k, S, e);
+            if (e) L.poisoned[s] |= 1u << a;
+        }
+        Real &v = acc[2 * a];
+        if (A.kind == ACC_MAX) v = fmax(v, x);
+        else if (A.kind == ACC_MIN) v = fmin(v, x);
+        else if (sizeof(Real) == 8) v = v + x;
+        else {  // compensated (Kahan) sum in FP32
+            Real &c = acc[2 * a + 1];
+            const Real yk = x - c;
+            const Real t = v + yk;
+            c = (t - v) - yk;
+            v = t;
+        }
+    }
+    // triggers: check live slots, then cascade the arming within the step
+    uint32_t fired = 0;
+    const uint32_t live = L.armed[s] & ~L.resolved[s];
+    if (live) {
+        uint32_t newly = cond_bits<Real, NS>(H, L, s, live, k, tt, acc, S, haveS);
+        while (newly) {
+            L.resolved[s] |= newly;
+            uint32_t u = newly & H.until_mask;
+            while (u) {
+                const int i = __ffs(u) - 1;
+                u &= u - 1;
+                L.dead[s] |= P.trig[i].leaves & ~L.emitted[s];
+            }
+            uint32_t w = newly & H.when_mask;
+            fired |= w;
+            uint32_t arm = 0;
+            while (w) {
+                const int i = __ffs(w) - 1;
+                w &= w - 1;
+                arm |= P.trig[i].fire_arm;
+            }
+            arm &= ~L.armed[s];
+            L.armed[s] |= arm;
+            newly = arm ? cond_bits<Real, NS>(H, L, s, arm, k, tt, acc, S, haveS) : 0u;
+        }
+    }
+    // smoothed until weights of every armed smoothed slot (armed ones included)
+    if (H.smooth) {
+        uint32_t sm = L.armed[s] & H.until_mask & H.price_mask;
+        while (sm) {
+            const int i = __ffs(sm) - 1;
+            sm &= sm - 1;
+            const KxTrig &T = P.trig[i];
+            if (T.cond_kind != CK_SPOT_CMP) continue;
+            surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, L.y[s], H.thr[s * KX_MAX_SPOT + T.spot_slot], H.inv_w);
+        }
+    }
+    // flows acquired at step k (pricer.rs:380-405)
+    uint32_t acq = k == 0 ? H.root_leaves : 0u;
+    while (fired) {
+        const int i = __ffs(fired) - 1;
+        fired &= fired - 1;
+        acq |= P.trig[i].leaves;
+    }
+    acq &= ~L.emitted[s];
+    while (acq) {
+        const int j = __ffs(acq) - 1;
+        acq &= acq - 1;
+        const KxLeaf &F = P.leaf[j];
+        const bool is_dead = (L.dead[s] >> j) & 1u;
+        if (is_dead && !F.err_capable) continue;
+        double amt;
+        if (F.kind == AK_CONST) {
+            amt = F.sign;
+        } else {
+            if (!haveS) { S = spot_of(H, L, s); haveS = true; }
+            uint32_t e = 0;
+            amt = (double)eval_code<Real>(P, F.code_off, F.code_len, acc, L.poisoned[s], k, S, e);
+            L.err |= e;
+        }
+        if (is_dead) continue;
+        if (H.smooth) {
+            uint32_t us = H.until_mask & H.price_mask & L.armed[s];
+            while (us) {
+                const int i = __ffs(us) - 1;
+                us &= us - 1;
+                const KxTrig &T = P.trig[i];
+                if (T.cond_kind == CK_SPOT_CMP && ((T.leaves >> j) & 1u)) amt *= (double)surv[T.spot_slot];
+            }
+        }
+        L.pv[s] += amt * H.D[(size_t)s * H.n_times + k];
+        L.emitted[s] |= 1u << j;
+    }
+    return !H.err_capable && (H.all_leaves & ~(L.emitted[s] | L.dead[s])) == 0u;
+}
+
+template <class Real, int MODEL, int NS>
+__global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *smem = reinterpret_cast<Real *>(smem_raw);
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
+    constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
+    constexpr uint32_t ALL = (1u << NS) - 1u;
+
+    // warp-uniform work state
+    int cur = -1, pend = -1;
+    uint64_t nx = 0, end = 0, pnx = 0, pend_end = 0;
+    bool drained = false;
+    Hot<Real, NS> H;
+    H.P = nullptr;
+
+    // lane state
+    long long path = -1;
+    int k = 0;
+    uint32_t done = 0;
+    Lane<Real, NS> L;
+    L.err = 0;
+    unsigned long long my_steps = 0;
+    const int slots = (int)A.slots;
+    const int nthr = (int)blockDim.x;
+
+    auto accv = [&](int s) { return AccView<Real>{smem + (size_t)s * slots * nthr + threadIdx.x, nthr}; };
+    auto survv = [&](int s) {
+        return AccView<Real>{smem + ((size_t)s * slots + A.surv_base) * nthr + threadIdx.x, nthr};
+    };
+
+    auto bind_contract = [&](int c) {
+        cur = c;
+        const ContractDev *C = A.cons + c;
+        H.C = C;
+        H.P = A.progs + C->prog;
+        H.R = reinterpret_cast<const StepRec<Real> *>(A.steps) + C->step_off;
+        H.D = A.disc + C->disc_off;
+        H.thr = reinterpret_cast<const Real *>(A.thr) + (size_t)c * KX_MAX_NS * KX_MAX_SPOT;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            H.s0[s] = pick<Real>(C->s0[s], C->s0f[s]);
+            H.drift[s] = pick<Real>(C->drift[s], C->driftf[s]);
+            H.sig[s] = pick<Real>(C->sigma[s], C->sigmaf[s]);
+        }
+        H.kap = pick<Real>(C->kappa, C->kappaf);
+        H.th = pick<Real>(C->theta, C->thetaf);
+        H.sv = pick<Real>(C->sigma_v, C->sigma_vf);
+        H.rho = pick<Real>(C->rho, C->rhof);
+        H.rp = pick<Real>(C->rho_perp, C->rho_perpf);
+        H.r = pick<Real>(C->r, C->rf);
+        H.v0 = pick<Real>(C->v0, C->v0f);
+        H.inv_w = pick<Real>(C->inv_w, C->inv_wf);
+        H.n_times = C->n_times;
+        H.smooth = C->smooth;
+        H.scheme = C->heston_scheme;
+        const KxProgram &P = *H.P;
+        H.n_acc = P.n_acc;
+        H.spot_each = P.spot_each_step;
+        H.time_mask = P.time_mask;
+        H.price_mask = P.price_mask;
+        H.until_mask = P.until_mask;
+        H.when_mask = P.when_mask;
+        H.all_leaves = P.all_leaves;
+        H.err_capable = P.err_capable;
+        H.root_arm = P.root_arm;
+        H.root_leaves = P.root_leaves;
+    };
+
+    auto finish_path = [&]() {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) A.pv[(uint64_t)s * A.pv_stride + H.C->pv_off + (uint64_t)path] = L.pv[s];
+        path = -1;
+    };
+
+    while (true) {
+        // ---- hand paths to idle lanes (warp-uniform control) ----
+        unsigned idle = __ballot_sync(FULL, path < 0);
+        while (idle) {
+            if (nx >= end) {
+                if (pend >= 0) {
+                    if (idle != FULL) break;  // finish the current contract first
+                    bind_contract(pend);
+                    nx = pnx;
+                    end = pend_end;
+                    pend = -1;
+                    continue;
+                }
+                if (drained) break;
+                int it = 0;
+                if (lane == 0) it = (int)atomicAdd(A.item_counter, 1u);
+                it = __shfl_sync(FULL, it, 0);
+                if (it >= (int)A.n_items) { drained = true; break; }
+                const WorkItem w = A.items[it];
+                if (w.contract != cur) {
+                    if (cur >= 0 && idle != FULL) {
+                        pend = w.contract;
+                        pnx = w.first;
+                        pend_end = w.first + w.count;
+                        break;
+                    }
+                    bind_contract(w.contract);
+                }
+                nx = w.first;
+                end = w.first + w.count;
+                continue;
+            }
+            const int nidle = __popc(idle);
+            const uint64_t avail = end - nx;
+            const int take = avail < (uint64_t)nidle ? (int)avail : nidle;
+            if (path < 0 && __popc(idle & lt) < take) {
+                path = (long long)(nx + (uint64_t)__popc(idle & lt));
+                // new path: state at t = 0 (S = s0), then the contract at step 0
+                const KxProgram &P = *H.P;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    L.y[s] = Real(0);
+                    L.v[s] = fmax(H.v0, Real(0));
+                    L.armed[s] = H.root_arm;
+                    L.resolved[s] = L.dead[s] = L.emitted[s] = L.poisoned[s] = 0u;
+                    L.pv[s] = 0.0;
+                    AccView<Real> av = accv(s), sv = survv(s);
+                    for (int a = 0; a < H.n_acc; ++a) {
+                        av[2 * a] = P.acc[a].kind == ACC_MAX ? Real(-INFINITY) : P.acc[a].kind == ACC_MIN ? Real(INFINITY) : Real(0);
+                        av[2 * a + 1] = Real(0);
+                    }
+                    if (H.smooth)
+                        for (int q = 0; q < P.n_spot_cmp; ++q) sv[q] = Real(1);
+                }
+                done = 0;
+                const uint32_t tt0 = H.R[0].tt;
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+                    if (contract_step<Real, NS>(H, L, s, 0, tt0, accv(s), survv(s))) done |= 1u << s;
+                k = 1;
+                if (H.n_times <= 1 || done == ALL) finish_path();
+            }
+            nx += (uint64_t)take;
+            if (take == 0) break;
+            idle = __ballot_sync(FULL, path < 0);
+        }
+        if (__ballot_sync(FULL, path >= 0) == 0u) {
+            if (drained && pend < 0 && nx >= end) break;
+            continue;
+        }
+
+        // ---- advance busy lanes by one Philox block of grid steps ----
+        if (path >= 0) {
+            const int nt = H.n_times;
+            Real z0, z1, z2, z3;
+            if (A.z64 == nullptr && A.z32 == nullptr) {
+                const uint32_t blk = (uint32_t)((k - 1) / SPB);
+                const uint64_t seed = H.C->seed;
+                const uint4 w = philox4x32_10(
+                    make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32), H.C->stream), (uint32_t)seed,
+                    (uint32_t)(seed >> 32));
+                box_muller(w.x, w.y, z0, z1);
+                box_muller(w.z, w.w, z2, z3);
+            } else {
+                const uint64_t d0 = (uint64_t)(k - 1) * DRAWS;
+                const uint64_t base = (uint64_t)path * A.z_dpp + d0;
+                Real zz[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    zz[j] = d0 + j < A.z_dpp ? (A.z64 ? (Real)A.z64[base + j] : (Real)A.z32[base + j]) : Real(0);
+                z0 = zz[0]; z1 = zz[1]; z2 = zz[2]; z3 = zz[3];
+            }
+#pragma unroll 1
+            for (int j = 0; j < SPB; ++j) {
+                const int kk = k + j;
+                if (kk >= nt || done == ALL) break;
+                const StepRec<Real> rec = H.R[kk];
+                const Real za = j == 0 ? z0 : j == 1 ? z1 : j == 2 ? z2 : z3;  // GBM draw of step kk
+                const Real h1 = j == 0 ? z0 : z2, h2 = j == 0 ? z1 : z3;     // Heston draws of step kk
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    if ((done >> s) & 1u) continue;
+                    if (MODEL == M_GBM) {
+                        // log-space exact GBM step (simulator.rs:238-245)
+                        if (NS == 1) L.y[s] += rec.c0 + rec.c1 * za;
+                        else L.y[s] += H.drift[s] * rec.c0 + H.sig[s] * rec.c1 * za;
+                    } else {
+                        // Heston Euler step (simulator.rs:517-534); rec.c0 = dt, rec.c1 = sqrt(dt)
+                        const Real dt = rec.c0, sq = rec.c1;
+                        const Real vv = L.v[s];
+                        const Real vp = H.scheme == KX_HESTON_FULL_TRUNCATION ? fmax(vv, Real(0)) : vv;
+                        const Real sqv = fsqrt<Real>(vp);
+                        L.y[s] += H.r * dt - Real(0.5) * vp * dt + sqv * (h1 * sq);
+                        const Real nv = vv + H.kap * (H.th - vp) * dt + H.sv * sqv * ((H.rho * h1 + H.rp * h2) * sq);
+                        L.v[s] = H.scheme == KX_HESTON_FULL_TRUNCATION ? nv : fmax(nv, Real(0));
+                    }
+                    if (contract_step<Real, NS>(H, L, s, kk, rec.tt, accv(s), survv(s))) done |= 1u << s;
+                }
+                ++my_steps;
+            }
+            k += SPB;
+            if (k >= nt || done == ALL) finish_path();
+        }
+    }
+    // counters: one atomic per warp
+    unsigned long long tot = my_steps;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    uint32_t err = L.err;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) err |= __shfl_xor_sync(FULL, err, o);
+    if (lane == 0) {
+        if (tot) atomicAdd(A.steps_done, tot);
+        if (err) atomicOr(A.err_word, err);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic chunk statistics: each block takes one fixed chunk of values
+// and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes).
+// ---------------------------------------------------------------------------
+struct ChunkDesc {
+    uint64_t begin;
+    uint32_t count;
+    uint32_t pad;
+};
+struct ChunkOut {
+    double n, mean, m2;
+};
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    t = red[0];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns,
+                                                     const double *__restrict__ w, const ChunkDesc *__restrict__ ch,
+                                                     ChunkOut *__restrict__ out) {
+    __shared__ double red[32];
+    const ChunkDesc c = ch[blockIdx.x];
+    double ww[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
+    auto val = [&](uint64_t i) {
+        double x = 0.0;
+        for (int s = 0; s < ns; ++s) x += ww[s] * vals[(uint64_t)s * stride + c.begin + i];
+        return x;
+    };
+    double a = 0.0;
+    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) a += val(i);
+    const double sum = block_sum(a, red);
+    const double mean = sum / (double)c.count;
+    double b = 0.0;
+    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) {
+        const double d = val(i) - mean;
+        b += d * d;
+    }
+    const double m2 = block_sum(b, red);
+    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
+}
+
+std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, const std::vector<StatsJob> &jobs) {
+    const uint32_t CH = 16384;
+    std::vector<ChunkDesc> chunks;
+    std::vector<size_t> first(jobs.size() + 1, 0);
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        first[j] = chunks.size();
+        for (uint64_t b = 0; b < jobs[j].n; b += CH)
+            chunks.push_back(ChunkDesc{jobs[j].begin + b, (uint32_t)std::min<uint64_t>(CH, jobs[j].n - b), 0});
+    }
+    first[jobs.size()] = chunks.size();
+    std::vector<Stats> res(jobs.size());
+    if (chunks.empty()) return res;
+    // jobs with different weights run as separate launches
+    c.chunks.ensure(chunks.size() * sizeof(ChunkDesc));
+    c.chunk_out.ensure(chunks.size() * sizeof(ChunkOut));
+    c.weights.ensure(jobs.size() * 8 * sizeof(double));
+    std::vector<double> wts(jobs.size() * 8);
+    for (size_t j = 0; j < jobs.size(); ++j)
+        for (int s = 0; s < 8; ++s) wts[j * 8 + s] = jobs[j].w[s];
+    KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.weights.p, wts.data(), wts.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        const size_t nc = first[j + 1] - first[j];
+        if (!nc) continue;
+        k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, c.weights.as<double>() + j * 8,
+                                                          c.chunks.as<ChunkDesc>() + first[j],
+                                                          c.chunk_out.as<ChunkOut>() + first[j]);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    }
+    std::vector<ChunkOut> h(chunks.size());
+    KX_CUDA(cudaMemcpyAsync(h.data(), c.chunk_out.p, h.size() * sizeof(ChunkOut), cudaMemcpyDeviceToHost, c.stream));
+    KX_CUDA(cudaStreamSynchronize(c.stream));
+    c.last.d2h_bytes += h.size() * sizeof(ChunkOut);
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        Stats s;
+        for (size_t q = first[j]; q < first[j + 1]; ++q) {  // Chan et al. pairwise merge, fixed order
+            const ChunkOut &o = h[q];
+            if (s.n == 0) { s.n = o.n; s.mean = o.mean; s.m2 = o.m2; continue; }
+            const double n = s.n + o.n;
+            const double d = o.mean - s.mean;
+            s.mean = s.mean + d * (o.n / n);
+            s.m2 = s.m2 + o.m2 + d * d * (s.n * o.n / n);
+            s.n = n;
+        }
+        res[j] = s;
+    }
+    return res;
+}
+
+kx_price_result finish(const Stats &s) {  // pricer.rs:303-328
+    const double Z95 = 1.959963984540054;
+    kx_price_result r{};
+    const uint64_t n = (uint64_t)s.n;
+    r.price = n ? s.mean : 0.0;
+    r.sample_std = n > 1 ? std::sqrt(s.m2 / ((double)n - 1.0)) : 0.0;
+    r.std_error = n > 0 ? r.sample_std / std::sqrt((double)n) : 0.0;
+    r.ci95_low = r.price - Z95 * r.std_error;
+    r.ci95_high = r.price + Z95 * r.std_error;
+    r.n_paths = n;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// host side of a path launch
+// ---------------------------------------------------------------------------
+struct Job {  // one contract of a launch
+    KxProgram prog;
+    StepTables tab;
+    ContractDev dev;
+    Model model;
+    std::vector<double> thr;  // [KX_MAX_NS][KX_MAX_SPOT] log(B / s0_s)
+};
+
+static void check_cfg(const kx_mc_config *cfg) {
+    if (!cfg) raise(KX_INVALID_ARGUMENT, "config is NULL");
+    if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
+    if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
+    if (cfg->flags != 0) raise(KX_INVALID_ARGUMENT, "flags must be 0");
+    if (cfg->n_paths > (1ull << 40)) raise(KX_INVALID_ARGUMENT, "n_paths too large");
+}
+
+// Scenario parameters (bump scenarios share the normals of a path).
+struct Scenario {
+    double s0, mu, sigma, rate;
+};
+
+static Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, const std::vector<double> &grid,
+                    const std::vector<Scenario> &scen_in, int smooth, double smooth_w) {
+    Job j;
+    j.model = m;
+    validate_model(m);
+    validate_grid(grid);
+    std::vector<Scenario> scen = scen_in;
+    if (scen.empty()) scen.push_back(Scenario{m.s0, m.mu, m.sigma, cfg.rate});
+    const int ns = (int)scen.size();
+    Model m0 = m;
+    m0.s0 = scen[0].s0;
+    m0.mu = scen[0].mu;
+    m0.sigma = scen[0].sigma;
+    bind(p.low, grid, m0, scen[0].rate, j.prog, j.tab);
+    const size_t n = grid.size();
+    if (ns > 1) {  // bump scenarios step with dt / sqrt(dt) and their own drift and volatility
+        for (size_t k = 0; k < n; ++k) {
+            const double dt = k == 0 ? grid[0] : grid[k] - grid[k - 1];
+            j.tab.c0[k] = dt;
+            j.tab.c1[k] = std::sqrt(dt);
+        }
+        j.tab.disc.resize(n * ns);
+        for (int s = 0; s < ns; ++s)
+            for (size_t k = 0; k < n; ++k) j.tab.disc[s * n + k] = std::exp(-scen[s].rate * grid[k]);
+    }
+    // log-spot thresholds of Spot-cmp-Const conditions, per scenario
+    bool nonpos = false;
+    for (auto &sc : scen) nonpos |= !(sc.s0 > 0.0);
+    if (nonpos) {  // log-space compare impossible: evaluate those conditions in full
+        for (int i = 0; i < j.prog.n_trig; ++i)
+            if (j.prog.trig[i].cond_kind == CK_SPOT_CMP) j.prog.trig[i].cond_kind = CK_GENERAL;
+        j.prog.spot_each_step = 1;
+    }
+    j.thr.assign((size_t)KX_MAX_NS * KX_MAX_SPOT, 0.0);
+    for (int s = 0; s < KX_MAX_NS; ++s) {
+        const Scenario &sc = scen[std::min(s, ns - 1)];
+        for (size_t q = 0; q < p.low.spot_cmp.size() && q < (size_t)KX_MAX_SPOT; ++q)
+            if (sc.s0 > 0.0) j.thr[(size_t)s * KX_MAX_SPOT + q] = std::log(p.low.spot_cmp[q].c / sc.s0);
+    }
+    ContractDev &d = j.dev;
+    memset(&d, 0, sizeof d);
+    d.n_times = (int32_t)n;
+    d.n_paths = cfg.n_paths;
+    d.seed = cfg.seed;
+    d.stream = 0;
+    d.smooth = smooth;
+    d.heston_scheme = m.scheme;
+    for (int s = 0; s < KX_MAX_NS; ++s) {
+        const Scenario &sc = scen[std::min(s, ns - 1)];
+        d.s0[s] = sc.s0;
+        d.drift[s] = sc.mu - 0.5 * sc.sigma * sc.sigma;
+        d.sigma[s] = sc.sigma;
+        d.s0f[s] = (float)d.s0[s];
+        d.driftf[s] = (float)d.drift[s];
+        d.sigmaf[s] = (float)d.sigma[s];
+    }
+    d.v0 = m.v0; d.kappa = m.kappa; d.theta = m.theta; d.sigma_v = m.sigma_v; d.rho = m.rho;
+    d.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));  // simulator.rs:510
+    d.r = m.r;
+    d.inv_w = smooth ? 1.0 / smooth_w : 0.0;
+    d.v0f = (float)d.v0; d.kappaf = (float)d.kappa; d.thetaf = (float)d.theta; d.sigma_vf = (float)d.sigma_v;
+    d.rhof = (float)d.rho; d.rho_perpf = (float)d.rho_perp; d.rf = (float)d.r; d.inv_wf = (float)d.inv_w;
+    return j;
+}
+
+template <class Real>
+static void pack_steps(const StepTables &t, std::vector<unsigned char> &out) {
+    const size_t n = t.c0.size();
+    const size_t off = out.size();
+    out.resize(off + n * sizeof(StepRec<Real>));
+    StepRec<Real> *r = reinterpret_cast<StepRec<Real> *>(out.data() + off);
+    for (size_t k = 0; k < n; ++k) r[k] = StepRec<Real>{(Real)t.c0[k], (Real)t.c1[k], t.time_true[k], 0u};
+}
+
+template <class Real, int MODEL, int NS>
+static const void *kernel_ptr() {
+    return reinterpret_cast<const void *>(&k_paths<Real, MODEL, NS>);
+}
+
+// Launch the fused path kernel over `jobs` (all of one model kind, one
+// precision and one scenario count). Per-path values land in c.pv:
+// scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
+static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out) {
+    const bool f64 = cfg.precision == KX_PREC_FP64;
+    const int model = jobs[0].model.kind;
+    std::vector<KxProgram> progs;
+    std::vector<unsigned char> steps;
+    std::vector<double> disc;
+    std::vector<ContractDev> cons;
+    std::vector<unsigned char> thr;
+    std::vector<WorkItem> items;
+    uint64_t total = 0, path_steps = 0;
+    int max_spot = 0, max_acc = 0;
+    for (auto &j : jobs) {
+        ContractDev d = j.dev;
+        d.prog = (int32_t)progs.size();
+        progs.push_back(j.prog);
+        d.step_off = (int32_t)(steps.size() / (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+        if (f64) pack_steps<double>(j.tab, steps);
+        else pack_steps<float>(j.tab, steps);
+        d.disc_off = (int32_t)disc.size();
+        disc.insert(disc.end(), j.tab.disc.begin(), j.tab.disc.end());
+        d.pv_off = total;
+        j.dev.pv_off = total;
+        total += d.n_paths;
+        path_steps += d.n_paths * (uint64_t)(d.n_times > 0 ? d.n_times - 1 : 0);
+        max_spot = std::max(max_spot, j.prog.n_spot_cmp);
+        max_acc = std::max(max_acc, j.prog.n_acc);
+        const size_t toff = thr.size();
+        if (f64) {
+            thr.resize(toff + j.thr.size() * sizeof(double));
+            memcpy(thr.data() + toff, j.thr.data(), j.thr.size() * sizeof(double));
+        } else {
+            thr.resize(toff + j.thr.size() * sizeof(float));
+            float *t = reinterpret_cast<float *>(thr.data() + toff);
+            for (size_t q = 0; q < j.thr.size(); ++q) t[q] = (float)j.thr[q];
+        }
+        cons.push_back(d);
+    }
+    c.last.path_steps += path_steps;
+    stride_out = total;
+    // work items: contiguous per contract, costliest contracts first
+    std::vector<int> order(jobs.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return cons[a].n_paths * (uint64_t)cons[a].n_times > cons[b].n_paths * (uint64_t)cons[b].n_times;
+    });
+    const int block = KX_BLOCK;
+    const bool smooth = jobs[0].dev.smooth != 0;
+    const uint32_t surv_base = 2u * (uint32_t)max_acc;
+    const uint32_t slots = surv_base + (smooth ? (uint32_t)max_spot : 0u);
+    const size_t smem = (size_t)ns * slots * block * (f64 ? 8 : 4);
+    const void *kfn = nullptr;
+    if (model == KX_MODEL_GBM) {
+        if (ns == 1) kfn = f64 ? kernel_ptr<double, M_GBM, 1>() : kernel_ptr<float, M_GBM, 1>();
+        else kfn = f64 ? kernel_ptr<double, M_GBM, KX_MAX_NS>() : kernel_ptr<float, M_GBM, KX_MAX_NS>();
+    } else {
+        if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
+        kfn = f64 ? kernel_ptr<double, M_HESTON, 1>() : kernel_ptr<float, M_HESTON, 1>();
+    }
+    if (smem > 48 * 1024) KX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int full = persistent_blocks(kfn, block, smem);
+    const uint64_t warps_total = (uint64_t)full * (block / 32);
+    uint64_t all_paths = 0;
+    for (auto &d : cons) all_paths += d.n_paths;
+    for (int ci : order) {
+        const uint64_t n = cons[ci].n_paths;
+        uint64_t item = all_paths / std::max<uint64_t>(1, warps_total * 8);
+        item = std::max<uint64_t>(64, std::min<uint64_t>(2048, item));
+        item = (item + 31) / 32 * 32;
+        for (uint64_t b = 0; b < n; b += item) items.push_back(WorkItem{ci, 0, b, std::min(item, n - b)});
+    }
+    if (items.empty()) return total;
+    const int grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (items.size() + 7) / 8 + 1);
+    // uploads
+    c.progs.ensure(progs.size() * sizeof(KxProgram));
+    c.steps.ensure(steps.size());
+    c.disc.ensure(disc.size() * sizeof(double));
+    c.cons.ensure(cons.size() * sizeof(ContractDev));
+    c.thr.ensure(thr.size());
+    c.items.ensure(items.size() * sizeof(WorkItem));
+    c.counters.ensure(64);
+    c.pv.ensure(std::max<uint64_t>(1, total * ns) * sizeof(double));
+    KX_CUDA(cudaMemcpyAsync(c.progs.p, progs.data(), progs.size() * sizeof(KxProgram), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.disc.p, disc.data(), disc.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.cons.p, cons.data(), cons.size() * sizeof(ContractDev), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.thr.p, thr.data(), thr.size(), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.items.p, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
+    c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + disc.size() * sizeof(double) +
+                        cons.size() * sizeof(ContractDev) + thr.size() + items.size() * sizeof(WorkItem);
+
+    PathArgs a{};
+    a.progs = c.progs.as<KxProgram>();
+    a.steps = c.steps.p;
+    a.disc = c.disc.as<double>();
+    a.cons = c.cons.as<ContractDev>();
+    a.thr = c.thr.p;
+    a.items = c.items.as<WorkItem>();
+    a.n_items = (uint32_t)items.size();
+    a.slots = slots;
+    a.surv_base = surv_base;
+    a.item_counter = c.counters.as<uint32_t>();
+    a.err_word = c.counters.as<uint32_t>() + 1;
+    a.steps_done = reinterpret_cast<unsigned long long *>(c.counters.as<uint32_t>() + 2);
+    a.pv = c.pv.as<double>();
+    a.pv_stride = total;
+    if (cfg.rng == KX_RNG_SHARED_DRAWS) {
+        DrawStore &ds = c.draws;
+        if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
+        for (auto &j : jobs) {
+            const uint64_t need = (uint64_t)(j.dev.n_times - 1) * j.model.draws_per_step();
+            if (ds.n_paths < j.dev.n_paths || ds.dpp < need)
+                raise(KX_INVALID_ARGUMENT, "shared draws too small: need " + std::to_string(j.dev.n_paths) + " paths x " +
+                                               std::to_string(need) + " draws");
+        }
+        a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
+        a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
+        a.z_dpp = ds.dpp;
+    }
+    void *args[] = {&a};
+    KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+    KX_CUDA(cudaLaunchKernel(kfn, dim3(grid_blocks), dim3(block), args, smem, c.stream));
+    KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+    c.last.kernel_launches++;
+    c.last.grid_blocks = (uint32_t)grid_blocks;
+    c.last.block_threads = (uint32_t)block;
+    uint32_t hc[4] = {0, 0, 0, 0};
+    KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
+    KX_CUDA(cudaStreamSynchronize(c.stream));
+    float ms = 0.f;
+    KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.last.kernel_ms += ms;
+    uint64_t sim = 0;
+    memcpy(&sim, &hc[2], sizeof sim);
+    c.last.steps_simulated += sim;
+    const uint32_t err = hc[1];
+    if (err & KX_ERR_LOOKAHEAD)
+        raise(KX_UNSUPPORTED, "an average window is read before it closes (look-ahead average)");
+    if (err & KX_ERR_MALFORMED) raise(KX_MALFORMED_CONTRACT, "average window inverted or empty at an evaluation date");
+    return total;
+}
+
+static void begin_call(Ctx &c) {
+    memset(&c.last, 0, sizeof c.last);
+    c.last.total_ms = -now_ms();
+}
+static void end_call(Ctx &c) { c.last.total_ms += now_ms(); }
+
+}  // namespace kx
+
+using namespace kx;
+
+extern "C" {
+
+kx_status kx_device_info(char *name, size_t cap, int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor) {
+    return guarded([&] {
+        Ctx &c = ctx();
+        if (name && cap) {
+            strncpy(name, c.name.c_str(), cap - 1);
+            name[cap - 1] = 0;
+        }
+        if (sm_count) *sm_count = c.sm_count;
+        if (cc_major) *cc_major = c.cc_major;
+        if (cc_minor) *cc_minor = c.cc_minor;
+    });
+}
+
+kx_status kx_last_launch_stats(kx_launch_stats *out) {
+    return guarded([&] {
+        if (!out) raise(KX_INVALID_ARGUMENT, "out is NULL");
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        *out = c.last;
+    });
+}
+
+kx_status kx_set_shared_draws(const double *z64, const float *z32, uint64_t n_paths, uint64_t draws_per_path) {
+    return guarded([&] {
+        if ((z64 == nullptr) == (z32 == nullptr)) raise(KX_INVALID_ARGUMENT, "exactly one of z64 / z32 must be given");
+        if (n_paths == 0 || draws_per_path == 0) raise(KX_INVALID_ARGUMENT, "empty draws");
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        DrawStore &d = c.draws;
+        const size_t n = (size_t)(n_paths * draws_per_path);
+        if (z64) {
+            d.z64.ensure(n * sizeof(double));
+            KX_CUDA(cudaMemcpy(d.z64.p, z64, n * sizeof(double), cudaMemcpyHostToDevice));
+        } else {
+            d.z32.ensure(n * sizeof(float));
+            KX_CUDA(cudaMemcpy(d.z32.p, z32, n * sizeof(float), cudaMemcpyHostToDevice));
+        }
+        d.is64 = z64 != nullptr;
+        d.n_paths = n_paths;
+        d.dpp = draws_per_path;
+        d.set = true;
+    });
+}
+
+kx_status kx_clear_shared_draws(void) {
+    return guarded([&] {
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        c.draws.set = false;
+    });
+}
+
+kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg, kx_price_result *out,
+                   double *per_path_pv) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        if (!out) raise(KX_INVALID_ARGUMENT, "out is NULL");
+        validate_model(m);
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, m.requires_fine_grid());  // pricer.rs:104
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        std::vector<Job> jobs;
+        jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
+        uint64_t stride = 0;
+        run_paths(c, jobs, *cfg, 1, stride);
+        std::vector<StatsJob> sj(1);
+        sj[0].begin = 0;
+        sj[0].n = cfg->n_paths;
+        *out = finish(device_stats(c, c.pv.as<double>(), stride, sj)[0]);
+        if (per_path_pv && cfg->n_paths) {
+            KX_CUDA(cudaMemcpyAsync(per_path_pv, c.pv.p, cfg->n_paths * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            KX_CUDA(cudaStreamSynchronize(c.stream));
+            c.last.d2h_bytes += cfg->n_paths * sizeof(double);
+        }
+        end_call(c);
+    });
+}
+
+kx_status kx_price_batch_shared(size_t n, const kx_program *const *progs, const kx_model *model,
+                                const kx_mc_config *cfg, kx_price_result *out) {
+    return guarded([&] {
+        if (n == 0) return;  // pricer.rs:255-257
+        if (!progs || !out) raise(KX_INVALID_ARGUMENT, "NULL array");
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        validate_model(m);
+        // merged plan (pricer.rs:260-279)
+        Plan merged;
+        for (size_t i = 0; i < n; ++i) {
+            const Program &p = program_of(progs[i]);
+            merged.fixed_dates.insert(merged.fixed_dates.end(), p.plan.fixed_dates.begin(), p.plan.fixed_dates.end());
+            merged.horizon = std::max(merged.horizon, p.plan.horizon);
+            merged.needs_fine_grid = merged.needs_fine_grid || p.plan.needs_fine_grid;
+        }
+        auto grid = time_grid_forced(merged, cfg->steps_per_year, m.requires_fine_grid());
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        // Every contract is valued on the same paths: the same seed and grid
+        // give each contract the same counter-based normals, hence the same
+        // simulated path, as the reference's single shared simulation.
+        std::vector<Job> jobs;
+        for (size_t i = 0; i < n; ++i) jobs.push_back(make_job(program_of(progs[i]), m, *cfg, grid, {}, 0, 0.0));
+        uint64_t stride = 0;
+        run_paths(c, jobs, *cfg, 1, stride);
+        std::vector<StatsJob> sj(n);
+        for (size_t i = 0; i < n; ++i) {
+            sj[i].begin = jobs[i].dev.pv_off;
+            sj[i].n = cfg->n_paths;
+        }
+        auto st = device_stats(c, c.pv.as<double>(), stride, sj);
+        for (size_t i = 0; i < n; ++i) out[i] = finish(st[i]);
+        end_call(c);
+    });
+}
+
+kx_status kx_price_portfolio(size_t n, const kx_program *const *progs, const kx_model *models,
+                             const kx_mc_config *cfgs, kx_price_result *out, kx_sens *sens) {
+    return guarded([&] {
+        if (n == 0) return;
+        if (!progs || !models || !cfgs || !out) raise(KX_INVALID_ARGUMENT, "NULL array");
+        if (sens) raise(KX_UNSUPPORTED, "portfolio sensitivities are not available in this build");
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        // group by (model kind, precision): one persistent launch per group
+        std::vector<size_t> idx(n);
+        for (size_t i = 0; i < n; ++i) idx[i] = i;
+        std::vector<std::vector<size_t>> groups;
+        for (int kind = 0; kind < 2; ++kind)
+            for (int prec = 0; prec < 2; ++prec) {
+                std::vector<size_t> gset;
+                for (size_t i = 0; i < n; ++i)
+                    if (models[i].kind == kind && cfgs[i].precision == prec) gset.push_back(i);
+                if (!gset.empty()) groups.push_back(gset);
+            }
+        for (auto &gset : groups) {
+            std::vector<Job> jobs;
+            for (size_t i : gset) {
+                check_cfg(&cfgs[i]);
+                if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "portfolio pricing uses Philox normals");
+                const Program &p = program_of(progs[i]);
+                Model m = model_from_c(&models[i]);
+                validate_model(m);
+                auto grid = time_grid_forced(p.plan, cfgs[i].steps_per_year, m.requires_fine_grid());
+                jobs.push_back(make_job(p, m, cfgs[i], grid, {}, 0, 0.0));
+            }
+            uint64_t stride = 0;
+            run_paths(c, jobs, cfgs[gset[0]], 1, stride);
+            std::vector<StatsJob> sj(gset.size());
+            for (size_t q = 0; q < gset.size(); ++q) {
+                sj[q].begin = jobs[q].dev.pv_off;
+                sj[q].n = jobs[q].dev.n_paths;
+            }
+            auto st = device_stats(c, c.pv.as<double>(), stride, sj);
+            for (size_t q = 0; q < gset.size(); ++q) out[gset[q]] = finish(st[q]);
+        }
+        end_call(c);
+    });
+}
+
+kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                         const kx_bumps *bumps, kx_greeks *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        if (!out) raise(KX_INVALID_ARGUMENT, "out is NULL");
+        if (m.kind != KX_MODEL_GBM) raise(KX_UNSUPPORTED, "bump-and-reprice Greeks need a GBM model (greeks.rs:60)");
+        validate_model(m);
+        kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
+        const double r = cfg->rate;
+        const double hs = b.relative ? b.spot * m.s0 : b.spot;
+        const double hv = b.relative ? b.vol * m.sigma : b.vol;
+        const double hr = b.relative ? b.rate * r : b.rate;
+        if (!(hs > 0) || !(hv > 0) || !(hr > 0)) raise(KX_INVALID_ARGUMENT, "bump sizes must be positive");
+        // greeks.rs:65-97: drift = rate, seven reprices sharing the normals
+        std::vector<Scenario> sc = {{m.s0, r, m.sigma, r},      {m.s0 + hs, r, m.sigma, r}, {m.s0 - hs, r, m.sigma, r},
+                                    {m.s0, r, m.sigma + hv, r}, {m.s0, r, m.sigma - hv, r}, {m.s0, r + hr, m.sigma, r + hr},
+                                    {m.s0, r - hr, m.sigma, r - hr}};
+        if (m.sigma - hv < 0) raise(KX_MALFORMED_CONTRACT, "GBM sigma must be non-negative (vol bump too large)");
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, false);
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        Model mb = m;
+        mb.mu = r;
+        std::vector<Job> jobs;
+        double w = b.smoothing_width;
+        jobs.push_back(make_job(p, mb, *cfg, grid, sc, b.smooth ? 1 : 0, w > 0 ? w : 1.0));
+        uint64_t stride = 0;
+        run_paths(c, jobs, *cfg, KX_MAX_NS, stride);
+        std::vector<StatsJob> sj(5);
+        for (auto &j : sj) {
+            j.begin = 0;
+            j.n = cfg->n_paths;
+            j.ns = KX_MAX_NS;
+            std::fill(j.w, j.w + 8, 0.0);
+        }
+        sj[0].w[0] = 1.0;                                                           // price
+        sj[1].w[1] = 1.0 / (2 * hs); sj[1].w[2] = -1.0 / (2 * hs);                 // delta
+        sj[2].w[1] = 1.0 / (hs * hs); sj[2].w[0] = -2.0 / (hs * hs); sj[2].w[2] = 1.0 / (hs * hs);  // gamma
+        sj[3].w[3] = 1.0 / (2 * hv); sj[3].w[4] = -1.0 / (2 * hv);                 // vega
+        sj[4].w[5] = 1.0 / (2 * hr); sj[4].w[6] = -1.0 / (2 * hr);                 // rho
+        auto st = device_stats(c, c.pv.as<double>(), stride, sj);
+        kx_price_result r0 = finish(st[0]), r1 = finish(st[1]), r2 = finish(st[2]), r3 = finish(st[3]), r4 = finish(st[4]);
+        out->price = r0.price; out->price_se = r0.std_error;
+        out->delta = r1.price; out->delta_se = r1.std_error;
+        out->gamma = r2.price; out->gamma_se = r2.std_error;
+        out->vega = r3.price; out->vega_se = r3.std_error;
+        out->rho = r4.price; out->rho_se = r4.std_error;
+        end_call(c);
+    });
+}
+
+}  // extern "C"

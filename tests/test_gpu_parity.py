@@ -1,0 +1,126 @@
+"""GPU parity: the engine (through the C ABI) against the oracle on the same
+normals. FP64 path arithmetic must match per path within 1e-12 (relative to
+max(|pv|, 1)); FP32 within 1e-5 relative to max(|pv|, s0) except paths whose
+barrier decision flips because a spot lies within 1e-5 of the barrier."""
+import numpy as np
+import pytest
+
+import kontracts_gb300 as kx
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def _cmp64(pv, ref):
+    pv, ref = np.asarray(pv), np.asarray(ref)
+    err = np.abs(pv - ref) / np.maximum(np.abs(ref), 1.0)
+    return float(err.max()) if len(err) else 0.0
+
+
+CONTRACTS = {
+    "euro_call": lambda: kx.european_call("X", 100.0, 1.0),
+    "euro_put": lambda: kx.european_put("X", 105.0, 0.75),
+    "up_and_out": lambda: kx.up_and_out_call("X", 100.0, 130.0, 1.0),
+    "down_and_out": lambda: kx.down_and_out_call("X", 100.0, 90.0, 1.0),
+    "asian": lambda: kx.scale((kx.average(kx.S("X")) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "lookback": lambda: kx.scale((kx.running_max(kx.S("X")) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "digital": lambda: kx.cash_or_nothing_call("X", 100.0, 10.0, 1.0),
+    "anytime_touch": lambda: kx.anytime(kx.S("X") >= 115.0, kx.one() @ kx.at(1.0)),
+    "straddle_give": lambda: kx.straddle("X", 100.0, 1.0) + kx.give(kx.zero_coupon_bond("USD", 0.5)),
+    "window_avg": lambda: kx.scale((kx.average_over(kx.S("X"), 0.25, 0.75) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "nested_when": lambda: kx.when(kx.at(0.5), kx.until(kx.S("X") <= 95.0, kx.scale(kx.S("X"), kx.one()) @ kx.at(1.0))),
+    "knock_at_zero": lambda: kx.until(kx.S("X") <= 200.0, kx.european_call("X", 100.0, 1.0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CONTRACTS))
+def test_fp64_philox_per_path_matches_oracle(orc, name):
+    c = CONTRACTS[name]()
+    model = kx.GBM(s0=100.0, sigma=0.25, r=0.05, asset="X")
+    n = 3000
+    res, pv = c.price(model, n_paths=n, seed=7, steps_per_year=52, precision="fp64", per_path=True)
+    ref, rpv = orc.price(c.to_json(), model, n_paths=n, seed=7, steps_per_year=52, per_path=True)
+    assert _cmp64(pv, rpv) < TOL64
+    assert abs(res.price - ref.price) <= TOL64 * max(1.0, abs(ref.price))
+    assert abs(res.sample_std - ref.sample_std) <= 1e-9 * max(1.0, ref.sample_std)
+    assert res.n_paths == n
+
+
+@pytest.mark.parametrize("name", sorted(CONTRACTS))
+def test_fp32_philox_per_path_close_to_oracle(orc, name):
+    c = CONTRACTS[name]()
+    model = kx.GBM(s0=100.0, sigma=0.25, r=0.05, asset="X")
+    n = 3000
+    res, pv = c.price(model, n_paths=n, seed=11, steps_per_year=52, precision="fp32", per_path=True)
+    ref, rpv = orc.price(c.to_json(), model, n_paths=n, seed=11, steps_per_year=52, per_path=True)
+    pv, rpv = np.asarray(pv), np.asarray(rpv)
+    err = np.abs(pv - rpv) / np.maximum(np.abs(rpv), 100.0)
+    bad = err > TOL32
+    # only barrier/threshold flips may differ: at most a handful of paths
+    assert bad.sum() <= max(2, n // 500), (name, int(bad.sum()), float(err.max()))
+    assert abs(res.price - ref.price) < 3 * ref.std_error + 1e-9
+
+
+@pytest.mark.parametrize("scheme", ["reference", "full_truncation"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_heston_per_path(orc, scheme, prec):
+    c = kx.european_call("X", 100.0, 1.0)
+    model = kx.heston(100.0, 0.04, 2.0, 0.04, 0.9, -0.5, 0.05, asset="X", scheme=scheme)
+    n = 2000
+    res, pv = c.price(model, n_paths=n, seed=3, steps_per_year=100, precision=prec, per_path=True)
+    ref, rpv = orc.price(c.to_json(), model, n_paths=n, seed=3, steps_per_year=100, per_path=True)
+    if prec == "fp64":
+        assert _cmp64(pv, rpv) < TOL64
+    else:
+        err = np.abs(np.asarray(pv) - rpv) / np.maximum(np.abs(rpv), 100.0)
+        assert (err > TOL32).sum() <= n // 500 + 1, float(err.max())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_shared_draws_per_path(orc, prec):
+    rng = np.random.default_rng(2024)
+    n, spy = 2000, 52
+    c = kx.up_and_out_call("X", 100.0, 125.0, 1.0)
+    z = rng.standard_normal((n, 60))
+    kx.set_shared_draws(z if prec == "fp64" else z.astype(np.float32))
+    orc.set_shared_draws(z if prec == "fp64" else z.astype(np.float32).astype(np.float64))
+    model = kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
+    res, pv = c.price(model, n_paths=n, seed=0, steps_per_year=spy, precision=prec, shared_draws=True, per_path=True)
+    ref, rpv = orc.price(c.to_json(), model, n_paths=n, seed=0, steps_per_year=spy, shared=True, per_path=True)
+    if prec == "fp64":
+        assert _cmp64(pv, rpv) < TOL64
+    else:
+        err = np.abs(np.asarray(pv) - rpv) / np.maximum(np.abs(rpv), 100.0)
+        assert (err > TOL32).sum() <= 4, float(err.max())
+
+
+def test_sigma_zero_exact_combinators(kx):
+    # tests/pricer.rs:58-106 restated on the engine (sigma = 0: S_t = 100 e^{0.05 t})
+    flat = kx.GBM(s0=100.0, sigma=0.0, r=0.05, asset="AAPL")
+    flat0 = kx.GBM(s0=100.0, sigma=0.0, r=0.0, asset="AAPL")
+    import math
+    p = lambda c, m: c.price(m, n_paths=16, seed=1, steps_per_year=4, precision="fp64").price
+    assert p(kx.zero(), flat) == 0.0
+    assert abs(p(kx.one("USD"), flat) - 1.0) < 1e-12
+    assert abs(p(kx.give(kx.one("USD")), flat) + 1.0) < 1e-12
+    assert abs(p(kx.one() + (kx.one() + kx.one()), flat0) - 3.0) < 1e-12
+    assert abs(p(kx.scale(7.5, kx.one()), flat0) - 7.5) < 1e-12
+    assert abs(p(kx.one() @ kx.at(1.0), flat) - math.exp(-0.05)) < 1e-12
+    assert abs(p(kx.scale(kx.S("AAPL"), kx.one() @ kx.at(1.0)), flat) - 100.0) < 1e-9
+
+
+def test_or_is_unsupported(kx):
+    with pytest.raises(kx.KontractError) as e:
+        kx.one().or_(kx.one()).price(kx.GBM(100, 0.0, 0.0, asset="AAPL"), n_paths=16)
+    assert e.value.status == "Unsupported"
+
+
+def test_bump_greeks_match_oracle_shared_normals(orc):
+    c = kx.european_call("AAPL", 100.0, 1.0)
+    model = kx.GBM(s0=100.0, sigma=0.2, r=0.05, asset="AAPL")
+    g = c.greeks(model, n_paths=20000, seed=5, steps_per_year=1, precision="fp64")
+    ref = orc.greeks(c.to_json(), model, n_paths=20000, seed=5, steps_per_year=1)
+    for k in ("price", "delta", "gamma", "vega", "rho"):
+        assert abs(getattr(g, k) - ref[k]) <= 1e-9 * max(1.0, abs(ref[k])), (k, getattr(g, k), ref[k])
