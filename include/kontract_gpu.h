@@ -141,7 +141,8 @@ typedef struct kx_sens {
 
 /* Timing and counters of the last pricing call on the calling process. */
 typedef struct kx_launch_stats {
-    double kernel_ms;          /* CUDA-event time of the main kernel(s) */
+    double kernel_ms;          /* CUDA-event time of the main path kernel(s) */
+    double reduce_ms;          /* CUDA-event time of the reduction kernels */
     double total_ms;           /* wall time of the whole call */
     uint64_t path_steps;       /* nominal path-steps (n_paths * grid steps) */
     uint64_t steps_simulated;  /* steps actually simulated (early exit skips) */
@@ -245,6 +246,13 @@ kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model,
                                 const kx_mc_config *cfg, const double *dates,
                                 size_t n_dates, int32_t n_basis,
                                 kx_price_result *out);
+
+/* Calibration microbenchmark (no reference counterpart): measured throughput
+ * of one GPU pipe on device 0, used as the roofline denominator of the path
+ * kernels. what = 0: MUFU (lg2/ex2/sin/cos approximations, results/s);
+ * 1: FP32 FMA (FMAs/s); 2: 32-bit integer multiply-high (IMAD.HI/s, the
+ * Philox multiply). */
+kx_status kx_measure_peak(int32_t what, double *ops_per_s);
 
 /* Counters of the last pricing call (see kx_launch_stats). */
 kx_status kx_last_launch_stats(kx_launch_stats *out);

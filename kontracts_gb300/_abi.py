@@ -90,7 +90,7 @@ class KxSens(C.Structure):
 
 class KxLaunchStats(C.Structure):
     _fields_ = [
-        ("kernel_ms", C.c_double), ("total_ms", C.c_double),
+        ("kernel_ms", C.c_double), ("reduce_ms", C.c_double), ("total_ms", C.c_double),
         ("path_steps", C.c_uint64), ("steps_simulated", C.c_uint64),
         ("kernel_launches", C.c_uint32), ("grid_blocks", C.c_uint32),
         ("block_threads", C.c_uint32), ("reserved", C.c_uint32),
@@ -137,6 +137,7 @@ SIGNATURES = {
     "kx_price_american_lsm": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                         C.POINTER(C.c_double), C.c_size_t, C.c_int32,
                                         C.POINTER(KxPriceResult)]),
+    "kx_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "kx_last_launch_stats": (C.c_int, [C.POINTER(KxLaunchStats)]),
     "kx_device_info": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_int32),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

@@ -17,8 +17,9 @@ kx_status fail_status(const Error &e) {
     g_last_error = e.msg;
     return e.code;
 }
-const Program &program_of(const kx_program *h) {
+const Program &program_of(const kx_program *h, bool need_lowered) {
     if (!h) raise(KX_INVALID_ARGUMENT, "program handle is NULL");
+    h->p.check(need_lowered);
     return h->p;
 }
 }  // namespace kx
@@ -40,8 +41,18 @@ kx_status kx_compile(const char *contract_json, kx_program **out) {
         try {
             h->p.json = contract_json ? contract_json : "";
             h->p.ast = parse_contract_json(contract_json);
-            h->p.plan = compile_plan(*h->p.ast);
-            lower(h->p);
+            try {
+                h->p.plan = compile_plan(*h->p.ast);
+                try {
+                    lower(h->p);
+                } catch (const Error &e) {
+                    h->p.low_status = e.code;
+                    h->p.low_msg = e.msg;
+                }
+            } catch (const Error &e) {
+                h->p.plan_status = e.code;
+                h->p.plan_msg = e.msg;
+            }
         } catch (...) {
             delete h;
             throw;
@@ -55,7 +66,7 @@ void kx_program_free(kx_program *prog) { delete prog; }
 kx_status kx_program_plan(const kx_program *prog, kx_plan_info *info, double *fixed_dates, size_t dates_cap,
                           char *assets_buf, size_t assets_cap) {
     return guarded([&] {
-        const Program &p = program_of(prog);
+        const Program &p = program_of(prog, false);
         if (!info) raise(KX_INVALID_ARGUMENT, "info is NULL");
         info->n_assets = (uint32_t)p.plan.assets.size();
         info->n_fixed_dates = (uint32_t)p.plan.fixed_dates.size();
@@ -81,7 +92,7 @@ kx_status kx_program_plan(const kx_program *prog, kx_plan_info *info, double *fi
 kx_status kx_time_grid(const kx_program *prog, uint32_t steps_per_year, int32_t force_fine, double *out, size_t cap,
                        size_t *n) {
     return guarded([&] {
-        const Program &p = program_of(prog);
+        const Program &p = program_of(prog, false);
         if (!n) raise(KX_INVALID_ARGUMENT, "n is NULL");
         auto g = time_grid_forced(p.plan, steps_per_year, force_fine != 0);
         *n = g.size();

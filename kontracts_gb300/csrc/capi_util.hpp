@@ -10,7 +10,7 @@ struct kx_program;
 namespace kx {
 extern thread_local std::string g_last_error;
 kx_status fail_status(const Error &e);
-const Program &program_of(const kx_program *h);
+const Program &program_of(const kx_program *h, bool need_lowered = true);
 
 // Run `f`, translating exceptions into kx_status and the thread's message.
 template <class F>

@@ -6,6 +6,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "../../include/kontract_gpu.h"
 #include "devprog.hpp"
 
 namespace kx {
@@ -100,8 +101,16 @@ __device__ __forceinline__ Real acc_value(const KxProgram &P, int a, AccView<Rea
 // the reference's `?` operators do, including the short-circuit of
 // `a && b` / `a || b` (observable.rs:164-165).
 template <class Real>
-__device__ Real eval_code(const KxProgram &P, int off, int len, AccView<Real> acc, uint32_t poisoned, int k,
-                          Real S, uint32_t &err) {
+struct EvalOut {
+    Real v;
+    uint32_t err;
+};
+
+template <class Real>
+__device__ __noinline__ EvalOut<Real> eval_code_impl(const KxProgram *__restrict__ Pp, int off, int len, Real *acc_base,
+                                                     int acc_stride, uint32_t poisoned, int k, Real S) {
+    const KxProgram &P = *Pp;
+    const AccView<Real> acc{acc_base, acc_stride};
     Real st[KX_MAX_STACK];
     uint32_t eb[KX_MAX_STACK];
     int sp = 0;
@@ -148,8 +157,65 @@ __device__ Real eval_code(const KxProgram &P, int off, int len, AccView<Real> ac
         }
         }
     }
-    err |= eb[0];
-    return st[0];
+    return EvalOut<Real>{st[0], eb[0]};
+}
+
+// Out-of-line so the (rare) interpreter does not weigh on the registers of
+// the per-step path that calls it.
+template <class Real>
+__device__ __forceinline__ Real eval_code(const KxProgram &P, int off, int len, AccView<Real> acc, uint32_t poisoned,
+                                          int k, Real S, uint32_t &err) {
+    const EvalOut<Real> o = eval_code_impl<Real>(&P, off, len, acc.base, acc.stride, poisoned, k, S);
+    err |= o.err;
+    return o.v;
+}
+
+template <class Real>
+struct StepRec {  // grid step k (k = 0 carries only the time bits)
+    Real c0, c1;  // GBM single scenario: drift*dt, sigma*sqrt(dt); otherwise dt, sqrt(dt)
+    uint32_t tt;  // CK_TIME trigger bits true at step k
+    uint32_t pad;
+};
+
+template <class Real> __device__ __forceinline__ Real pick(double d, float f);
+template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
+
+template <class Real> __device__ __forceinline__ Real fsqrt(Real x);
+template <> __device__ __forceinline__ float fsqrt<float>(float x) { return sqrt_approx(x); }
+template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(x); }
+
+// Heston Euler step (simulator.rs:506-541) in log-spot; dt and sqrt(dt) come
+// from the step table. The variance update keeps the reference's operation
+// order without fused multiply-adds in FP64, so on shared normals it rounds
+// exactly like the reference (v near 0 feeds sqrt, which would magnify any
+// rounding difference). REFERENCE_FLOOR floors v after the step; full
+// truncation (Lord et al. 2010) uses max(v, 0) inside the step instead.
+template <class Real>
+__device__ __forceinline__ void heston_step(Real r, Real kap, Real th, Real sv, Real rho, Real rp, int scheme, Real dt,
+                                            Real sq, Real z1, Real z2, Real &y, Real &v);
+template <>
+__device__ __forceinline__ void heston_step<float>(float r, float kap, float th, float sv, float rho, float rp,
+                                                   int scheme, float dt, float sq, float z1, float z2, float &y,
+                                                   float &v) {
+    const float vp = scheme == KX_HESTON_FULL_TRUNCATION ? fmaxf(v, 0.f) : v;
+    const float sqv = sqrt_approx(vp);
+    y += r * dt - 0.5f * vp * dt + sqv * (z1 * sq);
+    const float nv = v + kap * (th - vp) * dt + sv * sqv * ((rho * z1 + rp * z2) * sq);
+    v = scheme == KX_HESTON_FULL_TRUNCATION ? nv : fmaxf(nv, 0.f);
+}
+template <>
+__device__ __forceinline__ void heston_step<double>(double r, double kap, double th, double sv, double rho, double rp,
+                                                    int scheme, double dt, double sq, double z1, double z2, double &y,
+                                                    double &v) {
+    const double vp = scheme == KX_HESTON_FULL_TRUNCATION ? fmax(v, 0.0) : v;
+    const double sqv = sqrt(vp);
+    const double dw_s = __dmul_rn(z1, sq);
+    const double dw_v = __dmul_rn(__dadd_rn(__dmul_rn(rho, z1), __dmul_rn(rp, z2)), sq);
+    y += __dadd_rn(__dsub_rn(__dmul_rn(r, dt), __dmul_rn(__dmul_rn(0.5, vp), dt)), __dmul_rn(sqv, dw_s));
+    const double nv = __dadd_rn(__dadd_rn(v, __dmul_rn(__dmul_rn(kap, __dsub_rn(th, vp)), dt)),
+                                __dmul_rn(__dmul_rn(sv, sqv), dw_v));
+    v = scheme == KX_HESTON_FULL_TRUNCATION ? nv : (nv != nv ? 0.0 : fmax(nv, 0.0));
 }
 
 }  // namespace kx

@@ -127,8 +127,9 @@ struct KxProgram {
     // bound per launch:
     int32_t at_index[KX_MAX_AT];        // OP_AT: first step with t + 1e-12 >= date
     double spot_thr[KX_MAX_TRIG];       // CK_SPOT_CMP: log(Const / s0)
+    int32_t first_true[KX_MAX_TRIG];    // CK_TIME: first step whose condition holds (INT32_MAX: never)
+    uint32_t mono_mask;                 // CK_TIME slots whose condition stays true once true
     int32_t n_times;                    // grid points (step 0 is t = 0)
-    int32_t pad1;
 };
 
 // device-side error bits (OR-ed into one word per launch)

@@ -87,13 +87,6 @@ double now_ms() {
 // ---------------------------------------------------------------------------
 // device data layout
 // ---------------------------------------------------------------------------
-template <class Real>
-struct StepRec {  // grid step k (k = 0 carries only the time bits)
-    Real c0, c1;  // GBM single scenario: drift*dt, sigma*sqrt(dt); otherwise dt, sqrt(dt)
-    uint32_t tt;  // CK_TIME trigger bits true at step k
-    uint32_t pad;
-};
-
 constexpr int KX_MAX_SPOT = KX_MAX_TRIG;
 
 struct ContractDev {
@@ -145,37 +138,72 @@ struct PathArgs {
 
 enum { M_GBM = 0, M_HESTON = 1 };
 
-template <class Real> __device__ __forceinline__ Real pick(double d, float f);
-template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
-template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
-
-template <class Real> __device__ __forceinline__ Real fsqrt(Real x);
-template <> __device__ __forceinline__ float fsqrt<float>(float x) { return sqrt_approx(x); }
-template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(x); }
-
-// Per-contract values a warp keeps in registers while it works on a contract.
+// Per-contract values a warp keeps in registers: only what the per-step hot
+// path reads. Everything else is read from the (L1-resident) program table
+// when something fires.
 template <class Real, int NS>
 struct Hot {
     const KxProgram *P;
-    const ContractDev *C;
     const StepRec<Real> *R;
-    const double *D;
-    const Real *thr;  // [NS][KX_MAX_SPOT]
-    Real s0[NS], drift[NS], sig[NS];
-    Real kap, th, sv, rho, rp, r, v0, inv_w;
-    int n_times, n_acc;
-    uint32_t spot_each, time_mask, price_mask, until_mask, when_mask, all_leaves, err_capable, root_arm, root_leaves;
-    int smooth, scheme;
+    uint32_t fast_bit;   // the one Spot-cmp-Const slot checked from registers
+    uint32_t gen_mask;   // price-dependent slots needing the interpreter
+    uint32_t time_mask;
+    uint32_t flags;      // HF_* below
+    int n_times;
+    int n_acc;
+    Real fsign;          // y * fsign  >= / >  fthr[s]
+    Real fthr[NS];
+    Real s0[NS];
 };
+enum : uint32_t { HF_SPOT_EACH = 1, HF_SMOOTH = 2, HF_STRICT = 4, HF_FULLTRUNC = 8 };
 
 template <class Real, int NS>
 struct Lane {
     Real y[NS];  // log(S / s0) of each scenario
     Real v[NS];  // Heston variance
     uint32_t armed[NS], resolved[NS], dead[NS], emitted[NS], poisoned[NS];
+    int nte[NS];  // next step at which a live time-only slot can change
     double pv[NS];
     uint32_t err;
 };
+
+template <class Real, int NS>
+__device__ __forceinline__ void load_hot(Hot<Real, NS> &H, const PathArgs &A, int c) {
+    const ContractDev *C = A.cons + c;
+    H.P = A.progs + C->prog;
+    H.R = reinterpret_cast<const StepRec<Real> *>(A.steps) + C->step_off;
+    const Real *thr = reinterpret_cast<const Real *>(A.thr) + (size_t)c * KX_MAX_NS * KX_MAX_SPOT;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) H.s0[s] = pick<Real>(C->s0[s], C->s0f[s]);
+    H.n_times = C->n_times;
+    const KxProgram &P = *H.P;
+    H.n_acc = P.n_acc;
+    H.time_mask = P.time_mask;
+    H.flags = (P.spot_each_step ? HF_SPOT_EACH : 0u) | (C->smooth ? HF_SMOOTH : 0u) |
+              (C->heston_scheme == KX_HESTON_FULL_TRUNCATION ? HF_FULLTRUNC : 0u);
+    H.fast_bit = 0;
+    H.fsign = Real(1);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) H.fthr[s] = Real(0);
+    uint32_t pm = P.price_mask;
+    if (C->smooth) pm &= ~P.until_mask;  // smoothed untils never knock
+    uint32_t gen = pm;
+    while (pm) {
+        const int i = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const KxTrig &T = P.trig[i];
+        if (T.cond_kind == CK_SPOT_CMP) {
+            H.fast_bit = 1u << i;
+            gen &= ~H.fast_bit;
+            if (T.cmp == CMP_GT || T.cmp == CMP_LT) H.flags |= HF_STRICT;
+            H.fsign = (T.cmp == CMP_LE || T.cmp == CMP_LT) ? Real(-1) : Real(1);
+#pragma unroll
+            for (int s = 0; s < NS; ++s) H.fthr[s] = H.fsign * thr[s * KX_MAX_SPOT + T.spot_slot];
+            break;
+        }
+    }
+    H.gen_mask = gen;
+}
 
 template <class Real>
 __device__ __forceinline__ bool cmp_y(uint8_t cmp, Real y, Real thr) {
@@ -196,31 +224,26 @@ __device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, R
     return Real(1) / (Real(1) + fast_exp<Real>(x));
 }
 
-template <class Real, int NS>
-__device__ __forceinline__ Real spot_of(const Hot<Real, NS> &H, const Lane<Real, NS> &L, int s) {
-    return H.s0[s] * fast_exp<Real>(L.y[s]);
-}
-
-// Conditions of the trigger slots in `mask` at step k for scenario s.
-template <class Real, int NS>
-__device__ __forceinline__ uint32_t cond_bits(const Hot<Real, NS> &H, Lane<Real, NS> &L, int s, uint32_t mask, int k,
-                                              uint32_t tt, AccView<Real> acc, Real &S, bool &haveS) {
-    const KxProgram &P = *H.P;
-    uint32_t bits = mask & H.time_mask & tt;
-    uint32_t pm = mask & H.price_mask;
+// Full condition evaluation of the slots in `mask` at step k: time bits from
+// the table, Spot-cmp-Const from the thresholds, anything else through the
+// expression interpreter.
+template <class Real>
+__device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const StepRec<Real> *R, const Real *thr,
+                                                   bool smooth, Real y, Real S, uint32_t poisoned, uint32_t mask, int k,
+                                                   AccView<Real> acc, uint32_t &err) {
+    uint32_t bits = mask & P.time_mask;
+    if (bits) bits &= R[k].tt;
+    uint32_t pm = mask & ~P.time_mask;
     while (pm) {
         const int i = __ffs(pm) - 1;
         pm &= pm - 1;
         const KxTrig &T = P.trig[i];
         bool b;
         if (T.cond_kind == CK_SPOT_CMP) {
-            if (H.smooth && T.kind == TK_UNTIL) continue;  // weighted instead of knocked
-            b = cmp_y<Real>(T.cmp, L.y[s], H.thr[s * KX_MAX_SPOT + T.spot_slot]);
+            if (smooth && T.kind == TK_UNTIL) continue;  // weighted instead of knocked
+            b = cmp_y<Real>(T.cmp, y, thr[T.spot_slot]);
         } else {
-            if (!haveS) { S = spot_of(H, L, s); haveS = true; }
-            uint32_t e = 0;
-            b = eval_code<Real>(P, T.code_off, T.code_len, acc, L.poisoned[s], k, S, e) != Real(0);
-            L.err |= e;
+            b = eval_code<Real>(P, T.code_off, T.code_len, acc, poisoned, k, S, err) != Real(0);
         }
         if (b) bits |= 1u << i;
     }
@@ -230,27 +253,27 @@ __device__ __forceinline__ uint32_t cond_bits(const Hot<Real, NS> &H, Lane<Real,
 // Everything the contract does at grid step k for scenario s, after the
 // model moved to step k. Returns true when no flow can change any more.
 template <class Real, int NS>
-__device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, Lane<Real, NS> &L, int s, int k, uint32_t tt,
-                                              AccView<Real> acc, AccView<Real> surv) {
+__device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const PathArgs &A, int cur, Lane<Real, NS> &L,
+                                              int s, int k, AccView<Real> acc, AccView<Real> surv) {
     const KxProgram &P = *H.P;
+    const bool smooth = (H.flags & HF_SMOOTH) != 0u;
     Real S = Real(0);
-    bool haveS = false;
-    if (H.spot_each) { S = spot_of(H, L, s); haveS = true; }
+    if (H.flags & HF_SPOT_EACH) S = H.s0[s] * fast_exp<Real>(L.y[s]);
     // accumulators (observable.rs:120-140), inner ones first (slot order)
     for (int a = 0; a < H.n_acc; ++a) {
-        const KxAcc &A = P.acc[a];
-        if (k < A.i_from || k > A.i_to) continue;
+        const KxAcc &Ac = P.acc[a];
+        if (k < Ac.i_from || k > Ac.i_to) continue;
         Real x;
-        if (A.inner == IK_SPOT) {
+        if (Ac.inner == IK_SPOT) {
             x = S;
         } else {
             uint32_t e = 0;
-            x = eval_code<Real>(P, A.code_off, A.code_len, acc, L.poisoned[s], k, S, e);
+            x = eval_code<Real>(P, Ac.code_off, Ac.code_len, acc, L.poisoned[s], k, S, e);
             if (e) L.poisoned[s] |= 1u << a;
         }
         Real &v = acc[2 * a];
-        if (A.kind == ACC_MAX) v = fmax(v, x);
-        else if (A.kind == ACC_MIN) v = fmin(v, x);
+        if (Ac.kind == ACC_MAX) v = fmax(v, x);
+        else if (Ac.kind == ACC_MIN) v = fmin(v, x);
         else if (sizeof(Real) == 8) v = v + x;
         else {  // compensated (Kahan) sum in FP32
             Real &c = acc[2 * a + 1];
@@ -260,45 +283,68 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, Lane<Real,
             v = t;
         }
     }
-    // triggers: check live slots, then cascade the arming within the step
-    uint32_t fired = 0;
     const uint32_t live = L.armed[s] & ~L.resolved[s];
-    if (live) {
-        uint32_t newly = cond_bits<Real, NS>(H, L, s, live, k, tt, acc, S, haveS);
-        while (newly) {
-            L.resolved[s] |= newly;
-            uint32_t u = newly & H.until_mask;
-            while (u) {
-                const int i = __ffs(u) - 1;
-                u &= u - 1;
-                L.dead[s] |= P.trig[i].leaves & ~L.emitted[s];
-            }
-            uint32_t w = newly & H.when_mask;
-            fired |= w;
-            uint32_t arm = 0;
-            while (w) {
-                const int i = __ffs(w) - 1;
-                w &= w - 1;
-                arm |= P.trig[i].fire_arm;
-            }
-            arm &= ~L.armed[s];
-            L.armed[s] |= arm;
-            newly = arm ? cond_bits<Real, NS>(H, L, s, arm, k, tt, acc, S, haveS) : 0u;
-        }
+    uint32_t bits = 0;
+    if (live & H.fast_bit) {
+        const Real yy = H.fsign * L.y[s];
+        const bool b = (H.flags & HF_STRICT) ? yy > H.fthr[s] : yy >= H.fthr[s];
+        if (b) bits = H.fast_bit;
     }
-    // smoothed until weights of every armed smoothed slot (armed ones included)
-    if (H.smooth) {
-        uint32_t sm = L.armed[s] & H.until_mask & H.price_mask;
+    if (k >= L.nte[s]) bits |= live & H.time_mask & H.R[k].tt;
+    const bool need_rare = bits || k == 0 || (live & H.gen_mask) || smooth;
+    if (!need_rare) return false;
+
+    // ---- rare path: general conditions, smoothing, firing, flows ----
+    const ContractDev &C = A.cons[cur];
+    const Real *thr = reinterpret_cast<const Real *>(A.thr) + ((size_t)cur * KX_MAX_NS + s) * KX_MAX_SPOT;
+    const double *D = A.disc + C.disc_off + (size_t)s * H.n_times;
+    const Real inv_w = pick<Real>(C.inv_w, C.inv_wf);
+    const Real y = L.y[s];
+    S = H.s0[s] * fast_exp<Real>(y);
+    if (live & H.gen_mask) bits |= cond_bits_full<Real>(P, H.R, thr, smooth, y, S, L.poisoned[s], live & H.gen_mask, k, acc, L.err);
+    if (smooth) {  // smoothed until weights of the slots armed before this step
+        uint32_t sm = L.armed[s] & P.until_mask & ~P.time_mask;
         while (sm) {
             const int i = __ffs(sm) - 1;
             sm &= sm - 1;
             const KxTrig &T = P.trig[i];
-            if (T.cond_kind != CK_SPOT_CMP) continue;
-            surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, L.y[s], H.thr[s * KX_MAX_SPOT + T.spot_slot], H.inv_w);
+            if (T.cond_kind == CK_SPOT_CMP) surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, y, thr[T.spot_slot], inv_w);
+        }
+    }
+    if (!bits && k != 0) return false;
+    uint32_t fired = 0;
+    uint32_t newly = bits;
+    while (newly) {
+        L.resolved[s] |= newly;
+        uint32_t u = newly & P.until_mask;
+        while (u) {
+            const int i = __ffs(u) - 1;
+            u &= u - 1;
+            L.dead[s] |= P.trig[i].leaves & ~L.emitted[s];
+        }
+        uint32_t w = newly & P.when_mask;
+        fired |= w;
+        uint32_t arm = 0;
+        while (w) {
+            const int i = __ffs(w) - 1;
+            w &= w - 1;
+            arm |= P.trig[i].fire_arm;
+        }
+        arm &= ~L.armed[s];
+        L.armed[s] |= arm;
+        newly = arm ? cond_bits_full<Real>(P, H.R, thr, smooth, y, S, L.poisoned[s], arm, k, acc, L.err) : 0u;
+        if (smooth && arm) {  // smoothed slots armed now weigh this step too
+            uint32_t sm = arm & P.until_mask & ~P.time_mask;
+            while (sm) {
+                const int i = __ffs(sm) - 1;
+                sm &= sm - 1;
+                const KxTrig &T = P.trig[i];
+                if (T.cond_kind == CK_SPOT_CMP) surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, y, thr[T.spot_slot], inv_w);
+            }
         }
     }
     // flows acquired at step k (pricer.rs:380-405)
-    uint32_t acq = k == 0 ? H.root_leaves : 0u;
+    uint32_t acq = k == 0 ? P.root_leaves : 0u;
     while (fired) {
         const int i = __ffs(fired) - 1;
         fired &= fired - 1;
@@ -311,18 +357,11 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, Lane<Real,
         const KxLeaf &F = P.leaf[j];
         const bool is_dead = (L.dead[s] >> j) & 1u;
         if (is_dead && !F.err_capable) continue;
-        double amt;
-        if (F.kind == AK_CONST) {
-            amt = F.sign;
-        } else {
-            if (!haveS) { S = spot_of(H, L, s); haveS = true; }
-            uint32_t e = 0;
-            amt = (double)eval_code<Real>(P, F.code_off, F.code_len, acc, L.poisoned[s], k, S, e);
-            L.err |= e;
-        }
+        double amt = F.kind == AK_CONST ? F.sign
+                                        : (double)eval_code<Real>(P, F.code_off, F.code_len, acc, L.poisoned[s], k, S, L.err);
         if (is_dead) continue;
-        if (H.smooth) {
-            uint32_t us = H.until_mask & H.price_mask & L.armed[s];
+        if (smooth) {
+            uint32_t us = P.until_mask & ~P.time_mask & L.armed[s];
             while (us) {
                 const int i = __ffs(us) - 1;
                 us &= us - 1;
@@ -330,14 +369,35 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, Lane<Real,
                 if (T.cond_kind == CK_SPOT_CMP && ((T.leaves >> j) & 1u)) amt *= (double)surv[T.spot_slot];
             }
         }
-        L.pv[s] += amt * H.D[(size_t)s * H.n_times + k];
+        L.pv[s] += amt * D[k];
         L.emitted[s] |= 1u << j;
     }
-    return !H.err_capable && (H.all_leaves & ~(L.emitted[s] | L.dead[s])) == 0u;
+    // next step at which a live time-only slot can change
+    const uint32_t live_t = L.armed[s] & ~L.resolved[s] & P.time_mask;
+    int nte = INT_MAX;
+    if (live_t & ~P.mono_mask) {
+        nte = k + 1;
+    } else {
+        uint32_t t = live_t;
+        while (t) {
+            const int i = __ffs(t) - 1;
+            t &= t - 1;
+            nte = min(nte, P.first_true[i]);
+        }
+    }
+    L.nte[s] = nte;
+    return !P.err_capable && (P.all_leaves & ~(L.emitted[s] | L.dead[s])) == 0u;
+}
+
+template <class Real, int NS>
+__device__ __forceinline__ void write_path(const PathArgs &A, int cur, int64_t path, const Lane<Real, NS> &L) {
+    const uint64_t off = A.cons[cur].pv_off + (uint64_t)path;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) A.pv[(uint64_t)s * A.pv_stride + off] = L.pv[s];
 }
 
 template <class Real, int MODEL, int NS>
-__global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
+__global__ void __launch_bounds__(KX_BLOCK, NS == 1 ? 4 : 2) k_paths(const PathArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *smem = reinterpret_cast<Real *>(smem_raw);
     const unsigned FULL = 0xffffffffu;
@@ -346,136 +406,98 @@ __global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
     constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
     constexpr uint32_t ALL = (1u << NS) - 1u;
+    const int nthr = KX_BLOCK;
 
-    // warp-uniform work state
+    // warp-uniform work state (path indices are per contract, < 2^32)
     int cur = -1, pend = -1;
-    uint64_t nx = 0, end = 0, pnx = 0, pend_end = 0;
+    uint32_t nx = 0, end = 0;
     bool drained = false;
     Hot<Real, NS> H;
-    H.P = nullptr;
+    Real hr = 0, hk = 0, hth = 0, hsv = 0, hrho = 0, hrp = 0, hv0 = 0;  // Heston parameters
 
     // lane state
-    long long path = -1;
+    int64_t path = -1;
     int k = 0;
     uint32_t done = 0;
     Lane<Real, NS> L;
     L.err = 0;
-    unsigned long long my_steps = 0;
-    const int slots = (int)A.slots;
-    const int nthr = (int)blockDim.x;
-
-    auto accv = [&](int s) { return AccView<Real>{smem + (size_t)s * slots * nthr + threadIdx.x, nthr}; };
-    auto survv = [&](int s) {
-        return AccView<Real>{smem + ((size_t)s * slots + A.surv_base) * nthr + threadIdx.x, nthr};
-    };
-
-    auto bind_contract = [&](int c) {
-        cur = c;
-        const ContractDev *C = A.cons + c;
-        H.C = C;
-        H.P = A.progs + C->prog;
-        H.R = reinterpret_cast<const StepRec<Real> *>(A.steps) + C->step_off;
-        H.D = A.disc + C->disc_off;
-        H.thr = reinterpret_cast<const Real *>(A.thr) + (size_t)c * KX_MAX_NS * KX_MAX_SPOT;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            H.s0[s] = pick<Real>(C->s0[s], C->s0f[s]);
-            H.drift[s] = pick<Real>(C->drift[s], C->driftf[s]);
-            H.sig[s] = pick<Real>(C->sigma[s], C->sigmaf[s]);
-        }
-        H.kap = pick<Real>(C->kappa, C->kappaf);
-        H.th = pick<Real>(C->theta, C->thetaf);
-        H.sv = pick<Real>(C->sigma_v, C->sigma_vf);
-        H.rho = pick<Real>(C->rho, C->rhof);
-        H.rp = pick<Real>(C->rho_perp, C->rho_perpf);
-        H.r = pick<Real>(C->r, C->rf);
-        H.v0 = pick<Real>(C->v0, C->v0f);
-        H.inv_w = pick<Real>(C->inv_w, C->inv_wf);
-        H.n_times = C->n_times;
-        H.smooth = C->smooth;
-        H.scheme = C->heston_scheme;
-        const KxProgram &P = *H.P;
-        H.n_acc = P.n_acc;
-        H.spot_each = P.spot_each_step;
-        H.time_mask = P.time_mask;
-        H.price_mask = P.price_mask;
-        H.until_mask = P.until_mask;
-        H.when_mask = P.when_mask;
-        H.all_leaves = P.all_leaves;
-        H.err_capable = P.err_capable;
-        H.root_arm = P.root_arm;
-        H.root_leaves = P.root_leaves;
-    };
-
-    auto finish_path = [&]() {
-#pragma unroll
-        for (int s = 0; s < NS; ++s) A.pv[(uint64_t)s * A.pv_stride + H.C->pv_off + (uint64_t)path] = L.pv[s];
-        path = -1;
-    };
+    uint32_t my_steps = 0;
 
     while (true) {
         // ---- hand paths to idle lanes (warp-uniform control) ----
         unsigned idle = __ballot_sync(FULL, path < 0);
         while (idle) {
             if (nx >= end) {
-                if (pend >= 0) {
-                    if (idle != FULL) break;  // finish the current contract first
-                    bind_contract(pend);
-                    nx = pnx;
-                    end = pend_end;
-                    pend = -1;
-                    continue;
-                }
-                if (drained) break;
-                int it = 0;
-                if (lane == 0) it = (int)atomicAdd(A.item_counter, 1u);
-                it = __shfl_sync(FULL, it, 0);
-                if (it >= (int)A.n_items) { drained = true; break; }
-                const WorkItem w = A.items[it];
-                if (w.contract != cur) {
-                    if (cur >= 0 && idle != FULL) {
-                        pend = w.contract;
-                        pnx = w.first;
-                        pend_end = w.first + w.count;
+                int it = pend;
+                if (it < 0) {
+                    if (drained) break;
+                    if (lane == 0) it = (int)atomicAdd(A.item_counter, 1u);
+                    it = __shfl_sync(FULL, it, 0);
+                    if (it >= (int)A.n_items) {
+                        drained = true;
                         break;
                     }
-                    bind_contract(w.contract);
                 }
-                nx = w.first;
-                end = w.first + w.count;
+                const WorkItem w = A.items[it];
+                if (w.contract != cur) {
+                    if (cur >= 0 && idle != FULL) {  // finish the current contract first
+                        pend = it;
+                        break;
+                    }
+                    cur = w.contract;
+                    load_hot<Real, NS>(H, A, cur);
+                    if (MODEL == M_HESTON) {
+                        const ContractDev &C = A.cons[cur];
+                        hr = pick<Real>(C.r, C.rf);
+                        hk = pick<Real>(C.kappa, C.kappaf);
+                        hth = pick<Real>(C.theta, C.thetaf);
+                        hsv = pick<Real>(C.sigma_v, C.sigma_vf);
+                        hrho = pick<Real>(C.rho, C.rhof);
+                        hrp = pick<Real>(C.rho_perp, C.rho_perpf);
+                        hv0 = pick<Real>(C.v0, C.v0f);
+                    }
+                }
+                pend = -1;
+                nx = (uint32_t)w.first;
+                end = (uint32_t)(w.first + w.count);
                 continue;
             }
             const int nidle = __popc(idle);
-            const uint64_t avail = end - nx;
-            const int take = avail < (uint64_t)nidle ? (int)avail : nidle;
-            if (path < 0 && __popc(idle & lt) < take) {
-                path = (long long)(nx + (uint64_t)__popc(idle & lt));
+            const uint32_t avail = end - nx;
+            const int take = avail < (uint32_t)nidle ? (int)avail : nidle;
+            const int rank = __popc(idle & lt);
+            if (path < 0 && rank < take) {
+                path = (int64_t)(nx + (uint32_t)rank);
                 // new path: state at t = 0 (S = s0), then the contract at step 0
                 const KxProgram &P = *H.P;
+                done = 0;
 #pragma unroll
                 for (int s = 0; s < NS; ++s) {
                     L.y[s] = Real(0);
-                    L.v[s] = fmax(H.v0, Real(0));
-                    L.armed[s] = H.root_arm;
+                    L.v[s] = fmax(hv0, Real(0));
+                    L.armed[s] = P.root_arm;
                     L.resolved[s] = L.dead[s] = L.emitted[s] = L.poisoned[s] = 0u;
+                    L.nte[s] = 0;
                     L.pv[s] = 0.0;
-                    AccView<Real> av = accv(s), sv = survv(s);
+                    AccView<Real> av{smem + (s * (int)A.slots) * nthr + threadIdx.x, nthr};
+                    AccView<Real> sv{smem + (s * (int)A.slots + (int)A.surv_base) * nthr + threadIdx.x, nthr};
                     for (int a = 0; a < H.n_acc; ++a) {
-                        av[2 * a] = P.acc[a].kind == ACC_MAX ? Real(-INFINITY) : P.acc[a].kind == ACC_MIN ? Real(INFINITY) : Real(0);
+                        av[2 * a] = P.acc[a].kind == ACC_MAX   ? Real(-INFINITY)
+                                    : P.acc[a].kind == ACC_MIN ? Real(INFINITY)
+                                                               : Real(0);
                         av[2 * a + 1] = Real(0);
                     }
-                    if (H.smooth)
+                    if (H.flags & HF_SMOOTH)
                         for (int q = 0; q < P.n_spot_cmp; ++q) sv[q] = Real(1);
+                    if (contract_step<Real, NS>(H, A, cur, L, s, 0, av, sv)) done |= 1u << s;
                 }
-                done = 0;
-                const uint32_t tt0 = H.R[0].tt;
-#pragma unroll
-                for (int s = 0; s < NS; ++s)
-                    if (contract_step<Real, NS>(H, L, s, 0, tt0, accv(s), survv(s))) done |= 1u << s;
                 k = 1;
-                if (H.n_times <= 1 || done == ALL) finish_path();
+                if (H.n_times <= 1 || done == ALL) {
+                    write_path<Real, NS>(A, cur, path, L);
+                    path = -1;
+                }
             }
-            nx += (uint64_t)take;
+            nx += (uint32_t)take;
             if (take == 0) break;
             idle = __ballot_sync(FULL, path < 0);
         }
@@ -489,11 +511,10 @@ __global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
             const int nt = H.n_times;
             Real z0, z1, z2, z3;
             if (A.z64 == nullptr && A.z32 == nullptr) {
+                const ContractDev &C = A.cons[cur];
                 const uint32_t blk = (uint32_t)((k - 1) / SPB);
-                const uint64_t seed = H.C->seed;
-                const uint4 w = philox4x32_10(
-                    make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32), H.C->stream), (uint32_t)seed,
-                    (uint32_t)(seed >> 32));
+                const uint4 w = philox4x32_10(make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32), C.stream),
+                                              (uint32_t)C.seed, (uint32_t)(C.seed >> 32));
                 box_muller(w.x, w.y, z0, z1);
                 box_muller(w.z, w.w, z2, z3);
             } else {
@@ -503,7 +524,10 @@ __global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                     zz[j] = d0 + j < A.z_dpp ? (A.z64 ? (Real)A.z64[base + j] : (Real)A.z32[base + j]) : Real(0);
-                z0 = zz[0]; z1 = zz[1]; z2 = zz[2]; z3 = zz[3];
+                z0 = zz[0];
+                z1 = zz[1];
+                z2 = zz[2];
+                z3 = zz[3];
             }
 #pragma unroll 1
             for (int j = 0; j < SPB; ++j) {
@@ -517,28 +541,33 @@ __global__ void __launch_bounds__(KX_BLOCK) k_paths(const PathArgs A) {
                     if ((done >> s) & 1u) continue;
                     if (MODEL == M_GBM) {
                         // log-space exact GBM step (simulator.rs:238-245)
-                        if (NS == 1) L.y[s] += rec.c0 + rec.c1 * za;
-                        else L.y[s] += H.drift[s] * rec.c0 + H.sig[s] * rec.c1 * za;
+                        if (NS == 1) {
+                            L.y[s] += rec.c0 + rec.c1 * za;
+                        } else {
+                            const ContractDev &C = A.cons[cur];
+                            L.y[s] += pick<Real>(C.drift[s], C.driftf[s]) * rec.c0 +
+                                      pick<Real>(C.sigma[s], C.sigmaf[s]) * rec.c1 * za;
+                        }
                     } else {
-                        // Heston Euler step (simulator.rs:517-534); rec.c0 = dt, rec.c1 = sqrt(dt)
-                        const Real dt = rec.c0, sq = rec.c1;
-                        const Real vv = L.v[s];
-                        const Real vp = H.scheme == KX_HESTON_FULL_TRUNCATION ? fmax(vv, Real(0)) : vv;
-                        const Real sqv = fsqrt<Real>(vp);
-                        L.y[s] += H.r * dt - Real(0.5) * vp * dt + sqv * (h1 * sq);
-                        const Real nv = vv + H.kap * (H.th - vp) * dt + H.sv * sqv * ((H.rho * h1 + H.rp * h2) * sq);
-                        L.v[s] = H.scheme == KX_HESTON_FULL_TRUNCATION ? nv : fmax(nv, Real(0));
+                        heston_step<Real>(hr, hk, hth, hsv, hrho, hrp,
+                                          (H.flags & HF_FULLTRUNC) ? KX_HESTON_FULL_TRUNCATION : KX_HESTON_REFERENCE_FLOOR,
+                                          rec.c0, rec.c1, h1, h2, L.y[s], L.v[s]);
                     }
-                    if (contract_step<Real, NS>(H, L, s, kk, rec.tt, accv(s), survv(s))) done |= 1u << s;
+                    AccView<Real> av{smem + (s * (int)A.slots) * nthr + threadIdx.x, nthr};
+                    AccView<Real> sv{smem + (s * (int)A.slots + (int)A.surv_base) * nthr + threadIdx.x, nthr};
+                    if (contract_step<Real, NS>(H, A, cur, L, s, kk, av, sv)) done |= 1u << s;
                 }
                 ++my_steps;
             }
             k += SPB;
-            if (k >= nt || done == ALL) finish_path();
+            if (k >= nt || done == ALL) {
+                write_path<Real, NS>(A, cur, path, L);
+                path = -1;
+            }
         }
     }
     // counters: one atomic per warp
-    unsigned long long tot = my_steps;
+    unsigned long long tot = (unsigned long long)my_steps;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
     uint32_t err = L.err;
@@ -630,6 +659,7 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
         for (int s = 0; s < 8; ++s) wts[j * 8 + s] = jobs[j].w[s];
     KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice, c.stream));
     KX_CUDA(cudaMemcpyAsync(c.weights.p, wts.data(), wts.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaEventRecord(c.ev0, c.stream));
     for (size_t j = 0; j < jobs.size(); ++j) {
         const size_t nc = first[j + 1] - first[j];
         if (!nc) continue;
@@ -639,9 +669,13 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
         KX_CUDA(cudaGetLastError());
         c.last.kernel_launches++;
     }
+    KX_CUDA(cudaEventRecord(c.ev1, c.stream));
     std::vector<ChunkOut> h(chunks.size());
     KX_CUDA(cudaMemcpyAsync(h.data(), c.chunk_out.p, h.size() * sizeof(ChunkOut), cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));
+    float rms = 0.f;
+    KX_CUDA(cudaEventElapsedTime(&rms, c.ev0, c.ev1));
+    c.last.reduce_ms += rms;
     c.last.d2h_bytes += h.size() * sizeof(ChunkOut);
     for (size_t j = 0; j < jobs.size(); ++j) {
         Stats s;
@@ -688,7 +722,7 @@ static void check_cfg(const kx_mc_config *cfg) {
     if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
     if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
     if (cfg->flags != 0) raise(KX_INVALID_ARGUMENT, "flags must be 0");
-    if (cfg->n_paths > (1ull << 40)) raise(KX_INVALID_ARGUMENT, "n_paths too large");
+    if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
 }
 
 // Scenario parameters (bump scenarios share the normals of a path).
@@ -926,11 +960,85 @@ static void begin_call(Ctx &c) {
 }
 static void end_call(Ctx &c) { c.last.total_ms += now_ms(); }
 
+// ---------------------------------------------------------------------------
+// calibration kernels: 8 independent dependency chains per thread, enough
+// warps per SM to fill the pipe; the result is stored so nothing is elided.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_peak_mufu(float *out, int iters) {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = 0.5f + 1e-3f * (threadIdx.x + i);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            float x;
+            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(x) : "f"(a[i]));
+            asm volatile("lg2.approx.ftz.f32 %0, %1;" : "=f"(a[i]) : "f"(x));
+        }
+    }
+    float t = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t += a[i];
+    if (t == 12345.f) out[threadIdx.x] = t;
+}
+__global__ void __launch_bounds__(256) k_peak_fma(float *out, int iters) {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = 1e-3f * (threadIdx.x + i);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = fmaf(a[i], 0.999f, 1e-4f);
+    }
+    float t = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t += a[i];
+    if (t == 12345.f) out[threadIdx.x] = t;
+}
+__global__ void __launch_bounds__(256) k_peak_imad(unsigned *out, int iters) {
+    unsigned a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = threadIdx.x * 2654435761u + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = __umulhi(a[i], 0xD2511F53u) + a[i];
+    }
+    unsigned t = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t ^= a[i];
+    if (t == 12345u) out[threadIdx.x] = t;
+}
+
 }  // namespace kx
 
 using namespace kx;
 
 extern "C" {
+
+kx_status kx_measure_peak(int32_t what, double *ops_per_s) {
+    return guarded([&] {
+        if (!ops_per_s || what < 0 || what > 2) raise(KX_INVALID_ARGUMENT, "bad arguments");
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        c.misc.ensure(4096);
+        const int blocks = c.sm_count * 8, threads = 256, iters = 4096;
+        double best = 0.0;
+        for (int rep = 0; rep < 4; ++rep) {
+            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+            if (what == 0) k_peak_mufu<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
+            else if (what == 1) k_peak_fma<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
+            else k_peak_imad<<<blocks, threads, 0, c.stream>>>(c.misc.as<unsigned>(), iters);
+            KX_CUDA(cudaGetLastError());
+            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+            KX_CUDA(cudaEventSynchronize(c.ev1));
+            float ms = 0.f;
+            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+            const double ops = (double)blocks * threads * iters * 8 * (what == 0 ? 2 : 1);
+            best = std::max(best, ops / (ms * 1e-3));
+        }
+        *ops_per_s = best;
+    });
+}
+
 
 kx_status kx_device_info(char *name, size_t cap, int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor) {
     return guarded([&] {

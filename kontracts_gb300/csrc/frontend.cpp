@@ -806,6 +806,21 @@ void bind(const Lowered &low, const std::vector<double> &grid, const Model &m, d
             if (P.trig[i].cond_kind == CK_TIME && eval_time_cond(*low.time_cond[i], grid[k], low)) bits |= 1u << i;
         tab.time_true[k] = bits;
     }
+    // time-only slots: first step they hold, and whether they then keep holding
+    P.mono_mask = 0;
+    for (int i = 0; i < P.n_trig; ++i) {
+        P.first_true[i] = INT32_MAX;
+        if (P.trig[i].cond_kind != CK_TIME) continue;
+        int first = -1;
+        bool mono = true;
+        for (int k = 0; k < n; ++k) {
+            const bool b = (tab.time_true[k] >> i) & 1u;
+            if (b && first < 0) first = k;
+            if (!b && first >= 0) mono = false;
+        }
+        P.first_true[i] = first < 0 ? INT32_MAX : first;
+        if (mono) P.mono_mask |= 1u << i;
+    }
 }
 
 }  // namespace kx

@@ -76,6 +76,15 @@ struct Program {  // what kx_program points at
     Plan plan;
     Lowered low;
     std::string json;
+    // The reference parses in Contract::from_json but only compiles inside
+    // price_gbm (pricer.rs:102), so compile/lowering errors are kept here and
+    // raised by the calls that need the plan or the lowered table.
+    kx_status plan_status = KX_OK, low_status = KX_OK;
+    std::string plan_msg, low_msg;
+    void check(bool need_lowered) const {
+        if (plan_status != KX_OK) raise(plan_status, plan_msg);
+        if (need_lowered && low_status != KX_OK) raise(low_status, low_msg);
+    }
 };
 
 void lower(Program &p);

@@ -1,7 +1,399 @@
-// lsm.cu — Longstaff-Schwartz American pricing (placeholder until the kernels land).
+// lsm.cu — Longstaff-Schwartz American pricing on the GPU
+// (price_american_lsm / backward_induction, src/lsm.rs:80-229).
+//
+//  1. k_lsm_forward simulates every path on the grid [0, dates...] (the same
+//     Philox counters as the European kernels, so the same paths) and stores
+//     S at each exercise date in HBM, date-major: S[d * n_paths + i], so that
+//     consecutive threads write and read consecutive addresses.
+//  2. One k_lsm_step launch per exercise date, walking backwards. Launch d
+//     applies the exercise decision of date d to every path's realised value
+//     (lsm.rs:196-222) and, in the same pass, accumulates the FP64 normal
+//     equations A^T A, A^T y of date d-1 over the in-the-money paths
+//     (lsm.rs:259-288: monomial basis 1, S, ..., S^(m-1)). Each block writes
+//     its partial sums to a fixed slot; the last block to finish adds them in
+//     block order (deterministic) and solves the m x m system by Gauss
+//     elimination with partial pivoting, exactly as numerics::solve_linear
+//     (numerics.rs:190-236): a pivot below 1e-12 gives zero coefficients.
+//  3. k_lsm_final discounts the values to t = 0; the per-path values then go
+//     through the same deterministic statistics as every price.
+// The launches are queued back to back with no host synchronisation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "device_common.cuh"
 #include "engine.hpp"
+
+namespace kx {
+
+constexpr int LSM_BLOCK = 256;
+constexpr int LSM_MAXM = 6;
+constexpr int LSM_COEF = 8;  // coef[d * LSM_COEF + j], j < m; [7] = have-fit flag
+
+struct LsmArgs {
+    const KxProgram *P;  // bound payoff program (root flows only)
+    const void *steps;   // StepRec<Real>[n_times]
+    const double *disc;  // disc[d] = exp(-rate (t_{d+1} - t_d)), d < n_ex - 1; disc[n_ex - 1] = exp(-rate t_0)
+    int n_times;         // 1 + n_ex
+    int n_ex;
+    uint64_t n_paths;
+    uint64_t seed;
+    int model;
+    int scheme;
+    double s0, v0, kappa, theta, sigma_v, rho, rho_perp, r;
+    const double *z64;
+    const float *z32;
+    uint64_t z_dpp;
+    void *S;           // Real[n_ex][n_paths]
+    void *value;       // Real[n_paths]: realised value at the current date
+    double *pv;        // final per-path values
+    double *partial;   // [gridDim][nsum]
+    double *coef;      // [n_ex][LSM_COEF]
+    unsigned *ticket;
+};
+
+// Value of the exercised contract at exercise step k (lsm.rs:238-251): the
+// lowered payoff has only flows acquired at once, so each flow's discount to
+// the exercise date is exp(0) = 1 and the value is the sum of the amounts.
+template <class Real>
+__device__ __forceinline__ Real lsm_payoff(const KxProgram &P, Real S, int k) {
+    Real v = Real(0);
+    AccView<Real> none{nullptr, 0};
+    for (int j = 0; j < P.n_leaf; ++j) {
+        const KxLeaf &F = P.leaf[j];
+        uint32_t e = 0;
+        v += F.kind == AK_CONST ? (Real)F.sign : eval_code<Real>(P, F.code_off, F.code_len, none, 0u, k, S, e);
+    }
+    return v;
+}
+
+template <class Real, int MODEL>
+__global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward(const LsmArgs A) {
+    constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
+    const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+    Real *S = reinterpret_cast<Real *>(A.S);
+    const Real s0 = (Real)A.s0, r = (Real)A.r, kap = (Real)A.kappa, th = (Real)A.theta, sv = (Real)A.sigma_v,
+               rho = (Real)A.rho, rp = (Real)A.rho_perp;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        Real y = Real(0), v = (Real)fmax(A.v0, 0.0);
+        Real z[4];
+        for (int k = 1; k < A.n_times; ++k) {
+            const uint64_t d = (uint64_t)(k - 1) * DRAWS;
+            if ((d & 3u) == 0) {
+                if (A.z64 == nullptr && A.z32 == nullptr) {
+                    const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)i, (uint32_t)(i >> 32), 0u),
+                                                  (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+                    box_muller(w.x, w.y, z[0], z[1]);
+                    box_muller(w.z, w.w, z[2], z[3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        z[j] = d + j < A.z_dpp ? (A.z64 ? (Real)A.z64[i * A.z_dpp + d + j] : (Real)A.z32[i * A.z_dpp + d + j])
+                                               : Real(0);
+                }
+            }
+            const StepRec<Real> rec = R[k];
+            const int q = (int)(d & 3u);
+            if (MODEL == KX_MODEL_GBM) {
+                y += rec.c0 + rec.c1 * z[q];
+            } else {
+                heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[q], z[q + 1], y, v);
+            }
+            S[(uint64_t)(k - 1) * A.n_paths + i] = s0 * fast_exp<Real>(y);
+        }
+    }
+}
+
+// Block-wide sum of `n` doubles per thread into red[0..n) (fixed order).
+__device__ void block_sums(double *vals, int n, double *red) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int q = 0; q < n; ++q) {
+        double v = vals[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (l == 0) red[q * 32 + w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        double t = 0.0;
+        for (int j = 0; j < nw; ++j) t += red[threadIdx.x * 32 + j];
+        red[32 * 64 + threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+// numerics.rs:190-236 for m <= LSM_MAXM, on one thread.
+__device__ void solve_gauss(double a[LSM_MAXM][LSM_MAXM], double b[LSM_MAXM], int m, double x[LSM_MAXM]) {
+    for (int col = 0; col < m; ++col) {
+        int piv = col;
+        double best = fabs(a[col][col]);
+        for (int row = col + 1; row < m; ++row) {
+            const double v = fabs(a[row][col]);
+            if (v > best) { best = v; piv = row; }
+        }
+        if (best < 1e-12) {
+            for (int j = 0; j < m; ++j) x[j] = 0.0;
+            return;
+        }
+        for (int c = 0; c < m; ++c) { const double t = a[col][c]; a[col][c] = a[piv][c]; a[piv][c] = t; }
+        { const double t = b[col]; b[col] = b[piv]; b[piv] = t; }
+        for (int row = col + 1; row < m; ++row) {
+            const double factor = __ddiv_rn(a[row][col], a[col][col]);
+            for (int c = col; c < m; ++c) a[row][c] = __dsub_rn(a[row][c], __dmul_rn(factor, a[col][c]));
+            b[row] = __dsub_rn(b[row], __dmul_rn(factor, b[col]));
+        }
+    }
+    for (int row = m - 1; row >= 0; --row) {
+        double sum = b[row];
+        for (int c = row + 1; c < m; ++c) sum = __dsub_rn(sum, __dmul_rn(a[row][c], x[c]));
+        x[row] = __ddiv_rn(sum, a[row][row]);
+    }
+}
+
+// One backward launch: update the values with the decision of date `upd`
+// (upd < 0: initialise them with the payoff at the last date), then
+// accumulate the regression of date `gram` (gram < 0: none).
+template <class Real, int M>
+__global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd, int gram) {
+    constexpr int NA = M * (M + 1) / 2;
+    constexpr int NS = NA + M + 1;  // A upper triangle, A^T y, ITM count
+    __shared__ double red[32 * 64 + 64];
+    __shared__ bool last;
+    const KxProgram &P = *A.P;
+    const Real *S = reinterpret_cast<const Real *>(A.S);
+    Real *V = reinterpret_cast<Real *>(A.value);
+    double acc[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) acc[q] = 0.0;
+    double cu[M];
+    bool have = false;
+    if (upd >= 0) {
+        have = A.coef[upd * LSM_COEF + 7] != 0.0;
+#pragma unroll
+        for (int j = 0; j < M; ++j) cu[j] = A.coef[upd * LSM_COEF + j];
+    }
+    const double disc_u = upd >= 0 ? A.disc[upd] : 0.0;
+    const double disc_g = gram >= 0 ? A.disc[gram] : 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        Real val;
+        if (upd < 0) {
+            val = lsm_payoff<Real>(P, S[(uint64_t)(A.n_ex - 1) * A.n_paths + i], A.n_ex);
+        } else {
+            const Real s = S[(uint64_t)upd * A.n_paths + i];
+            const Real pay = lsm_payoff<Real>(P, s, upd + 1);
+            const double discounted = (double)V[i] * disc_u;
+            double nv = discounted;
+            if (pay > Real(0)) {
+                double cont = discounted;
+                if (have) {  // poly_eval, lsm.rs:293-295 (Horner from the top coefficient)
+                    cont = 0.0;
+#pragma unroll
+                    for (int j = M - 1; j >= 0; --j) cont = __dadd_rn(__dmul_rn(cont, (double)s), cu[j]);
+                }
+                nv = (double)pay > cont ? (double)pay : discounted;
+            }
+            val = (Real)nv;
+        }
+        V[i] = val;
+        if (gram >= 0) {
+            const Real sg = S[(uint64_t)gram * A.n_paths + i];
+            if (lsm_payoff<Real>(P, sg, gram + 1) > Real(0)) {
+                const double x = (double)sg;
+                const double y = (double)val * disc_g;
+                double pw[M];
+                pw[0] = 1.0;
+#pragma unroll
+                for (int j = 1; j < M; ++j) pw[j] = __dmul_rn(pw[j - 1], x);
+                int q = 0;
+#pragma unroll
+                for (int r = 0; r < M; ++r)
+#pragma unroll
+                    for (int c = r; c < M; ++c) acc[q++] += __dmul_rn(pw[r], pw[c]);
+#pragma unroll
+                for (int r = 0; r < M; ++r) acc[NA + r] += __dmul_rn(pw[r], y);
+                acc[NS - 1] += 1.0;
+            }
+        }
+    }
+    if (gram < 0) return;
+    block_sums(acc, NS, red);
+    if (threadIdx.x < NS) A.partial[(size_t)blockIdx.x * 64 + threadIdx.x] = red[32 * 64 + threadIdx.x];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(A.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < NS) {
+        double t = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) t += A.partial[(size_t)b * 64 + threadIdx.x];
+        red[threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a[LSM_MAXM][LSM_MAXM], b[LSM_MAXM], x[LSM_MAXM];
+        int q = 0;
+        for (int r = 0; r < M; ++r)
+            for (int c = r; c < M; ++c) { a[r][c] = red[q]; a[c][r] = red[q]; ++q; }
+        for (int r = 0; r < M; ++r) b[r] = red[NA + r];
+        const double count = red[NS - 1];
+        const bool fit = count >= (double)M;  // lsm.rs:190-194
+        if (fit) solve_gauss(a, b, M, x);
+        for (int j = 0; j < M; ++j) A.coef[gram * LSM_COEF + j] = fit ? x[j] : 0.0;
+        A.coef[gram * LSM_COEF + 7] = fit ? 1.0 : 0.0;
+        *A.ticket = 0u;
+    }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(LSM_BLOCK) k_lsm_final(const LsmArgs A) {
+    const Real *V = reinterpret_cast<const Real *>(A.value);
+    const double d0 = A.disc[A.n_ex - 1];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        A.pv[i] = (double)V[i] * d0;
+}
+
+template <class Real, int M>
+static void launch_steps(Ctx &c, const LsmArgs &a, int blocks) {
+    const int n_ex = a.n_ex;
+    k_lsm_step<Real, M><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, -1, n_ex - 2);
+    KX_CUDA(cudaGetLastError());
+    c.last.kernel_launches++;
+    for (int d = n_ex - 2; d >= 0; --d) {
+        k_lsm_step<Real, M><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, d, d - 1);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    }
+}
+
+template <class Real>
+static void run_lsm(Ctx &c, LsmArgs &a, int m, int model) {
+    const int blocks = c.sm_count * 4;
+    if (model == KX_MODEL_GBM) k_lsm_forward<Real, KX_MODEL_GBM><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
+    else k_lsm_forward<Real, KX_MODEL_HESTON><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
+    KX_CUDA(cudaGetLastError());
+    c.last.kernel_launches++;
+    switch (m) {
+    case 2: launch_steps<Real, 2>(c, a, blocks); break;
+    case 3: launch_steps<Real, 3>(c, a, blocks); break;
+    case 4: launch_steps<Real, 4>(c, a, blocks); break;
+    case 5: launch_steps<Real, 5>(c, a, blocks); break;
+    default: launch_steps<Real, 6>(c, a, blocks); break;
+    }
+    k_lsm_final<Real><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
+    KX_CUDA(cudaGetLastError());
+    c.last.kernel_launches++;
+}
+
+}  // namespace kx
+
 using namespace kx;
-extern "C" kx_status kx_price_american_lsm(const kx_program *, const kx_model *, const kx_mc_config *,
-                                           const double *, size_t, int32_t, kx_price_result *) {
-    return guarded([&] { raise(KX_UNSUPPORTED, "LSM not built yet"); });
+
+extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                                           const double *dates, size_t n_dates, int32_t n_basis,
+                                           kx_price_result *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        if (!cfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (cfg->flags != 0 || (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) ||
+            (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64))
+            raise(KX_INVALID_ARGUMENT, "bad config");
+        // lsm.rs:87-105
+        if (n_dates == 0 || !dates) raise(KX_MALFORMED_CONTRACT, "LSM: at least one exercise date required");
+        for (size_t i = 1; i < n_dates; ++i)
+            if (!(dates[i] > dates[i - 1])) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
+        if (!(dates[0] > 0.0)) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
+        if (n_basis < 2) raise(KX_MALFORMED_CONTRACT, "LSM: n_basis >= 2 required");
+        if (n_basis > LSM_MAXM) raise(KX_UNSUPPORTED, "LSM: n_basis above 6 is not supported on the device");
+        const KxProgram &L = p.low.prog;
+        if (L.n_trig != 0 || L.n_acc != 0)
+            raise(KX_UNSUPPORTED, "LSM payoff must be an immediate function of the spot "
+                                  "(no when/until/anytime, averages or running extrema)");
+        validate_model(m);
+        std::vector<double> grid{0.0};
+        grid.insert(grid.end(), dates, dates + n_dates);
+        validate_grid(grid);
+        const bool f64 = cfg->precision == KX_PREC_FP64;
+        const uint64_t np = cfg->n_paths;
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        memset(&c.last, 0, sizeof c.last);
+        c.last.total_ms = -now_ms();
+        KxProgram P;
+        StepTables tab;
+        bind(p.low, grid, m, cfg->rate, P, tab);
+        const int n_ex = (int)n_dates;
+        std::vector<double> disc(n_ex);
+        for (int d = 0; d + 1 < n_ex; ++d) disc[d] = std::exp(-cfg->rate * (dates[d + 1] - dates[d]));  // lsm.rs:176
+        disc[n_ex - 1] = std::exp(-cfg->rate * dates[0]);                                            // lsm.rs:226
+        std::vector<unsigned char> steps(grid.size() * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+        for (size_t k = 0; k < grid.size(); ++k) {
+            if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {tab.c0[k], tab.c1[k], 0u, 0u};
+            else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)tab.c0[k], (float)tab.c1[k], 0u, 0u};
+        }
+        const size_t rs = f64 ? 8 : 4;
+        const int blocks = c.sm_count * 4;
+        c.progs.ensure(sizeof(KxProgram));
+        c.steps.ensure(steps.size());
+        c.disc.ensure(disc.size() * sizeof(double));
+        c.lsm_paths.ensure(std::max<uint64_t>(1, np * n_ex) * rs);
+        c.lsm_value.ensure(std::max<uint64_t>(1, np) * rs);
+        c.pv.ensure(std::max<uint64_t>(1, np) * sizeof(double));
+        c.lsm_stats.ensure((size_t)blocks * 64 * sizeof(double) + (size_t)n_ex * LSM_COEF * sizeof(double));
+        c.counters.ensure(64);
+        KX_CUDA(cudaMemcpyAsync(c.progs.p, &P, sizeof P, cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.disc.p, disc.data(), disc.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
+        c.last.h2d_bytes += sizeof P + steps.size() + disc.size() * sizeof(double);
+        LsmArgs a{};
+        a.P = c.progs.as<KxProgram>();
+        a.steps = c.steps.p;
+        a.disc = c.disc.as<double>();
+        a.n_times = (int)grid.size();
+        a.n_ex = n_ex;
+        a.n_paths = np;
+        a.seed = cfg->seed;
+        a.model = m.kind;
+        a.scheme = m.scheme;
+        a.s0 = m.s0;
+        a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
+        a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
+        a.r = m.r;
+        if (cfg->rng == KX_RNG_SHARED_DRAWS) {
+            DrawStore &ds = c.draws;
+            if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
+            if (ds.n_paths < np || ds.dpp < (uint64_t)n_ex * m.draws_per_step())
+                raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
+            a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
+            a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
+            a.z_dpp = ds.dpp;
+        }
+        a.S = c.lsm_paths.p;
+        a.value = c.lsm_value.p;
+        a.pv = c.pv.as<double>();
+        a.partial = c.lsm_stats.as<double>();
+        a.coef = c.lsm_stats.as<double>() + (size_t)blocks * 64;
+        a.ticket = c.counters.as<unsigned>();
+        if (np > 0) {
+            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+            if (f64) run_lsm<double>(c, a, n_basis, m.kind);
+            else run_lsm<float>(c, a, n_basis, m.kind);
+            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+            KX_CUDA(cudaEventSynchronize(c.ev1));
+            float ms = 0.f;
+            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+            c.last.kernel_ms += ms;
+        }
+        c.last.path_steps += np * (uint64_t)n_ex;
+        c.last.steps_simulated += np * (uint64_t)n_ex;
+        std::vector<StatsJob> sj(1);
+        sj[0].n = np;
+        *out = finish(device_stats(c, c.pv.as<double>(), np, sj)[0]);
+        c.last.total_ms += now_ms();
+    });
 }

@@ -81,6 +81,7 @@ class Oracle:
             fn = getattr(L, f)
             fn.restype = D
             fn.argtypes = [D] * n
+        L.ko_value_on_path.argtypes = [C.c_char_p, P(D), P(D), C.c_size_t, C.c_char_p, D, P(D)]
         L.ko_bs_call_greeks.argtypes = [D] * 5 + [P(D)]
         L.ko_crr_american.restype = D
         L.ko_crr_american.argtypes = [D, D, D, D, D, C.c_int, C.c_int]
@@ -189,6 +190,15 @@ class Oracle:
                                            C.byref(r),
                                            pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
         return (Result(r), pp[:n_paths]) if per_path else Result(r)
+
+    def value_on_path(self, js: str, times, values, asset: str = "S", rate: float = 0.0) -> float:
+        t = np.ascontiguousarray(times, dtype=np.float64)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        out = C.c_double()
+        self._chk(self.L.ko_value_on_path(js.encode(), t.ctypes.data_as(C.POINTER(C.c_double)),
+                                          v.ctypes.data_as(C.POINTER(C.c_double)), len(t), asset.encode(),
+                                          float(rate), C.byref(out)))
+        return out.value
 
     # ---- closed forms ----
     def bs_call(self, s, k, t, r, sigma): return self.L.ko_bs_call(s, k, t, r, sigma)

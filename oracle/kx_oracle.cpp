@@ -1132,6 +1132,19 @@ int ko_price_american(const char *json, const kx_model *model, const kx_mc_confi
     });
 }
 
+// present_value of a contract on one hand-built path (tests/observable.rs
+// builds paths this way): times[n], spot values of `asset`, discount rate.
+int ko_value_on_path(const char *json, const double *times, const double *values, size_t n, const char *asset,
+                     double rate, double *out) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        std::vector<double> g(times, times + n);
+        std::string a = asset ? asset : "ASSET";
+        PathView pv{&g, values, &a};
+        *out = present_value(*c, pv, g, rate);
+    });
+}
+
 // ---- closed forms used as oracle values ------------------------------------
 double ko_norm_cdf_as(double x) { return norm_cdf_as(x); }
 

@@ -1,0 +1,81 @@
+"""GPU Longstaff-Schwartz against the oracle's restatement of lsm.rs.
+
+On shared FP64 normals the engine must reproduce the oracle path by path
+(1e-12) except where an exercise decision flips because payoff and fitted
+continuation value agree to ~1e-12 (the Gram sums are added in a different
+order); on Philox normals and in FP32 the price must sit within 3 combined
+standard errors, and the American put must match the CRR tree (the
+reference's own check, tests/j17_lsm.rs:40-72)."""
+import math
+
+import numpy as np
+import pytest
+
+import kontracts_gb300 as kx
+
+pytestmark = pytest.mark.gpu
+
+
+def put(k, asset="X"):
+    return kx.scale((kx.const_(k) - kx.S(asset)).clip(0.0), kx.one())
+
+
+def dates(t, n):
+    return [t * i / n for i in range(1, n + 1)]
+
+
+@pytest.mark.parametrize("n_basis", [2, 3, 4])
+def test_lsm_shared_draws_fp64_per_path(orc, n_basis):
+    rng = np.random.default_rng(n_basis)
+    n, nd = 4000, 25
+    z = rng.standard_normal((n, nd))
+    kx.set_shared_draws(z)
+    orc.set_shared_draws(z)
+    m = kx.GBM(s0=40.0, sigma=0.2, r=0.06, asset="X")
+    c = put(40.0)
+    ds = dates(1.0, nd)
+    res = c.price_american(m, ds, n_paths=n, seed=0, n_basis=n_basis, precision="fp64", shared_draws=True)
+    ref = orc.price_american(c.to_json(), m, ds, n_paths=n, seed=0, n_basis=n_basis, shared=True)
+    assert abs(res.price - ref.price) <= 1e-12 * abs(ref.price) + 2e-3 * ref.std_error
+    assert res.n_paths == n
+
+
+def test_lsm_philox_fp64_and_fp32_match_oracle(orc):
+    m = kx.GBM(s0=36.0, sigma=0.2, r=0.06, asset="X")
+    c = put(40.0)
+    ds = dates(1.0, 50)
+    ref = orc.price_american(c.to_json(), m, ds, n_paths=50_000, seed=9, n_basis=4)
+    r64 = c.price_american(m, ds, n_paths=50_000, seed=9, n_basis=4, precision="fp64")
+    assert abs(r64.price - ref.price) < 1e-6 * ref.price
+    r32 = c.price_american(m, ds, n_paths=50_000, seed=9, n_basis=4, precision="fp32")
+    assert abs(r32.price - ref.price) < 3 * ref.std_error
+
+
+@pytest.mark.parametrize("s0,sigma,t", [(36.0, 0.2, 1.0), (40.0, 0.4, 2.0), (44.0, 0.2, 2.0)])
+def test_american_put_vs_crr(orc, s0, sigma, t):
+    """Longstaff-Schwartz (2001) table cases, 50 exercise dates a year, 1M paths."""
+    m = kx.GBM(s0=s0, sigma=sigma, r=0.06, asset="X")
+    res = put(40.0).price_american(m, dates(t, int(50 * t)), n_paths=1_000_000, seed=42, n_basis=4)
+    crr = orc.crr_american(s0, 40.0, t, 0.06, sigma, 1000, False)
+    # LSM with a finite basis is biased low by a few cents at 50 dates a year
+    assert abs(res.price - crr) < 0.01 * crr + 4 * res.std_error, (res.price, crr)
+    assert res.price > orc.bs_put(s0, 40.0, t, 0.06, sigma)
+
+
+def test_lsm_validation_and_unsupported_payoffs():
+    m = kx.GBM(s0=40.0, sigma=0.2, r=0.06, asset="X")
+    for ds, nb in (([], 3), ([0.5, 0.5], 3), ([0.0, 1.0], 3), ([1.0], 1)):
+        with pytest.raises(kx.KontractError) as e:
+            put(40.0).price_american(m, ds, n_paths=100, n_basis=nb)
+        assert e.value.status == "MalformedContract"
+    with pytest.raises(kx.KontractError) as e:
+        (put(40.0) @ kx.at(1.0)).price_american(m, [0.5, 1.0], n_paths=100)
+    assert e.value.status == "Unsupported"
+
+
+def test_lsm_heston_matches_oracle(orc):
+    h = kx.heston(40.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.06, asset="X")
+    ds = dates(1.0, 12)
+    ref = orc.price_american(put(40.0).to_json(), h, ds, n_paths=30_000, seed=5, n_basis=3)
+    res = put(40.0).price_american(h, ds, n_paths=30_000, seed=5, n_basis=3, precision="fp64")
+    assert abs(res.price - ref.price) < 1e-6 * ref.price
