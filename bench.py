@@ -162,6 +162,52 @@ def run_reference(args, ws, rank) -> None:
     print(json.dumps(line), flush=True)
 
 
+def price_greeks(c, m, n_paths, seed, spy) -> dict:
+    """Price + delta/vega/rho of the workload: the pathwise adjoint (one reverse
+    sweep per path, checkpoints every 16 steps, logistic barrier of the
+    default width) against GPU CRN bump-and-reprice of the same smoothed
+    payoff (seven scenarios sharing each path's normals, h = 1e-3 relative).
+    Equal standard error: the bump cost is scaled by the worst
+    (SE_bump / SE_adjoint)^2 over the three Greeks (MC time ~ paths ~ SE^-2)."""
+    import kontracts_gb300 as kx
+
+    def timed(fn, reps=3):
+        best = None
+        for _ in range(reps):
+            out = fn()
+            st = kx.last_launch_stats()
+            t = (st["kernel_ms"] + st["reduce_ms"]) * 1e-3
+            best = t if best is None or t < best else best
+        return out, best
+
+    adj, t_adj = timed(lambda: c.adjoint(m, n_paths=n_paths, seed=seed, steps_per_year=spy, checkpoint_every=16))
+    w = adj.smoothing_width
+    bump, t_bump = timed(lambda: c.greeks(m, n_paths=n_paths, seed=seed, steps_per_year=spy,
+                                          bumps=(1e-3, 1e-3, 1e-3), relative=True, smooth_width=w))
+    raw, t_raw = timed(lambda: c.greeks(m, n_paths=n_paths, seed=seed, steps_per_year=spy,
+                                        bumps=(1e-3, 1e-3, 1e-3), relative=True), reps=1)
+    pairs = {"delta": (adj.d_s0, adj.se_s0, bump.delta, bump.delta_se, raw.delta, raw.delta_se),
+             "vega": (adj.d_sigma, adj.se_sigma, bump.vega, bump.vega_se, raw.vega, raw.vega_se),
+             "rho": (adj.d_r, adj.se_r, bump.rho, bump.rho_se, raw.rho, raw.rho_se)}
+    se_scale = max((b_se / a_se) ** 2 for (_, a_se, _, b_se, _, _) in pairs.values())
+    se_scale_raw = max((r_se / a_se) ** 2 for (_, a_se, _, _, _, r_se) in pairs.values())
+    return {
+        "workload": "same contract/model/paths as value; FP32 paths",
+        "smoothing_width_logspot": w,
+        "adjoint": {"seconds": t_adj, "price_greeks_per_s": 1.0 / t_adj, "price": adj.price,
+                    **{k: v[0] for k, v in pairs.items()}, **{k + "_se": v[1] for k, v in pairs.items()}},
+        "bump_smoothed": {"seconds": t_bump, "price_greeks_per_s": 1.0 / t_bump, "price": bump.price,
+                          **{k: v[2] for k, v in pairs.items()}, **{k + "_se": v[3] for k, v in pairs.items()}},
+        "bump_raw_payoff": {"seconds": t_raw, **{k: v[4] for k, v in pairs.items()},
+                            **{k + "_se": v[5] for k, v in pairs.items()}},
+        "rel_diff_adjoint_vs_bump": {k: abs(v[0] - v[2]) / max(abs(v[2]), 1e-12) for k, v in pairs.items()},
+        "equal_se_speedup_vs_bump_smoothed": t_bump * se_scale / t_adj,
+        "equal_se_speedup_vs_bump_raw": t_raw * se_scale_raw / t_adj,
+        "price_greeks_per_s_equal_se": {"adjoint": 1.0 / t_adj, "bump_smoothed": 1.0 / (t_bump * se_scale),
+                                        "bump_raw_payoff": 1.0 / (t_raw * se_scale_raw)},
+    }
+
+
 def run_ours(args, ws, rank, local) -> None:
     import torch
 
@@ -241,6 +287,7 @@ def run_ours(args, ws, rank, local) -> None:
                 "steps_simulated_fraction": sim_steps / (nominal * args.steps),
                 "measured_peaks_gops": {k: v / 1e9 for k, v in peaks.items()},
                 "issue_view_paths_steps_per_s_simulated": sim_steps / (ker_ms * 1e-3)}
+    greeks = None if args.no_greeks else price_greeks(c, m, n_paths, seed, w["steps_per_year"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -250,6 +297,8 @@ def run_ours(args, ws, rank, local) -> None:
         "price": results[-1].price, "std_error": results[-1].std_error,
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
     }
+    if greeks is not None:
+        line["price_greeks"] = greeks
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:
@@ -266,6 +315,7 @@ def main() -> None:
     ap.add_argument("--ref-paths", type=int, default=400_000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-greeks", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -231,6 +231,26 @@ class Greeks:
                 f"vega={self.vega:.6f}, rho={self.rho:.6f})")
 
 
+class Sensitivities:
+    """Pathwise-adjoint price and sensitivities (kx_sens): d_s0, d_sigma, d_r
+    for GBM; d_s0, d_v0, d_kappa, d_theta, d_sigma_v, d_rho, d_r for Heston;
+    each with its standard error (se_*)."""
+
+    __slots__ = tuple(n for n, _ in _abi.KxSens._fields_)
+
+    def __init__(self, s: _abi.KxSens):
+        for k in self.__slots__:
+            setattr(self, k, getattr(s, k))
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k in self.__slots__}
+
+    def __repr__(self):
+        return (f"Sensitivities(price={self.price:.6f}, d_s0={self.d_s0:.6f}, d_sigma={self.d_sigma:.6f}, "
+                f"d_r={self.d_r:.6f}, d_v0={self.d_v0:.6f}, d_kappa={self.d_kappa:.6f}, "
+                f"d_theta={self.d_theta:.6f}, d_sigma_v={self.d_sigma_v:.6f}, d_rho={self.d_rho:.6f})")
+
+
 class GBM:
     """GBM(s0, sigma, r, q=0.0, asset="ASSET"): drift r - q, discount r
     (src/bindings.rs:478-522)."""
@@ -406,6 +426,23 @@ class Contract:
             _check(_lib().kx_greeks_bump(self._handle().h, C.byref(cm), C.byref(cfg), C.byref(b), C.byref(out)))
         return Greeks(out)
 
+    def adjoint(self, model, n_paths: int = 200_000, seed: int = 42, steps_per_year: int = 50, *,
+                checkpoint_every: int = 16, smoothing_width: float = 0.0, precision: str = "fp32",
+                shared_draws: bool = False) -> Sensitivities:
+        """Pathwise-adjoint sensitivities in one reverse sweep per path
+        (kx_greeks_adjoint). Barrier untils are smoothed by a logistic of
+        `smoothing_width` in log-spot (<= 0: 0.5 sigma sqrt(dt))."""
+        if not isinstance(model, (GBM, Model)):
+            raise TypeError("expected a GBM or Model")
+        cm = model._c()
+        cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, shared_draws)
+        ac = _abi.KxAdjointCfg(checkpoint_every=int(checkpoint_every), reserved=0,
+                               smoothing_width=float(smoothing_width))
+        out = _abi.KxSens()
+        with _lock:
+            _check(_lib().kx_greeks_adjoint(self._handle().h, C.byref(cm), C.byref(cfg), C.byref(ac), C.byref(out)))
+        return Sensitivities(out)
+
     def price_american(self, model, exercise_dates: Sequence[float], n_paths: int = 100_000, seed: int = 42,
                        n_basis: int = 3, *, precision: str = "fp32", shared_draws: bool = False) -> PriceResult:
         """Longstaff-Schwartz American pricing (lsm.rs:80-124); `self` is the
@@ -546,7 +583,7 @@ def down_and_out_call(asset: str, k: float, barrier: float, t: float, ccy: str =
 
 __all__ = [
     "__version__", "KontractError", "Observable", "Condition", "Contract", "GBM", "Model", "PriceResult",
-    "Greeks", "zero", "one", "give", "S", "spot", "const_", "at", "bool_", "scale", "when", "anytime",
+    "Greeks", "Sensitivities", "zero", "one", "give", "S", "spot", "const_", "at", "bool_", "scale", "when", "anytime",
     "until", "and_", "or_", "USD", "EUR", "GBP", "JPY", "average", "average_over", "running_max",
     "running_min", "heston", "zero_coupon_bond", "european_call", "european_put", "forward", "straddle",
     "bull_call_spread", "cash_or_nothing_call", "up_and_out_call", "down_and_out_call", "price_batch",

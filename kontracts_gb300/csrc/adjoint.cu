@@ -1,7 +1,573 @@
-// adjoint.cu — pathwise adjoint Greeks (placeholder until the kernels land).
+// adjoint.cu — pathwise adjoint Greeks with a reverse sweep per path.
+//
+// No reference counterpart: the reference only bumps and reprices
+// (greeks.rs:60-98). Supported contracts are those whose payoff is a smooth
+// (or smoothed) function of the path:
+//   * when/anytime conditions depend on time only, so every flow date and every
+//     until arming date is path-independent (the host computes that schedule);
+//   * until(Spot cmp Const) barriers are replaced by a logistic survival weight
+//     prod_k sigma(-+(y_k - b) / w) over the steps the until is armed, of a
+//     stated width w in log-spot; time-only untils knock out deterministically;
+//   * flow amounts are expressions of the spot, constants, arithmetic, max/min
+//     and Average / RunningMax / RunningMin of the spot.
+//
+// Per path: a forward pass simulates the path (the same Philox counters as the
+// pricing kernel), evaluates the smoothed payoff with forward-mode derivatives
+// of each amount with respect to its inputs, and stores the state (y, v) every
+// `K` steps. The reverse sweep then walks the segments backwards: each segment
+// is recomputed from its checkpoint (regenerating its normals from Philox),
+// and the adjoints lambda = dPV/dlog S, mu = dPV/dv are propagated through
+// every step, accumulating the parameter sensitivities. Memory per path is
+// (N / K + 1) states plus one K-step segment.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "device_common.cuh"
 #include "engine.hpp"
+
+namespace kx {
+
+constexpr int ADJ_BLOCK = 128;
+constexpr int ADJ_MAXF = 4;    // flows
+constexpr int ADJ_MAXU = 2;    // smoothed untils
+constexpr int ADJ_MAXA = 2;    // accumulators
+constexpr int ADJ_MAXCK = 72;  // checkpoints
+constexpr int ADJ_KMAX = 32;   // checkpoint interval
+constexpr int ADJ_OUT = 8;     // per-path outputs
+
+struct AdjFlow {
+    int t;             // step the flow is paid at
+    int kind;          // KxAmountKind
+    int code_off, code_len;
+    double sign;
+    uint32_t su_mask;  // smoothed untils above the flow
+};
+struct AdjUntil {
+    int arm;           // first step it weighs
+    int cmp;           // KxCmp
+    double thr;        // log(B / s0)
+};
+struct AdjAcc {
+    int kind;          // KxAccKind
+    int i_from, i_to;  // window (i_to: INT_MAX for running)
+};
+
+struct AdjArgs {
+    const KxProgram *P;   // for the amount programs
+    const void *steps;    // StepRec<Real>: GBM c0 = dt, c1 = sqrt(dt); Heston the same
+    const double *disc;   // exp(-rate t_k)
+    const double *times;  // t_k
+    int n_times;
+    int n_flows, n_su, n_acc;
+    AdjFlow flow[ADJ_MAXF];
+    AdjUntil su[ADJ_MAXU];
+    AdjAcc acc[ADJ_MAXA];
+    int K;                // checkpoint interval (multiple of 4)
+    int model, scheme;
+    uint64_t n_paths, seed;
+    double s0, mu, sigma;                         // GBM (mu = drift)
+    double v0, kappa, theta, sigma_v, rho, rho_perp, r;
+    double inv_w;
+    const double *z64;
+    const float *z32;
+    uint64_t z_dpp;
+    double *out;          // [ADJ_OUT][n_paths]
+};
+
+// Forward-mode value of an amount program with derivatives with respect to
+// the spot (index 0) and each accumulator (index 1 + a).
+template <class Real>
+struct Dual {
+    Real v, d[1 + ADJ_MAXA];
+};
+
+template <class Real>
+__device__ Dual<Real> eval_dual(const KxProgram &P, int off, int len, Real S, const Real *accv) {
+    Dual<Real> st[KX_MAX_STACK];
+    int sp = 0;
+    for (int pc = off; pc < off + len; ++pc) {
+        const KxIns ins = P.code[pc];
+        Dual<Real> r;
+#pragma unroll
+        for (int q = 0; q < 1 + ADJ_MAXA; ++q) r.d[q] = Real(0);
+        switch (ins.op) {
+        case OP_CONST: r.v = (Real)P.cpool[ins.arg]; st[sp++] = r; continue;
+        case OP_SPOT: r.v = S; r.d[0] = Real(1); st[sp++] = r; continue;
+        case OP_ACC: r.v = accv[ins.arg]; r.d[1 + ins.arg] = Real(1); st[sp++] = r; continue;
+        case OP_NEG:
+            st[sp - 1].v = -st[sp - 1].v;
+#pragma unroll
+            for (int q = 0; q < 1 + ADJ_MAXA; ++q) st[sp - 1].d[q] = -st[sp - 1].d[q];
+            continue;
+        default: break;
+        }
+        --sp;
+        const Dual<Real> a = st[sp - 1], b = st[sp];
+        switch (ins.op) {
+        case OP_ADD: r.v = a.v + b.v; for (int q = 0; q < 1 + ADJ_MAXA; ++q) r.d[q] = a.d[q] + b.d[q]; break;
+        case OP_SUB: r.v = a.v - b.v; for (int q = 0; q < 1 + ADJ_MAXA; ++q) r.d[q] = a.d[q] - b.d[q]; break;
+        case OP_MUL: r.v = a.v * b.v; for (int q = 0; q < 1 + ADJ_MAXA; ++q) r.d[q] = a.d[q] * b.v + a.v * b.d[q]; break;
+        case OP_DIV: {
+            r.v = a.v / b.v;
+            for (int q = 0; q < 1 + ADJ_MAXA; ++q) r.d[q] = (a.d[q] - r.v * b.d[q]) / b.v;
+            break;
+        }
+        case OP_MAX: r = (a.v >= b.v || b.v != b.v) ? a : b; break;  // fmax: NaN-ignoring, ties keep a
+        case OP_MIN: r = (a.v <= b.v || b.v != b.v) ? a : b; break;
+        default: r.v = Real(0); break;
+        }
+        st[sp - 1] = r;
+    }
+    return st[0];
+}
+
+template <class Real>
+__device__ __forceinline__ void draws4(const AdjArgs &A, uint64_t path, uint64_t d, Real z[4]) {
+    if (A.z64 == nullptr && A.z32 == nullptr) {
+        const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
+                                      (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+        box_muller(w.x, w.y, z[0], z[1]);
+        box_muller(w.z, w.w, z[2], z[3]);
+    } else {
+        for (int j = 0; j < 4; ++j) {
+            const uint64_t q = d + j;
+            z[j] = q < A.z_dpp ? (A.z64 ? (Real)A.z64[path * A.z_dpp + q] : (Real)A.z32[path * A.z_dpp + q]) : Real(0);
+        }
+    }
+}
+
+// One model step k (from k-1), returning the new (y, v) and the draws used.
+template <class Real, int MODEL>
+__device__ __forceinline__ void model_step(const AdjArgs &A, const StepRec<Real> &rec, Real z1, Real z2, Real &y,
+                                           Real &v) {
+    if (MODEL == KX_MODEL_GBM) {
+        const Real dt = rec.c0, sq = rec.c1;
+        y += ((Real)A.mu - Real(0.5) * (Real)A.sigma * (Real)A.sigma) * dt + (Real)A.sigma * sq * z1;
+    } else {
+        heston_step<Real>((Real)A.r, (Real)A.kappa, (Real)A.theta, (Real)A.sigma_v, (Real)A.rho, (Real)A.rho_perp,
+                          A.scheme, rec.c0, rec.c1, z1, z2, y, v);
+    }
+}
+
+template <class Real, int MODEL>
+__global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
+    constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
+    const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+    const KxProgram &P = *A.P;
+    const int N = A.n_times - 1;  // steps
+    const int K = A.K;
+    const Real s0 = (Real)A.s0;
+    const Real inv_w = (Real)A.inv_w;
+    for (uint64_t path = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; path < A.n_paths;
+         path += (uint64_t)gridDim.x * blockDim.x) {
+        // ------------------------------ forward ------------------------------
+        Real ck_y[ADJ_MAXCK], ck_v[ADJ_MAXCK];
+        Real y = Real(0), v = (Real)fmax(A.v0, 0.0);
+        Real accv[ADJ_MAXA], accraw[ADJ_MAXA];
+        int argx[ADJ_MAXA];
+        for (int a = 0; a < ADJ_MAXA; ++a) {
+            accraw[a] = a < A.n_acc ? (A.acc[a].kind == ACC_MAX ? Real(-INFINITY) : A.acc[a].kind == ACC_MIN ? Real(INFINITY) : Real(0)) : Real(0);
+            argx[a] = 0;
+            accv[a] = Real(0);
+        }
+        Real surv[ADJ_MAXU];
+        for (int u = 0; u < ADJ_MAXU; ++u) surv[u] = Real(1);
+        // flow records
+        double fP[ADJ_MAXF];
+        Real fcs[ADJ_MAXF], fca[ADJ_MAXF][ADJ_MAXA];
+        int farg[ADJ_MAXF][ADJ_MAXA];
+        double pv = 0.0, pv_t = 0.0;  // price and sum_f t_f P_f
+        Real z[4];
+        for (int k = 0; k <= N; ++k) {
+            if (k > 0) {
+                const uint64_t d = (uint64_t)(k - 1) * DRAWS;
+                if ((d & 3u) == 0) draws4<Real>(A, path, d, z);
+                const int q = (int)(d & 3u);
+                model_step<Real, MODEL>(A, R[k], z[q], DRAWS == 2 ? z[q + 1] : Real(0), y, v);
+            }
+            if (k % K == 0) {
+                ck_y[k / K] = y;
+                ck_v[k / K] = v;
+            }
+            const Real S = s0 * fast_exp<Real>(y);
+            for (int a = 0; a < A.n_acc; ++a) {
+                const AdjAcc &Ac = A.acc[a];
+                if (k < Ac.i_from || k > Ac.i_to) continue;
+                if (Ac.kind == ACC_MAX) { if (S > accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                else if (Ac.kind == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                else accraw[a] += S;
+            }
+            for (int u = 0; u < A.n_su; ++u)
+                if (k >= A.su[u].arm) {
+                    Real x = (y - (Real)A.su[u].thr) * inv_w;
+                    if (A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT) x = -x;
+                    surv[u] *= Real(1) / (Real(1) + fast_exp<Real>(x));
+                }
+            for (int f = 0; f < A.n_flows; ++f) {
+                const AdjFlow &F = A.flow[f];
+                if (F.t != k) continue;
+                for (int a = 0; a < A.n_acc; ++a)
+                    accv[a] = A.acc[a].kind == ACC_SUM ? accraw[a] / (Real)(min(k, A.acc[a].i_to) - A.acc[a].i_from + 1)
+                                                       : accraw[a];
+                Dual<Real> amt;
+                if (F.kind == AK_CONST) {
+                    amt.v = (Real)F.sign;
+                    for (int q = 0; q < 1 + ADJ_MAXA; ++q) amt.d[q] = Real(0);
+                } else {
+                    amt = eval_dual<Real>(P, F.code_off, F.code_len, S, accv);
+                }
+                Real w = Real(1);
+                for (int u = 0; u < A.n_su; ++u)
+                    if ((F.su_mask >> u) & 1u) w *= surv[u];
+                const double df = A.disc[k];
+                fP[f] = (double)amt.v * (double)w * df;
+                fcs[f] = (Real)((double)(amt.d[0] * w) * df);
+                for (int a = 0; a < ADJ_MAXA; ++a) {
+                    Real c = (Real)((double)(amt.d[1 + a] * w) * df);
+                    if (a < A.n_acc && A.acc[a].kind == ACC_SUM)
+                        c /= (Real)(min(k, A.acc[a].i_to) - A.acc[a].i_from + 1);
+                    fca[f][a] = c;
+                    farg[f][a] = argx[a];
+                }
+                pv += fP[f];
+                pv_t += A.times[k] * fP[f];
+            }
+        }
+        // ------------------------------ reverse ------------------------------
+        Real sy[ADJ_KMAX + 1], sv[ADJ_KMAX + 1], sz1[ADJ_KMAX + 1], sz2[ADJ_KMAX + 1];
+        Real lam = Real(0), mu = Real(0);  // dPV/dy_{k+1}, dPV/dv_{k+1}
+        Real Q[ADJ_MAXU] = {};             // sum of P_f (t_f >= k) under each smoothed until
+        Real G[ADJ_MAXA] = {};             // per average: sum of coefficients whose window holds k
+        Real g_sig = 0, g_r = 0, g_k = 0, g_th = 0, g_sv = 0, g_rho = 0;
+        const int nseg = (N + K - 1) / K;
+        for (int c = nseg - 1; c >= 0; --c) {
+            const int k0 = c * K;
+            const int k1 = min(k0 + K, N);
+            // recompute states k0..k1 and the draws of steps k0+1..k1
+            Real yy = ck_y[c], vv = ck_v[c];
+            sy[0] = yy;
+            sv[0] = vv;
+            for (int k = k0 + 1; k <= k1; ++k) {
+                const uint64_t d = (uint64_t)(k - 1) * DRAWS;
+                if ((d & 3u) == 0 || k == k0 + 1) draws4<Real>(A, path, d & ~3ull, z);
+                const int q = (int)(d & 3u);
+                const Real a1 = z[q], a2 = DRAWS == 2 ? z[q + 1] : Real(0);
+                model_step<Real, MODEL>(A, R[k], a1, a2, yy, vv);
+                sy[k - k0] = yy;
+                sv[k - k0] = vv;
+                sz1[k - k0] = a1;
+                sz2[k - k0] = a2;
+            }
+            const int ktop = (c == nseg - 1) ? k1 : k1 - 1;
+            for (int k = ktop; k >= k0; --k) {
+                const int j = k - k0;
+                if (k < N) {
+                    // adjoint of step k -> k+1 (state k, draws of step k+1)
+                    const StepRec<Real> rec = R[k + 1];
+                    const Real dt = rec.c0, sq = rec.c1;
+                    const Real z1 = sz1[j + 1], z2 = sz2[j + 1];
+                    if (MODEL == KX_MODEL_GBM) {
+                        g_sig += lam * (-(Real)A.sigma * dt + sq * z1);
+                        g_r += lam * dt;
+                    } else {
+                        const Real vk = sv[j];
+                        const bool ft = A.scheme == KX_HESTON_FULL_TRUNCATION;
+                        const Real vp = ft ? fmax(vk, Real(0)) : vk;
+                        const Real dvp = (ft && vk <= Real(0)) ? Real(0) : Real(1);
+                        const Real sqv = sqrt(vp);
+                        const Real dsq = sqv > Real(0) ? Real(0.5) / sqv : Real(0);  // d sqrt(v)/dv, 0 at v = 0
+                        const Real mix = (Real)A.rho * z1 + (Real)A.rho_perp * z2;
+                        // v_{k+1} before the floor; the floor passes the adjoint only where it did not bite
+                        const Real vn = vk + (Real)A.kappa * ((Real)A.theta - vp) * dt + (Real)A.sigma_v * sqv * mix * sq;
+                        const Real m = (ft || vn > Real(0)) ? mu : Real(0);
+                        const Real dx_dv = (Real(-0.5) * dt + z1 * sq * dsq) * dvp;
+                        const Real dvn_dv = Real(1) + (-(Real)A.kappa * dt + (Real)A.sigma_v * mix * sq * dsq) * dvp;
+                        g_r += lam * dt;
+                        g_k += m * ((Real)A.theta - vp) * dt;
+                        g_th += m * (Real)A.kappa * dt;
+                        g_sv += m * sqv * mix * sq;
+                        const Real drp = A.rho_perp > 0 ? (Real)(-A.rho / A.rho_perp) : Real(0);
+                        g_rho += m * (Real)A.sigma_v * sqv * (z1 + drp * z2) * sq;
+                        mu = lam * dx_dv + m * dvn_dv;
+                    }
+                }
+                // direct contributions at state k
+                const Real yk = sy[j];
+                const Real Sk = s0 * fast_exp<Real>(yk);
+                Real g = Real(0);
+                for (int f = 0; f < A.n_flows; ++f) {
+                    // an average read at t_f covers [i_from, min(t_f, i_to)]: its coefficient
+                    // joins when the sweep reaches the window's last step
+                    for (int a = 0; a < A.n_acc; ++a)
+                        if (A.acc[a].kind == ACC_SUM && k == min(A.flow[f].t, A.acc[a].i_to)) G[a] += fca[f][a];
+                    if (A.flow[f].t != k) continue;
+                    g += fcs[f] * Sk;
+                    for (int u = 0; u < A.n_su; ++u)
+                        if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
+                }
+                for (int f = 0; f < A.n_flows; ++f)  // running max/min: at the arg-extremum
+                    if (A.flow[f].t >= k)
+                        for (int a = 0; a < A.n_acc; ++a)
+                            if (A.acc[a].kind != ACC_SUM && farg[f][a] == k) g += fca[f][a] * Sk;
+                for (int a = 0; a < A.n_acc; ++a)  // averages: inside the window
+                    if (A.acc[a].kind == ACC_SUM && k >= A.acc[a].i_from) g += G[a] * Sk;
+                for (int u = 0; u < A.n_su; ++u)
+                    if (k >= A.su[u].arm && Q[u] != Real(0)) {
+                        Real x = (yk - (Real)A.su[u].thr) * inv_w;
+                        const bool down = A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT;
+                        if (down) x = -x;
+                        const Real s = Real(1) / (Real(1) + fast_exp<Real>(x));
+                        const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy|
+                        g += Q[u] * (down ? dls : -dls);
+                    }
+                // leaving an average window when walking below its first step
+                for (int a = 0; a < A.n_acc; ++a)
+                    if (A.acc[a].kind == ACC_SUM && k == A.acc[a].i_from) G[a] = Real(0);
+                lam += g;
+            }
+        }
+        double *o = A.out;
+        const uint64_t n = A.n_paths;
+        o[0 * n + path] = pv;
+        o[1 * n + path] = (double)lam / A.s0;                  // d/ds0
+        if (MODEL == KX_MODEL_GBM) {
+            o[2 * n + path] = (double)g_sig;                    // d/dsigma
+            o[3 * n + path] = (double)g_r - pv_t;               // d/dr: drift and discount
+        } else {
+            o[2 * n + path] = A.v0 > 0 ? (double)mu : 0.0;      // d/dv0
+            o[3 * n + path] = (double)g_r - pv_t;               // d/dr
+            o[4 * n + path] = (double)g_k;                      // d/dkappa
+            o[5 * n + path] = (double)g_th;                     // d/dtheta
+            o[6 * n + path] = (double)g_sv;                     // d/dsigma_v
+            o[7 * n + path] = (double)g_rho;                    // d/drho
+        }
+    }
+}
+
+// Static schedule of a supported contract on a grid (host).
+static void schedule(const Lowered &low, const KxProgram &P, const StepTables &tab, const Model &m, AdjArgs &a) {
+    const int n = P.n_times;
+    const int NEVER = INT_MAX;
+    // the slot whose firing arms slot i (-1: armed at step 0)
+    std::vector<int> parent(P.n_trig, -1);
+    for (int i = 0; i < P.n_trig; ++i)
+        for (int j = 0; j < P.n_trig; ++j)
+            if ((P.trig[i].fire_arm >> j) & 1u) parent[j] = i;
+    std::vector<int> arm(P.n_trig, NEVER), fire(P.n_trig, NEVER);
+    auto first_from = [&](int i, int from) {
+        for (int k = std::max(from, 0); k < n; ++k)
+            if ((tab.time_true[k] >> i) & 1u) return k;
+        return NEVER;
+    };
+    for (int i = 0; i < P.n_trig; ++i) {  // slots are numbered parents first
+        const KxTrig &T = P.trig[i];
+        arm[i] = parent[i] < 0 ? 0 : fire[parent[i]];
+        if (T.kind == TK_WHEN) {
+            if (T.cond_kind != CK_TIME)
+                raise(KX_UNSUPPORTED, "adjoint: when/anytime conditions must depend on time only");
+            fire[i] = arm[i] == NEVER ? NEVER : first_from(i, arm[i]);
+        } else {
+            if (T.cond_kind == CK_TIME) fire[i] = arm[i] == NEVER ? NEVER : first_from(i, arm[i]);  // knock step
+            else if (T.cond_kind != CK_SPOT_CMP)
+                raise(KX_UNSUPPORTED, "adjoint: until conditions must be Spot vs Const or time only");
+        }
+    }
+    for (int a2 = 0; a2 < P.n_acc; ++a2)
+        if (P.acc[a2].inner != IK_SPOT) raise(KX_UNSUPPORTED, "adjoint: averages / running extrema must be of the spot");
+    if (P.n_acc > ADJ_MAXA) raise(KX_UNSUPPORTED, "adjoint: at most 2 averages / running extrema");
+    a.n_acc = P.n_acc;
+    for (int q = 0; q < P.n_acc; ++q) {
+        a.acc[q].kind = P.acc[q].kind;
+        a.acc[q].i_from = P.acc[q].i_from;
+        a.acc[q].i_to = P.acc[q].i_to;
+        if (P.acc[q].kind == ACC_SUM && P.acc[q].static_err) raise(KX_MALFORMED_CONTRACT, "empty average window");
+    }
+    // smoothed untils
+    std::vector<int> su_index(P.n_trig, -1);
+    a.n_su = 0;
+    for (int i = 0; i < P.n_trig; ++i) {
+        const KxTrig &T = P.trig[i];
+        if (T.kind != TK_UNTIL || T.cond_kind != CK_SPOT_CMP || arm[i] == NEVER) continue;
+        if (a.n_su >= ADJ_MAXU) raise(KX_UNSUPPORTED, "adjoint: at most 2 barrier untils");
+        su_index[i] = a.n_su;
+        AdjUntil &U = a.su[a.n_su++];
+        U.arm = arm[i];
+        U.cmp = T.cmp;
+        U.thr = std::log(low.spot_cmp[T.spot_slot].c / m.s0);
+    }
+    // live flows
+    a.n_flows = 0;
+    for (int j = 0; j < P.n_leaf; ++j) {
+        int acq = -1;
+        for (int i = 0; i < P.n_trig; ++i)
+            if (P.trig[i].kind == TK_WHEN && ((P.trig[i].leaves >> j) & 1u)) acq = i;
+        const int t = acq < 0 ? 0 : fire[acq];
+        if (t == NEVER) continue;
+        bool dead = false;
+        uint32_t mask = 0;
+        for (int i = 0; i < P.n_trig; ++i) {
+            const KxTrig &T = P.trig[i];
+            if (T.kind != TK_UNTIL || !((T.leaves >> j) & 1u)) continue;
+            if (T.cond_kind == CK_TIME && fire[i] <= t) dead = true;  // knocked at or before the flow
+            if (su_index[i] >= 0) mask |= 1u << su_index[i];
+        }
+        if (dead) continue;
+        if (a.n_flows >= ADJ_MAXF) raise(KX_UNSUPPORTED, "adjoint: at most 4 flows");
+        const KxLeaf &F = P.leaf[j];
+        for (int c = F.code_off; c < F.code_off + F.code_len; ++c) {
+            const uint8_t op = P.code[c].op;
+            if (op == OP_ACC && P.acc[P.code[c].arg].kind == ACC_SUM) {
+                const KxAcc &Ac = P.acc[P.code[c].arg];
+                if (Ac.fixed && Ac.i_to > t) raise(KX_UNSUPPORTED, "adjoint: average window ends after the flow date");
+                if (!Ac.fixed && t < Ac.e_min) raise(KX_MALFORMED_CONTRACT, "average window inverted at the flow date");
+            }
+        }
+        AdjFlow &fl = a.flow[a.n_flows++];
+        fl.t = t;
+        fl.kind = F.kind;
+        fl.code_off = F.code_off;
+        fl.code_len = F.code_len;
+        fl.sign = F.sign;
+        fl.su_mask = mask;
+    }
+}
+
+template <class Real, int MODEL>
+static const void *adj_kernel() {
+    return reinterpret_cast<const void *>(&k_adjoint<Real, MODEL>);
+}
+
+}  // namespace kx
+
 using namespace kx;
-extern "C" kx_status kx_greeks_adjoint(const kx_program *, const kx_model *, const kx_mc_config *,
-                                       const kx_adjoint_cfg *, kx_sens *) {
-    return guarded([&] { raise(KX_UNSUPPORTED, "adjoint not built yet"); });
+
+extern "C" kx_status kx_greeks_adjoint(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                                       const kx_adjoint_cfg *acfg, kx_sens *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        if (!cfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (cfg->flags != 0 || (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) ||
+            (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64))
+            raise(KX_INVALID_ARGUMENT, "bad config");
+        if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
+        validate_model(m);
+        if (!(m.s0 > 0.0)) raise(KX_UNSUPPORTED, "adjoint: s0 must be positive");
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, m.requires_fine_grid());
+        validate_grid(grid);
+        const int n = (int)grid.size();
+        const int N = n - 1;
+        KxProgram P;
+        StepTables tab;
+        bind(p.low, grid, m, cfg->rate, P, tab);
+        AdjArgs a{};
+        schedule(p.low, P, tab, m, a);
+        uint32_t K = acfg && acfg->checkpoint_every ? acfg->checkpoint_every : 16u;
+        K = (K + 3) / 4 * 4;
+        if (K > (uint32_t)ADJ_KMAX) K = ADJ_KMAX;
+        while ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK && K < (uint32_t)ADJ_KMAX) K += 4;
+        if ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK) raise(KX_UNSUPPORTED, "adjoint: grid too long for the checkpoint store");
+        a.K = (int)K;
+        // smoothing width: default 0.5 * sigma_eff * sqrt(mean dt)
+        double w = acfg ? acfg->smoothing_width : 0.0;
+        const double dtm = N > 0 ? grid.back() / N : 1.0;
+        if (!(w > 0.0)) {
+            const double se = m.kind == KX_MODEL_GBM ? m.sigma : std::sqrt(std::max(m.v0, m.theta));
+            w = 0.5 * std::max(se, 1e-8) * std::sqrt(dtm);
+        }
+        a.inv_w = 1.0 / w;
+        a.n_times = n;
+        a.model = m.kind;
+        a.scheme = m.scheme;
+        a.n_paths = cfg->n_paths;
+        a.seed = cfg->seed;
+        a.s0 = m.s0;
+        a.mu = m.kind == KX_MODEL_GBM ? m.mu : m.r;
+        a.sigma = m.sigma;
+        a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
+        a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
+        a.r = m.r;
+        const bool f64 = cfg->precision == KX_PREC_FP64;
+        std::vector<unsigned char> steps(n * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+        for (int k = 0; k < n; ++k) {
+            const double dt = k == 0 ? 0.0 : grid[k] - grid[k - 1];
+            if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {dt, std::sqrt(dt), 0u, 0u};
+            else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)dt, (float)std::sqrt(dt), 0u, 0u};
+        }
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        memset(&c.last, 0, sizeof c.last);
+        c.last.total_ms = -now_ms();
+        const uint64_t np = cfg->n_paths;
+        c.progs.ensure(sizeof(KxProgram));
+        c.steps.ensure(steps.size());
+        c.disc.ensure(2 * n * sizeof(double));
+        c.pv.ensure(std::max<uint64_t>(1, np) * ADJ_OUT * sizeof(double));
+        KX_CUDA(cudaMemcpyAsync(c.progs.p, &P, sizeof P, cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.disc.p, tab.disc.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.disc.as<double>() + n, grid.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np) * ADJ_OUT * sizeof(double), c.stream));
+        c.last.h2d_bytes += sizeof P + steps.size() + 2 * n * sizeof(double);
+        a.P = c.progs.as<KxProgram>();
+        a.steps = c.steps.p;
+        a.disc = c.disc.as<double>();
+        a.times = c.disc.as<double>() + n;
+        a.out = c.pv.as<double>();
+        if (cfg->rng == KX_RNG_SHARED_DRAWS) {
+            DrawStore &ds = c.draws;
+            if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
+            if (ds.n_paths < np || ds.dpp < (uint64_t)N * m.draws_per_step())
+                raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
+            a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
+            a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
+            a.z_dpp = ds.dpp;
+        }
+        const void *kfn = m.kind == KX_MODEL_GBM ? (f64 ? adj_kernel<double, KX_MODEL_GBM>() : adj_kernel<float, KX_MODEL_GBM>())
+                                                 : (f64 ? adj_kernel<double, KX_MODEL_HESTON>() : adj_kernel<float, KX_MODEL_HESTON>());
+        if (np > 0) {
+            const int full = persistent_blocks(kfn, ADJ_BLOCK, 0);
+            const int blocks = (int)std::min<uint64_t>((uint64_t)full, (np + ADJ_BLOCK - 1) / ADJ_BLOCK);
+            void *args[] = {&a};
+            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+            KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(ADJ_BLOCK), args, 0, c.stream));
+            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+            KX_CUDA(cudaEventSynchronize(c.ev1));
+            float ms = 0.f;
+            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+            c.last.kernel_ms += ms;
+            c.last.kernel_launches++;
+            c.last.grid_blocks = (uint32_t)blocks;
+            c.last.block_threads = ADJ_BLOCK;
+        }
+        c.last.path_steps += np * (uint64_t)N;
+        c.last.steps_simulated += np * (uint64_t)N * 2;  // forward + recompute
+        std::vector<StatsJob> sj(ADJ_OUT);
+        for (int q = 0; q < ADJ_OUT; ++q) {
+            sj[q].begin = (uint64_t)q * np;
+            sj[q].n = np;
+        }
+        auto st = device_stats(c, c.pv.as<double>(), np, sj);
+        auto R = [&](int q) { return finish(st[q]); };
+        memset(out, 0, sizeof *out);
+        out->price = R(0).price;
+        out->price_se = R(0).std_error;
+        out->d_s0 = R(1).price;
+        out->se_s0 = R(1).std_error;
+        out->smoothing_width = w;
+        if (m.kind == KX_MODEL_GBM) {
+            out->d_sigma = R(2).price; out->se_sigma = R(2).std_error;
+            out->d_r = R(3).price; out->se_r = R(3).std_error;
+        } else {
+            out->d_v0 = R(2).price; out->se_v0 = R(2).std_error;
+            out->d_r = R(3).price; out->se_r = R(3).std_error;
+            out->d_kappa = R(4).price; out->se_kappa = R(4).std_error;
+            out->d_theta = R(5).price; out->se_theta = R(5).std_error;
+            out->d_sigma_v = R(6).price; out->se_sigma_v = R(6).std_error;
+            out->d_rho = R(7).price; out->se_rho = R(7).std_error;
+        }
+        c.last.total_ms += now_ms();
+    });
 }

@@ -129,6 +129,7 @@ struct KxProgram {
     double spot_thr[KX_MAX_TRIG];       // CK_SPOT_CMP: log(Const / s0)
     int32_t first_true[KX_MAX_TRIG];    // CK_TIME: first step whose condition holds (INT32_MAX: never)
     uint32_t mono_mask;                 // CK_TIME slots whose condition stays true once true
+    int32_t init_nte;                   // next time event after step 0 when nothing fires at t = 0
     int32_t n_times;                    // grid points (step 0 is t = 0)
 };
 

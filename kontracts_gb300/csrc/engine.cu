@@ -18,15 +18,16 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 
 #include "device_common.cuh"
 #include "engine.hpp"
+#include "paths_kernel.cuh"
 
 namespace kx {
-
-constexpr int KX_MAX_NS = 7;
-constexpr int KX_BLOCK = 256;
 
 // ---------------------------------------------------------------------------
 // context
@@ -82,501 +83,6 @@ int persistent_blocks(const void *kernel, int block, size_t smem) {
 double now_ms() {
     using namespace std::chrono;
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
-}
-
-// ---------------------------------------------------------------------------
-// device data layout
-// ---------------------------------------------------------------------------
-constexpr int KX_MAX_SPOT = KX_MAX_TRIG;
-
-struct ContractDev {
-    int32_t n_times;
-    int32_t step_off;   // first StepRec of this contract
-    int32_t disc_off;   // first discount factor (scenario s: + s * n_times)
-    int32_t prog;       // index into the program array
-    uint64_t n_paths;
-    uint64_t pv_off;    // first output slot (scenario s: + s * pv_stride)
-    uint64_t seed;
-    uint32_t stream;    // Philox stream id
-    int32_t smooth;     // 1: until(Spot cmp Const) is a logistic survival weight
-    int32_t heston_scheme;
-    int32_t pad;
-    // per-scenario values, in both precisions so the FP32 kernel never converts
-    double s0[KX_MAX_NS], drift[KX_MAX_NS], sigma[KX_MAX_NS];
-    float s0f[KX_MAX_NS], driftf[KX_MAX_NS], sigmaf[KX_MAX_NS];
-    double v0, kappa, theta, sigma_v, rho, rho_perp, r, inv_w;
-    float v0f, kappaf, thetaf, sigma_vf, rhof, rho_perpf, rf, inv_wf;
-};
-
-struct WorkItem {
-    int32_t contract;
-    int32_t pad;
-    uint64_t first;
-    uint64_t count;
-};
-
-struct PathArgs {
-    const KxProgram *progs;
-    const void *steps;
-    const double *disc;
-    const ContractDev *cons;
-    const void *thr;     // Real[contract][KX_MAX_NS][KX_MAX_SPOT] log-spot thresholds
-    const WorkItem *items;
-    uint32_t n_items;
-    uint32_t slots;      // shared-memory slots per thread per scenario
-    uint32_t surv_base;  // first survival slot (after 2 slots per accumulator)
-    uint32_t pad;
-    uint32_t *item_counter;
-    uint32_t *err_word;
-    unsigned long long *steps_done;
-    double *pv;
-    uint64_t pv_stride;
-    const double *z64;   // shared draws (path-major) or null
-    const float *z32;
-    uint64_t z_dpp;
-};
-
-enum { M_GBM = 0, M_HESTON = 1 };
-
-// Per-contract values a warp keeps in registers: only what the per-step hot
-// path reads. Everything else is read from the (L1-resident) program table
-// when something fires.
-template <class Real, int NS>
-struct Hot {
-    const KxProgram *P;
-    const StepRec<Real> *R;
-    uint32_t fast_bit;   // the one Spot-cmp-Const slot checked from registers
-    uint32_t gen_mask;   // price-dependent slots needing the interpreter
-    uint32_t time_mask;
-    uint32_t flags;      // HF_* below
-    int n_times;
-    int n_acc;
-    Real fsign;          // y * fsign  >= / >  fthr[s]
-    Real fthr[NS];
-    Real s0[NS];
-};
-enum : uint32_t { HF_SPOT_EACH = 1, HF_SMOOTH = 2, HF_STRICT = 4, HF_FULLTRUNC = 8 };
-
-template <class Real, int NS>
-struct Lane {
-    Real y[NS];  // log(S / s0) of each scenario
-    Real v[NS];  // Heston variance
-    uint32_t armed[NS], resolved[NS], dead[NS], emitted[NS], poisoned[NS];
-    int nte[NS];  // next step at which a live time-only slot can change
-    double pv[NS];
-    uint32_t err;
-};
-
-template <class Real, int NS>
-__device__ __forceinline__ void load_hot(Hot<Real, NS> &H, const PathArgs &A, int c) {
-    const ContractDev *C = A.cons + c;
-    H.P = A.progs + C->prog;
-    H.R = reinterpret_cast<const StepRec<Real> *>(A.steps) + C->step_off;
-    const Real *thr = reinterpret_cast<const Real *>(A.thr) + (size_t)c * KX_MAX_NS * KX_MAX_SPOT;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) H.s0[s] = pick<Real>(C->s0[s], C->s0f[s]);
-    H.n_times = C->n_times;
-    const KxProgram &P = *H.P;
-    H.n_acc = P.n_acc;
-    H.time_mask = P.time_mask;
-    H.flags = (P.spot_each_step ? HF_SPOT_EACH : 0u) | (C->smooth ? HF_SMOOTH : 0u) |
-              (C->heston_scheme == KX_HESTON_FULL_TRUNCATION ? HF_FULLTRUNC : 0u);
-    H.fast_bit = 0;
-    H.fsign = Real(1);
-#pragma unroll
-    for (int s = 0; s < NS; ++s) H.fthr[s] = Real(0);
-    uint32_t pm = P.price_mask;
-    if (C->smooth) pm &= ~P.until_mask;  // smoothed untils never knock
-    uint32_t gen = pm;
-    while (pm) {
-        const int i = __ffs(pm) - 1;
-        pm &= pm - 1;
-        const KxTrig &T = P.trig[i];
-        if (T.cond_kind == CK_SPOT_CMP) {
-            H.fast_bit = 1u << i;
-            gen &= ~H.fast_bit;
-            if (T.cmp == CMP_GT || T.cmp == CMP_LT) H.flags |= HF_STRICT;
-            H.fsign = (T.cmp == CMP_LE || T.cmp == CMP_LT) ? Real(-1) : Real(1);
-#pragma unroll
-            for (int s = 0; s < NS; ++s) H.fthr[s] = H.fsign * thr[s * KX_MAX_SPOT + T.spot_slot];
-            break;
-        }
-    }
-    H.gen_mask = gen;
-}
-
-template <class Real>
-__device__ __forceinline__ bool cmp_y(uint8_t cmp, Real y, Real thr) {
-    switch (cmp) {
-    case CMP_GE: return y >= thr;
-    case CMP_GT: return y > thr;
-    case CMP_LE: return y <= thr;
-    default: return y < thr;
-    }
-}
-
-// Survival weight of one step under a smoothed until(S cmp B): the breach
-// indicator 1{y cmp b} is replaced by the logistic sigma(+-(y - b) / w).
-template <class Real>
-__device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, Real inv_w) {
-    Real x = (y - thr) * inv_w;  // > 0 beyond the barrier for >=, >
-    if (cmp == CMP_LE || cmp == CMP_LT) x = -x;
-    return Real(1) / (Real(1) + fast_exp<Real>(x));
-}
-
-// Full condition evaluation of the slots in `mask` at step k: time bits from
-// the table, Spot-cmp-Const from the thresholds, anything else through the
-// expression interpreter.
-template <class Real>
-__device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const StepRec<Real> *R, const Real *thr,
-                                                   bool smooth, Real y, Real S, uint32_t poisoned, uint32_t mask, int k,
-                                                   AccView<Real> acc, uint32_t &err) {
-    uint32_t bits = mask & P.time_mask;
-    if (bits) bits &= R[k].tt;
-    uint32_t pm = mask & ~P.time_mask;
-    while (pm) {
-        const int i = __ffs(pm) - 1;
-        pm &= pm - 1;
-        const KxTrig &T = P.trig[i];
-        bool b;
-        if (T.cond_kind == CK_SPOT_CMP) {
-            if (smooth && T.kind == TK_UNTIL) continue;  // weighted instead of knocked
-            b = cmp_y<Real>(T.cmp, y, thr[T.spot_slot]);
-        } else {
-            b = eval_code<Real>(P, T.code_off, T.code_len, acc, poisoned, k, S, err) != Real(0);
-        }
-        if (b) bits |= 1u << i;
-    }
-    return bits;
-}
-
-// Everything the contract does at grid step k for scenario s, after the
-// model moved to step k. Returns true when no flow can change any more.
-template <class Real, int NS>
-__device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const PathArgs &A, int cur, Lane<Real, NS> &L,
-                                              int s, int k, AccView<Real> acc, AccView<Real> surv) {
-    const KxProgram &P = *H.P;
-    const bool smooth = (H.flags & HF_SMOOTH) != 0u;
-    Real S = Real(0);
-    if (H.flags & HF_SPOT_EACH) S = H.s0[s] * fast_exp<Real>(L.y[s]);
-    // accumulators (observable.rs:120-140), inner ones first (slot order)
-    for (int a = 0; a < H.n_acc; ++a) {
-        const KxAcc &Ac = P.acc[a];
-        if (k < Ac.i_from || k > Ac.i_to) continue;
-        Real x;
-        if (Ac.inner == IK_SPOT) {
-            x = S;
-        } else {
-            uint32_t e = 0;
-            x = eval_code<Real>(P, Ac.code_off, Ac.code_len, acc, L.poisoned[s], k, S, e);
-            if (e) L.poisoned[s] |= 1u << a;
-        }
-        Real &v = acc[2 * a];
-        if (Ac.kind == ACC_MAX) v = fmax(v, x);
-        else if (Ac.kind == ACC_MIN) v = fmin(v, x);
-        else if (sizeof(Real) == 8) v = v + x;
-        else {  // compensated (Kahan) sum in FP32
-            Real &c = acc[2 * a + 1];
-            const Real yk = x - c;
-            const Real t = v + yk;
-            c = (t - v) - yk;
-            v = t;
-        }
-    }
-    const uint32_t live = L.armed[s] & ~L.resolved[s];
-    uint32_t bits = 0;
-    if (live & H.fast_bit) {
-        const Real yy = H.fsign * L.y[s];
-        const bool b = (H.flags & HF_STRICT) ? yy > H.fthr[s] : yy >= H.fthr[s];
-        if (b) bits = H.fast_bit;
-    }
-    if (k >= L.nte[s]) bits |= live & H.time_mask & H.R[k].tt;
-    const bool need_rare = bits || k == 0 || (live & H.gen_mask) || smooth;
-    if (!need_rare) return false;
-
-    // ---- rare path: general conditions, smoothing, firing, flows ----
-    const ContractDev &C = A.cons[cur];
-    const Real *thr = reinterpret_cast<const Real *>(A.thr) + ((size_t)cur * KX_MAX_NS + s) * KX_MAX_SPOT;
-    const double *D = A.disc + C.disc_off + (size_t)s * H.n_times;
-    const Real inv_w = pick<Real>(C.inv_w, C.inv_wf);
-    const Real y = L.y[s];
-    S = H.s0[s] * fast_exp<Real>(y);
-    if (live & H.gen_mask) bits |= cond_bits_full<Real>(P, H.R, thr, smooth, y, S, L.poisoned[s], live & H.gen_mask, k, acc, L.err);
-    if (smooth) {  // smoothed until weights of the slots armed before this step
-        uint32_t sm = L.armed[s] & P.until_mask & ~P.time_mask;
-        while (sm) {
-            const int i = __ffs(sm) - 1;
-            sm &= sm - 1;
-            const KxTrig &T = P.trig[i];
-            if (T.cond_kind == CK_SPOT_CMP) surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, y, thr[T.spot_slot], inv_w);
-        }
-    }
-    if (!bits && k != 0) return false;
-    uint32_t fired = 0;
-    uint32_t newly = bits;
-    while (newly) {
-        L.resolved[s] |= newly;
-        uint32_t u = newly & P.until_mask;
-        while (u) {
-            const int i = __ffs(u) - 1;
-            u &= u - 1;
-            L.dead[s] |= P.trig[i].leaves & ~L.emitted[s];
-        }
-        uint32_t w = newly & P.when_mask;
-        fired |= w;
-        uint32_t arm = 0;
-        while (w) {
-            const int i = __ffs(w) - 1;
-            w &= w - 1;
-            arm |= P.trig[i].fire_arm;
-        }
-        arm &= ~L.armed[s];
-        L.armed[s] |= arm;
-        newly = arm ? cond_bits_full<Real>(P, H.R, thr, smooth, y, S, L.poisoned[s], arm, k, acc, L.err) : 0u;
-        if (smooth && arm) {  // smoothed slots armed now weigh this step too
-            uint32_t sm = arm & P.until_mask & ~P.time_mask;
-            while (sm) {
-                const int i = __ffs(sm) - 1;
-                sm &= sm - 1;
-                const KxTrig &T = P.trig[i];
-                if (T.cond_kind == CK_SPOT_CMP) surv[T.spot_slot] *= smooth_survival<Real>(T.cmp, y, thr[T.spot_slot], inv_w);
-            }
-        }
-    }
-    // flows acquired at step k (pricer.rs:380-405)
-    uint32_t acq = k == 0 ? P.root_leaves : 0u;
-    while (fired) {
-        const int i = __ffs(fired) - 1;
-        fired &= fired - 1;
-        acq |= P.trig[i].leaves;
-    }
-    acq &= ~L.emitted[s];
-    while (acq) {
-        const int j = __ffs(acq) - 1;
-        acq &= acq - 1;
-        const KxLeaf &F = P.leaf[j];
-        const bool is_dead = (L.dead[s] >> j) & 1u;
-        if (is_dead && !F.err_capable) continue;
-        double amt = F.kind == AK_CONST ? F.sign
-                                        : (double)eval_code<Real>(P, F.code_off, F.code_len, acc, L.poisoned[s], k, S, L.err);
-        if (is_dead) continue;
-        if (smooth) {
-            uint32_t us = P.until_mask & ~P.time_mask & L.armed[s];
-            while (us) {
-                const int i = __ffs(us) - 1;
-                us &= us - 1;
-                const KxTrig &T = P.trig[i];
-                if (T.cond_kind == CK_SPOT_CMP && ((T.leaves >> j) & 1u)) amt *= (double)surv[T.spot_slot];
-            }
-        }
-        L.pv[s] += amt * D[k];
-        L.emitted[s] |= 1u << j;
-    }
-    // next step at which a live time-only slot can change
-    const uint32_t live_t = L.armed[s] & ~L.resolved[s] & P.time_mask;
-    int nte = INT_MAX;
-    if (live_t & ~P.mono_mask) {
-        nte = k + 1;
-    } else {
-        uint32_t t = live_t;
-        while (t) {
-            const int i = __ffs(t) - 1;
-            t &= t - 1;
-            nte = min(nte, P.first_true[i]);
-        }
-    }
-    L.nte[s] = nte;
-    return !P.err_capable && (P.all_leaves & ~(L.emitted[s] | L.dead[s])) == 0u;
-}
-
-template <class Real, int NS>
-__device__ __forceinline__ void write_path(const PathArgs &A, int cur, int64_t path, const Lane<Real, NS> &L) {
-    const uint64_t off = A.cons[cur].pv_off + (uint64_t)path;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) A.pv[(uint64_t)s * A.pv_stride + off] = L.pv[s];
-}
-
-template <class Real, int MODEL, int NS>
-__global__ void __launch_bounds__(KX_BLOCK, NS == 1 ? 4 : 2) k_paths(const PathArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Real *smem = reinterpret_cast<Real *>(smem_raw);
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
-    constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
-    constexpr uint32_t ALL = (1u << NS) - 1u;
-    const int nthr = KX_BLOCK;
-
-    // warp-uniform work state (path indices are per contract, < 2^32)
-    int cur = -1, pend = -1;
-    uint32_t nx = 0, end = 0;
-    bool drained = false;
-    Hot<Real, NS> H;
-    Real hr = 0, hk = 0, hth = 0, hsv = 0, hrho = 0, hrp = 0, hv0 = 0;  // Heston parameters
-
-    // lane state
-    int64_t path = -1;
-    int k = 0;
-    uint32_t done = 0;
-    Lane<Real, NS> L;
-    L.err = 0;
-    uint32_t my_steps = 0;
-
-    while (true) {
-        // ---- hand paths to idle lanes (warp-uniform control) ----
-        unsigned idle = __ballot_sync(FULL, path < 0);
-        while (idle) {
-            if (nx >= end) {
-                int it = pend;
-                if (it < 0) {
-                    if (drained) break;
-                    if (lane == 0) it = (int)atomicAdd(A.item_counter, 1u);
-                    it = __shfl_sync(FULL, it, 0);
-                    if (it >= (int)A.n_items) {
-                        drained = true;
-                        break;
-                    }
-                }
-                const WorkItem w = A.items[it];
-                if (w.contract != cur) {
-                    if (cur >= 0 && idle != FULL) {  // finish the current contract first
-                        pend = it;
-                        break;
-                    }
-                    cur = w.contract;
-                    load_hot<Real, NS>(H, A, cur);
-                    if (MODEL == M_HESTON) {
-                        const ContractDev &C = A.cons[cur];
-                        hr = pick<Real>(C.r, C.rf);
-                        hk = pick<Real>(C.kappa, C.kappaf);
-                        hth = pick<Real>(C.theta, C.thetaf);
-                        hsv = pick<Real>(C.sigma_v, C.sigma_vf);
-                        hrho = pick<Real>(C.rho, C.rhof);
-                        hrp = pick<Real>(C.rho_perp, C.rho_perpf);
-                        hv0 = pick<Real>(C.v0, C.v0f);
-                    }
-                }
-                pend = -1;
-                nx = (uint32_t)w.first;
-                end = (uint32_t)(w.first + w.count);
-                continue;
-            }
-            const int nidle = __popc(idle);
-            const uint32_t avail = end - nx;
-            const int take = avail < (uint32_t)nidle ? (int)avail : nidle;
-            const int rank = __popc(idle & lt);
-            if (path < 0 && rank < take) {
-                path = (int64_t)(nx + (uint32_t)rank);
-                // new path: state at t = 0 (S = s0), then the contract at step 0
-                const KxProgram &P = *H.P;
-                done = 0;
-#pragma unroll
-                for (int s = 0; s < NS; ++s) {
-                    L.y[s] = Real(0);
-                    L.v[s] = fmax(hv0, Real(0));
-                    L.armed[s] = P.root_arm;
-                    L.resolved[s] = L.dead[s] = L.emitted[s] = L.poisoned[s] = 0u;
-                    L.nte[s] = 0;
-                    L.pv[s] = 0.0;
-                    AccView<Real> av{smem + (s * (int)A.slots) * nthr + threadIdx.x, nthr};
-                    AccView<Real> sv{smem + (s * (int)A.slots + (int)A.surv_base) * nthr + threadIdx.x, nthr};
-                    for (int a = 0; a < H.n_acc; ++a) {
-                        av[2 * a] = P.acc[a].kind == ACC_MAX   ? Real(-INFINITY)
-                                    : P.acc[a].kind == ACC_MIN ? Real(INFINITY)
-                                                               : Real(0);
-                        av[2 * a + 1] = Real(0);
-                    }
-                    if (H.flags & HF_SMOOTH)
-                        for (int q = 0; q < P.n_spot_cmp; ++q) sv[q] = Real(1);
-                    if (contract_step<Real, NS>(H, A, cur, L, s, 0, av, sv)) done |= 1u << s;
-                }
-                k = 1;
-                if (H.n_times <= 1 || done == ALL) {
-                    write_path<Real, NS>(A, cur, path, L);
-                    path = -1;
-                }
-            }
-            nx += (uint32_t)take;
-            if (take == 0) break;
-            idle = __ballot_sync(FULL, path < 0);
-        }
-        if (__ballot_sync(FULL, path >= 0) == 0u) {
-            if (drained && pend < 0 && nx >= end) break;
-            continue;
-        }
-
-        // ---- advance busy lanes by one Philox block of grid steps ----
-        if (path >= 0) {
-            const int nt = H.n_times;
-            Real z0, z1, z2, z3;
-            if (A.z64 == nullptr && A.z32 == nullptr) {
-                const ContractDev &C = A.cons[cur];
-                const uint32_t blk = (uint32_t)((k - 1) / SPB);
-                const uint4 w = philox4x32_10(make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32), C.stream),
-                                              (uint32_t)C.seed, (uint32_t)(C.seed >> 32));
-                box_muller(w.x, w.y, z0, z1);
-                box_muller(w.z, w.w, z2, z3);
-            } else {
-                const uint64_t d0 = (uint64_t)(k - 1) * DRAWS;
-                const uint64_t base = (uint64_t)path * A.z_dpp + d0;
-                Real zz[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    zz[j] = d0 + j < A.z_dpp ? (A.z64 ? (Real)A.z64[base + j] : (Real)A.z32[base + j]) : Real(0);
-                z0 = zz[0];
-                z1 = zz[1];
-                z2 = zz[2];
-                z3 = zz[3];
-            }
-#pragma unroll 1
-            for (int j = 0; j < SPB; ++j) {
-                const int kk = k + j;
-                if (kk >= nt || done == ALL) break;
-                const StepRec<Real> rec = H.R[kk];
-                const Real za = j == 0 ? z0 : j == 1 ? z1 : j == 2 ? z2 : z3;  // GBM draw of step kk
-                const Real h1 = j == 0 ? z0 : z2, h2 = j == 0 ? z1 : z3;     // Heston draws of step kk
-#pragma unroll
-                for (int s = 0; s < NS; ++s) {
-                    if ((done >> s) & 1u) continue;
-                    if (MODEL == M_GBM) {
-                        // log-space exact GBM step (simulator.rs:238-245)
-                        if (NS == 1) {
-                            L.y[s] += rec.c0 + rec.c1 * za;
-                        } else {
-                            const ContractDev &C = A.cons[cur];
-                            L.y[s] += pick<Real>(C.drift[s], C.driftf[s]) * rec.c0 +
-                                      pick<Real>(C.sigma[s], C.sigmaf[s]) * rec.c1 * za;
-                        }
-                    } else {
-                        heston_step<Real>(hr, hk, hth, hsv, hrho, hrp,
-                                          (H.flags & HF_FULLTRUNC) ? KX_HESTON_FULL_TRUNCATION : KX_HESTON_REFERENCE_FLOOR,
-                                          rec.c0, rec.c1, h1, h2, L.y[s], L.v[s]);
-                    }
-                    AccView<Real> av{smem + (s * (int)A.slots) * nthr + threadIdx.x, nthr};
-                    AccView<Real> sv{smem + (s * (int)A.slots + (int)A.surv_base) * nthr + threadIdx.x, nthr};
-                    if (contract_step<Real, NS>(H, A, cur, L, s, kk, av, sv)) done |= 1u << s;
-                }
-                ++my_steps;
-            }
-            k += SPB;
-            if (k >= nt || done == ALL) {
-                write_path<Real, NS>(A, cur, path, L);
-                path = -1;
-            }
-        }
-    }
-    // counters: one atomic per warp
-    unsigned long long tot = (unsigned long long)my_steps;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
-    uint32_t err = L.err;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) err |= __shfl_xor_sync(FULL, err, o);
-    if (lane == 0) {
-        if (tot) atomicAdd(A.steps_done, tot);
-        if (err) atomicOr(A.err_word, err);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -790,6 +296,20 @@ static Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, c
     d.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));  // simulator.rs:510
     d.r = m.r;
     d.inv_w = smooth ? 1.0 / smooth_w : 0.0;
+    // uniform grid: every step's coefficients equal in the launch precision
+    d.uniform = 0;
+    if (n > 1) {
+        bool uni = true;
+        for (size_t k = 2; k < n && uni; ++k) {
+            if (cfg.precision == KX_PREC_FP64) uni = j.tab.c0[k] == j.tab.c0[1] && j.tab.c1[k] == j.tab.c1[1];
+            else uni = (float)j.tab.c0[k] == (float)j.tab.c0[1] && (float)j.tab.c1[k] == (float)j.tab.c1[1];
+        }
+        d.uniform = uni ? 1 : 0;
+        d.uc0 = j.tab.c0[1];
+        d.uc1 = j.tab.c1[1];
+        d.uc0f = (float)d.uc0;
+        d.uc1f = (float)d.uc1;
+    }
     d.v0f = (float)d.v0; d.kappaf = (float)d.kappa; d.thetaf = (float)d.theta; d.sigma_vf = (float)d.sigma_v;
     d.rhof = (float)d.rho; d.rho_perpf = (float)d.rho_perp; d.rf = (float)d.r; d.inv_wf = (float)d.inv_w;
     return j;
@@ -804,15 +324,98 @@ static void pack_steps(const StepTables &t, std::vector<unsigned char> &out) {
     for (size_t k = 0; k < n; ++k) r[k] = StepRec<Real>{(Real)t.c0[k], (Real)t.c1[k], t.time_true[k], 0u};
 }
 
-template <class Real, int MODEL, int NS>
-static const void *kernel_ptr() {
-    return reinterpret_cast<const void *>(&k_paths<Real, MODEL, NS>);
-}
-
 // Launch the fused path kernel over `jobs` (all of one model kind, one
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
+static const void *select_kernel(int model, bool f64, int ns, int minb) {
+    if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
+    if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
+    return paths_kernel_heston(f64, minb);
+}
+
+static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
+                            int minb);
+
+// Project autotuner: the path kernel exists at a few register budgets
+// (minimum resident blocks per SM). The first launch of each kind (model,
+// precision, scenario count, program features) times every variant on a
+// calibration batch of the same contracts and keeps the fastest. All variants
+// compute every path identically, so the choice never changes results.
+// KX_TUNE=0 disables tuning (the default budget is used).
+struct TuneEntry {
+    int minb;
+    float ms[8];
+};
+static std::map<std::string, TuneEntry> g_tune;
+
+static std::string tune_key(const std::vector<Job> &jobs, const kx_mc_config &cfg, int ns) {
+    int acc = 0, gen = 0, smooth = 0, spot = 0;
+    for (auto &j : jobs) {
+        acc = std::max(acc, j.prog.n_acc);
+        spot |= j.prog.spot_each_step ? 1 : 0;
+        smooth |= j.dev.smooth;
+        for (int i = 0; i < j.prog.n_trig; ++i) gen |= j.prog.trig[i].cond_kind == CK_GENERAL;
+    }
+    char buf[128];
+    snprintf(buf, sizeof buf, "m%d-p%d-ns%d-acc%d-gen%d-sm%d-sp%d", jobs[0].model.kind, cfg.precision, ns, acc > 0, gen,
+             smooth, spot);
+    return buf;
+}
+
+static const int *variants(int model, int ns, int &n) {
+    static const int v1[] = {4, 3, 2};
+    static const int v7[] = {2, 1};
+    (void)model;
+    if (ns == 1) { n = 3; return v1; }
+    n = 2;
+    return v7;
+}
+
 static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out) {
+    int nv = 0;
+    const int *vs = variants(jobs[0].model.kind, ns, nv);
+    const char *env = getenv("KX_TUNE");
+    const bool tune = !(env && env[0] == '0');
+    const std::string key = tune_key(jobs, cfg, ns);
+    auto it = g_tune.find(key);
+    if (tune && it == g_tune.end()) {
+        // calibration batch: the same contracts with fewer paths
+        uint64_t total = 0;
+        for (auto &j : jobs) total += j.dev.n_paths;
+        if (total >= (1u << 16)) {
+            std::vector<Job> cal = jobs;
+            const double scale = std::min(1.0, (double)(1u << 20) / (double)total);
+            for (auto &j : cal) j.dev.n_paths = std::max<uint64_t>(1, (uint64_t)(j.dev.n_paths * scale));
+            const kx_launch_stats saved = c.last;
+            TuneEntry e{};
+            float best = 1e30f;
+            for (int q = 0; q < nv; ++q) {
+                float t = 1e30f;
+                for (int rep = 0; rep < 2; ++rep) {
+                    c.last.kernel_ms = 0;
+                    uint64_t st = 0;
+                    run_paths_v(c, cal, cfg, ns, st, vs[q]);
+                    t = std::min(t, (float)c.last.kernel_ms);
+                }
+                e.ms[q] = t;
+                if (t < best) { best = t; e.minb = vs[q]; }
+            }
+            c.last = saved;
+            it = g_tune.emplace(key, e).first;
+            const char *vb = getenv("KX_TUNE_VERBOSE");
+            if (vb && vb[0] == '1') {
+                fprintf(stderr, "[kx tune] %s:", key.c_str());
+                for (int q = 0; q < nv; ++q) fprintf(stderr, " minb%d=%.3fms", vs[q], e.ms[q]);
+                fprintf(stderr, " -> minb%d\n", e.minb);
+            }
+        }
+    }
+    const int minb = it != g_tune.end() ? it->second.minb : vs[0];
+    return run_paths_v(c, jobs, cfg, ns, stride_out, minb);
+}
+
+static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
+                            int minb) {
     const bool f64 = cfg.precision == KX_PREC_FP64;
     const int model = jobs[0].model.kind;
     std::vector<KxProgram> progs;
@@ -862,14 +465,8 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
     const uint32_t surv_base = 2u * (uint32_t)max_acc;
     const uint32_t slots = surv_base + (smooth ? (uint32_t)max_spot : 0u);
     const size_t smem = (size_t)ns * slots * block * (f64 ? 8 : 4);
-    const void *kfn = nullptr;
-    if (model == KX_MODEL_GBM) {
-        if (ns == 1) kfn = f64 ? kernel_ptr<double, M_GBM, 1>() : kernel_ptr<float, M_GBM, 1>();
-        else kfn = f64 ? kernel_ptr<double, M_GBM, KX_MAX_NS>() : kernel_ptr<float, M_GBM, KX_MAX_NS>();
-    } else {
-        if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
-        kfn = f64 ? kernel_ptr<double, M_HESTON, 1>() : kernel_ptr<float, M_HESTON, 1>();
-    }
+    const void *kfn = select_kernel(model, f64, ns, minb);
+    if (!kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (smem > 48 * 1024) KX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int full = persistent_blocks(kfn, block, smem);
     const uint64_t warps_total = (uint64_t)full * (block / 32);

@@ -821,6 +821,11 @@ void bind(const Lowered &low, const std::vector<double> &grid, const Model &m, d
         P.first_true[i] = first < 0 ? INT32_MAX : first;
         if (mono) P.mono_mask |= 1u << i;
     }
+    // next time event after step 0 for the slots armed at 0 (if none fires then)
+    P.init_nte = INT32_MAX;
+    const uint32_t t0 = P.root_arm & P.time_mask;
+    for (int i = 0; i < P.n_trig; ++i)
+        if ((t0 >> i) & 1u) P.init_nte = ((P.mono_mask >> i) & 1u) ? std::min(P.init_nte, P.first_true[i]) : 1;
 }
 
 }  // namespace kx
