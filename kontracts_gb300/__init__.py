@@ -475,9 +475,11 @@ def price_batch(contracts: Sequence[Contract], model, n_paths: int = 100_000, se
 
 def price_portfolio(contracts: Sequence[Contract], models: Sequence[Any], n_paths: Sequence[int],
                     seeds: Sequence[int] | int = 42, steps_per_year: int = 252, *,
-                    precision: str = "fp32") -> list[PriceResult]:
+                    precision: str = "fp32", greeks: bool = False):
     """An uneven book in one persistent launch: contract i priced under
-    models[i] with n_paths[i] paths (no reference counterpart)."""
+    models[i] with n_paths[i] paths (no reference counterpart). With
+    greeks=True also returns per-contract pathwise Sensitivities (barriers
+    smoothed for the derivatives; the prices keep the hard barriers)."""
     n = len(contracts)
     if isinstance(seeds, int):
         seeds = [seeds] * n
@@ -486,9 +488,13 @@ def price_portfolio(contracts: Sequence[Contract], models: Sequence[Any], n_path
     cfgs = (_abi.KxMcConfig * n)(*[_cfg(n_paths[i], seeds[i], steps_per_year, models[i].rate, precision, False)
                                    for i in range(n)])
     out = (_abi.KxPriceResult * n)()
+    sens = (_abi.KxSens * n)() if greeks else None
     with _lock:
-        _check(_lib().kx_price_portfolio(n, hs, ms, cfgs, out, None))
-    return [PriceResult(r) for r in out]
+        _check(_lib().kx_price_portfolio(n, hs, ms, cfgs, out, sens))
+    res = [PriceResult(r) for r in out]
+    if greeks:
+        return res, [Sensitivities(s) for s in sens]
+    return res
 
 
 def set_shared_draws(z) -> None:

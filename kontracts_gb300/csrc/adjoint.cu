@@ -35,7 +35,7 @@ constexpr int ADJ_MAXU = 2;    // smoothed untils
 constexpr int ADJ_MAXA = 2;    // accumulators
 constexpr int ADJ_MAXCK = 72;  // checkpoints
 constexpr int ADJ_KMAX = 32;   // checkpoint interval
-constexpr int ADJ_OUT = 8;     // per-path outputs
+constexpr int ADJ_OUT = 9;     // per-path outputs (slot 8: price with hard barriers)
 
 struct AdjFlow {
     int t;             // step the flow is paid at
@@ -73,7 +73,7 @@ struct AdjArgs {
     const double *z64;
     const float *z32;
     uint64_t z_dpp;
-    double *out;          // [ADJ_OUT][n_paths]
+    uint64_t out_off;     // first output slot of this contract in each output row
 };
 
 // Forward-mode value of an amount program with derivatives with respect to
@@ -151,17 +151,29 @@ __device__ __forceinline__ void model_step(const AdjArgs &A, const StepRec<Real>
     }
 }
 
+// One launch covers a list of contracts (each with its own model, grid and
+// path count): the global path index runs over all of them (prefix offsets
+// `off`), so an uneven book is one persistent launch.
 template <class Real, int MODEL>
-__global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
+__global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict__ all, const uint64_t *__restrict__ off,
+                                                       int n_contracts, uint64_t total, double *__restrict__ out) {
     constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
-    const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
-    const KxProgram &P = *A.P;
-    const int N = A.n_times - 1;  // steps
-    const int K = A.K;
-    const Real s0 = (Real)A.s0;
-    const Real inv_w = (Real)A.inv_w;
-    for (uint64_t path = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; path < A.n_paths;
-         path += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
+         gp += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_contracts - 1;  // contract of global path gp
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= gp) lo = mid;
+            else hi = mid - 1;
+        }
+        const AdjArgs &A = all[lo];
+        const uint64_t path = gp - off[lo];
+        const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+        const KxProgram &P = *A.P;
+        const int N = A.n_times - 1;  // steps
+        const int K = A.K;
+        const Real s0 = (Real)A.s0;
+        const Real inv_w = (Real)A.inv_w;
         // ------------------------------ forward ------------------------------
         Real ck_y[ADJ_MAXCK], ck_v[ADJ_MAXCK];
         Real y = Real(0), v = (Real)fmax(A.v0, 0.0);
@@ -173,7 +185,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
             accv[a] = Real(0);
         }
         Real surv[ADJ_MAXU];
-        for (int u = 0; u < ADJ_MAXU; ++u) surv[u] = Real(1);
+        int knock[ADJ_MAXU];  // first step the (unsmoothed) barrier holds
+        for (int u = 0; u < ADJ_MAXU; ++u) {
+            surv[u] = Real(1);
+            knock[u] = INT_MAX;
+        }
+        double pv_hard = 0.0;
         // flow records
         double fP[ADJ_MAXF];
         Real fcs[ADJ_MAXF], fca[ADJ_MAXF][ADJ_MAXA];
@@ -201,9 +218,18 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
             }
             for (int u = 0; u < A.n_su; ++u)
                 if (k >= A.su[u].arm) {
-                    Real x = (y - (Real)A.su[u].thr) * inv_w;
+                    const Real thr = (Real)A.su[u].thr;
+                    Real x = (y - thr) * inv_w;
                     if (A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT) x = -x;
                     surv[u] *= Real(1) / (Real(1) + fast_exp<Real>(x));
+                    bool hit;
+                    switch (A.su[u].cmp) {
+                    case CMP_GE: hit = y >= thr; break;
+                    case CMP_GT: hit = y > thr; break;
+                    case CMP_LE: hit = y <= thr; break;
+                    default: hit = y < thr; break;
+                    }
+                    if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
             for (int f = 0; f < A.n_flows; ++f) {
                 const AdjFlow &F = A.flow[f];
@@ -233,6 +259,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
                 }
                 pv += fP[f];
                 pv_t += A.times[k] * fP[f];
+                bool alive = true;  // the flow under the hard barriers (pricer.rs:407-413)
+                for (int u = 0; u < A.n_su; ++u)
+                    if (((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
+                if (alive) pv_hard += (double)amt.v * df;
             }
         }
         // ------------------------------ reverse ------------------------------
@@ -328,20 +358,21 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs A) {
                 lam += g;
             }
         }
-        double *o = A.out;
-        const uint64_t n = A.n_paths;
-        o[0 * n + path] = pv;
-        o[1 * n + path] = (double)lam / A.s0;                  // d/ds0
+        double *o = out + A.out_off + path;
+        const uint64_t n = total;
+        o[8 * n] = pv_hard;
+        o[0 * n] = pv;
+        o[1 * n] = (double)lam / A.s0;                  // d/ds0
         if (MODEL == KX_MODEL_GBM) {
-            o[2 * n + path] = (double)g_sig;                    // d/dsigma
-            o[3 * n + path] = (double)g_r - pv_t;               // d/dr: drift and discount
+            o[2 * n] = (double)g_sig;                    // d/dsigma
+            o[3 * n] = (double)g_r - pv_t;               // d/dr: drift and discount
         } else {
-            o[2 * n + path] = A.v0 > 0 ? (double)mu : 0.0;      // d/dv0
-            o[3 * n + path] = (double)g_r - pv_t;               // d/dr
-            o[4 * n + path] = (double)g_k;                      // d/dkappa
-            o[5 * n + path] = (double)g_th;                     // d/dtheta
-            o[6 * n + path] = (double)g_sv;                     // d/dsigma_v
-            o[7 * n + path] = (double)g_rho;                    // d/drho
+            o[2 * n] = A.v0 > 0 ? (double)mu : 0.0;      // d/dv0
+            o[3 * n] = (double)g_r - pv_t;               // d/dr
+            o[4 * n] = (double)g_k;                      // d/dkappa
+            o[5 * n] = (double)g_th;                     // d/dtheta
+            o[6 * n] = (double)g_sv;                     // d/dsigma_v
+            o[7 * n] = (double)g_rho;                    // d/drho
         }
     }
 }
@@ -439,6 +470,203 @@ static const void *adj_kernel() {
     return reinterpret_cast<const void *>(&k_adjoint<Real, MODEL>);
 }
 
+// One contract of an adjoint launch (host side).
+struct AdjJob {
+    AdjArgs a;                        // device pointers patched at upload
+    KxProgram P;
+    std::vector<unsigned char> steps;
+    std::vector<double> disc, times;
+    double w = 0.0;
+};
+
+static AdjJob make_adj_job(const Program &p, const Model &m, const kx_mc_config &cfg, const kx_adjoint_cfg *acfg) {
+    if (cfg.flags != 0 || (cfg.rng != KX_RNG_PHILOX && cfg.rng != KX_RNG_SHARED_DRAWS) ||
+        (cfg.precision != KX_PREC_FP32 && cfg.precision != KX_PREC_FP64))
+        raise(KX_INVALID_ARGUMENT, "bad config");
+    if (cfg.n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
+    validate_model(m);
+    if (!(m.s0 > 0.0)) raise(KX_UNSUPPORTED, "adjoint: s0 must be positive");
+    auto grid = time_grid_forced(p.plan, cfg.steps_per_year, m.requires_fine_grid());
+    validate_grid(grid);
+    const int n = (int)grid.size();
+    const int N = n - 1;
+    AdjJob J;
+    StepTables tab;
+    bind(p.low, grid, m, cfg.rate, J.P, tab);
+    AdjArgs &a = J.a;
+    memset(&a, 0, sizeof a);
+    schedule(p.low, J.P, tab, m, a);
+    uint32_t K = acfg && acfg->checkpoint_every ? acfg->checkpoint_every : 16u;
+    K = (K + 3) / 4 * 4;
+    if (K > (uint32_t)ADJ_KMAX) K = ADJ_KMAX;
+    while ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK && K < (uint32_t)ADJ_KMAX) K += 4;
+    if ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK) raise(KX_UNSUPPORTED, "adjoint: grid too long for the checkpoint store");
+    a.K = (int)K;
+    // smoothing width: default 0.5 * sigma_eff * sqrt(mean dt)
+    double w = acfg ? acfg->smoothing_width : 0.0;
+    const double dtm = N > 0 ? grid.back() / N : 1.0;
+    if (!(w > 0.0)) {
+        const double se = m.kind == KX_MODEL_GBM ? m.sigma : std::sqrt(std::max(m.v0, m.theta));
+        w = 0.5 * std::max(se, 1e-8) * std::sqrt(dtm);
+    }
+    J.w = w;
+    a.inv_w = 1.0 / w;
+    a.n_times = n;
+    a.model = m.kind;
+    a.scheme = m.scheme;
+    a.n_paths = cfg.n_paths;
+    a.seed = cfg.seed;
+    a.s0 = m.s0;
+    a.mu = m.kind == KX_MODEL_GBM ? m.mu : m.r;
+    a.sigma = m.sigma;
+    a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
+    a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
+    a.r = m.r;
+    const bool f64 = cfg.precision == KX_PREC_FP64;
+    J.steps.resize(n * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+    for (int k = 0; k < n; ++k) {
+        const double dt = k == 0 ? 0.0 : grid[k] - grid[k - 1];
+        if (f64) reinterpret_cast<StepRec<double> *>(J.steps.data())[k] = {dt, std::sqrt(dt), 0u, 0u};
+        else reinterpret_cast<StepRec<float> *>(J.steps.data())[k] = {(float)dt, (float)std::sqrt(dt), 0u, 0u};
+    }
+    J.disc = tab.disc;
+    J.times = grid;
+    return J;
+}
+
+// Launch the adjoint over `jobs` (one model kind, one precision); returns the
+// statistics of the ADJ_OUT per-path outputs of every contract.
+static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &jobs, bool f64, int model, int rng) {
+    const int nc = (int)jobs.size();
+    std::vector<KxProgram> progs;
+    std::vector<unsigned char> steps;
+    std::vector<double> dt;  // disc then times, per contract
+    std::vector<uint64_t> off(nc + 1, 0);
+    std::vector<size_t> soff(nc), doff(nc);
+    for (int i = 0; i < nc; ++i) {
+        progs.push_back(jobs[i].P);
+        soff[i] = steps.size();
+        steps.insert(steps.end(), jobs[i].steps.begin(), jobs[i].steps.end());
+        doff[i] = dt.size();
+        dt.insert(dt.end(), jobs[i].disc.begin(), jobs[i].disc.end());
+        dt.insert(dt.end(), jobs[i].times.begin(), jobs[i].times.end());
+        off[i + 1] = off[i] + jobs[i].a.n_paths;
+    }
+    const uint64_t total = off[nc];
+    c.progs.ensure(progs.size() * sizeof(KxProgram));
+    c.steps.ensure(steps.size());
+    c.disc.ensure(dt.size() * sizeof(double));
+    c.cons.ensure(nc * sizeof(AdjArgs));
+    c.items.ensure((nc + 1) * sizeof(uint64_t));
+    c.pv.ensure(std::max<uint64_t>(1, total) * ADJ_OUT * sizeof(double));
+    std::vector<AdjArgs> args(nc);
+    for (int i = 0; i < nc; ++i) {
+        AdjArgs a = jobs[i].a;
+        a.P = c.progs.as<KxProgram>() + i;
+        a.steps = c.steps.as<unsigned char>() + soff[i];
+        a.disc = c.disc.as<double>() + doff[i];
+        a.times = c.disc.as<double>() + doff[i] + jobs[i].disc.size();
+        a.out_off = off[i];
+        if (rng == KX_RNG_SHARED_DRAWS) {
+            DrawStore &ds = c.draws;
+            if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
+            const int N = a.n_times - 1;
+            if (ds.n_paths < a.n_paths || ds.dpp < (uint64_t)N * (model == KX_MODEL_HESTON ? 2 : 1))
+                raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
+            a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
+            a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
+            a.z_dpp = ds.dpp;
+        }
+        args[i] = a;
+    }
+    KX_CUDA(cudaMemcpyAsync(c.progs.p, progs.data(), progs.size() * sizeof(KxProgram), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.disc.p, dt.data(), dt.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.cons.p, args.data(), nc * sizeof(AdjArgs), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.items.p, off.data(), (nc + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.stream));
+    c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + dt.size() * sizeof(double) +
+                        nc * sizeof(AdjArgs) + (nc + 1) * sizeof(uint64_t);
+    const void *kfn = model == KX_MODEL_GBM ? (f64 ? adj_kernel<double, KX_MODEL_GBM>() : adj_kernel<float, KX_MODEL_GBM>())
+                                            : (f64 ? adj_kernel<double, KX_MODEL_HESTON>() : adj_kernel<float, KX_MODEL_HESTON>());
+    if (total > 0) {
+        const int full = persistent_blocks(kfn, ADJ_BLOCK, 0);
+        const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
+        const AdjArgs *ap = c.cons.as<AdjArgs>();
+        const uint64_t *op = c.items.as<uint64_t>();
+        double *outp = c.pv.as<double>();
+        void *kargs[] = {&ap, &op, (void *)&nc, (void *)&total, &outp};
+        KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+        KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(ADJ_BLOCK), kargs, 0, c.stream));
+        KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+        KX_CUDA(cudaEventSynchronize(c.ev1));
+        float ms = 0.f;
+        KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        c.last.kernel_ms += ms;
+        c.last.kernel_launches++;
+        c.last.grid_blocks = (uint32_t)blocks;
+        c.last.block_threads = ADJ_BLOCK;
+    }
+    std::vector<StatsJob> sj;
+    for (int i = 0; i < nc; ++i) {
+        c.last.path_steps += jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);
+        c.last.steps_simulated += 2 * jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);  // forward + recompute
+        for (int q = 0; q < ADJ_OUT; ++q) {
+            StatsJob j;
+            j.begin = (uint64_t)q * total + off[i];
+            j.n = jobs[i].a.n_paths;
+            sj.push_back(j);
+        }
+    }
+    auto st = device_stats(c, c.pv.as<double>(), 0, sj);
+    std::vector<std::vector<Stats>> res(nc);
+    for (int i = 0; i < nc; ++i) res[i].assign(st.begin() + (size_t)i * ADJ_OUT, st.begin() + (size_t)(i + 1) * ADJ_OUT);
+    return res;
+}
+
+static void fill_sens(const std::vector<Stats> &st, int model, double w, kx_sens *out) {
+    auto R = [&](int q) { return finish(st[q]); };
+    memset(out, 0, sizeof *out);
+    out->price = R(0).price;
+    out->price_se = R(0).std_error;
+    out->d_s0 = R(1).price;
+    out->se_s0 = R(1).std_error;
+    out->smoothing_width = w;
+    if (model == KX_MODEL_GBM) {
+        out->d_sigma = R(2).price; out->se_sigma = R(2).std_error;
+        out->d_r = R(3).price; out->se_r = R(3).std_error;
+    } else {
+        out->d_v0 = R(2).price; out->se_v0 = R(2).std_error;
+        out->d_r = R(3).price; out->se_r = R(3).std_error;
+        out->d_kappa = R(4).price; out->se_kappa = R(4).std_error;
+        out->d_theta = R(5).price; out->se_theta = R(5).std_error;
+        out->d_sigma_v = R(6).price; out->se_sigma_v = R(6).std_error;
+        out->d_rho = R(7).price; out->se_rho = R(7).std_error;
+    }
+}
+
+// Portfolio pricing with per-contract pathwise sensitivities: one adjoint
+// launch per (model kind, precision) group; prices use the hard barriers.
+void portfolio_adjoint(Ctx &c, size_t n, const kx_program *const *progs, const kx_model *models,
+                       const kx_mc_config *cfgs, kx_price_result *out, kx_sens *sens) {
+    for (int kind = 0; kind < 2; ++kind)
+        for (int prec = 0; prec < 2; ++prec) {
+            std::vector<size_t> idx;
+            for (size_t i = 0; i < n; ++i)
+                if (models[i].kind == kind && cfgs[i].precision == prec) idx.push_back(i);
+            if (idx.empty()) continue;
+            std::vector<AdjJob> jobs;
+            for (size_t i : idx) {
+                if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "portfolio pricing uses Philox normals");
+                jobs.push_back(make_adj_job(program_of(progs[i]), model_from_c(&models[i]), cfgs[i], nullptr));
+            }
+            auto st = run_adjoint(c, jobs, prec == KX_PREC_FP64, kind, KX_RNG_PHILOX);
+            for (size_t q = 0; q < idx.size(); ++q) {
+                out[idx[q]] = finish(st[q][8]);
+                fill_sens(st[q], kind, jobs[q].w, &sens[idx[q]]);
+            }
+        }
+}
+
 }  // namespace kx
 
 using namespace kx;
@@ -449,125 +677,14 @@ extern "C" kx_status kx_greeks_adjoint(const kx_program *prog, const kx_model *m
         const Program &p = program_of(prog);
         Model m = model_from_c(model);
         if (!cfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
-        if (cfg->flags != 0 || (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) ||
-            (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64))
-            raise(KX_INVALID_ARGUMENT, "bad config");
-        if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
-        validate_model(m);
-        if (!(m.s0 > 0.0)) raise(KX_UNSUPPORTED, "adjoint: s0 must be positive");
-        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, m.requires_fine_grid());
-        validate_grid(grid);
-        const int n = (int)grid.size();
-        const int N = n - 1;
-        KxProgram P;
-        StepTables tab;
-        bind(p.low, grid, m, cfg->rate, P, tab);
-        AdjArgs a{};
-        schedule(p.low, P, tab, m, a);
-        uint32_t K = acfg && acfg->checkpoint_every ? acfg->checkpoint_every : 16u;
-        K = (K + 3) / 4 * 4;
-        if (K > (uint32_t)ADJ_KMAX) K = ADJ_KMAX;
-        while ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK && K < (uint32_t)ADJ_KMAX) K += 4;
-        if ((N + (int)K - 1) / (int)K + 1 > ADJ_MAXCK) raise(KX_UNSUPPORTED, "adjoint: grid too long for the checkpoint store");
-        a.K = (int)K;
-        // smoothing width: default 0.5 * sigma_eff * sqrt(mean dt)
-        double w = acfg ? acfg->smoothing_width : 0.0;
-        const double dtm = N > 0 ? grid.back() / N : 1.0;
-        if (!(w > 0.0)) {
-            const double se = m.kind == KX_MODEL_GBM ? m.sigma : std::sqrt(std::max(m.v0, m.theta));
-            w = 0.5 * std::max(se, 1e-8) * std::sqrt(dtm);
-        }
-        a.inv_w = 1.0 / w;
-        a.n_times = n;
-        a.model = m.kind;
-        a.scheme = m.scheme;
-        a.n_paths = cfg->n_paths;
-        a.seed = cfg->seed;
-        a.s0 = m.s0;
-        a.mu = m.kind == KX_MODEL_GBM ? m.mu : m.r;
-        a.sigma = m.sigma;
-        a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
-        a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
-        a.r = m.r;
-        const bool f64 = cfg->precision == KX_PREC_FP64;
-        std::vector<unsigned char> steps(n * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
-        for (int k = 0; k < n; ++k) {
-            const double dt = k == 0 ? 0.0 : grid[k] - grid[k - 1];
-            if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {dt, std::sqrt(dt), 0u, 0u};
-            else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)dt, (float)std::sqrt(dt), 0u, 0u};
-        }
+        std::vector<AdjJob> jobs;
+        jobs.push_back(make_adj_job(p, m, *cfg, acfg));
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         memset(&c.last, 0, sizeof c.last);
         c.last.total_ms = -now_ms();
-        const uint64_t np = cfg->n_paths;
-        c.progs.ensure(sizeof(KxProgram));
-        c.steps.ensure(steps.size());
-        c.disc.ensure(2 * n * sizeof(double));
-        c.pv.ensure(std::max<uint64_t>(1, np) * ADJ_OUT * sizeof(double));
-        KX_CUDA(cudaMemcpyAsync(c.progs.p, &P, sizeof P, cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.disc.p, tab.disc.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.disc.as<double>() + n, grid.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np) * ADJ_OUT * sizeof(double), c.stream));
-        c.last.h2d_bytes += sizeof P + steps.size() + 2 * n * sizeof(double);
-        a.P = c.progs.as<KxProgram>();
-        a.steps = c.steps.p;
-        a.disc = c.disc.as<double>();
-        a.times = c.disc.as<double>() + n;
-        a.out = c.pv.as<double>();
-        if (cfg->rng == KX_RNG_SHARED_DRAWS) {
-            DrawStore &ds = c.draws;
-            if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
-            if (ds.n_paths < np || ds.dpp < (uint64_t)N * m.draws_per_step())
-                raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
-            a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
-            a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
-            a.z_dpp = ds.dpp;
-        }
-        const void *kfn = m.kind == KX_MODEL_GBM ? (f64 ? adj_kernel<double, KX_MODEL_GBM>() : adj_kernel<float, KX_MODEL_GBM>())
-                                                 : (f64 ? adj_kernel<double, KX_MODEL_HESTON>() : adj_kernel<float, KX_MODEL_HESTON>());
-        if (np > 0) {
-            const int full = persistent_blocks(kfn, ADJ_BLOCK, 0);
-            const int blocks = (int)std::min<uint64_t>((uint64_t)full, (np + ADJ_BLOCK - 1) / ADJ_BLOCK);
-            void *args[] = {&a};
-            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-            KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(ADJ_BLOCK), args, 0, c.stream));
-            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
-            KX_CUDA(cudaEventSynchronize(c.ev1));
-            float ms = 0.f;
-            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
-            c.last.kernel_ms += ms;
-            c.last.kernel_launches++;
-            c.last.grid_blocks = (uint32_t)blocks;
-            c.last.block_threads = ADJ_BLOCK;
-        }
-        c.last.path_steps += np * (uint64_t)N;
-        c.last.steps_simulated += np * (uint64_t)N * 2;  // forward + recompute
-        std::vector<StatsJob> sj(ADJ_OUT);
-        for (int q = 0; q < ADJ_OUT; ++q) {
-            sj[q].begin = (uint64_t)q * np;
-            sj[q].n = np;
-        }
-        auto st = device_stats(c, c.pv.as<double>(), np, sj);
-        auto R = [&](int q) { return finish(st[q]); };
-        memset(out, 0, sizeof *out);
-        out->price = R(0).price;
-        out->price_se = R(0).std_error;
-        out->d_s0 = R(1).price;
-        out->se_s0 = R(1).std_error;
-        out->smoothing_width = w;
-        if (m.kind == KX_MODEL_GBM) {
-            out->d_sigma = R(2).price; out->se_sigma = R(2).std_error;
-            out->d_r = R(3).price; out->se_r = R(3).std_error;
-        } else {
-            out->d_v0 = R(2).price; out->se_v0 = R(2).std_error;
-            out->d_r = R(3).price; out->se_r = R(3).std_error;
-            out->d_kappa = R(4).price; out->se_kappa = R(4).std_error;
-            out->d_theta = R(5).price; out->se_theta = R(5).std_error;
-            out->d_sigma_v = R(6).price; out->se_sigma_v = R(6).std_error;
-            out->d_rho = R(7).price; out->se_rho = R(7).std_error;
-        }
+        auto st = run_adjoint(c, jobs, cfg->precision == KX_PREC_FP64, m.kind, cfg->rng);
+        fill_sens(st[0], m.kind, jobs[0].w, out);
         c.last.total_ms += now_ms();
     });
 }

@@ -166,14 +166,19 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
     KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice, c.stream));
     KX_CUDA(cudaMemcpyAsync(c.weights.p, wts.data(), wts.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-    for (size_t j = 0; j < jobs.size(); ++j) {
-        const size_t nc = first[j + 1] - first[j];
-        if (!nc) continue;
-        k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, c.weights.as<double>() + j * 8,
-                                                          c.chunks.as<ChunkDesc>() + first[j],
-                                                          c.chunk_out.as<ChunkOut>() + first[j]);
-        KX_CUDA(cudaGetLastError());
-        c.last.kernel_launches++;
+    // one launch per run of consecutive jobs with the same weights
+    for (size_t j = 0; j < jobs.size();) {
+        size_t e = j + 1;
+        while (e < jobs.size() && jobs[e].ns == jobs[j].ns && !memcmp(jobs[e].w, jobs[j].w, sizeof jobs[j].w)) ++e;
+        const size_t nc = first[e] - first[j];
+        if (nc) {
+            k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, c.weights.as<double>() + j * 8,
+                                                              c.chunks.as<ChunkDesc>() + first[j],
+                                                              c.chunk_out.as<ChunkOut>() + first[j]);
+            KX_CUDA(cudaGetLastError());
+            c.last.kernel_launches++;
+        }
+        j = e;
     }
     KX_CUDA(cudaEventRecord(c.ev1, c.stream));
     std::vector<ChunkOut> h(chunks.size());
@@ -551,6 +556,22 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     return total;
 }
 
+// Value `progs` on `grid` with the path kernel, all with the same model,
+// config and seed (so on the same simulated paths). Per-contract statistics.
+std::vector<Stats> batch_paths(Ctx &c, const std::vector<const Program *> &progs, const Model &m,
+                               const kx_mc_config &cfg, const std::vector<double> &grid) {
+    std::vector<Job> jobs;
+    for (auto *p : progs) jobs.push_back(make_job(*p, m, cfg, grid, {}, 0, 0.0));
+    uint64_t stride = 0;
+    run_paths(c, jobs, cfg, 1, stride);
+    std::vector<StatsJob> sj(progs.size());
+    for (size_t i = 0; i < progs.size(); ++i) {
+        sj[i].begin = jobs[i].dev.pv_off;
+        sj[i].n = cfg.n_paths;
+    }
+    return device_stats(c, c.pv.as<double>(), stride, sj);
+}
+
 static void begin_call(Ctx &c) {
     memset(&c.last, 0, sizeof c.last);
     c.last.total_ms = -now_ms();
@@ -718,53 +739,20 @@ kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_co
     });
 }
 
-kx_status kx_price_batch_shared(size_t n, const kx_program *const *progs, const kx_model *model,
-                                const kx_mc_config *cfg, kx_price_result *out) {
-    return guarded([&] {
-        if (n == 0) return;  // pricer.rs:255-257
-        if (!progs || !out) raise(KX_INVALID_ARGUMENT, "NULL array");
-        Model m = model_from_c(model);
-        check_cfg(cfg);
-        validate_model(m);
-        // merged plan (pricer.rs:260-279)
-        Plan merged;
-        for (size_t i = 0; i < n; ++i) {
-            const Program &p = program_of(progs[i]);
-            merged.fixed_dates.insert(merged.fixed_dates.end(), p.plan.fixed_dates.begin(), p.plan.fixed_dates.end());
-            merged.horizon = std::max(merged.horizon, p.plan.horizon);
-            merged.needs_fine_grid = merged.needs_fine_grid || p.plan.needs_fine_grid;
-        }
-        auto grid = time_grid_forced(merged, cfg->steps_per_year, m.requires_fine_grid());
-        Ctx &c = ctx();
-        std::lock_guard<std::mutex> g(c.mu);
-        begin_call(c);
-        // Every contract is valued on the same paths: the same seed and grid
-        // give each contract the same counter-based normals, hence the same
-        // simulated path, as the reference's single shared simulation.
-        std::vector<Job> jobs;
-        for (size_t i = 0; i < n; ++i) jobs.push_back(make_job(program_of(progs[i]), m, *cfg, grid, {}, 0, 0.0));
-        uint64_t stride = 0;
-        run_paths(c, jobs, *cfg, 1, stride);
-        std::vector<StatsJob> sj(n);
-        for (size_t i = 0; i < n; ++i) {
-            sj[i].begin = jobs[i].dev.pv_off;
-            sj[i].n = cfg->n_paths;
-        }
-        auto st = device_stats(c, c.pv.as<double>(), stride, sj);
-        for (size_t i = 0; i < n; ++i) out[i] = finish(st[i]);
-        end_call(c);
-    });
-}
-
 kx_status kx_price_portfolio(size_t n, const kx_program *const *progs, const kx_model *models,
                              const kx_mc_config *cfgs, kx_price_result *out, kx_sens *sens) {
     return guarded([&] {
         if (n == 0) return;
         if (!progs || !models || !cfgs || !out) raise(KX_INVALID_ARGUMENT, "NULL array");
-        if (sens) raise(KX_UNSUPPORTED, "portfolio sensitivities are not available in this build");
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         begin_call(c);
+        if (sens) {  // prices and pathwise delta / vega / rho in one adjoint launch per group
+            for (size_t i = 0; i < n; ++i) check_cfg(&cfgs[i]);
+            portfolio_adjoint(c, n, progs, models, cfgs, out, sens);
+            end_call(c);
+            return;
+        }
         // group by (model kind, precision): one persistent launch per group
         std::vector<size_t> idx(n);
         for (size_t i = 0; i < n; ++i) idx[i] = i;

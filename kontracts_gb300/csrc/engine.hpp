@@ -68,4 +68,13 @@ struct StatsJob {
 std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, const std::vector<StatsJob> &jobs);
 kx_price_result finish(const Stats &s);
 
+// Path-kernel valuation of several contracts on one grid with one model and
+// seed (engine.cu).
+std::vector<Stats> batch_paths(Ctx &c, const std::vector<const Program *> &progs, const Model &m,
+                               const kx_mc_config &cfg, const std::vector<double> &grid);
+
+// Portfolio prices (hard barriers) with pathwise sensitivities (adjoint.cu).
+void portfolio_adjoint(Ctx &c, size_t n, const kx_program *const *progs, const kx_model *models,
+                       const kx_mc_config *cfgs, kx_price_result *out, kx_sens *sens);
+
 }  // namespace kx

@@ -828,4 +828,50 @@ void bind(const Lowered &low, const std::vector<double> &grid, const Model &m, d
         if ((t0 >> i) & 1u) P.init_nte = ((P.mono_mask >> i) & 1u) ? std::min(P.init_nte, P.first_true[i]) : 1;
 }
 
+StaticSchedule static_schedule(const KxProgram &P, const StepTables &tab) {
+    StaticSchedule S;
+    const int n = P.n_times;
+    const int NEVER = StaticSchedule::NEVER;
+    S.arm.assign(P.n_trig, NEVER);
+    S.fire.assign(P.n_trig, NEVER);
+    std::vector<int> parent(P.n_trig, -1);  // the when slot whose firing arms slot j
+    for (int i = 0; i < P.n_trig; ++i)
+        for (int j = 0; j < P.n_trig; ++j)
+            if ((P.trig[i].fire_arm >> j) & 1u) parent[j] = i;
+    auto first_from = [&](int i, int from) {
+        for (int k = std::max(from, 0); k < n; ++k)
+            if ((tab.time_true[k] >> i) & 1u) return k;
+        return NEVER;
+    };
+    for (int i = 0; i < P.n_trig; ++i) {  // slots are numbered parents first
+        const KxTrig &T = P.trig[i];
+        S.arm[i] = parent[i] < 0 ? 0 : S.fire[parent[i]];
+        if (T.cond_kind == CK_TIME) {
+            S.fire[i] = S.arm[i] == NEVER ? NEVER : first_from(i, S.arm[i]);
+        } else if (T.kind == TK_WHEN) {
+            S.static_ok = false;
+        }
+    }
+    for (int j = 0; j < P.n_leaf; ++j) {
+        int acq = -1;
+        for (int i = 0; i < P.n_trig; ++i)
+            if (P.trig[i].kind == TK_WHEN && ((P.trig[i].leaves >> j) & 1u)) acq = i;
+        const int t = acq < 0 ? 0 : S.fire[acq];
+        if (t == NEVER) continue;
+        bool dead = false;
+        uint32_t pu = 0;
+        for (int i = 0; i < P.n_trig; ++i) {
+            const KxTrig &T = P.trig[i];
+            if (T.kind != TK_UNTIL || !((T.leaves >> j) & 1u)) continue;
+            if (T.cond_kind == CK_TIME) {
+                if (S.fire[i] <= t) dead = true;  // knocked at or before the flow (pricer.rs:407-413)
+            } else if (S.arm[i] != NEVER) {
+                pu |= 1u << i;
+            }
+        }
+        if (!dead) S.flows.push_back(StaticSchedule::Flow{j, t, pu});
+    }
+    return S;
+}
+
 }  // namespace kx

@@ -117,4 +117,21 @@ struct StepTables {
 void bind(const Lowered &low, const std::vector<double> &grid, const Model &m, double rate,
           KxProgram &out, StepTables &tab);
 
+// Static schedule of a bound program whose when/anytime conditions depend on
+// time only: every slot's arming and firing step is then path-independent.
+// until slots with price conditions are listed in `price_untils` (their
+// arming step is static too); time-only untils knock at a static step.
+struct StaticSchedule {
+    static constexpr int NEVER = 0x7fffffff;
+    std::vector<int> arm, fire;        // per trigger slot (fire = knock step for untils)
+    struct Flow {
+        int leaf;
+        int step;                      // the flow date (grid index)
+        uint32_t price_untils;         // price-condition until slots above the flow
+    };
+    std::vector<Flow> flows;           // flows that are paid (not knocked by a time-only until)
+    bool static_ok = true;             // false if some when/anytime condition reads prices
+};
+StaticSchedule static_schedule(const KxProgram &P, const StepTables &tab);
+
 }  // namespace kx

@@ -370,7 +370,7 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const Path
             L.nte[s] = H.init_nte;
             return false;
         }
-        if (!bits) return false;
+        if (!bits && k != 0) return false;
         if (bits == H.fast_bit && (H.flags & HF_FAST_UNTIL) && k > 0) {  // barrier knock-out, inline
             L.resolved[s] |= bits;
             L.dead[s] |= H.fast_kill & ~L.emitted[s];
