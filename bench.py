@@ -11,8 +11,11 @@ call over that batch.
              steps (a 256 MB write);
   e2e        the same metric through the C ABI call kx_price from the host
              (lowering, table upload, kernels, result download) by wall clock;
-  roofline   the path kernel against the measured MUFU throughput (the pipe
-             the Box-Muller normals bind on; 2 results per normal);
+  roofline   the path kernel's simulated steps/s against the ceiling measured
+             in the same run: the bare simulation loop (Philox draw,
+             Box-Muller, log-space update, no contract) on the same GPU.
+             The kernel moves 8 bytes per path to HBM and is bound by
+             instruction issue, not by HBM or tensor cores;
   cpu_baseline  the oracle (CPU restatement of the reference pricer) on a
              bounded sample of the same workload on this host's cores.
 
@@ -229,7 +232,7 @@ def run_ours(args, ws, rank, local) -> None:
     for i in range(args.warmup):
         r = price(seed + i)
     peaks = {}
-    for what, name in ((0, "mufu"), (1, "fp32_fma"), (2, "imad_hi")):
+    for what, name in ((0, "mufu"), (1, "fp32_fma"), (2, "imad_hi"), (3, "bare_path_steps")):
         v = C.c_double()
         if lib.kx_measure_peak(what, C.byref(v)) == 0:
             peaks[name] = v.value
@@ -269,24 +272,26 @@ def run_ours(args, ws, rank, local) -> None:
     e2e = {"value": ws * nominal * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
            "ms_per_step": 1e3 * e2e_s / args.steps}
-    # ---- roofline of the path kernel: MUFU results (2 per normal, 1 normal per simulated step) ----
-    xu_ops = 2.0 * sim_steps
-    achieved = xu_ops / (ker_ms * 1e-3) / 1e9
-    peak = peaks.get("mufu", float("nan")) / 1e9
-    prof = os.path.join(ROOT, "profiles", "k_paths_up_and_out_traffic.json")
+    # ---- roofline of the path kernel: simulated steps/s against the bare simulation loop ----
+    achieved = sim_steps / (ker_ms * 1e-3) / 1e9
+    peak = peaks.get("bare_path_steps", float("nan")) / 1e9
+    prof = os.path.join(ROOT, "profiles", "k_lean_up_and_out_traffic.json")
     traffic = None
     if os.path.exists(prof):
         try:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch_full_workload")
         except Exception:
             traffic = None
-    roofline = {"bound": "xu", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+    kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>"}.get(kx.last_launch_stats()["path_kernel"], "?")
+    roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
                 "frac": achieved / peak if peak == peak and peak > 0 else None, "traffic": traffic,
-                "peak_source": "measured in this run by kx_measure_peak (MUFU ex2/lg2 chains)",
-                "kernel": "k_paths<float,GBM,1>", "ops_per_step": "2 MUFU results per normal (Box-Muller)",
+                "peak_source": "measured in this run: kx_measure_peak(3), the bare Philox4x32-10 + Box-Muller "
+                               "+ GBM step loop (no contract, no scheduling) on this GPU",
+                "kernel": kname, "algorithmic_bytes_per_path": 8,
+                "achieved_hbm_gbs": 8.0 * n_paths * args.steps / (ker_ms * 1e-3) / 1e9,
                 "steps_simulated_fraction": sim_steps / (nominal * args.steps),
-                "measured_peaks_gops": {k: v / 1e9 for k, v in peaks.items()},
-                "issue_view_paths_steps_per_s_simulated": sim_steps / (ker_ms * 1e-3)}
+                "mufu_results_per_s_share": 2.0 * sim_steps / (ker_ms * 1e-3) / peaks.get("mufu", float("nan")),
+                "measured_peaks_per_s": dict(peaks)}
     greeks = None if args.no_greeks else price_greeks(c, m, n_paths, seed, w["steps_per_year"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

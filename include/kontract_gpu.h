@@ -149,7 +149,8 @@ typedef struct kx_launch_stats {
     uint32_t kernel_launches;  /* kernels launched by the call */
     uint32_t grid_blocks;
     uint32_t block_threads;
-    uint32_t reserved;
+    uint32_t path_kernel;      /* last path kernel: 0 none, 1 k_paths (every
+                                  contract), 2 k_lean (barrier/time contracts) */
     uint64_t h2d_bytes, d2h_bytes;
 } kx_launch_stats;
 
@@ -251,7 +252,9 @@ kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model,
  * of one GPU pipe on device 0, used as the roofline denominator of the path
  * kernels. what = 0: MUFU (lg2/ex2/sin/cos approximations, results/s);
  * 1: FP32 FMA (FMAs/s); 2: 32-bit integer multiply-high (IMAD.HI/s, the
- * Philox multiply). */
+ * Philox multiply); 3: FP32 GBM steps/s of the bare simulation loop (Philox
+ * draw, Box-Muller, log-space update; no contract, no scheduling), the
+ * ceiling of the path kernels. */
 kx_status kx_measure_peak(int32_t what, double *ops_per_s);
 
 /* Counters of the last pricing call (see kx_launch_stats). */

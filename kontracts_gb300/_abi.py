@@ -93,7 +93,7 @@ class KxLaunchStats(C.Structure):
         ("kernel_ms", C.c_double), ("reduce_ms", C.c_double), ("total_ms", C.c_double),
         ("path_steps", C.c_uint64), ("steps_simulated", C.c_uint64),
         ("kernel_launches", C.c_uint32), ("grid_blocks", C.c_uint32),
-        ("block_threads", C.c_uint32), ("reserved", C.c_uint32),
+        ("block_threads", C.c_uint32), ("path_kernel", C.c_uint32),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
     ]
 

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
             if (MODEL == KX_MODEL_GBM) y += rec.c0 + rec.c1 * z[q];
             else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[q], z[q + 1], y, v);
             if (k == nf) {
-                pay_flows<Real>(A, k, s0 * fast_exp<Real>(y), path);
+                pay_flows<Real>(A, k, spot_of<Real>(s0, y), path);
                 nf = A.next[k + 1];
             }
         }

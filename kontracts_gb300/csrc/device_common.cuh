@@ -67,6 +67,15 @@ __device__ __forceinline__ float fast_exp<float>(float x) { return __expf(x); }
 template <>
 __device__ __forceinline__ double fast_exp<double>(double x) { return exp(x); }
 
+// S = s0 * exp(y) rounded once, so that no later use is fused into an FMA
+// with it: every kernel then sees the same S bit for bit.
+template <class Real>
+__device__ __forceinline__ Real spot_of(Real s0, Real y);
+template <>
+__device__ __forceinline__ float spot_of<float>(float s0, float y) { return __fmul_rn(s0, __expf(y)); }
+template <>
+__device__ __forceinline__ double spot_of<double>(double s0, double y) { return __dmul_rn(s0, exp(y)); }
+
 // ---------------------------------------------------------------------------
 // Accumulators live in shared memory, one column per thread:
 // slot j of this thread is base[j * stride].

@@ -79,13 +79,25 @@ struct KxTrig {
 
 enum KxAmountKind : uint8_t { AK_CONST = 0, AK_GENERAL = 1 };
 
+// Closed forms of the commonest AK_GENERAL amounts, evaluated inline with the
+// interpreter's own operations (same result bit for bit); the result is
+// negated when sign < 0.
+enum KxFastAmount : uint8_t {
+    FA_NONE = 0,
+    FA_CALL = 1,   // max(S - K, 0)
+    FA_PUT = 2,    // max(K - S, 0)
+    FA_SPOT = 3,   // S
+    FA_CONST = 4,  // K
+};
+
 struct KxLeaf {
     uint8_t kind;       // KxAmountKind
     uint8_t err_capable;
     uint16_t code_off;
     uint16_t code_len;
-    uint16_t pad;
-    double sign;        // AK_CONST amount (+1 / -1)
+    uint8_t fast;       // KxFastAmount of an AK_GENERAL amount
+    uint8_t fast_k;     // its constant K: index into cpool
+    double sign;        // AK_CONST amount (+1 / -1); sign of a fast amount
 };
 
 enum KxAccKind : uint8_t { ACC_MAX = 0, ACC_MIN = 1, ACC_SUM = 2 };
@@ -118,7 +130,7 @@ struct KxProgram {
     uint32_t all_leaves;
     uint32_t err_capable;  // some evaluation can raise MalformedContract / look-ahead
     uint32_t spot_each_step; // some accumulator or general condition reads S every step
-    uint32_t pad0;
+    uint32_t simple_leaves;  // flow slots whose amount is AK_CONST or has a fast form
     KxTrig trig[KX_MAX_TRIG];
     KxLeaf leaf[KX_MAX_LEAF];
     KxAcc acc[KX_MAX_ACC];

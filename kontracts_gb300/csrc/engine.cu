@@ -25,7 +25,8 @@
 
 #include "device_common.cuh"
 #include "engine.hpp"
-#include "paths_kernel.cuh"
+#include "launch.hpp"
+#include "stats.cuh"
 
 namespace kx {
 
@@ -94,30 +95,6 @@ struct ChunkDesc {
     uint32_t count;
     uint32_t pad;
 };
-struct ChunkOut {
-    double n, mean, m2;
-};
-
-__device__ __forceinline__ double block_sum(double v, double *red) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) red[0] = t;
-    __syncthreads();
-    t = red[0];
-    __syncthreads();
-    return t;
-}
-
 __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns,
                                                      const double *__restrict__ w, const ChunkDesc *__restrict__ ch,
                                                      ChunkOut *__restrict__ out) {
@@ -145,7 +122,7 @@ __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ 
 }
 
 std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, const std::vector<StatsJob> &jobs) {
-    const uint32_t CH = 16384;
+    const uint32_t CH = KX_STATS_CHUNK;
     std::vector<ChunkDesc> chunks;
     std::vector<size_t> first(jobs.size() + 1, 0);
     for (size_t j = 0; j < jobs.size(); ++j) {
@@ -220,15 +197,7 @@ kx_price_result finish(const Stats &s) {  // pricer.rs:303-328
 // ---------------------------------------------------------------------------
 // host side of a path launch
 // ---------------------------------------------------------------------------
-struct Job {  // one contract of a launch
-    KxProgram prog;
-    StepTables tab;
-    ContractDev dev;
-    Model model;
-    std::vector<double> thr;  // [KX_MAX_NS][KX_MAX_SPOT] log(B / s0_s)
-};
-
-static void check_cfg(const kx_mc_config *cfg) {
+void check_cfg(const kx_mc_config *cfg) {
     if (!cfg) raise(KX_INVALID_ARGUMENT, "config is NULL");
     if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
     if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
@@ -236,13 +205,8 @@ static void check_cfg(const kx_mc_config *cfg) {
     if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
 }
 
-// Scenario parameters (bump scenarios share the normals of a path).
-struct Scenario {
-    double s0, mu, sigma, rate;
-};
-
-static Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, const std::vector<double> &grid,
-                    const std::vector<Scenario> &scen_in, int smooth, double smooth_w) {
+Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, const std::vector<double> &grid,
+             const std::vector<Scenario> &scen_in, int smooth, double smooth_w) {
     Job j;
     j.model = m;
     validate_model(m);
@@ -321,25 +285,48 @@ static Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, c
 }
 
 template <class Real>
-static void pack_steps(const StepTables &t, std::vector<unsigned char> &out) {
+void pack_steps(const StepTables &t, std::vector<unsigned char> &out) {
     const size_t n = t.c0.size();
     const size_t off = out.size();
     out.resize(off + n * sizeof(StepRec<Real>));
     StepRec<Real> *r = reinterpret_cast<StepRec<Real> *>(out.data() + off);
     for (size_t k = 0; k < n; ++k) r[k] = StepRec<Real>{(Real)t.c0[k], (Real)t.c1[k], t.time_true[k], 0u};
 }
+template void pack_steps<float>(const StepTables &, std::vector<unsigned char> &);
+template void pack_steps<double>(const StepTables &, std::vector<unsigned char> &);
 
 // Launch the fused path kernel over `jobs` (all of one model kind, one
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
-static const void *select_kernel(int model, bool f64, int ns, int minb) {
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean) {
+    if (lean) return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb) : lean_kernel_heston(f64, minb);
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
     if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
     return paths_kernel_heston(f64, minb);
 }
 
+// k_lean serves launches whose contracts test the price only through
+// Spot-cmp-Const conditions and keep no averages or extrema (one scenario,
+// no smoothing). Both kernels value every path identically; KX_PATH_KERNEL
+// = "general" or "lean" forces one of them (the lean one only where it applies).
+static bool lean_applies(const std::vector<Job> &jobs, int ns) {
+    if (ns != 1) return false;
+    for (auto &j : jobs) {
+        if (j.dev.smooth || j.prog.n_acc || j.prog.spot_each_step) return false;
+        for (int i = 0; i < j.prog.n_trig; ++i)
+            if (j.prog.trig[i].cond_kind == CK_GENERAL) return false;
+    }
+    return true;
+}
+
+bool use_lean(const std::vector<Job> &jobs, int ns) {
+    const char *env = getenv("KX_PATH_KERNEL");
+    if (env && strcmp(env, "general") == 0) return false;
+    return lean_applies(jobs, ns);
+}
+
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
-                            int minb);
+                            int minb, bool lean);
 
 // Project autotuner: the path kernel exists at a few register budgets
 // (minimum resident blocks per SM). The first launch of each kind (model,
@@ -362,15 +349,23 @@ static std::string tune_key(const std::vector<Job> &jobs, const kx_mc_config &cf
         for (int i = 0; i < j.prog.n_trig; ++i) gen |= j.prog.trig[i].cond_kind == CK_GENERAL;
     }
     char buf[128];
-    snprintf(buf, sizeof buf, "m%d-p%d-ns%d-acc%d-gen%d-sm%d-sp%d", jobs[0].model.kind, cfg.precision, ns, acc > 0, gen,
-             smooth, spot);
+    snprintf(buf, sizeof buf, "m%d-p%d-ns%d-acc%d-gen%d-sm%d-sp%d-l%d", jobs[0].model.kind, cfg.precision, ns, acc > 0,
+             gen, smooth, spot, use_lean(jobs, ns) ? 1 : 0);
     return buf;
 }
 
-static const int *variants(int model, int ns, int &n) {
+const int *variants(int model, bool f64, int ns, bool lean, int &n) {
     static const int v1[] = {4, 3, 2};
     static const int v7[] = {2, 1};
-    (void)model;
+    static const int l32[] = {4, 5, 6};
+    static const int lg64[] = {4, 3};
+    static const int lh64[] = {3};
+    if (lean) {
+        if (!f64) { n = 3; return l32; }
+        if (model == KX_MODEL_GBM) { n = 2; return lg64; }
+        n = 1;
+        return lh64;
+    }
     if (ns == 1) { n = 3; return v1; }
     n = 2;
     return v7;
@@ -378,7 +373,8 @@ static const int *variants(int model, int ns, int &n) {
 
 static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out) {
     int nv = 0;
-    const int *vs = variants(jobs[0].model.kind, ns, nv);
+    const bool lean = use_lean(jobs, ns);
+    const int *vs = variants(jobs[0].model.kind, cfg.precision == KX_PREC_FP64, ns, lean, nv);
     const char *env = getenv("KX_TUNE");
     const bool tune = !(env && env[0] == '0');
     const std::string key = tune_key(jobs, cfg, ns);
@@ -399,7 +395,7 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
                 for (int rep = 0; rep < 2; ++rep) {
                     c.last.kernel_ms = 0;
                     uint64_t st = 0;
-                    run_paths_v(c, cal, cfg, ns, st, vs[q]);
+                    run_paths_v(c, cal, cfg, ns, st, vs[q], lean);
                     t = std::min(t, (float)c.last.kernel_ms);
                 }
                 e.ms[q] = t;
@@ -416,11 +412,11 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
         }
     }
     const int minb = it != g_tune.end() ? it->second.minb : vs[0];
-    return run_paths_v(c, jobs, cfg, ns, stride_out, minb);
+    return run_paths_v(c, jobs, cfg, ns, stride_out, minb, lean);
 }
 
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
-                            int minb) {
+                            int minb, bool lean) {
     const bool f64 = cfg.precision == KX_PREC_FP64;
     const int model = jobs[0].model.kind;
     std::vector<KxProgram> progs;
@@ -470,7 +466,7 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     const uint32_t surv_base = 2u * (uint32_t)max_acc;
     const uint32_t slots = surv_base + (smooth ? (uint32_t)max_spot : 0u);
     const size_t smem = (size_t)ns * slots * block * (f64 ? 8 : 4);
-    const void *kfn = select_kernel(model, f64, ns, minb);
+    const void *kfn = select_kernel(model, f64, ns, minb, lean);
     if (!kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (smem > 48 * 1024) KX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int full = persistent_blocks(kfn, block, smem);
@@ -540,6 +536,7 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.last.kernel_launches++;
     c.last.grid_blocks = (uint32_t)grid_blocks;
     c.last.block_threads = (uint32_t)block;
+    c.last.path_kernel = lean ? 2u : 1u;
     uint32_t hc[4] = {0, 0, 0, 0};
     KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));
@@ -572,11 +569,11 @@ std::vector<Stats> batch_paths(Ctx &c, const std::vector<const Program *> &progs
     return device_stats(c, c.pv.as<double>(), stride, sj);
 }
 
-static void begin_call(Ctx &c) {
+void begin_call(Ctx &c) {
     memset(&c.last, 0, sizeof c.last);
     c.last.total_ms = -now_ms();
 }
-static void end_call(Ctx &c) { c.last.total_ms += now_ms(); }
+void end_call(Ctx &c) { c.last.total_ms += now_ms(); }
 
 // ---------------------------------------------------------------------------
 // calibration kernels: 8 independent dependency chains per thread, enough
@@ -625,6 +622,27 @@ __global__ void __launch_bounds__(256) k_peak_imad(unsigned *out, int iters) {
     for (int i = 0; i < 8; ++i) t ^= a[i];
     if (t == 12345u) out[threadIdx.x] = t;
 }
+// The bare simulation loop of the path kernels: one Philox4x32-10 block per
+// 4 steps, Box-Muller, the log-space GBM update; no contract, no scheduling.
+// Its step rate is the ceiling of any FP32 GBM path kernel on this RNG.
+__global__ void __launch_bounds__(256) k_peak_path(float *out, int paths_per_thread, int n_steps) {
+    float acc = 0.f;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int q = 0; q < paths_per_thread; ++q) {
+        const uint32_t path = tid * (uint32_t)paths_per_thread + (uint32_t)q;
+        float y = 0.f;
+        for (int b = 0; b < n_steps / 4; ++b) {
+            const uint4 w = philox4x32_10(make_uint4((uint32_t)b, path, 0u, 0u), 42u, 0u);
+            float z[4];
+            box_muller(w.x, w.y, z[0], z[1]);
+            box_muller(w.z, w.w, z[2], z[3]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) y += 1e-4f + 0.013f * z[j];
+        }
+        acc += y;
+    }
+    if (acc == 12345.f) out[threadIdx.x] = acc;
+}
 
 }  // namespace kx
 
@@ -634,7 +652,7 @@ extern "C" {
 
 kx_status kx_measure_peak(int32_t what, double *ops_per_s) {
     return guarded([&] {
-        if (!ops_per_s || what < 0 || what > 2) raise(KX_INVALID_ARGUMENT, "bad arguments");
+        if (!ops_per_s || what < 0 || what > 3) raise(KX_INVALID_ARGUMENT, "bad arguments");
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         c.misc.ensure(4096);
@@ -644,13 +662,15 @@ kx_status kx_measure_peak(int32_t what, double *ops_per_s) {
             KX_CUDA(cudaEventRecord(c.ev0, c.stream));
             if (what == 0) k_peak_mufu<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
             else if (what == 1) k_peak_fma<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
-            else k_peak_imad<<<blocks, threads, 0, c.stream>>>(c.misc.as<unsigned>(), iters);
+            else if (what == 2) k_peak_imad<<<blocks, threads, 0, c.stream>>>(c.misc.as<unsigned>(), iters);
+            else k_peak_path<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), 4, 256);
             KX_CUDA(cudaGetLastError());
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
             KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
-            const double ops = (double)blocks * threads * iters * 8 * (what == 0 ? 2 : 1);
+            const double ops = what == 3 ? (double)blocks * threads * 4 * 256
+                                         : (double)blocks * threads * iters * 8 * (what == 0 ? 2 : 1);
             best = std::max(best, ops / (ms * 1e-3));
         }
         *ops_per_s = best;

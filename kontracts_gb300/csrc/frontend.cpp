@@ -623,6 +623,7 @@ struct Lowerer {
             if (untils >> u & 1u) P.trig[u].leaves |= 1u << j;
         if (scales.empty()) {
             l.kind = AK_CONST;
+            P.simple_leaves |= 1u << j;
             return;
         }
         // amount = scale_1 * scale_2 * ... (then * sign); pricer.rs:391-395
@@ -644,6 +645,31 @@ struct Lowerer {
         l.code_off = (uint16_t)start;
         l.code_len = (uint16_t)(P.n_code - start);
         if (depth > P.max_stack) P.max_stack = depth;
+        fast_form(l);
+    }
+
+    // Recognise the amounts that have a closed form (KxFastAmount).
+    void fast_form(KxLeaf &l) {
+        const KxIns *c = P.code + l.code_off;
+        int n = l.code_len;
+        if (n >= 1 && c[n - 1].op == OP_NEG) --n;  // the sign is kept in l.sign
+        const int j = (int)(&l - P.leaf);
+        auto is_zero = [&](const KxIns &i) { return i.op == OP_CONST && P.cpool[i.arg] == 0.0; };
+        if (n == 1 && c[0].op == OP_SPOT) {
+            l.fast = FA_SPOT;
+        } else if (n == 1 && c[0].op == OP_CONST) {
+            l.fast = FA_CONST;
+            l.fast_k = (uint8_t)c[0].arg;
+        } else if (n == 5 && c[2].op == OP_SUB && is_zero(c[3]) && c[4].op == OP_MAX) {
+            if (c[0].op == OP_SPOT && c[1].op == OP_CONST) {
+                l.fast = FA_CALL;
+                l.fast_k = (uint8_t)c[1].arg;
+            } else if (c[0].op == OP_CONST && c[1].op == OP_SPOT) {
+                l.fast = FA_PUT;
+                l.fast_k = (uint8_t)c[0].arg;
+            }
+        }
+        if (l.fast != FA_NONE && !l.err_capable) P.simple_leaves |= 1u << j;
     }
 };
 

@@ -214,6 +214,21 @@ __device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const Ste
     return bits;
 }
 
+// Amount of a flow slot with a closed form (KxFastAmount): the operations of
+// the interpreter on its code, in the same order, so the value is identical.
+template <class Real>
+__device__ __forceinline__ Real fast_amount(const KxProgram &P, const KxLeaf &F, Real S) {
+    const Real K = (Real)P.cpool[F.fast_k];
+    Real r;
+    switch (F.fast) {
+    case FA_CALL: r = fmax(S - K, Real(0)); break;
+    case FA_PUT: r = fmax(K - S, Real(0)); break;
+    case FA_SPOT: r = S; break;
+    default: r = K; break;
+    }
+    return F.sign < 0.0 ? -r : r;
+}
+
 // Trigger state of one path and scenario, passed by value to the out-of-line
 // event handler so that the kernel's registers never have their address taken.
 struct Trig {
@@ -234,7 +249,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
     const AccView<Real> acc{acc_base, stride};
     const AccView<Real> surv{surv_base, stride};
     const Real inv_w = pick<Real>(Cp->inv_w, Cp->inv_wf);
-    const Real S = s0 * fast_exp<Real>(y);
+    const Real S = spot_of<Real>(s0, y);
     const uint32_t live = st.armed & ~st.resolved;
     if (live & gen_mask) bits |= cond_bits_full<Real>(P, R, thr, smooth, y, S, st.poisoned, live & gen_mask, k, acc, st.err);
     if (smooth) {  // smoothed until weights of the slots armed before this step
@@ -293,6 +308,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
         const bool is_dead = (st.dead >> j) & 1u;
         if (is_dead && !F.err_capable) continue;
         double amt = F.kind == AK_CONST ? F.sign
+                     : F.fast           ? (double)fast_amount<Real>(P, F, S)
                                         : (double)eval_code<Real>(P, F.code_off, F.code_len, acc, st.poisoned, k, S, st.err);
         if (is_dead) continue;
         if (smooth) {
@@ -304,7 +320,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
                 if (T.cond_kind == CK_SPOT_CMP && ((T.leaves >> j) & 1u)) amt *= (double)surv[T.spot_slot];
             }
         }
-        st.pv += amt * D[k];
+        st.pv = __dadd_rn(st.pv, __dmul_rn(amt, D[k]));
         st.emitted |= 1u << j;
     }
     // next step at which a live time-only slot can change
@@ -333,7 +349,7 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const Path
     const AccView<Real> acc{smem + (s * (int)A.slots) * KX_BLOCK + threadIdx.x, KX_BLOCK};
     if (H.n_acc) {  // accumulators (observable.rs:120-140), inner ones first (slot order)
         const KxProgram &P = *H.P;
-        const Real S = H.s0[s] * fast_exp<Real>(L.y[s]);
+        const Real S = spot_of<Real>(H.s0[s], L.y[s]);
         for (int a = 0; a < H.n_acc; ++a) {
             const KxAcc &Ac = P.acc[a];
             if (k < Ac.i_from || k > Ac.i_to) continue;

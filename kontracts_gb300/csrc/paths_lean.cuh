@@ -1,0 +1,337 @@
+// paths_lean.cuh — the path kernel for barrier contracts (k_lean).
+//
+// Same job as k_paths (simulate, evaluate the contract, write one value per
+// path) for the contracts whose price-dependent conditions are all
+// `Spot cmp Const` and which keep no running averages or extrema: European
+// and Bermudan payoffs, single and double barriers (knock-out and knock-in),
+// first-touch and digital contracts, scaled flows. The per-step work of such
+// a contract reduces to one test: the log-spot left the open interval
+// (lo, hi) of the live barriers, or the step reached the next step at which
+// a time condition can change. A lane runs its path without looking at the
+// contract until that test fires; the event itself (firing cascade, flows,
+// knock-out) is the general handler `on_event` of k_paths, so both kernels
+// give the same value for every path.
+//
+// Lanes are not step-synchronous: each lane draws the Philox block of its
+// own next step (4 GBM steps or 2 Heston steps per 128-bit draw) and may
+// stop inside it at an event; after the event it resumes from the same block
+// with the used normals skipped. Idle lanes take new paths at the top of the
+// next block, as in k_paths; step 0 of a new path is its first event, so the
+// kernel has a single call site of the out-of-line handler.
+#pragma once
+#include "paths_kernel.cuh"
+
+namespace kx {
+
+__device__ __forceinline__ float next_up(float t) { return nextafterf(t, INFINITY); }
+__device__ __forceinline__ double next_up(double t) { return ::nextafter(t, (double)INFINITY); }
+__device__ __forceinline__ float next_down(float t) { return nextafterf(t, -INFINITY); }
+__device__ __forceinline__ double next_down(double t) { return ::nextafter(t, -(double)INFINITY); }
+
+// Interval test of the live barrier slots: an up slot (>=, >) fires when
+// y >= hi, a down slot (<=, <) when y <= lo. Strict comparisons use the next
+// representable threshold, which gives the same decision for finite y.
+template <class Real>
+__device__ __forceinline__ void lean_window(const KxProgram &P, const Real *thr, uint32_t live, Real &hi, Real &lo) {
+    hi = Real(INFINITY);
+    lo = Real(-INFINITY);
+    uint32_t m = live & P.price_mask;
+    while (m) {
+        const int i = __ffs(m) - 1;
+        m &= m - 1;
+        const KxTrig &T = P.trig[i];
+        const Real t = thr[T.spot_slot];
+        switch (T.cmp) {
+        case CMP_GE: hi = fmin(hi, t); break;
+        case CMP_GT: hi = fmin(hi, next_up(t)); break;
+        case CMP_LE: lo = fmax(lo, t); break;
+        default: lo = fmax(lo, next_down(t)); break;
+        }
+    }
+}
+
+// Everything the contract does at step k for a lane whose test fired (or at
+// t = 0). Returns the new state; st.done is set when no flow can change.
+template <class Real>
+__device__ __forceinline__ Trig lean_event(const KxProgram *Pp, const ContractDev *Cp, const StepRec<Real> *R,
+                                           const Real *thr, const double *D, Real s0, Real y, int k, Trig st) {
+    const KxProgram &P = *Pp;
+    const uint32_t live = st.armed & ~st.resolved;
+    uint32_t bits = 0;
+    uint32_t m = live & P.price_mask;
+    while (m) {
+        const int i = __ffs(m) - 1;
+        m &= m - 1;
+        const KxTrig &T = P.trig[i];
+        if (cmp_y<Real>(T.cmp, y, thr[T.spot_slot])) bits |= 1u << i;
+    }
+    if (k >= st.nte) bits |= live & P.time_mask & R[k].tt;
+    if (k > 0) {
+        if (!bits) return st;
+        if ((bits & ~P.until_mask) == 0u) {  // knock-out only: drop the flows below, nothing is acquired
+            st.resolved |= bits;
+            uint32_t u = bits;
+            while (u) {
+                const int i = __ffs(u) - 1;
+                u &= u - 1;
+                st.dead |= P.trig[i].leaves & ~st.emitted;
+            }
+            st.done = !P.err_capable && (P.all_leaves & ~(st.emitted | st.dead)) == 0u;
+            return st;
+        }
+    } else if (!bits && !P.root_leaves) {  // nothing happens at t = 0
+        st.nte = P.init_nte;
+        return st;
+    }
+    // Inline when the firing arms nothing new and every acquired flow has a
+    // constant or closed-form amount: on_event's steps in on_event's order
+    // (knock-outs first, then the flows in slot order, then the next time
+    // event), so the value is the same.
+    uint32_t arm = 0, acq = k == 0 ? P.root_leaves : 0u;
+    uint32_t w = bits & P.when_mask;
+    while (w) {
+        const int i = __ffs(w) - 1;
+        w &= w - 1;
+        arm |= P.trig[i].fire_arm;
+        acq |= P.trig[i].leaves;
+    }
+    acq &= ~st.emitted;
+    if ((arm & ~st.armed) == 0u && !P.err_capable && (acq & ~P.simple_leaves) == 0u) {
+        st.resolved |= bits;
+        uint32_t u = bits & P.until_mask;
+        while (u) {
+            const int i = __ffs(u) - 1;
+            u &= u - 1;
+            st.dead |= P.trig[i].leaves & ~st.emitted;
+        }
+        acq &= ~st.dead;
+        if (acq) {
+            const Real S = spot_of<Real>(s0, y);
+            while (acq) {
+                const int j = __ffs(acq) - 1;
+                acq &= acq - 1;
+                const KxLeaf &F = P.leaf[j];
+                const double amt = F.kind == AK_CONST ? F.sign : (double)fast_amount<Real>(P, F, S);
+                st.pv = __dadd_rn(st.pv, __dmul_rn(amt, D[k]));
+                st.emitted |= 1u << j;
+            }
+        }
+        const uint32_t live_t = st.armed & ~st.resolved & P.time_mask;
+        int nte = INT_MAX;
+        if (live_t & ~P.mono_mask) {
+            nte = k + 1;
+        } else {
+            uint32_t t = live_t;
+            while (t) {
+                const int i = __ffs(t) - 1;
+                t &= t - 1;
+                nte = min(nte, P.first_true[i]);
+            }
+        }
+        st.nte = nte;
+        st.done = (P.all_leaves & ~(st.emitted | st.dead)) == 0u;
+        return st;
+    }
+    return on_event<Real>(Pp, Cp, R, thr, D, nullptr, nullptr, KX_BLOCK, s0, y, k, bits, 0u, 0, st);
+}
+
+template <class Real>
+struct HestonPar {
+    Real r, kappa, theta, sigma_v, rho, rho_perp;
+    int scheme;
+};
+
+// The steps of one Philox block from offset `off` on, up to the first step at
+// which the barrier window or the step limit fires (returns true; k is that
+// step) or to the end of the block (k is the next step). UNI: every step has
+// the coefficients (uc0, uc1), so the step table is not read.
+template <class Real, int MODEL, bool UNI>
+__device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Real uc1, const HestonPar<Real> &hp,
+                                           const Real (&zz)[4], int off, Real hi, Real lo, int lim, Real &y, Real &v,
+                                           int &k) {
+    constexpr int SPB = MODEL == M_GBM ? 4 : 2;
+    bool ev = false;
+#pragma unroll
+    for (int j = 0; j < SPB; ++j) {
+        if (j >= off && !ev) {
+            Real c0 = uc0, c1 = uc1;
+            if (!UNI) {
+                const StepRec<Real> rec = R[k];
+                c0 = rec.c0;
+                c1 = rec.c1;
+            }
+            if (MODEL == M_GBM) {
+                y += c0 + c1 * zz[j];  // log-space exact GBM step (simulator.rs:238-245)
+            } else {
+                heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
+                                  zz[2 * j], zz[2 * j + 1], y, v);
+            }
+            if (y >= hi || y <= lo || k >= lim) ev = true;
+            else ++k;
+        }
+    }
+    return ev;
+}
+
+template <class Real, int MODEL, int MINB>
+__global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
+    constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
+
+    // warp-uniform work state (path indices are per contract, < 2^32)
+    int cur = -1, pend = -1;
+    uint32_t nx = 0, end = 0;
+    bool drained = false;
+    const KxProgram *P = nullptr;
+    const ContractDev *C = nullptr;
+    const StepRec<Real> *R = nullptr;
+    const Real *thr = nullptr;
+    const double *D = nullptr;
+    uint64_t pv_off = 0, seed = 0;
+    uint32_t stream = 0;
+    int nt = 0;
+    bool uniform = false;
+    Real s0 = 1, uc0 = 0, uc1 = 0;
+    Real hr = 0, hk = 0, hth = 0, hsv = 0, hrho = 0, hrp = 0, hv0 = 0;
+    int scheme = KX_HESTON_REFERENCE_FLOOR;
+
+    // lane state
+    bool busy = false;
+    uint32_t path = 0;
+    int k = 0, lim = 0;
+    Real y = 0, v = 0, hi = 0, lo = 0;
+    Trig st{0, 0, 0, 0, 0, 0, 0, 0, 0.0};
+    uint32_t my_steps = 0;
+
+    while (true) {
+        // ---- hand paths to idle lanes (warp-uniform control) ----
+        unsigned idle = __ballot_sync(FULL, !busy);
+        while (idle) {
+            if (nx >= end) {
+                int it = pend;
+                if (it < 0) {
+                    if (drained) break;
+                    if (lane == 0) it = (int)atomicAdd(A.item_counter, 1u);
+                    it = __shfl_sync(FULL, it, 0);
+                    if (it >= (int)A.n_items) {
+                        drained = true;
+                        break;
+                    }
+                }
+                const WorkItem w = A.items[it];
+                if (w.contract != cur) {
+                    if (cur >= 0 && idle != FULL) {  // finish the current contract first
+                        pend = it;
+                        break;
+                    }
+                    cur = w.contract;
+                    C = A.cons + cur;
+                    P = A.progs + C->prog;
+                    R = reinterpret_cast<const StepRec<Real> *>(A.steps) + C->step_off;
+                    thr = reinterpret_cast<const Real *>(A.thr) + (size_t)cur * KX_MAX_NS * KX_MAX_SPOT;
+                    D = A.disc + C->disc_off;
+                    pv_off = C->pv_off;
+                    seed = C->seed;
+                    stream = C->stream;
+                    nt = C->n_times;
+                    uniform = C->uniform != 0;
+                    s0 = pick<Real>(C->s0[0], C->s0f[0]);
+                    uc0 = pick<Real>(C->uc0, C->uc0f);
+                    uc1 = pick<Real>(C->uc1, C->uc1f);
+                    if (MODEL == M_HESTON) {
+                        hr = pick<Real>(C->r, C->rf);
+                        hk = pick<Real>(C->kappa, C->kappaf);
+                        hth = pick<Real>(C->theta, C->thetaf);
+                        hsv = pick<Real>(C->sigma_v, C->sigma_vf);
+                        hrho = pick<Real>(C->rho, C->rhof);
+                        hrp = pick<Real>(C->rho_perp, C->rho_perpf);
+                        hv0 = pick<Real>(C->v0, C->v0f);
+                        scheme = C->heston_scheme;
+                    }
+                }
+                pend = -1;
+                nx = (uint32_t)w.first;
+                end = (uint32_t)(w.first + w.count);
+                continue;
+            }
+            const int nidle = __popc(idle);
+            const uint32_t avail = end - nx;
+            const int take = avail < (uint32_t)nidle ? (int)avail : nidle;
+            const int rank = __popc(idle & lt);
+            if (!busy && rank < take) {
+                // new path: S = s0; the contract at step 0 runs as this lane's first event
+                path = nx + (uint32_t)rank;
+                busy = true;
+                y = Real(0);
+                v = fmax(hv0, Real(0));
+                st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
+                k = 0;
+            }
+            nx += (uint32_t)take;
+            if (take == 0) break;
+            idle = __ballot_sync(FULL, !busy);
+        }
+        if (__ballot_sync(FULL, busy) == 0u) {
+            if (drained && pend < 0 && nx >= end) break;
+            continue;
+        }
+
+        // ---- one Philox block of this lane's path, up to the next event ----
+        if (busy) {
+            bool ev = k == 0;
+            if (!ev) {
+                const uint32_t km1 = (uint32_t)(k - 1);
+                const uint32_t blk = km1 / SPB;
+                const int off = (int)(km1 % SPB);
+                Real zz[4];
+                if (A.z64 == nullptr && A.z32 == nullptr) {
+                    const uint4 w =
+                        philox4x32_10(make_uint4(blk, path, 0u, stream), (uint32_t)seed, (uint32_t)(seed >> 32));
+                    box_muller(w.x, w.y, zz[0], zz[1]);
+                    box_muller(w.z, w.w, zz[2], zz[3]);
+                } else {
+                    const uint64_t d0 = (uint64_t)blk * SPB * DRAWS;
+                    const uint64_t base = (uint64_t)path * A.z_dpp + d0;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        zz[j] = d0 + j < A.z_dpp ? (A.z64 ? (Real)A.z64[base + j] : (Real)A.z32[base + j]) : Real(0);
+                }
+                const int k_in = k;
+                const HestonPar<Real> hp{hr, hk, hth, hsv, hrho, hrp, scheme};
+                if (uniform) ev = lean_steps<Real, MODEL, true>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k);
+                else ev = lean_steps<Real, MODEL, false>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k);
+                my_steps += (uint32_t)(k - k_in) + (ev ? 1u : 0u);
+            }
+            if (ev) {
+                st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
+                lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
+                lim = min(st.nte, nt - 1);
+                ++k;
+                if (st.done || k >= nt) {
+                    A.pv[pv_off + path] = st.pv;
+                    busy = false;
+                }
+            }
+        }
+    }
+    // counters: one atomic per warp
+    unsigned long long tot = (unsigned long long)my_steps;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    uint32_t err = st.err;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) err |= __shfl_xor_sync(FULL, err, o);
+    if (lane == 0) {
+        if (tot) atomicAdd(A.steps_done, tot);
+        if (err) atomicOr(A.err_word, err);
+    }
+}
+
+// which: fp64 0/1; returns nullptr for a missing register budget.
+const void *lean_kernel_gbm(int fp64, int minb);
+const void *lean_kernel_heston(int fp64, int minb);
+
+}  // namespace kx

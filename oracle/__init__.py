@@ -85,6 +85,8 @@ class Oracle:
         L.ko_bs_call_greeks.argtypes = [D] * 5 + [P(D)]
         L.ko_crr_american.restype = D
         L.ko_crr_american.argtypes = [D, D, D, D, D, C.c_int, C.c_int]
+        L.ko_heston_call.restype = D
+        L.ko_heston_call.argtypes = [D] * 9
         if threads:
             L.ko_set_threads(threads)
 
@@ -215,3 +217,6 @@ class Oracle:
 
     def crr_american(self, s0, k, t, r, sigma, n, is_call):
         return self.L.ko_crr_american(s0, k, t, r, sigma, n, int(is_call))
+
+    def heston_call(self, s0, k, t, r, v0, kappa, theta, sigma_v, rho):
+        return self.L.ko_heston_call(s0, k, t, r, v0, kappa, theta, sigma_v, rho)

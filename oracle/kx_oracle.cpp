@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -1214,6 +1215,54 @@ double ko_up_and_out_call(double s, double k, double h, double r, double sigma, 
     double D = phi * s * std::pow(h / s, 2.0 * (mu + 1.0)) * N(eta * y2) -
                phi * k * df * std::pow(h / s, 2.0 * mu) * N(eta * y2 - eta * st);
     return A - B + C - D;
+}
+
+// Heston (1993) European call by Fourier inversion, in the characteristic
+// function form of Albrecher, Mayer, Schoutens and Tistaert, "The little
+// Heston trap" (Wilmott, 2007), which stays on the principal branch of the
+// complex logarithm: C = S0 P1 - K e^{-rT} P2 with
+// Pj = 1/2 + (1/pi) int_0^inf Re[e^{-iu ln K} f_j(u) / (iu)] du,
+// f_2(u) = phi(u), f_1(u) = phi(u - i) / phi(-i), phi the characteristic
+// function of ln S_T. The integral runs over (0, 200] by composite Simpson
+// with 20000 panels. Continuous-time model: the value the discretised
+// schemes (simulator.rs:506-541, full truncation) converge to as dt -> 0.
+// Not in the reference (it has no Heston closed form).
+static std::complex<double> heston_cf(std::complex<double> u, double s0, double t, double r, double v0, double kappa,
+                                      double theta, double sv, double rho) {
+    using cd = std::complex<double>;
+    const cd i(0.0, 1.0);
+    const double sv2 = sv * sv;
+    const cd b = kappa - rho * sv * i * u;
+    const cd d = std::sqrt(b * b + sv2 * (i * u + u * u));
+    const cd g = (b - d) / (b + d);
+    const cd e = std::exp(-d * t);
+    const cd A = i * u * (std::log(s0) + r * t);
+    const cd B = kappa * theta / sv2 * ((b - d) * t - 2.0 * std::log((1.0 - g * e) / (1.0 - g)));
+    const cd Cc = v0 / sv2 * (b - d) * (1.0 - e) / (1.0 - g * e);
+    return std::exp(A + B + Cc);
+}
+
+double ko_heston_call(double s0, double k, double t, double r, double v0, double kappa, double theta, double sigma_v,
+                      double rho) {
+    using cd = std::complex<double>;
+    const cd i(0.0, 1.0);
+    const double lk = std::log(k);
+    const cd phi_mi = heston_cf(cd(0.0, -1.0), s0, t, r, v0, kappa, theta, sigma_v, rho);
+    auto integrand = [&](double u, int j) {
+        const cd uc(u, 0.0);
+        const cd f = j == 1 ? heston_cf(uc - i, s0, t, r, v0, kappa, theta, sigma_v, rho) / phi_mi
+                            : heston_cf(uc, s0, t, r, v0, kappa, theta, sigma_v, rho);
+        return std::real(std::exp(-i * uc * lk) * f / (i * uc));
+    };
+    const int n = 20000;  // even
+    const double a = 1e-8, bnd = 200.0, h = (bnd - a) / n;
+    double p[2];
+    for (int j = 1; j <= 2; ++j) {
+        double acc = integrand(a, j) + integrand(bnd, j);
+        for (int q = 1; q < n; ++q) acc += (q % 2 ? 4.0 : 2.0) * integrand(a + q * h, j);
+        p[j - 1] = 0.5 + acc * h / 3.0 / M_PI;
+    }
+    return s0 * p[0] - k * std::exp(-r * t) * p[1];
 }
 
 // Cox-Ross-Rubinstein binomial tree for American options (tests/j17_lsm.rs:40-72).

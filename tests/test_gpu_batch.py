@@ -89,3 +89,16 @@ def test_portfolio_sensitivities_equal_individual_adjoints():
         assert abs(g.d_sigma - a.d_sigma) <= 1e-12 * max(1.0, abs(a.d_sigma))
         p = c.price(m, n_paths=n, seed=s, steps_per_year=252, precision="fp64")
         assert abs(r.price - p.price) <= 1e-10 * max(1.0, abs(p.price))  # hard-barrier price
+
+
+def test_heston_book_matches_fourier_price(orc):
+    """The Heston book shape (strikes x maturities on one simulation, full
+    truncation, FP32 paths): every price within 3 standard errors plus the
+    Euler bias allowance (0.03 at 252 steps a year) of the Fourier price."""
+    h = kx.heston(100.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.05, asset="X", scheme="full_truncation")
+    ks, ts = (80.0, 95.0, 100.0, 110.0, 120.0), (0.5, 1.0, 2.0)
+    book = [kx.european_call("X", k, t) for t in ts for k in ks]
+    res = kx.price_batch(book, h, n_paths=1_000_000, seed=42, steps_per_year=252)
+    for (t, k), r in zip([(t, k) for t in ts for k in ks], res):
+        cf = orc.heston_call(100.0, k, t, 0.05, 0.04, 2.0, 0.04, 0.3, -0.5)
+        assert abs(r.price - cf) < 3 * r.std_error + 0.03, (k, t, r.price, r.std_error, cf)

@@ -1,0 +1,72 @@
+"""The two path kernels value every path identically: k_lean (barrier and
+time-event contracts) against k_paths (every contract), forced through
+KX_PATH_KERNEL, in both precisions and both models, bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+import kontracts_gb300 as kx
+
+pytestmark = pytest.mark.gpu
+
+S = kx.S("X")
+
+LEAN = {
+    "euro_call": lambda: kx.european_call("X", 100.0, 1.0),
+    "up_and_out": lambda: kx.up_and_out_call("X", 100.0, 130.0, 1.0),
+    "up_and_out_strict": lambda: kx.until(S > 130.0, kx.european_call("X", 100.0, 1.0)),
+    "down_and_out_put": lambda: kx.until(S < 80.0, kx.european_put("X", 100.0, 1.0)),
+    "double_barrier": lambda: kx.until(S >= 125.0, kx.until(S <= 85.0, kx.european_call("X", 100.0, 1.0))),
+    "knock_in": lambda: kx.anytime(S >= 120.0, kx.european_call("X", 100.0, 1.0)),
+    "first_touch_pays": lambda: kx.one() @ (S <= 90.0),
+    "digital": lambda: kx.cash_or_nothing_call("X", 100.0, 10.0, 1.0),
+    "nested_when": lambda: kx.when(kx.at(0.5), kx.until(S <= 95.0, kx.scale(S, kx.one()) @ kx.at(1.0))),
+    "bermudan_strip": lambda: kx.european_call("X", 100.0, 0.3) + kx.european_call("X", 105.0, 0.61)
+    + kx.give(kx.european_put("X", 95.0, 0.9)),
+    "knock_at_zero": lambda: kx.until(S <= 200.0, kx.european_call("X", 100.0, 1.0)),
+    "late_barrier": lambda: kx.when(kx.at(0.4), kx.until(S >= 115.0, kx.european_call("X", 100.0, 1.0))),
+}
+
+
+def _run(c, model, prec, kernel, n=4000, spy=52):
+    old = os.environ.get("KX_PATH_KERNEL")
+    os.environ["KX_PATH_KERNEL"] = kernel
+    try:
+        return c.price(model, n_paths=n, seed=19, steps_per_year=spy, precision=prec, per_path=True)
+    finally:
+        if old is None:
+            del os.environ["KX_PATH_KERNEL"]
+        else:
+            os.environ["KX_PATH_KERNEL"] = old
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", sorted(LEAN))
+def test_lean_equals_general_gbm(name, prec):
+    c = LEAN[name]()
+    m = kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X")
+    r1, p1 = _run(c, m, prec, "general")
+    r2, p2 = _run(c, m, prec, "lean")
+    assert np.array_equal(np.asarray(p1), np.asarray(p2)), name
+    assert r1.price == r2.price and r1.std_error == r2.std_error
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", ["up_and_out", "double_barrier", "knock_in", "bermudan_strip"])
+def test_lean_equals_general_heston(name, prec):
+    c = LEAN[name]()
+    m = kx.heston(100.0, 0.04, 1.5, 0.04, 0.5, -0.7, 0.03, asset="X")
+    _, p1 = _run(c, m, prec, "general", n=2000, spy=100)
+    _, p2 = _run(c, m, prec, "lean", n=2000, spy=100)
+    assert np.array_equal(np.asarray(p1), np.asarray(p2)), name
+
+
+def test_lean_daily_grid_long_paths():
+    """The benchmark's shape (daily grid, barrier far from spot) at a size
+    where lanes hold paths of very different lengths."""
+    c = kx.up_and_out_call("X", 100.0, 200.0, 1.0)
+    m = kx.GBM(s0=180.0, sigma=0.25, r=0.05, asset="X")
+    _, p1 = _run(c, m, "fp32", "general", n=100_000, spy=365)
+    _, p2 = _run(c, m, "fp32", "lean", n=100_000, spy=365)
+    assert np.array_equal(np.asarray(p1), np.asarray(p2))

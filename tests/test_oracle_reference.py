@@ -352,3 +352,19 @@ def test_philox_normals_are_standard(orc):
     assert abs(z.mean()) < 4 / math.sqrt(len(z))
     assert abs(z.var() - 1) < 0.02
     assert not np.array_equal(orc.normals(42, 0, 8), orc.normals(43, 0, 8))
+
+
+def test_heston_closed_form_limits_and_monte_carlo(orc):
+    """The Heston Fourier price (oracle extra, not in the reference): as
+    sigma_v -> 0 it tends to Black-Scholes at sigma = sqrt(theta) = sqrt(v0),
+    linearly in rho * sigma_v; a fine-grid full-truncation Monte Carlo of the
+    oracle agrees within 3 standard errors."""
+    bs = orc.bs_call(100.0, 100.0, 1.0, 0.05, 0.2)
+    d1 = orc.heston_call(100.0, 100.0, 1.0, 0.05, 0.04, 2.0, 0.04, 0.01, -0.5) - bs
+    d2 = orc.heston_call(100.0, 100.0, 1.0, 0.05, 0.04, 2.0, 0.04, 0.001, -0.5) - bs
+    assert abs(d1) < 0.01 and abs(d2) < 0.001 and abs(d1 / d2 - 10.0) < 1.0
+    import kontracts_gb300 as kx
+    m = kx.heston(100.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.05, asset="X", scheme="full_truncation")
+    r = orc.price(kx.european_call("X", 100.0, 1.0).to_json(), m, n_paths=100_000, seed=5, steps_per_year=400)
+    cf = orc.heston_call(100.0, 100.0, 1.0, 0.05, 0.04, 2.0, 0.04, 0.3, -0.5)
+    assert abs(r.price - cf) < 3 * r.std_error + 0.01, (r.price, r.std_error, cf)
