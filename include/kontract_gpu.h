@@ -207,6 +207,23 @@ kx_status kx_price(const kx_program *prog, const kx_model *model,
                    const kx_mc_config *cfg, kx_price_result *out,
                    double *per_path_pv);
 
+/* kx_price for callers that must not allocate device memory while pricing
+ * (no counterpart in the reference). Same arguments and same result as
+ * kx_price; every device buffer of the call lives in one static device array
+ * of fixed size (about 9 MiB), so the call itself allocates nothing.
+ * Limits: n_paths <= KX_FIXED_MAX_PATHS, time grid <= KX_FIXED_MAX_POINTS
+ * points, cfg->rng == KX_RNG_PHILOX; otherwise KX_INVALID_ARGUMENT and nothing
+ * runs. The first call of a process does the set-up (device made current,
+ * address of the array looked up, library stream created): make it before
+ * any stream capture. The array is shared by all calls of the process, so
+ * calls are serialised by the library lock; the call returns when its
+ * results are on the host. */
+#define KX_FIXED_MAX_PATHS 1048576u
+#define KX_FIXED_MAX_POINTS 8192u
+kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_model *model,
+                                 const kx_mc_config *cfg, kx_price_result *out,
+                                 double *per_path_pv);
+
 /* price_batch_gbm (src/pricer.rs:250-294): one shared simulation on the
  * merged grid of all contracts, each contract valued on the same paths. */
 kx_status kx_price_batch_shared(size_t n, const kx_program *const *progs,

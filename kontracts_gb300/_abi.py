@@ -125,6 +125,8 @@ SIGNATURES = {
     "kx_clear_shared_draws": (C.c_int, []),
     "kx_price": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                            C.POINTER(KxPriceResult), C.POINTER(C.c_double)]),
+    "kx_price_fixed_scratch": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
+                                         C.POINTER(KxPriceResult), C.POINTER(C.c_double)]),
     "kx_price_batch_shared": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
                                         C.POINTER(KxMcConfig), C.POINTER(KxPriceResult)]),
     "kx_price_portfolio": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
