@@ -211,6 +211,135 @@ def price_greeks(c, m, n_paths, seed, spy) -> dict:
     }
 
 
+def _dev_seconds(kx) -> float:
+    st = kx.last_launch_stats()
+    return (st["kernel_ms"] + st["reduce_ms"]) * 1e-3
+
+
+def _hbm_peak() -> tuple:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+
+
+def heston_book(reps=3) -> dict:
+    """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
+    {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
+    96 contracts on one shared simulation (price_batch); plus the pathwise
+    adjoint sensitivities (s0, v0, kappa, theta, sigma_v, rho) of the T = 1,
+    K = 100 call with a checkpoint every 16 steps."""
+    import kontracts_gb300 as kx
+    h = kx.heston(100.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.05, asset="S", scheme="full_truncation")
+    ks = [80.0 + 40.0 * i / 31 for i in range(32)]
+    book = [kx.european_call("S", k, t) for t in (0.5, 1.0, 2.0) for k in ks]
+    n = 2_000_000
+    best = None
+    for _ in range(reps):
+        res = kx.price_batch(book, h, n_paths=n, seed=42, steps_per_year=252)
+        t = _dev_seconds(kx)
+        best = t if best is None or t < best else best
+    steps = n * 504
+    adj = None
+    for _ in range(2):
+        a = kx.european_call("S", 100.0, 1.0).adjoint(h, n_paths=n, seed=7, steps_per_year=252, checkpoint_every=16)
+        ta = _dev_seconds(kx)
+        adj = (a, ta) if adj is None or ta < adj[1] else adj
+    a, ta = adj
+    return {"workload": "96 Heston calls (32 strikes x 3 maturities) on one 2M-path simulation, full truncation, "
+                        "252 steps/yr, FP32", "seconds": best, "path_steps_per_s": steps / best,
+            "contracts_per_s": len(book) / best, "price_T1_K100": res[32 + 15].price,
+            "adjoint_T1_K100": {"seconds": ta, "price": a.price, "d_s0": a.d_s0, "d_v0": a.d_v0,
+                                "d_kappa": a.d_kappa, "d_theta": a.d_theta, "d_sigma_v": a.d_sigma_v,
+                                "d_rho": a.d_rho, "se_v0": a.se_v0, "checkpoint_every": 16}}
+
+
+def book_256(reps=5) -> dict:
+    """The 256-contract book (tests/golden/portfolio_256.json: seeded 50/30/20
+    European / up-and-out / arithmetic-Asian calls, uneven paths and steps):
+    (1) prices by replaying the book's CUDA graph; (2) price + delta + vega of
+    every contract by the pathwise adjoint (one launch) against GPU CRN
+    bump-and-reprice of the same smoothed payoffs (h = 1e-3 relative), the
+    bump cost scaled to the adjoint's standard errors (time ~ SE^-2), per
+    contract by its worse Greek."""
+    import kontracts_gb300 as kx
+    fx = json.load(open(os.path.join(ROOT, "tests", "golden", "portfolio_256.json")))["contracts"]
+    cs = [kx.Contract.from_json(c["json"]) for c in fx]
+    ms = [kx.GBM(s0=c["s0"], sigma=c["sigma"], r=c["r"], asset="S") for c in fx]
+    ns = [int(c["n_paths"]) for c in fx]
+    seeds = [int(c["seed"]) for c in fx]
+    t0 = time.perf_counter()
+    book = kx.Book(cs, ms, ns, seeds, steps_per_year=252, tune=True)
+    create_s = time.perf_counter() - t0
+    info = book.info()
+    best = None
+    for _ in range(reps):
+        book.price()
+        t = kx.last_launch_stats()["kernel_ms"] * 1e-3
+        best = t if best is None or t < best else best
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        book.price()
+    e2e = (time.perf_counter() - t0) / reps
+    out = {"workload": "256-contract book, FP32 paths, 252 steps/yr", "n_paths": info["n_paths"],
+           "path_steps": info["path_steps"], "book_create_s": create_s, "tuning": info,
+           "graph_seconds": best, "path_steps_per_s": info["path_steps"] / best, "contracts_per_s": 256 / best,
+           "e2e_seconds": e2e, "e2e_contracts_per_s": 256 / e2e}
+    book.close()
+    # price + delta + vega: adjoint (one launch) vs CRN bump per contract
+    _, sens = kx.price_portfolio(cs, ms, ns, seeds, steps_per_year=252, greeks=True)
+    t_adj = _dev_seconds(kx)
+    t_bump_eq, t_bump, worst = 0.0, 0.0, []
+    for c, m, n, sd, g in zip(cs, ms, ns, seeds, sens):
+        b = c.greeks(m, n_paths=n, seed=sd, steps_per_year=252, bumps=(1e-3, 1e-3, 1e-3), relative=True,
+                     smooth_width=g.smoothing_width)
+        tb = _dev_seconds(kx)
+        scale = max((b.delta_se / max(g.se_s0, 1e-300)) ** 2, (b.vega_se / max(g.se_sigma, 1e-300)) ** 2)
+        t_bump += tb
+        t_bump_eq += tb * scale
+        worst.append(max(abs(g.d_s0 - b.delta) / max(abs(b.delta), 1e-8), abs(g.d_sigma - b.vega) / max(abs(b.vega), 1e-8)))
+    out["price_delta_vega"] = {"adjoint_seconds": t_adj, "bump_seconds": t_bump, "bump_seconds_equal_se": t_bump_eq,
+                               "equal_se_speedup": t_bump_eq / t_adj,
+                               "median_rel_diff_adjoint_vs_bump": sorted(worst)[len(worst) // 2]}
+    return out
+
+
+def lsm_cases(reps=2) -> dict:
+    """American puts by Longstaff-Schwartz: s0 in {36, 40, 44}, K = 40,
+    sigma in {0.2, 0.4}, r = 0.06, T in {1, 2}, 50 dates a year, 1,000,000
+    paths stored FP32, 4 weighted-Laguerre functions. HBM roofline: bytes per
+    path = 4 (store S) + 16 per backward date (read S twice, read and write
+    the FP32 value) + 12 (final value to FP64) per date set."""
+    import kontracts_gb300 as kx
+    peak, src = _hbm_peak()
+    n = 1_000_000
+    cases, tot_s, tot_bytes = [], 0.0, 0.0
+    for s0 in (36.0, 40.0, 44.0):
+        for sig in (0.2, 0.4):
+            for t in (1.0, 2.0):
+                nd = int(50 * t)
+                ds = [t * i / nd for i in range(1, nd + 1)]
+                put = kx.scale((kx.const_(40.0) - kx.S("S")).clip(0.0), kx.one())
+                m = kx.GBM(s0=s0, sigma=sig, r=0.06, asset="S")
+                best = None
+                for _ in range(reps):
+                    r = put.price_american(m, ds, n_paths=n, seed=42, n_basis=4, basis="laguerre")
+                    st = kx.last_launch_stats()
+                    ts = st["kernel_ms"] * 1e-3
+                    best = ts if best is None or ts < best else best
+                byts = n * (4.0 * nd + 16.0 * nd + 12.0)
+                cases.append({"s0": s0, "sigma": sig, "T": t, "price": r.price, "se": r.std_error, "seconds": best,
+                              "hbm_gbs": byts / best / 1e9})
+                tot_s += best
+                tot_bytes += byts
+    ach = tot_bytes / tot_s / 1e9
+    return {"workload": "12 LSM American puts, 1M paths FP32 in HBM, 4 weighted-Laguerre functions",
+            "seconds_total": tot_s, "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                                 "frac": ach / peak, "peak_source": src},
+            "cases": cases}
+
+
 def run_ours(args, ws, rank, local) -> None:
     import torch
 
@@ -304,6 +433,8 @@ def run_ours(args, ws, rank, local) -> None:
     }
     if greeks is not None:
         line["price_greeks"] = greeks
+    if rank == 0 and not args.no_extra:
+        line["other_configs"] = {"heston_book_96": heston_book(), "book_256": book_256(), "lsm_12": lsm_cases()}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:
@@ -321,6 +452,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the Heston book, 256-contract book and LSM lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

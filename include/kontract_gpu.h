@@ -265,6 +265,49 @@ kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model,
                                 size_t n_dates, int32_t n_basis,
                                 kx_price_result *out);
 
+/* kx_price_american_lsm with a choice of regression basis (the reference has
+ * only the monomials): KX_LSM_MONOMIAL = kx_price_american_lsm;
+ * KX_LSM_LAGUERRE regresses on the weighted Laguerre functions
+ * e^(-x/2) L_j(x), j < n_basis, of x = S / s0 (s0 the model's spot). */
+#define KX_LSM_MONOMIAL 0
+#define KX_LSM_LAGUERRE 1
+kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *model,
+                                      const kx_mc_config *cfg, const double *dates,
+                                      size_t n_dates, int32_t n_basis, int32_t basis,
+                                      kx_price_result *out);
+
+/* ---- books: a portfolio priced by replaying one CUDA graph ------------------
+ * No reference counterpart (the reference prices contract by contract,
+ * pricer.rs:97, or one shared simulation, pricer.rs:250). A book lowers and
+ * binds its contracts once, keeps their tables in device memory it owns,
+ * groups them by (model kind, precision, kernel family) and captures the
+ * pricing step (one persistent path kernel per group over its (contract,
+ * path-block) work queue, the chunk statistics, the copy of the results) in
+ * one CUDA graph. Each contract keeps its own model, n_paths, seed and
+ * steps_per_year; prices equal kx_price's contract by contract. Philox only. */
+typedef struct kx_book kx_book;
+#define KX_BOOK_TUNE 1u /* time each group's register budgets and work-item
+                           sizes on the book at creation, keep the fastest */
+typedef struct kx_book_info {
+    uint32_t n_contracts, n_groups;
+    uint64_t n_paths, path_steps;  /* totals over the book */
+    double tune_ms;                /* time spent tuning at creation */
+    uint32_t group_kernel[4];      /* first 4 groups: 1 k_paths, 2 k_lean */
+    uint32_t group_minb[4];        /* tuned register budget */
+    uint32_t group_item_paths[4];  /* tuned paths per work item */
+    uint32_t group_contracts[4];
+} kx_book_info;
+kx_status kx_book_create(size_t n, const kx_program *const *progs,
+                         const kx_model *models, const kx_mc_config *cfgs,
+                         uint32_t flags, kx_book **out);
+/* Replays the graph; out receives n results, contract order. */
+kx_status kx_book_price(kx_book *book, kx_price_result *out);
+/* New model parameters (same kinds) for every contract, uploaded in place:
+ * the next kx_book_price prices the same paths under the new market. */
+kx_status kx_book_set_models(kx_book *book, const kx_model *models);
+kx_status kx_book_get_info(const kx_book *book, kx_book_info *info);
+void kx_book_free(kx_book *book);
+
 /* Calibration microbenchmark (no reference counterpart): measured throughput
  * of one GPU pipe on device 0, used as the roofline denominator of the path
  * kernels. what = 0: MUFU (lg2/ex2/sin/cos approximations, results/s);

@@ -444,9 +444,13 @@ class Contract:
         return Sensitivities(out)
 
     def price_american(self, model, exercise_dates: Sequence[float], n_paths: int = 100_000, seed: int = 42,
-                       n_basis: int = 3, *, precision: str = "fp32", shared_draws: bool = False) -> PriceResult:
+                       n_basis: int = 3, *, precision: str = "fp32", shared_draws: bool = False,
+                       basis: str = "monomial") -> PriceResult:
         """Longstaff-Schwartz American pricing (lsm.rs:80-124); `self` is the
-        exercised payoff, e.g. (K - S).clip(0) * one(USD)."""
+        exercised payoff, e.g. (K - S).clip(0) * one(USD). basis: "monomial"
+        (the reference's) or "laguerre" (weighted Laguerre functions of S/s0)."""
+        if basis not in ("monomial", "laguerre"):
+            raise ValueError("basis must be 'monomial' or 'laguerre'")
         if not isinstance(model, (GBM, Model)):
             raise TypeError("expected a GBM or Model")
         cm = model._c()
@@ -454,8 +458,10 @@ class Contract:
         d = (C.c_double * max(1, len(exercise_dates)))(*[float(x) for x in exercise_dates])
         out = _abi.KxPriceResult()
         with _lock:
-            _check(_lib().kx_price_american_lsm(self._handle().h, C.byref(cm), C.byref(cfg), d,
-                                                len(exercise_dates), int(n_basis), C.byref(out)))
+            _check(_lib().kx_price_american_lsm_basis(self._handle().h, C.byref(cm), C.byref(cfg), d,
+                                                      len(exercise_dates), int(n_basis),
+                                                      _abi.KX_LSM_LAGUERRE if basis == "laguerre" else _abi.KX_LSM_MONOMIAL,
+                                                      C.byref(out)))
         return PriceResult(out)
 
 
@@ -495,6 +501,70 @@ def price_portfolio(contracts: Sequence[Contract], models: Sequence[Any], n_path
     if greeks:
         return res, [Sensitivities(s) for s in sens]
     return res
+
+
+class Book:
+    """A book of contracts priced by replaying one CUDA graph (no reference
+    counterpart): contract i under models[i] with n_paths[i] paths and
+    seeds[i]. Built once (lowering, tables uploaded, launch shape tuned when
+    tune=True, graph captured); price() replays it; set_models() prices the
+    same paths under new model parameters. Prices equal Contract.price's."""
+
+    def __init__(self, contracts: Sequence[Contract], models: Sequence[Any], n_paths: Sequence[int],
+                 seeds: Sequence[int] | int = 42, steps_per_year: int | Sequence[int] = 252, *,
+                 precision: str = "fp32", tune: bool = True):
+        n = len(contracts)
+        if isinstance(seeds, int):
+            seeds = [seeds] * n
+        if isinstance(steps_per_year, int):
+            steps_per_year = [steps_per_year] * n
+        self._contracts = list(contracts)
+        self._handles = [c._handle() for c in contracts]  # keep the programs alive
+        self._rates = [m.rate for m in models]
+        hs = (C.c_void_p * n)(*[h.h.value for h in self._handles])
+        ms = (_abi.KxModel * n)(*[m._c() for m in models])
+        cfgs = (_abi.KxMcConfig * n)(*[_cfg(n_paths[i], seeds[i], steps_per_year[i], models[i].rate, precision, False)
+                                       for i in range(n)])
+        self.n = n
+        self._b = C.c_void_p()
+        with _lock:
+            _check(_lib().kx_book_create(n, hs, ms, cfgs, _abi.KX_BOOK_TUNE if tune else 0, C.byref(self._b)))
+
+    def price(self) -> list[PriceResult]:
+        out = (_abi.KxPriceResult * self.n)()
+        with _lock:
+            _check(_lib().kx_book_price(self._b, out))
+        return [PriceResult(r) for r in out]
+
+    def set_models(self, models: Sequence[Any]) -> None:
+        """New parameters for every contract's model (same kinds and rates
+        as at creation)."""
+        if [m.rate for m in models] != self._rates:
+            raise ValueError("a book keeps each contract's discount rate")
+        ms = (_abi.KxModel * self.n)(*[m._c() for m in models])
+        with _lock:
+            _check(_lib().kx_book_set_models(self._b, ms))
+
+    def info(self) -> dict:
+        i = _abi.KxBookInfo()
+        _check(_lib().kx_book_get_info(self._b, C.byref(i)))
+        g = i.n_groups
+        return {"n_contracts": i.n_contracts, "n_groups": g, "n_paths": i.n_paths, "path_steps": i.path_steps,
+                "tune_ms": i.tune_ms,
+                "groups": [{"kernel": {1: "k_paths", 2: "k_lean"}.get(i.group_kernel[q], "?"),
+                            "minb": i.group_minb[q], "item_paths": i.group_item_paths[q],
+                            "contracts": i.group_contracts[q]} for q in range(min(g, 4))]}
+
+    def close(self) -> None:
+        if self._b:
+            _lib().kx_book_free(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def set_shared_draws(z) -> None:

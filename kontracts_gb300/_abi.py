@@ -17,6 +17,8 @@ KX_SERDE = 5
 KX_MALFORMED_CONTRACT = 6
 KX_UNSUPPORTED = 7
 KX_INVALID_ARGUMENT = 8
+KX_LSM_MONOMIAL = 0
+KX_LSM_LAGUERRE = 1
 KX_CUDA_ERROR = 9
 KX_DEVICE_TIMEOUT = 10
 KX_NO_DEVICE = 11
@@ -106,6 +108,16 @@ class KxPlanInfo(C.Structure):
     ]
 
 
+class KxBookInfo(C.Structure):
+    _fields_ = [
+        ("n_contracts", C.c_uint32), ("n_groups", C.c_uint32), ("n_paths", C.c_uint64), ("path_steps", C.c_uint64),
+        ("tune_ms", C.c_double), ("group_kernel", C.c_uint32 * 4), ("group_minb", C.c_uint32 * 4),
+        ("group_item_paths", C.c_uint32 * 4), ("group_contracts", C.c_uint32 * 4),
+    ]
+
+
+KX_BOOK_TUNE = 1
+
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "libkontract_gpu.so")
 
@@ -139,7 +151,16 @@ SIGNATURES = {
     "kx_price_american_lsm": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                         C.POINTER(C.c_double), C.c_size_t, C.c_int32,
                                         C.POINTER(KxPriceResult)]),
+    "kx_price_american_lsm_basis": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
+                                              C.POINTER(C.c_double), C.c_size_t, C.c_int32, C.c_int32,
+                                              C.POINTER(KxPriceResult)]),
     "kx_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+    "kx_book_create": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel), C.POINTER(KxMcConfig),
+                                 C.c_uint32, C.POINTER(_P)]),
+    "kx_book_price": (C.c_int, [_P, C.POINTER(KxPriceResult)]),
+    "kx_book_set_models": (C.c_int, [_P, C.POINTER(KxModel)]),
+    "kx_book_get_info": (C.c_int, [_P, C.POINTER(KxBookInfo)]),
+    "kx_book_free": (None, [_P]),
     "kx_last_launch_stats": (C.c_int, [C.POINTER(KxLaunchStats)]),
     "kx_device_info": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_int32),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

@@ -90,11 +90,6 @@ double now_ms() {
 // Deterministic chunk statistics: each block takes one fixed chunk of values
 // and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes).
 // ---------------------------------------------------------------------------
-struct ChunkDesc {
-    uint64_t begin;
-    uint32_t count;
-    uint32_t pad;
-};
 __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns,
                                                      const double *__restrict__ w, const ChunkDesc *__restrict__ ch,
                                                      ChunkOut *__restrict__ out) {
@@ -165,20 +160,29 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
     KX_CUDA(cudaEventElapsedTime(&rms, c.ev0, c.ev1));
     c.last.reduce_ms += rms;
     c.last.d2h_bytes += h.size() * sizeof(ChunkOut);
-    for (size_t j = 0; j < jobs.size(); ++j) {
-        Stats s;
-        for (size_t q = first[j]; q < first[j + 1]; ++q) {  // Chan et al. pairwise merge, fixed order
-            const ChunkOut &o = h[q];
-            if (s.n == 0) { s.n = o.n; s.mean = o.mean; s.m2 = o.m2; continue; }
-            const double n = s.n + o.n;
-            const double d = o.mean - s.mean;
-            s.mean = s.mean + d * (o.n / n);
-            s.m2 = s.m2 + o.m2 + d * d * (s.n * o.n / n);
-            s.n = n;
-        }
-        res[j] = s;
-    }
+    for (size_t j = 0; j < jobs.size(); ++j) res[j] = merge_chunks(h.data() + first[j], first[j + 1] - first[j]);
     return res;
+}
+
+Stats merge_chunks(const ChunkOut *h, size_t n) {
+    Stats s;
+    for (size_t q = 0; q < n; ++q) {  // Chan et al. pairwise merge, fixed order
+        const ChunkOut &o = h[q];
+        if (s.n == 0) { s.n = o.n; s.mean = o.mean; s.m2 = o.m2; continue; }
+        const double tn = s.n + o.n;
+        const double d = o.mean - s.mean;
+        s.mean = s.mean + d * (o.n / tn);
+        s.m2 = s.m2 + o.m2 + d * d * (s.n * o.n / tn);
+        s.n = tn;
+    }
+    return s;
+}
+
+void launch_chunk_stats(cudaStream_t s, const double *values, uint64_t stride, int ns, const double *w,
+                        const ChunkDesc *chunks, ChunkOut *out, unsigned n_chunks) {
+    if (!n_chunks) return;
+    k_chunk_stats<<<n_chunks, 256, 0, s>>>(values, stride, ns, w, chunks, out);
+    KX_CUDA(cudaGetLastError());
 }
 
 kx_price_result finish(const Stats &s) {  // pricer.rs:303-328
@@ -415,107 +419,128 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
     return run_paths_v(c, jobs, cfg, ns, stride_out, minb, lean);
 }
 
-static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
-                            int minb, bool lean) {
-    const bool f64 = cfg.precision == KX_PREC_FP64;
-    const int model = jobs[0].model.kind;
-    std::vector<KxProgram> progs;
-    std::vector<unsigned char> steps;
-    std::vector<double> disc;
-    std::vector<ContractDev> cons;
-    std::vector<unsigned char> thr;
-    std::vector<WorkItem> items;
-    uint64_t total = 0, path_steps = 0;
+PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
+                    uint64_t item_paths) {
+    PathPlan P;
+    P.f64 = cfg.precision == KX_PREC_FP64;
+    P.lean = lean;
+    P.model = jobs[0].model.kind;
+    P.ns = ns;
+    P.minb = minb;
+    const bool f64 = P.f64;
     int max_spot = 0, max_acc = 0;
     for (auto &j : jobs) {
         ContractDev d = j.dev;
-        d.prog = (int32_t)progs.size();
-        progs.push_back(j.prog);
-        d.step_off = (int32_t)(steps.size() / (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
-        if (f64) pack_steps<double>(j.tab, steps);
-        else pack_steps<float>(j.tab, steps);
-        d.disc_off = (int32_t)disc.size();
-        disc.insert(disc.end(), j.tab.disc.begin(), j.tab.disc.end());
-        d.pv_off = total;
-        j.dev.pv_off = total;
-        total += d.n_paths;
-        path_steps += d.n_paths * (uint64_t)(d.n_times > 0 ? d.n_times - 1 : 0);
+        d.prog = (int32_t)P.progs.size();
+        P.progs.push_back(j.prog);
+        d.step_off = (int32_t)(P.steps.size() / (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+        if (f64) pack_steps<double>(j.tab, P.steps);
+        else pack_steps<float>(j.tab, P.steps);
+        d.disc_off = (int32_t)P.disc.size();
+        P.disc.insert(P.disc.end(), j.tab.disc.begin(), j.tab.disc.end());
+        d.pv_off = P.total;
+        j.dev.pv_off = P.total;
+        P.total += d.n_paths;
+        P.path_steps += d.n_paths * (uint64_t)(d.n_times > 0 ? d.n_times - 1 : 0);
         max_spot = std::max(max_spot, j.prog.n_spot_cmp);
         max_acc = std::max(max_acc, j.prog.n_acc);
-        const size_t toff = thr.size();
+        const size_t toff = P.thr.size();
         if (f64) {
-            thr.resize(toff + j.thr.size() * sizeof(double));
-            memcpy(thr.data() + toff, j.thr.data(), j.thr.size() * sizeof(double));
+            P.thr.resize(toff + j.thr.size() * sizeof(double));
+            memcpy(P.thr.data() + toff, j.thr.data(), j.thr.size() * sizeof(double));
         } else {
-            thr.resize(toff + j.thr.size() * sizeof(float));
-            float *t = reinterpret_cast<float *>(thr.data() + toff);
+            P.thr.resize(toff + j.thr.size() * sizeof(float));
+            float *t = reinterpret_cast<float *>(P.thr.data() + toff);
             for (size_t q = 0; q < j.thr.size(); ++q) t[q] = (float)j.thr[q];
         }
-        cons.push_back(d);
+        P.cons.push_back(d);
     }
-    c.last.path_steps += path_steps;
-    stride_out = total;
     // work items: contiguous per contract, costliest contracts first
     std::vector<int> order(jobs.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return cons[a].n_paths * (uint64_t)cons[a].n_times > cons[b].n_paths * (uint64_t)cons[b].n_times;
+        return P.cons[a].n_paths * (uint64_t)P.cons[a].n_times > P.cons[b].n_paths * (uint64_t)P.cons[b].n_times;
     });
     const int block = KX_BLOCK;
     const bool smooth = jobs[0].dev.smooth != 0;
-    const uint32_t surv_base = 2u * (uint32_t)max_acc;
-    const uint32_t slots = surv_base + (smooth ? (uint32_t)max_spot : 0u);
-    const size_t smem = (size_t)ns * slots * block * (f64 ? 8 : 4);
-    const void *kfn = select_kernel(model, f64, ns, minb, lean);
-    if (!kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
-    if (smem > 48 * 1024) KX_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int full = persistent_blocks(kfn, block, smem);
+    P.surv_base = 2u * (uint32_t)max_acc;
+    P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
+    P.smem = (size_t)ns * P.slots * block * (f64 ? 8 : 4);
+    P.kfn = select_kernel(P.model, f64, ns, minb, lean);
+    if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
+    if (P.smem > 48 * 1024)
+        KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+    const int full = persistent_blocks(P.kfn, block, P.smem);
     const uint64_t warps_total = (uint64_t)full * (block / 32);
-    uint64_t all_paths = 0;
-    for (auto &d : cons) all_paths += d.n_paths;
-    for (int ci : order) {
-        const uint64_t n = cons[ci].n_paths;
-        uint64_t item = all_paths / std::max<uint64_t>(1, warps_total * 8);
+    uint64_t item = item_paths;
+    if (item == 0) {  // about 8 items per warp, 64..2048 paths each
+        item = P.total / std::max<uint64_t>(1, warps_total * 8);
         item = std::max<uint64_t>(64, std::min<uint64_t>(2048, item));
-        item = (item + 31) / 32 * 32;
-        for (uint64_t b = 0; b < n; b += item) items.push_back(WorkItem{ci, 0, b, std::min(item, n - b)});
     }
-    if (items.empty()) return total;
-    const int grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (items.size() + 7) / 8 + 1);
-    // uploads
-    c.progs.ensure(progs.size() * sizeof(KxProgram));
-    c.steps.ensure(steps.size());
-    c.disc.ensure(disc.size() * sizeof(double));
-    c.cons.ensure(cons.size() * sizeof(ContractDev));
-    c.thr.ensure(thr.size());
-    c.items.ensure(items.size() * sizeof(WorkItem));
-    c.counters.ensure(64);
-    c.pv.ensure(std::max<uint64_t>(1, total * ns) * sizeof(double));
-    KX_CUDA(cudaMemcpyAsync(c.progs.p, progs.data(), progs.size() * sizeof(KxProgram), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.disc.p, disc.data(), disc.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.cons.p, cons.data(), cons.size() * sizeof(ContractDev), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.thr.p, thr.data(), thr.size(), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.items.p, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
-    c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + disc.size() * sizeof(double) +
-                        cons.size() * sizeof(ContractDev) + thr.size() + items.size() * sizeof(WorkItem);
+    item = (item + 31) / 32 * 32;
+    P.item_paths = item;
+    for (int ci : order) {
+        const uint64_t n = P.cons[ci].n_paths;
+        for (uint64_t b = 0; b < n; b += item) P.items.push_back(WorkItem{ci, 0, b, std::min(item, n - b)});
+    }
+    P.grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (P.items.size() + 7) / 8 + 1);
+    return P;
+}
 
+PathArgs path_args(const PathPlan &P, const PathBuffers &B) {
     PathArgs a{};
-    a.progs = c.progs.as<KxProgram>();
-    a.steps = c.steps.p;
-    a.disc = c.disc.as<double>();
-    a.cons = c.cons.as<ContractDev>();
-    a.thr = c.thr.p;
-    a.items = c.items.as<WorkItem>();
-    a.n_items = (uint32_t)items.size();
-    a.slots = slots;
-    a.surv_base = surv_base;
-    a.item_counter = c.counters.as<uint32_t>();
-    a.err_word = c.counters.as<uint32_t>() + 1;
-    a.steps_done = reinterpret_cast<unsigned long long *>(c.counters.as<uint32_t>() + 2);
-    a.pv = c.pv.as<double>();
-    a.pv_stride = total;
+    a.progs = static_cast<const KxProgram *>(B.progs);
+    a.steps = B.steps;
+    a.disc = static_cast<const double *>(B.disc);
+    a.cons = static_cast<const ContractDev *>(B.cons);
+    a.thr = B.thr;
+    a.items = static_cast<const WorkItem *>(B.items);
+    a.n_items = (uint32_t)P.items.size();
+    a.slots = P.slots;
+    a.surv_base = P.surv_base;
+    a.item_counter = B.counters;
+    a.err_word = B.counters + 1;
+    a.steps_done = reinterpret_cast<unsigned long long *>(B.counters + 2);
+    a.pv = B.pv;
+    a.pv_stride = P.total;
+    return a;
+}
+
+void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s) {
+    KX_CUDA(cudaMemcpyAsync(B.progs, P.progs.data(), P.progs.size() * sizeof(KxProgram), cudaMemcpyHostToDevice, s));
+    KX_CUDA(cudaMemcpyAsync(B.steps, P.steps.data(), P.steps.size(), cudaMemcpyHostToDevice, s));
+    KX_CUDA(cudaMemcpyAsync(B.disc, P.disc.data(), P.disc.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    KX_CUDA(cudaMemcpyAsync(B.cons, P.cons.data(), P.cons.size() * sizeof(ContractDev), cudaMemcpyHostToDevice, s));
+    KX_CUDA(cudaMemcpyAsync(B.thr, P.thr.data(), P.thr.size(), cudaMemcpyHostToDevice, s));
+    if (!P.items.empty())
+        KX_CUDA(cudaMemcpyAsync(B.items, P.items.data(), P.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+}
+
+size_t plan_upload_bytes(const PathPlan &P) {
+    return P.progs.size() * sizeof(KxProgram) + P.steps.size() + P.disc.size() * sizeof(double) +
+           P.cons.size() * sizeof(ContractDev) + P.thr.size() + P.items.size() * sizeof(WorkItem);
+}
+
+static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
+                            int minb, bool lean) {
+    PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0);
+    c.last.path_steps += P.path_steps;
+    stride_out = P.total;
+    if (P.items.empty()) return P.total;
+    c.progs.ensure(P.progs.size() * sizeof(KxProgram));
+    c.steps.ensure(P.steps.size());
+    c.disc.ensure(P.disc.size() * sizeof(double));
+    c.cons.ensure(P.cons.size() * sizeof(ContractDev));
+    c.thr.ensure(P.thr.size());
+    c.items.ensure(P.items.size() * sizeof(WorkItem));
+    c.counters.ensure(64);
+    c.pv.ensure(std::max<uint64_t>(1, P.total * ns) * sizeof(double));
+    const PathBuffers B{c.progs.p, c.steps.p, c.disc.p, c.cons.p, c.thr.p, c.items.p, c.counters.as<uint32_t>(),
+                        c.pv.as<double>()};
+    upload_plan(P, B, c.stream);
+    KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
+    c.last.h2d_bytes += plan_upload_bytes(P);
+    PathArgs a = path_args(P, B);
     if (cfg.rng == KX_RNG_SHARED_DRAWS) {
         DrawStore &ds = c.draws;
         if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
@@ -531,11 +556,11 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     }
     void *args[] = {&a};
     KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-    KX_CUDA(cudaLaunchKernel(kfn, dim3(grid_blocks), dim3(block), args, smem, c.stream));
+    KX_CUDA(cudaLaunchKernel(P.kfn, dim3(P.grid_blocks), dim3(KX_BLOCK), args, P.smem, c.stream));
     KX_CUDA(cudaEventRecord(c.ev1, c.stream));
     c.last.kernel_launches++;
-    c.last.grid_blocks = (uint32_t)grid_blocks;
-    c.last.block_threads = (uint32_t)block;
+    c.last.grid_blocks = (uint32_t)P.grid_blocks;
+    c.last.block_threads = (uint32_t)KX_BLOCK;
     c.last.path_kernel = lean ? 2u : 1u;
     uint32_t hc[4] = {0, 0, 0, 0};
     KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
@@ -546,11 +571,14 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     uint64_t sim = 0;
     memcpy(&sim, &hc[2], sizeof sim);
     c.last.steps_simulated += sim;
-    const uint32_t err = hc[1];
+    check_err_word(hc[1]);
+    return P.total;
+}
+
+void check_err_word(uint32_t err) {
     if (err & KX_ERR_LOOKAHEAD)
         raise(KX_UNSUPPORTED, "an average window is read before it closes (look-ahead average)");
     if (err & KX_ERR_MALFORMED) raise(KX_MALFORMED_CONTRACT, "average window inverted or empty at an evaluation date");
-    return total;
 }
 
 // Value `progs` on `grid` with the path kernel, all with the same model,

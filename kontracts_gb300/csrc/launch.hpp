@@ -5,6 +5,7 @@
 
 #include "engine.hpp"
 #include "paths_lean.cuh"
+#include "stats.cuh"
 
 namespace kx {
 
@@ -41,6 +42,47 @@ bool use_lean(const std::vector<Job> &jobs, int ns);
 // Register budgets (minimum resident blocks per SM) of a kernel family; the
 // first is the default when no tuning result is at hand.
 const int *variants(int model, bool f64, int ns, bool lean, int &n);
+
+// Host-side tables and geometry of one path-kernel launch over `jobs`.
+struct PathPlan {
+    bool f64 = false, lean = false;
+    int model = 0, ns = 1, minb = 0;
+    std::vector<KxProgram> progs;
+    std::vector<unsigned char> steps, thr;
+    std::vector<double> disc;
+    std::vector<ContractDev> cons;
+    std::vector<WorkItem> items;
+    uint64_t total = 0, path_steps = 0, item_paths = 0;
+    uint32_t slots = 0, surv_base = 0;
+    size_t smem = 0;
+    const void *kfn = nullptr;
+    int grid_blocks = 0;
+};
+
+// Device buffers a plan's tables are uploaded to (counters: 64 zeroed bytes).
+struct PathBuffers {
+    void *progs, *steps, *disc, *cons, *thr, *items;
+    uint32_t *counters;
+    double *pv;
+};
+
+// Lays out the tables of `jobs` (sets each job's pv offset) and the launch
+// geometry; item_paths = 0 picks the default work-item size.
+PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
+                    uint64_t item_paths);
+PathArgs path_args(const PathPlan &P, const PathBuffers &B);
+void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s);
+size_t plan_upload_bytes(const PathPlan &P);
+
+// Raises the error the device error word of a path launch reports.
+void check_err_word(uint32_t err);
+
+// Merge of consecutive chunk statistics in chunk order (Chan et al.).
+Stats merge_chunks(const ChunkOut *h, size_t n);
+// One launch of the chunk-statistics kernel: chunk q of `chunks` reduces
+// values[s * stride + begin + i] weighted by w[s], s < ns, into out[q].
+void launch_chunk_stats(cudaStream_t s, const double *values, uint64_t stride, int ns, const double *w,
+                        const ChunkDesc *chunks, ChunkOut *out, unsigned n_chunks);
 
 // Per-call bookkeeping of the launch statistics.
 void begin_call(Ctx &c);

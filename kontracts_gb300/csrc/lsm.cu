@@ -41,6 +41,7 @@ struct LsmArgs {
     int model;
     int scheme;
     double s0, v0, kappa, theta, sigma_v, rho, rho_perp, r;
+    double x_scale;    // KX_LSM_LAGUERRE: regressor x = S / x_scale (the model's spot)
     const double *z64;
     const float *z32;
     uint64_t z_dpp;
@@ -151,10 +152,54 @@ __device__ void solve_gauss(double a[LSM_MAXM][LSM_MAXM], double b[LSM_MAXM], in
     }
 }
 
+// Regression basis at spot s: monomials 1, s, ..., s^(M-1) (lsm.rs:273-278),
+// or weighted Laguerre polynomials e^(-x/2) L_j(x), x = s / x_scale, with
+// L_0 = 1, L_1 = 1 - x, (j + 1) L_(j+1) = (2j + 1 - x) L_j - j L_(j-1).
+// Every product and sum is rounded separately (no FMA), as on the host.
+template <int M, int B>
+__device__ __forceinline__ void lsm_basis(double s, double x_scale, double (&phi)[M]) {
+    if (B == KX_LSM_MONOMIAL) {
+        phi[0] = 1.0;
+#pragma unroll
+        for (int j = 1; j < M; ++j) phi[j] = __dmul_rn(phi[j - 1], s);
+    } else {
+        const double x = __ddiv_rn(s, x_scale);
+        const double w = exp(__dmul_rn(-0.5, x));
+        double lm = 1.0, l = __dsub_rn(1.0, x);
+        phi[0] = w;
+        if (M > 1) phi[1] = __dmul_rn(w, l);
+#pragma unroll
+        for (int j = 1; j + 1 < M; ++j) {
+            const double ln = __ddiv_rn(__dsub_rn(__dmul_rn(__dsub_rn((double)(2 * j + 1), x), l), __dmul_rn((double)j, lm)),
+                                        (double)(j + 1));
+            lm = l;
+            l = ln;
+            phi[j + 1] = __dmul_rn(w, l);
+        }
+    }
+}
+
+// Continuation value sum_j c_j phi_j(s): Horner from the top coefficient for
+// monomials (poly_eval, lsm.rs:293-295), the plain sum for Laguerre.
+template <int M, int B>
+__device__ __forceinline__ double lsm_continuation(const double (&c)[M], double s, double x_scale) {
+    double cont = 0.0;
+    if (B == KX_LSM_MONOMIAL) {
+#pragma unroll
+        for (int j = M - 1; j >= 0; --j) cont = __dadd_rn(__dmul_rn(cont, s), c[j]);
+    } else {
+        double phi[M];
+        lsm_basis<M, B>(s, x_scale, phi);
+#pragma unroll
+        for (int j = 0; j < M; ++j) cont = __dadd_rn(cont, __dmul_rn(c[j], phi[j]));
+    }
+    return cont;
+}
+
 // One backward launch: update the values with the decision of date `upd`
 // (upd < 0: initialise them with the payoff at the last date), then
 // accumulate the regression of date `gram` (gram < 0: none).
-template <class Real, int M>
+template <class Real, int M, int B>
 __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd, int gram) {
     constexpr int NA = M * (M + 1) / 2;
     constexpr int NS = NA + M + 1;  // A upper triangle, A^T y, ITM count
@@ -187,11 +232,7 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
             double nv = discounted;
             if (pay > Real(0)) {
                 double cont = discounted;
-                if (have) {  // poly_eval, lsm.rs:293-295 (Horner from the top coefficient)
-                    cont = 0.0;
-#pragma unroll
-                    for (int j = M - 1; j >= 0; --j) cont = __dadd_rn(__dmul_rn(cont, (double)s), cu[j]);
-                }
+                if (have) cont = lsm_continuation<M, B>(cu, (double)s, A.x_scale);
                 nv = (double)pay > cont ? (double)pay : discounted;
             }
             val = (Real)nv;
@@ -203,9 +244,7 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
                 const double x = (double)sg;
                 const double y = (double)val * disc_g;
                 double pw[M];
-                pw[0] = 1.0;
-#pragma unroll
-                for (int j = 1; j < M; ++j) pw[j] = __dmul_rn(pw[j - 1], x);
+                lsm_basis<M, B>(x, A.x_scale, pw);
                 int q = 0;
 #pragma unroll
                 for (int r = 0; r < M; ++r)
@@ -256,32 +295,38 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_final(const LsmArgs A) {
         A.pv[i] = (double)V[i] * d0;
 }
 
-template <class Real, int M>
-static void launch_steps(Ctx &c, const LsmArgs &a, int blocks) {
+template <class Real, int M, int B>
+static void launch_steps_b(Ctx &c, const LsmArgs &a, int blocks) {
     const int n_ex = a.n_ex;
-    k_lsm_step<Real, M><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, -1, n_ex - 2);
+    k_lsm_step<Real, M, B><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, -1, n_ex - 2);
     KX_CUDA(cudaGetLastError());
     c.last.kernel_launches++;
     for (int d = n_ex - 2; d >= 0; --d) {
-        k_lsm_step<Real, M><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, d, d - 1);
+        k_lsm_step<Real, M, B><<<blocks, LSM_BLOCK, 0, c.stream>>>(a, d, d - 1);
         KX_CUDA(cudaGetLastError());
         c.last.kernel_launches++;
     }
 }
 
+template <class Real, int M>
+static void launch_steps(Ctx &c, const LsmArgs &a, int blocks, int basis) {
+    if (basis == KX_LSM_LAGUERRE) launch_steps_b<Real, M, KX_LSM_LAGUERRE>(c, a, blocks);
+    else launch_steps_b<Real, M, KX_LSM_MONOMIAL>(c, a, blocks);
+}
+
 template <class Real>
-static void run_lsm(Ctx &c, LsmArgs &a, int m, int model) {
+static void run_lsm(Ctx &c, LsmArgs &a, int m, int model, int basis) {
     const int blocks = c.sm_count * 4;
     if (model == KX_MODEL_GBM) k_lsm_forward<Real, KX_MODEL_GBM><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
     else k_lsm_forward<Real, KX_MODEL_HESTON><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
     KX_CUDA(cudaGetLastError());
     c.last.kernel_launches++;
     switch (m) {
-    case 2: launch_steps<Real, 2>(c, a, blocks); break;
-    case 3: launch_steps<Real, 3>(c, a, blocks); break;
-    case 4: launch_steps<Real, 4>(c, a, blocks); break;
-    case 5: launch_steps<Real, 5>(c, a, blocks); break;
-    default: launch_steps<Real, 6>(c, a, blocks); break;
+    case 2: launch_steps<Real, 2>(c, a, blocks, basis); break;
+    case 3: launch_steps<Real, 3>(c, a, blocks, basis); break;
+    case 4: launch_steps<Real, 4>(c, a, blocks, basis); break;
+    case 5: launch_steps<Real, 5>(c, a, blocks, basis); break;
+    default: launch_steps<Real, 6>(c, a, blocks, basis); break;
     }
     k_lsm_final<Real><<<blocks, LSM_BLOCK, 0, c.stream>>>(a);
     KX_CUDA(cudaGetLastError());
@@ -292,10 +337,11 @@ static void run_lsm(Ctx &c, LsmArgs &a, int m, int model) {
 
 using namespace kx;
 
-extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
-                                           const double *dates, size_t n_dates, int32_t n_basis,
-                                           kx_price_result *out) {
+extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *model,
+                                                 const kx_mc_config *cfg, const double *dates, size_t n_dates,
+                                                 int32_t n_basis, int32_t basis, kx_price_result *out) {
     return guarded([&] {
+        if (basis != KX_LSM_MONOMIAL && basis != KX_LSM_LAGUERRE) raise(KX_INVALID_ARGUMENT, "unknown LSM basis");
         const Program &p = program_of(prog);
         Model m = model_from_c(model);
         if (!cfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
@@ -364,6 +410,7 @@ extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_mode
         a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
         a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
         a.r = m.r;
+        a.x_scale = m.s0;
         if (cfg->rng == KX_RNG_SHARED_DRAWS) {
             DrawStore &ds = c.draws;
             if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
@@ -381,8 +428,8 @@ extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_mode
         a.ticket = c.counters.as<unsigned>();
         if (np > 0) {
             KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-            if (f64) run_lsm<double>(c, a, n_basis, m.kind);
-            else run_lsm<float>(c, a, n_basis, m.kind);
+            if (f64) run_lsm<double>(c, a, n_basis, m.kind, basis);
+            else run_lsm<float>(c, a, n_basis, m.kind, basis);
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
@@ -396,4 +443,10 @@ extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_mode
         *out = finish(device_stats(c, c.pv.as<double>(), np, sj)[0]);
         c.last.total_ms += now_ms();
     });
+}
+
+extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                                           const double *dates, size_t n_dates, int32_t n_basis,
+                                           kx_price_result *out) {
+    return kx_price_american_lsm_basis(prog, model, cfg, dates, n_dates, n_basis, KX_LSM_MONOMIAL, out);
 }

@@ -17,7 +17,8 @@
 // stop inside it at an event; after the event it resumes from the same block
 // with the used normals skipped. Idle lanes take new paths at the top of the
 // next block, as in k_paths; step 0 of a new path is its first event, so the
-// kernel has a single call site of the out-of-line handler.
+// kernel has a single call site of the out-of-line handler. Lanes with an
+// event wait for one another (GBM) so that one handler round serves several.
 #pragma once
 #include "paths_kernel.cuh"
 
@@ -180,6 +181,13 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     const unsigned lt = (1u << lane) - 1u;
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
     constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
+    // Event batching: a lane whose path reached an event waits (up to
+    // EV_WAIT blocks) until EV_BATCH lanes of its warp have one, so the
+    // handler runs once for many lanes instead of once per lane. Worth it
+    // for GBM, whose blocks are short next to the handler; a Heston block is
+    // long enough that waiting costs more than it saves.
+    constexpr int EV_BATCH = MODEL == M_GBM ? 8 : 1;
+    constexpr int EV_WAIT = 8;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
     int cur = -1, pend = -1;
@@ -205,6 +213,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     Real y = 0, v = 0, hi = 0, lo = 0;
     Trig st{0, 0, 0, 0, 0, 0, 0, 0, 0.0};
     uint32_t my_steps = 0;
+    bool evp = false;  // this lane waits with an event at step k
+    int wait = 0;      // warp-uniform: blocks since the last handler round
 
     while (true) {
         // ---- hand paths to idle lanes (warp-uniform control) ----
@@ -280,9 +290,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
         }
 
         // ---- one Philox block of this lane's path, up to the next event ----
-        if (busy) {
-            bool ev = k == 0;
-            if (!ev) {
+        bool ev = busy && (k == 0 || evp);  // a waiting event or step 0 of a new path
+        if (busy && !ev) {
+            {
                 const uint32_t km1 = (uint32_t)(k - 1);
                 const uint32_t blk = km1 / SPB;
                 const int off = (int)(km1 % SPB);
@@ -305,14 +315,26 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 else ev = lean_steps<Real, MODEL, false>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k);
                 my_steps += (uint32_t)(k - k_in) + (ev ? 1u : 0u);
             }
-            if (ev) {
-                st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
-                lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
-                lim = min(st.nte, nt - 1);
-                ++k;
-                if (st.done || k >= nt) {
-                    A.pv[pv_off + path] = st.pv;
-                    busy = false;
+        }
+        // ---- events: handled together once enough lanes wait for one ----
+        evp = ev;
+        const unsigned pm = __ballot_sync(FULL, evp);
+        if (pm) {
+            const unsigned run = __ballot_sync(FULL, busy && !evp);  // lanes still stepping
+            const unsigned k0 = __ballot_sync(FULL, evp && k == 0);  // new paths wait for step 0
+            ++wait;
+            if (__popc(pm) >= EV_BATCH || run == 0u || wait >= EV_WAIT || k0) {
+                wait = 0;
+                if (evp) {
+                    evp = false;
+                    st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
+                    lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
+                    lim = min(st.nte, nt - 1);
+                    ++k;
+                    if (st.done || k >= nt) {
+                        A.pv[pv_off + path] = st.pv;
+                        busy = false;
+                    }
                 }
             }
         }

@@ -10,6 +10,11 @@ namespace kx {
 // or blocks a launch has, so every launch shape gives the same result.
 constexpr uint32_t KX_STATS_CHUNK = 16384;
 
+struct ChunkDesc {
+    uint64_t begin;
+    uint32_t count;
+    uint32_t pad;
+};
 struct ChunkOut {
     double n, mean, m2;
 };

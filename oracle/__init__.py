@@ -76,6 +76,8 @@ class Oracle:
                                 P(_abi.KxGreeks)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
+        L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
+                                              C.c_int, C.c_int, P(_abi.KxPriceResult), P(D)]
         for f, n in [("ko_bs_call", 5), ("ko_bs_put", 5), ("ko_down_and_out_call", 6), ("ko_up_and_out_call", 6),
                      ("ko_norm_cdf_as", 1)]:
             fn = getattr(L, f)
@@ -182,15 +184,15 @@ class Oracle:
         return {k: getattr(g, k) for k, _ in g._fields_}
 
     def price_american(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
-                       per_path=False):
+                       per_path=False, basis="monomial"):
         cm = _model_c(model)
         cfg = self.cfg(n_paths, seed, 50, _rate(model, None), shared)
         d = (C.c_double * len(dates))(*dates)
         r = _abi.KxPriceResult()
         pp = np.zeros(max(1, n_paths)) if per_path else None
-        self._chk(self.L.ko_price_american(js.encode(), C.byref(cm), C.byref(cfg), d, len(dates), n_basis,
-                                           C.byref(r),
-                                           pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
+        self._chk(self.L.ko_price_american_basis(js.encode(), C.byref(cm), C.byref(cfg), d, len(dates), n_basis,
+                                                 1 if basis == "laguerre" else 0, C.byref(r),
+                                                 pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
         return (Result(r), pp[:n_paths]) if per_path else Result(r)
 
     def value_on_path(self, js: str, times, values, asset: str = "S", rate: float = 0.0) -> float:

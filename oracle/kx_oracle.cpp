@@ -855,6 +855,44 @@ std::vector<double> poly_fit(const std::vector<double> &xs, const std::vector<do
     }
     return solve_linear(ata, aty);
 }
+// Weighted Laguerre basis e^(-x/2) L_j(x), x = s / x_scale, j < m (an extra
+// mode; the reference regresses on monomials only): L_0 = 1, L_1 = 1 - x,
+// (j + 1) L_(j+1) = (2j + 1 - x) L_j - j L_(j-1).
+void laguerre_basis(double s, double x_scale, size_t m, std::vector<double> &phi) {
+    const double x = s / x_scale;
+    const double w = std::exp(-0.5 * x);
+    double lm = 1.0, l = 1.0 - x;
+    phi[0] = w;
+    if (m > 1) phi[1] = w * l;
+    for (size_t j = 1; j + 1 < m; ++j) {
+        const double ln = ((double)(2 * j + 1) - x) * l - (double)j * lm;
+        const double lnn = ln / (double)(j + 1);
+        lm = l;
+        l = lnn;
+        phi[j + 1] = w * l;
+    }
+}
+std::vector<double> laguerre_fit(const std::vector<double> &xs, const std::vector<double> &ys, size_t m,
+                                 double x_scale) {
+    std::vector<std::vector<double>> ata(m, std::vector<double>(m, 0.0));
+    std::vector<double> aty(m, 0.0), phi(m);
+    for (size_t k = 0; k < xs.size(); ++k) {
+        laguerre_basis(xs[k], x_scale, m, phi);
+        for (size_t r = 0; r < m; ++r) {
+            aty[r] += phi[r] * ys[k];
+            for (size_t c = 0; c < m; ++c) ata[r][c] += phi[r] * phi[c];
+        }
+    }
+    return solve_linear(ata, aty);
+}
+double laguerre_eval(const std::vector<double> &c, double s, double x_scale) {
+    std::vector<double> phi(c.size());
+    laguerre_basis(s, x_scale, c.size(), phi);
+    double acc = 0.0;
+    for (size_t j = 0; j < c.size(); ++j) acc += c[j] * phi[j];
+    return acc;
+}
+
 double poly_eval(const std::vector<double> &c, double x) {  // lsm.rs:293-295
     double acc = 0.0;
     for (size_t i = c.size(); i-- > 0;) acc = acc * x + c[i];
@@ -1056,8 +1094,8 @@ int ko_greeks(const char *json, const kx_model *model, const kx_mc_config *cfg, 
 
 // price_american_lsm (lsm.rs:80-229). per_path (nullable) gets the value of
 // every path discounted to t = 0.
-int ko_price_american(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
-                      size_t n_dates, int n_basis, kx_price_result *out, double *per_path) {
+int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
+                            size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
     return run([&] {
         ConP c = parse_contract(json);
         Model m = to_model(model);
@@ -1115,11 +1153,12 @@ int ko_price_american(const char *json, const kx_model *model, const kx_mc_confi
                 if (payoff[d][i] > 0.0) { xs.push_back(spots[d][i]); ys.push_back(value[i] * disc); }
             bool have = xs.size() >= (size_t)n_basis;
             std::vector<double> coef;
-            if (have) coef = poly_fit(xs, ys, (size_t)n_basis);
+            if (have) coef = basis == 1 ? laguerre_fit(xs, ys, (size_t)n_basis, m.s0) : poly_fit(xs, ys, (size_t)n_basis);
             for (size_t i = 0; i < np; ++i) {
                 double discounted = value[i] * disc;
                 if (payoff[d][i] > 0.0) {
-                    double cont = have ? poly_eval(coef, spots[d][i]) : discounted;
+                    double cont = !have ? discounted
+                                  : basis == 1 ? laguerre_eval(coef, spots[d][i], m.s0) : poly_eval(coef, spots[d][i]);
                     value[i] = payoff[d][i] > cont ? payoff[d][i] : discounted;
                 } else {
                     value[i] = discounted;
@@ -1131,6 +1170,11 @@ int ko_price_american(const char *json, const kx_model *model, const kx_mc_confi
         *out = summarize(value);
         if (per_path) memcpy(per_path, value.data(), value.size() * sizeof(double));
     });
+}
+
+int ko_price_american(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
+                      size_t n_dates, int n_basis, kx_price_result *out, double *per_path) {
+    return ko_price_american_basis(json, model, cfg, dates, n_dates, n_basis, 0, out, per_path);
 }
 
 // present_value of a contract on one hand-built path (tests/observable.rs

@@ -79,3 +79,34 @@ def test_lsm_heston_matches_oracle(orc):
     ref = orc.price_american(put(40.0).to_json(), h, ds, n_paths=30_000, seed=5, n_basis=3)
     res = put(40.0).price_american(h, ds, n_paths=30_000, seed=5, n_basis=3, precision="fp64")
     assert abs(res.price - ref.price) < 1e-6 * ref.price
+
+
+@pytest.mark.parametrize("n_basis", [3, 4])
+def test_lsm_laguerre_shared_draws_fp64_matches_oracle(orc, n_basis):
+    """Weighted-Laguerre basis on shared FP64 normals: the device and the
+    oracle compute the same regression (up to the order of the Gram sums and
+    the last bit of exp), so the prices agree to 1e-9 relative plus a small
+    fraction of a standard error (a flipped exercise decision)."""
+    rng = np.random.default_rng(10 + n_basis)
+    n, nd = 4000, 25
+    z = rng.standard_normal((n, nd))
+    kx.set_shared_draws(z)
+    orc.set_shared_draws(z)
+    m = kx.GBM(s0=40.0, sigma=0.2, r=0.06, asset="X")
+    c = put(40.0)
+    ds = dates(1.0, nd)
+    res = c.price_american(m, ds, n_paths=n, seed=0, n_basis=n_basis, precision="fp64", shared_draws=True,
+                           basis="laguerre")
+    ref = orc.price_american(c.to_json(), m, ds, n_paths=n, seed=0, n_basis=n_basis, shared=True, basis="laguerre")
+    assert abs(res.price - ref.price) <= 1e-9 * abs(ref.price) + 2e-3 * ref.std_error
+
+
+@pytest.mark.parametrize("s0,sigma,t", [(36.0, 0.2, 1.0), (44.0, 0.4, 2.0)])
+def test_american_put_laguerre_vs_crr(orc, s0, sigma, t):
+    """The LSM benchmark shape with the weighted-Laguerre basis: 4 functions,
+    50 dates a year, 1M paths stored in FP32."""
+    m = kx.GBM(s0=s0, sigma=sigma, r=0.06, asset="X")
+    res = put(40.0).price_american(m, dates(t, int(50 * t)), n_paths=1_000_000, seed=42, n_basis=4,
+                                   basis="laguerre")
+    crr = orc.crr_american(s0, 40.0, t, 0.06, sigma, 1000, False)
+    assert abs(res.price - crr) < 0.01 * crr + 4 * res.std_error, (res.price, crr)

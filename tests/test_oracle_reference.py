@@ -368,3 +368,14 @@ def test_heston_closed_form_limits_and_monte_carlo(orc):
     r = orc.price(kx.european_call("X", 100.0, 1.0).to_json(), m, n_paths=100_000, seed=5, steps_per_year=400)
     cf = orc.heston_call(100.0, 100.0, 1.0, 0.05, 0.04, 2.0, 0.04, 0.3, -0.5)
     assert abs(r.price - cf) < 3 * r.std_error + 0.01, (r.price, r.std_error, cf)
+
+
+def test_lsm_laguerre_basis_vs_crr(orc):
+    """The weighted-Laguerre basis (an extra mode beside the reference's
+    monomials) prices the American put within 1% of the CRR tree, like the
+    monomial basis does (j17_lsm.rs:157-209 tolerance)."""
+    m = gbm(r=0.06, sigma=0.25)
+    for nb in (3, 4):
+        p = orc.price_american(_put(100.0), m, _dates(1.0, 50), n_paths=60_000, seed=7, n_basis=nb, basis="laguerre")
+        crr = orc.crr_american(100, 100, 1, 0.06, 0.25, 500, False)
+        assert abs(p.price - crr) / crr < 0.01, (nb, p.price, crr)
