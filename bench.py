@@ -411,7 +411,8 @@ def run_ours(args, ws, rank, local) -> None:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch_full_workload")
         except Exception:
             traffic = None
-    kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>"}.get(kx.last_launch_stats()["path_kernel"], "?")
+    kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>", 3: "k_lean<float,GBM,static schedule>"}.get(
+        kx.last_launch_stats()["path_kernel"], "?")
     roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
                 "frac": achieved / peak if peak == peak and peak > 0 else None, "traffic": traffic,
                 "peak_source": "measured in this run: kx_measure_peak(3), the bare Philox4x32-10 + Box-Muller "

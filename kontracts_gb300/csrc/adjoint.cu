@@ -143,8 +143,9 @@ template <class Real, int MODEL>
 __device__ __forceinline__ void model_step(const AdjArgs &A, const StepRec<Real> &rec, Real z1, Real z2, Real &y,
                                            Real &v) {
     if (MODEL == KX_MODEL_GBM) {
-        const Real dt = rec.c0, sq = rec.c1;
-        y += ((Real)A.mu - Real(0.5) * (Real)A.sigma * (Real)A.sigma) * dt + (Real)A.sigma * sq * z1;
+        const Real dt = rec.c0, sq = rec.c1, sg = (Real)A.sigma;
+        const Real drift = sub_rn((Real)A.mu, mul_rn(mul_rn(Real(0.5), sg), sg));
+        y = gbm_step(y, mul_rn(drift, dt), mul_rn(sg, sq), z1);
     } else {
         heston_step<Real>((Real)A.r, (Real)A.kappa, (Real)A.theta, (Real)A.sigma_v, (Real)A.rho, (Real)A.rho_perp,
                           A.scheme, rec.c0, rec.c1, z1, z2, y, v);

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
             }
             const StepRec<Real> rec = R[k];
             const int q = (int)(d & 3u);
-            if (MODEL == KX_MODEL_GBM) y += rec.c0 + rec.c1 * z[q];
+            if (MODEL == KX_MODEL_GBM) y = gbm_step(y, rec.c0, rec.c1, z[q]);
             else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[q], z[q + 1], y, v);
             if (k == nf) {
                 pay_flows<Real>(A, k, spot_of<Real>(s0, y), path);

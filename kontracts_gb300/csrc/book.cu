@@ -35,6 +35,7 @@ struct kx_book {
         kx::PathBuffers B;
         size_t pv_base = 0;  // first per-path value of the group in the value arena
         float tuned_ms = 0.f;
+        int family = 0;      // 0 k_paths, 1 k_lean, 2 k_lean with static schedules
     };
     std::vector<Group> groups;
     std::vector<const kx::Program *> progs;
@@ -72,16 +73,17 @@ std::vector<Job> group_jobs(kx_book &b, const kx_book::Group &g) {
 // Device pointers of a group's tables inside the arena: the table regions are
 // sized for the largest plan the tuner may build (work items of 64 paths).
 struct Region {
-    size_t progs, steps, disc, cons, thr, items;
+    size_t progs, steps, disc, cons, thr, items, statics;
 };
 
 Region region_sizes(const PathPlan &P, uint64_t max_items) {
     return Region{A256(P.progs.size() * sizeof(KxProgram)), A256(P.steps.size()), A256(P.disc.size() * sizeof(double)),
-                  A256(P.cons.size() * sizeof(ContractDev)), A256(P.thr.size()), A256(max_items * sizeof(WorkItem))};
+                  A256(P.cons.size() * sizeof(ContractDev)), A256(P.thr.size()), A256(max_items * sizeof(WorkItem)),
+                  A256(P.statics.size() * sizeof(StaticDev))};
 }
 
 float time_group(Ctx &c, kx_book &b, kx_book::Group &g, std::vector<Job> &jobs, int minb, uint64_t item) {
-    PathPlan P = plan_paths(jobs, g.cfg, 1, minb, g.plan.lean, item);
+    PathPlan P = plan_paths(jobs, g.cfg, 1, minb, g.plan.lean, item, g.plan.stat);
     upload_plan(P, g.B, c.stream);
     KX_CUDA(cudaMemsetAsync(g.B.counters, 0, 64, c.stream));
     PathArgs a = path_args(P, g.B);
@@ -174,18 +176,21 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
         std::lock_guard<std::mutex> lk(c.mu);
         begin_call(c);
         // groups: (model kind, precision, kernel family)
+        std::vector<int> fam(n);
+        for (size_t i = 0; i < n; ++i) {
+            std::vector<Job> one;
+            one.push_back(make_job(*b->progs[i], b->models[i], b->cfgs[i], b->grids[i], {}, 0, 0.0));
+            fam[i] = use_static(one, 1) ? 2 : use_lean(one, 1) ? 1 : 0;
+        }
         for (int kind = 0; kind < 2; ++kind)
             for (int prec = 0; prec < 2; ++prec)
-                for (int lean = 1; lean >= 0; --lean) {
+                for (int f = 2; f >= 0; --f) {
                     kx_book::Group g;
-                    for (size_t i = 0; i < n; ++i) {
-                        if (b->models[i].kind != kind || b->cfgs[i].precision != prec) continue;
-                        std::vector<Job> one;
-                        one.push_back(make_job(*b->progs[i], b->models[i], b->cfgs[i], b->grids[i], {}, 0, 0.0));
-                        if (use_lean(one, 1) == (lean == 1)) g.members.push_back(i);
-                    }
+                    for (size_t i = 0; i < n; ++i)
+                        if (b->models[i].kind == kind && b->cfgs[i].precision == prec && fam[i] == f) g.members.push_back(i);
                     if (g.members.empty()) continue;
                     g.cfg = b->cfgs[g.members[0]];
+                    g.family = f;
                     b->groups.push_back(std::move(g));
                 }
         // plans at the default shape; arena sized for the largest item table
@@ -196,14 +201,14 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
             auto &g = b->groups[q];
             jobs[q] = group_jobs(*b, g);
             int nv = 0;
-            const bool lean = use_lean(jobs[q], 1);
+            const bool lean = g.family >= 1;
             const int *vs = variants(b->models[g.members[0]].kind, g.cfg.precision == KX_PREC_FP64, 1, lean, nv);
-            g.plan = plan_paths(jobs[q], g.cfg, 1, vs[0], lean, 0);
+            g.plan = plan_paths(jobs[q], g.cfg, 1, vs[0], lean, 0, g.family == 2);
             uint64_t max_items = 0;
             for (auto &j : jobs[q]) max_items += (j.dev.n_paths + 63) / 64;
             regs.push_back(region_sizes(g.plan, max_items));
             const Region &r = regs.back();
-            bytes += r.progs + r.steps + r.disc + r.cons + r.thr + r.items;
+            bytes += r.progs + r.steps + r.disc + r.cons + r.thr + r.items + r.statics;
             g.pv_base = b->n_paths;
             b->n_paths += g.plan.total;
             b->path_steps += g.plan.path_steps;
@@ -252,6 +257,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
             g.B.cons = base + o; o += r.cons;
             g.B.thr = base + o; o += r.thr;
             g.B.items = base + o; o += r.items;
+            g.B.statics = base + o; o += r.statics;
             g.B.counters = b->d_counters + 16 * q;
             g.B.pv = b->d_pv + g.pv_base;
         }
@@ -280,7 +286,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
                     }
                 g.tuned_ms = best;
             }
-            g.plan = plan_paths(jobs[q], g.cfg, 1, minb, g.plan.lean, item);
+            g.plan = plan_paths(jobs[q], g.cfg, 1, minb, g.plan.lean, item, g.plan.stat);
             upload_plan(g.plan, g.B, c.stream);
             c.last.h2d_bytes += plan_upload_bytes(g.plan);
         }
@@ -314,7 +320,7 @@ kx_status kx_book_price(kx_book *b, kx_price_result *out) {
             c.last.steps_simulated += sim;
             check_err_word(hc[1]);
             if (!b->groups[q].plan.items.empty()) c.last.kernel_launches++;
-            c.last.path_kernel = b->groups[q].plan.lean ? 2u : 1u;
+            c.last.path_kernel = b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
         }
         if (b->n_chunks) c.last.kernel_launches++;
         const size_t n = b->progs.size();
@@ -344,10 +350,11 @@ kx_status kx_book_set_models(kx_book *b, const kx_model *models) {
         for (auto &g : b->groups) {
             if (g.plan.items.empty()) continue;
             std::vector<Job> jobs = group_jobs(*b, g);
-            if (use_lean(jobs, 1) != g.plan.lean)
+            if (use_lean(jobs, 1) != g.plan.lean || (g.plan.stat && !use_static(jobs, 1)))
                 raise(KX_INVALID_ARGUMENT, "new model parameters change a contract's kernel family");
-            PathPlan P = plan_paths(jobs, g.cfg, 1, g.plan.minb, g.plan.lean, g.plan.item_paths);
+            PathPlan P = plan_paths(jobs, g.cfg, 1, g.plan.minb, g.plan.lean, g.plan.item_paths, g.plan.stat);
             if (P.steps.size() != g.plan.steps.size() || P.items.size() != g.plan.items.size() ||
+                P.statics.size() != g.plan.statics.size() ||
                 P.grid_blocks != g.plan.grid_blocks || P.smem != g.plan.smem)
                 raise(KX_INVALID_ARGUMENT, "new model parameters change the book's layout");
             upload_plan(P, g.B, c.stream);
@@ -367,7 +374,7 @@ kx_status kx_book_get_info(const kx_book *b, kx_book_info *info) {
         info->path_steps = b->path_steps;
         info->tune_ms = b->tune_ms;
         for (size_t q = 0; q < b->groups.size() && q < 4; ++q) {
-            info->group_kernel[q] = b->groups[q].plan.lean ? 2u : 1u;
+            info->group_kernel[q] = b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
             info->group_minb[q] = (uint32_t)b->groups[q].plan.minb;
             info->group_item_paths[q] = (uint32_t)b->groups[q].plan.item_paths;
             info->group_contracts[q] = (uint32_t)b->groups[q].members.size();

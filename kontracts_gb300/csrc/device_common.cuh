@@ -67,6 +67,36 @@ __device__ __forceinline__ float fast_exp<float>(float x) { return __expf(x); }
 template <>
 __device__ __forceinline__ double fast_exp<double>(double x) { return exp(x); }
 
+// Separately rounded arithmetic in either precision (never fused into an FMA).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Amount of a flow slot with a closed form (KxFastAmount): the operations of
+// the interpreter on its code, in the same order, so the value is identical.
+template <class Real>
+__device__ __forceinline__ Real fast_amount(const KxProgram &P, const KxLeaf &F, Real S) {
+    const Real K = (Real)P.cpool[F.fast_k];
+    Real r;
+    switch (F.fast) {
+    case FA_CALL: r = fmax(S - K, Real(0)); break;
+    case FA_PUT: r = fmax(K - S, Real(0)); break;
+    case FA_SPOT: r = S; break;
+    default: r = K; break;
+    }
+    return F.sign < 0.0 ? -r : r;
+}
+
+// One log-space GBM step y += c0 + c1 z with its roundings fixed (one FMA,
+// one add), identical in every kernel that steps a path.
+__device__ __forceinline__ float gbm_step(float y, float c0, float c1, float z) {
+    return __fadd_rn(y, __fmaf_rn(c1, z, c0));
+}
+__device__ __forceinline__ double gbm_step(double y, double c0, double c1, double z) {
+    return __dadd_rn(y, __fma_rn(c1, z, c0));
+}
+
 // S = s0 * exp(y) rounded once, so that no later use is fused into an FMA
 // with it: every kernel then sees the same S bit for bit.
 template <class Real>
@@ -207,10 +237,13 @@ template <>
 __device__ __forceinline__ void heston_step<float>(float r, float kap, float th, float sv, float rho, float rp,
                                                    int scheme, float dt, float sq, float z1, float z2, float &y,
                                                    float &v) {
+    // every rounding spelled out, so that no kernel fuses it differently
     const float vp = scheme == KX_HESTON_FULL_TRUNCATION ? fmaxf(v, 0.f) : v;
     const float sqv = sqrt_approx(vp);
-    y += r * dt - 0.5f * vp * dt + sqv * (z1 * sq);
-    const float nv = v + kap * (th - vp) * dt + sv * sqv * ((rho * z1 + rp * z2) * sq);
+    const float drift = __fmaf_rn(__fmul_rn(-0.5f, vp), dt, __fmul_rn(r, dt));  // (r - v/2) dt
+    y = __fadd_rn(y, __fmaf_rn(sqv, __fmul_rn(z1, sq), drift));
+    const float zv = __fmaf_rn(rho, z1, __fmul_rn(rp, z2));
+    const float nv = __fmaf_rn(__fmul_rn(sv, sqv), __fmul_rn(zv, sq), __fmaf_rn(__fmul_rn(kap, __fsub_rn(th, vp)), dt, v));
     v = scheme == KX_HESTON_FULL_TRUNCATION ? nv : fmaxf(nv, 0.f);
 }
 template <>

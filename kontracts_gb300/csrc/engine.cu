@@ -302,8 +302,8 @@ template void pack_steps<double>(const StepTables &, std::vector<unsigned char> 
 // Launch the fused path kernel over `jobs` (all of one model kind, one
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
-const void *select_kernel(int model, bool f64, int ns, int minb, bool lean) {
-    if (lean) return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb) : lean_kernel_heston(f64, minb);
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat) {
+    if (lean) return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat) : lean_kernel_heston(f64, minb, stat);
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
     if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
     return paths_kernel_heston(f64, minb);
@@ -327,6 +327,67 @@ bool use_lean(const std::vector<Job> &jobs, int ns) {
     const char *env = getenv("KX_PATH_KERNEL");
     if (env && strcmp(env, "general") == 0) return false;
     return lean_applies(jobs, ns);
+}
+
+// The static schedule of a lean job (StaticDev), or false when the contract
+// has none: a when/anytime reading prices, an amount without closed form,
+// an error-capable evaluation, or more than KX_MAX_SEV event steps.
+bool build_static(const Job &j, StaticDev &T) {
+    const KxProgram &P = j.prog;
+    if (P.err_capable || (P.all_leaves & ~P.simple_leaves) != 0u || P.n_acc) return false;
+    const StaticSchedule S = static_schedule(P, j.tab);
+    if (!S.static_ok) return false;
+    memset(&T, 0, sizeof T);
+    std::map<int, std::pair<uint32_t, uint32_t>> at;  // step -> (armed barriers, paid flows)
+    for (auto &f : S.flows) {
+        at[f.step].second |= 1u << f.leaf;
+        T.all_flows |= 1u << f.leaf;
+        for (int i = 0; i < P.n_trig; ++i)
+            if ((f.price_untils >> i) & 1u) T.kill[i] |= 1u << f.leaf;
+    }
+    for (int i = 0; i < P.n_trig; ++i) {
+        const KxTrig &Tr = P.trig[i];
+        if (Tr.cond_kind == CK_GENERAL) return false;
+        if (Tr.cond_kind != CK_SPOT_CMP) continue;
+        if (Tr.kind != TK_UNTIL) return false;
+        if (S.arm[i] == StaticSchedule::NEVER || T.kill[i] == 0u) continue;  // never tested, or drops nothing
+        at[S.arm[i]].first |= 1u << i;
+        const double t = j.thr[Tr.spot_slot];
+        const float tf = (float)t;
+        const bool up = Tr.cmp == CMP_GE || Tr.cmp == CMP_GT;
+        if (up) T.up_mask |= 1u << i;
+        switch (Tr.cmp) {  // strict comparisons become inclusive at the next representable threshold
+        case CMP_GT: T.thr64[i] = std::nextafter(t, INFINITY); T.thr32[i] = std::nextafter(tf, INFINITY); break;
+        case CMP_LT: T.thr64[i] = std::nextafter(t, -INFINITY); T.thr32[i] = std::nextafter(tf, -INFINITY); break;
+        default: T.thr64[i] = t; T.thr32[i] = tf; break;
+        }
+    }
+    if (at.size() > (size_t)KX_MAX_SEV) return false;
+    for (auto &kv : at) {
+        T.ev_step[T.n_ev] = kv.first;
+        T.ev_arm[T.n_ev] = kv.second.first;
+        T.ev_pay[T.n_ev] = kv.second.second;
+        ++T.n_ev;
+    }
+    for (int q = 0; q < P.n_leaf; ++q) {
+        const KxLeaf &F = P.leaf[q];
+        T.f_fast[q] = F.kind == AK_CONST ? (uint8_t)FA_NONE : F.fast;
+        T.f_k[q] = F.kind == AK_CONST ? 0.0 : P.cpool[F.fast_k];
+        T.f_sign[q] = F.sign;
+    }
+    return true;
+}
+
+// Static schedules serve a lean launch whose every contract has one, unless
+// KX_PATH_KERNEL = "lean" asks for the general event handler.
+bool use_static(const std::vector<Job> &jobs, int ns) {
+    if (!use_lean(jobs, ns)) return false;
+    const char *env = getenv("KX_PATH_KERNEL");
+    if (env && strcmp(env, "lean") == 0) return false;
+    StaticDev T;
+    for (auto &j : jobs)
+        if (!build_static(j, T)) return false;
+    return true;
 }
 
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
@@ -354,7 +415,7 @@ static std::string tune_key(const std::vector<Job> &jobs, const kx_mc_config &cf
     }
     char buf[128];
     snprintf(buf, sizeof buf, "m%d-p%d-ns%d-acc%d-gen%d-sm%d-sp%d-l%d", jobs[0].model.kind, cfg.precision, ns, acc > 0,
-             gen, smooth, spot, use_lean(jobs, ns) ? 1 : 0);
+             gen, smooth, spot, use_static(jobs, ns) ? 2 : use_lean(jobs, ns) ? 1 : 0);
     return buf;
 }
 
@@ -420,10 +481,16 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
 }
 
 PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
-                    uint64_t item_paths) {
+                    uint64_t item_paths, bool stat) {
     PathPlan P;
     P.f64 = cfg.precision == KX_PREC_FP64;
     P.lean = lean;
+    P.stat = lean && stat;
+    if (P.stat) {
+        P.statics.resize(jobs.size());
+        for (size_t q = 0; q < jobs.size(); ++q)
+            if (!build_static(jobs[q], P.statics[q])) raise(KX_CUDA_ERROR, "static schedule expected");
+    }
     P.model = jobs[0].model.kind;
     P.ns = ns;
     P.minb = minb;
@@ -466,7 +533,7 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.surv_base = 2u * (uint32_t)max_acc;
     P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
     P.smem = (size_t)ns * P.slots * block * (f64 ? 8 : 4);
-    P.kfn = select_kernel(P.model, f64, ns, minb, lean);
+    P.kfn = select_kernel(P.model, f64, ns, minb, lean, P.stat);
     if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (P.smem > 48 * 1024)
         KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
@@ -503,6 +570,7 @@ PathArgs path_args(const PathPlan &P, const PathBuffers &B) {
     a.steps_done = reinterpret_cast<unsigned long long *>(B.counters + 2);
     a.pv = B.pv;
     a.pv_stride = P.total;
+    a.statics = P.stat ? B.statics : nullptr;
     return a;
 }
 
@@ -514,16 +582,20 @@ void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s) {
     KX_CUDA(cudaMemcpyAsync(B.thr, P.thr.data(), P.thr.size(), cudaMemcpyHostToDevice, s));
     if (!P.items.empty())
         KX_CUDA(cudaMemcpyAsync(B.items, P.items.data(), P.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+    if (P.stat)
+        KX_CUDA(cudaMemcpyAsync(B.statics, P.statics.data(), P.statics.size() * sizeof(StaticDev), cudaMemcpyHostToDevice,
+                                s));
 }
 
 size_t plan_upload_bytes(const PathPlan &P) {
     return P.progs.size() * sizeof(KxProgram) + P.steps.size() + P.disc.size() * sizeof(double) +
-           P.cons.size() * sizeof(ContractDev) + P.thr.size() + P.items.size() * sizeof(WorkItem);
+           P.cons.size() * sizeof(ContractDev) + P.thr.size() + P.items.size() * sizeof(WorkItem) +
+           P.statics.size() * sizeof(StaticDev);
 }
 
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
                             int minb, bool lean) {
-    PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0);
+    PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0, lean && use_static(jobs, ns));
     c.last.path_steps += P.path_steps;
     stride_out = P.total;
     if (P.items.empty()) return P.total;
@@ -535,8 +607,9 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.items.ensure(P.items.size() * sizeof(WorkItem));
     c.counters.ensure(64);
     c.pv.ensure(std::max<uint64_t>(1, P.total * ns) * sizeof(double));
-    const PathBuffers B{c.progs.p, c.steps.p, c.disc.p, c.cons.p, c.thr.p, c.items.p, c.counters.as<uint32_t>(),
-                        c.pv.as<double>()};
+    c.statics.ensure(std::max<size_t>(1, P.statics.size()) * sizeof(StaticDev));
+    const PathBuffers B{c.progs.p, c.steps.p, c.disc.p,  c.cons.p, c.thr.p, c.items.p, c.counters.as<uint32_t>(),
+                        c.pv.as<double>(), c.statics.p};
     upload_plan(P, B, c.stream);
     KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
     c.last.h2d_bytes += plan_upload_bytes(P);
@@ -561,7 +634,7 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.last.kernel_launches++;
     c.last.grid_blocks = (uint32_t)P.grid_blocks;
     c.last.block_threads = (uint32_t)KX_BLOCK;
-    c.last.path_kernel = lean ? 2u : 1u;
+    c.last.path_kernel = P.stat ? 3u : lean ? 2u : 1u;
     uint32_t hc[4] = {0, 0, 0, 0};
     KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));

@@ -34,10 +34,16 @@ template <class Real>
 void pack_steps(const StepTables &t, std::vector<unsigned char> &out);
 
 // Path kernel for a model, precision, scenario count and register budget.
-const void *select_kernel(int model, bool f64, int ns, int minb, bool lean);
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat = false);
 
 // Whether the lean kernel serves these jobs (KX_PATH_KERNEL may force the general one).
 bool use_lean(const std::vector<Job> &jobs, int ns);
+
+// Compiles the static schedule of a job; false when it has none.
+bool build_static(const Job &j, StaticDev &T);
+// Whether every job of a lean launch has a static schedule (KX_PATH_KERNEL =
+// "lean" forces the general event handler of k_lean).
+bool use_static(const std::vector<Job> &jobs, int ns);
 
 // Register budgets (minimum resident blocks per SM) of a kernel family; the
 // first is the default when no tuning result is at hand.
@@ -45,13 +51,14 @@ const int *variants(int model, bool f64, int ns, bool lean, int &n);
 
 // Host-side tables and geometry of one path-kernel launch over `jobs`.
 struct PathPlan {
-    bool f64 = false, lean = false;
+    bool f64 = false, lean = false, stat = false;
     int model = 0, ns = 1, minb = 0;
     std::vector<KxProgram> progs;
     std::vector<unsigned char> steps, thr;
     std::vector<double> disc;
     std::vector<ContractDev> cons;
     std::vector<WorkItem> items;
+    std::vector<StaticDev> statics;  // per contract, static-schedule launches
     uint64_t total = 0, path_steps = 0, item_paths = 0;
     uint32_t slots = 0, surv_base = 0;
     size_t smem = 0;
@@ -64,12 +71,13 @@ struct PathBuffers {
     void *progs, *steps, *disc, *cons, *thr, *items;
     uint32_t *counters;
     double *pv;
+    void *statics;
 };
 
 // Lays out the tables of `jobs` (sets each job's pv offset) and the launch
 // geometry; item_paths = 0 picks the default work-item size.
 PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
-                    uint64_t item_paths);
+                    uint64_t item_paths, bool stat);
 PathArgs path_args(const PathPlan &P, const PathBuffers &B);
 void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s);
 size_t plan_upload_bytes(const PathPlan &P);

@@ -41,7 +41,7 @@ struct LsmArgs {
     int model;
     int scheme;
     double s0, v0, kappa, theta, sigma_v, rho, rho_perp, r;
-    double x_scale;    // KX_LSM_LAGUERRE: regressor x = S / x_scale (the model's spot)
+    double x_scale;    // regressor x = S / x_scale (the model's spot): Laguerre basis, FP32 fits
     const double *z64;
     const float *z32;
     uint64_t z_dpp;
@@ -63,7 +63,9 @@ __device__ __forceinline__ Real lsm_payoff(const KxProgram &P, Real S, int k) {
     for (int j = 0; j < P.n_leaf; ++j) {
         const KxLeaf &F = P.leaf[j];
         uint32_t e = 0;
-        v += F.kind == AK_CONST ? (Real)F.sign : eval_code<Real>(P, F.code_off, F.code_len, none, 0u, k, S, e);
+        v += F.kind == AK_CONST ? (Real)F.sign
+             : F.fast           ? fast_amount<Real>(P, F, S)
+                                : eval_code<Real>(P, F.code_off, F.code_len, none, 0u, k, S, e);
     }
     return v;
 }
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward(const LsmArgs A) {
             const StepRec<Real> rec = R[k];
             const int q = (int)(d & 3u);
             if (MODEL == KX_MODEL_GBM) {
-                y += rec.c0 + rec.c1 * z[q];
+                y = gbm_step(y, rec.c0, rec.c1, z[q]);
             } else {
                 heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[q], z[q + 1], y, v);
             }
@@ -114,6 +116,25 @@ __device__ void block_sums(double *vals, int n, double *red) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (l == 0) red[q * 32 + w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        double t = 0.0;
+        for (int j = 0; j < nw; ++j) t += red[threadIdx.x * 32 + j];
+        red[32 * 64 + threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+// The same for FP32 partial sums: the warp adds its 32 lanes in FP32, the
+// warps' totals are added in FP64 (fixed order).
+__device__ void block_sums_f32(const float *vals, int n, double *red) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int q = 0; q < n; ++q) {
+        float v = vals[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (l == 0) red[q * 32 + w] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < n) {
@@ -179,6 +200,32 @@ __device__ __forceinline__ void lsm_basis(double s, double x_scale, double (&phi
     }
 }
 
+// FP32 paths: the basis of x = s / x_scale in FP32 (monomials x^j or the
+// weighted Laguerre functions); the regression is invariant to the scale, so
+// the fitted continuation is that of the reference's basis, while FP32 keeps
+// the per-path work off the slow FP64 pipe. FP64 is used only across threads
+// (block sums, cross-block sums) and for the solve.
+template <int M, int B>
+__device__ __forceinline__ void lsm_basis_f32(float x, float (&phi)[M]) {
+    if (B == KX_LSM_MONOMIAL) {
+        phi[0] = 1.0f;
+#pragma unroll
+        for (int j = 1; j < M; ++j) phi[j] = phi[j - 1] * x;
+    } else {
+        const float w = __expf(-0.5f * x);
+        float lm = 1.0f, l = 1.0f - x;
+        phi[0] = w;
+        if (M > 1) phi[1] = w * l;
+#pragma unroll
+        for (int j = 1; j + 1 < M; ++j) {
+            const float ln = (((float)(2 * j + 1) - x) * l - (float)j * lm) * (1.0f / (float)(j + 1));
+            lm = l;
+            l = ln;
+            phi[j + 1] = w * l;
+        }
+    }
+}
+
 // Continuation value sum_j c_j phi_j(s): Horner from the top coefficient for
 // monomials (poly_eval, lsm.rs:293-295), the plain sum for Laguerre.
 template <int M, int B>
@@ -208,23 +255,56 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
     const KxProgram &P = *A.P;
     const Real *S = reinterpret_cast<const Real *>(A.S);
     Real *V = reinterpret_cast<Real *>(A.value);
+    constexpr bool F32 = sizeof(Real) == 4;
     double acc[NS];
+    float accf[NS];
 #pragma unroll
-    for (int q = 0; q < NS; ++q) acc[q] = 0.0;
+    for (int q = 0; q < NS; ++q) {
+        acc[q] = 0.0;
+        accf[q] = 0.0f;
+    }
     double cu[M];
+    float cuf[M];
     bool have = false;
     if (upd >= 0) {
         have = A.coef[upd * LSM_COEF + 7] != 0.0;
 #pragma unroll
-        for (int j = 0; j < M; ++j) cu[j] = A.coef[upd * LSM_COEF + j];
+        for (int j = 0; j < M; ++j) {
+            cu[j] = A.coef[upd * LSM_COEF + j];
+            cuf[j] = (float)cu[j];
+        }
     }
+    const float inv_scale = (float)(1.0 / A.x_scale);
     const double disc_u = upd >= 0 ? A.disc[upd] : 0.0;
+    const float disc_uf = (float)disc_u;
     const double disc_g = gram >= 0 ? A.disc[gram] : 0.0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
          i += (uint64_t)gridDim.x * blockDim.x) {
         Real val;
         if (upd < 0) {
             val = lsm_payoff<Real>(P, S[(uint64_t)(A.n_ex - 1) * A.n_paths + i], A.n_ex);
+        } else if (F32) {  // the decision in FP32 (FP64 only across threads)
+            const float s = (float)S[(uint64_t)upd * A.n_paths + i];
+            const float pay = (float)lsm_payoff<Real>(P, (Real)s, upd + 1);
+            const float discounted = (float)V[i] * disc_uf;
+            float nv = discounted;
+            if (pay > 0.0f) {
+                float cont = discounted;
+                if (have) {
+                    float phi[M];
+                    lsm_basis_f32<M, B>(s * inv_scale, phi);
+                    cont = 0.0f;
+                    if (B == KX_LSM_MONOMIAL) {
+#pragma unroll
+                        for (int j = M - 1; j >= 0; --j) cont = cont * phi[1] + cuf[j];
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < M; ++j) cont += cuf[j] * phi[j];
+                    }
+                }
+                nv = pay > cont ? pay : discounted;
+            }
+            val = (Real)nv;
         } else {
             const Real s = S[(uint64_t)upd * A.n_paths + i];
             const Real pay = lsm_payoff<Real>(P, s, upd + 1);
@@ -241,23 +321,38 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
         if (gram >= 0) {
             const Real sg = S[(uint64_t)gram * A.n_paths + i];
             if (lsm_payoff<Real>(P, sg, gram + 1) > Real(0)) {
-                const double x = (double)sg;
-                const double y = (double)val * disc_g;
-                double pw[M];
-                lsm_basis<M, B>(x, A.x_scale, pw);
-                int q = 0;
+                if (F32) {
+                    const float yf = (float)val * (float)disc_g;
+                    float pw[M];
+                    lsm_basis_f32<M, B>((float)sg * inv_scale, pw);
+                    int q = 0;
 #pragma unroll
-                for (int r = 0; r < M; ++r)
+                    for (int r = 0; r < M; ++r)
 #pragma unroll
-                    for (int c = r; c < M; ++c) acc[q++] += __dmul_rn(pw[r], pw[c]);
+                        for (int c = r; c < M; ++c) accf[q++] += pw[r] * pw[c];
 #pragma unroll
-                for (int r = 0; r < M; ++r) acc[NA + r] += __dmul_rn(pw[r], y);
-                acc[NS - 1] += 1.0;
+                    for (int r = 0; r < M; ++r) accf[NA + r] += pw[r] * yf;
+                    accf[NS - 1] += 1.0f;
+                } else {
+                    const double x = (double)sg;
+                    const double y = (double)val * disc_g;
+                    double pw[M];
+                    lsm_basis<M, B>(x, A.x_scale, pw);
+                    int q = 0;
+#pragma unroll
+                    for (int r = 0; r < M; ++r)
+#pragma unroll
+                        for (int c = r; c < M; ++c) acc[q++] += __dmul_rn(pw[r], pw[c]);
+#pragma unroll
+                    for (int r = 0; r < M; ++r) acc[NA + r] += __dmul_rn(pw[r], y);
+                    acc[NS - 1] += 1.0;
+                }
             }
         }
     }
     if (gram < 0) return;
-    block_sums(acc, NS, red);
+    if (F32) block_sums_f32(accf, NS, red);
+    else block_sums(acc, NS, red);
     if (threadIdx.x < NS) A.partial[(size_t)blockIdx.x * 64 + threadIdx.x] = red[32 * 64 + threadIdx.x];
     __threadfence();
     __syncthreads();
@@ -265,10 +360,18 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (threadIdx.x < NS) {
-        double t = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) t += A.partial[(size_t)b * 64 + threadIdx.x];
-        red[threadIdx.x] = t;
+    // cross-block sums by the whole block: thread t adds blocks t, t + 256,
+    // ... in that order, then the fixed-order block sum (deterministic)
+    {
+        double part[NS];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) part[q] = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+            for (int q = 0; q < NS; ++q) part[q] += __ldcg(A.partial + (size_t)b * 64 + q);
+        }
+        block_sums(part, NS, red);
+        if (threadIdx.x < NS) red[threadIdx.x] = red[32 * 64 + threadIdx.x];
     }
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -6,10 +6,14 @@ template __global__ void k_paths<float, M_HESTON, 1, 4>(const PathArgs);
 template __global__ void k_paths<float, M_HESTON, 1, 3>(const PathArgs);
 template __global__ void k_paths<float, M_HESTON, 1, 2>(const PathArgs);
 template __global__ void k_paths<double, M_HESTON, 1, 2>(const PathArgs);
-template __global__ void k_lean<float, M_HESTON, 6>(const PathArgs);
-template __global__ void k_lean<float, M_HESTON, 5>(const PathArgs);
-template __global__ void k_lean<float, M_HESTON, 4>(const PathArgs);
-template __global__ void k_lean<double, M_HESTON, 3>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 6, false>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 6, true>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 5, false>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 5, true>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 4, false>(const PathArgs);
+template __global__ void k_lean<float, M_HESTON, 4, true>(const PathArgs);
+template __global__ void k_lean<double, M_HESTON, 3, false>(const PathArgs);
+template __global__ void k_lean<double, M_HESTON, 3, true>(const PathArgs);
 
 const void *paths_kernel_heston(int fp64, int minb) {
     if (fp64) return (const void *)&k_paths<double, M_HESTON, 1, 2>;
@@ -20,12 +24,17 @@ const void *paths_kernel_heston(int fp64, int minb) {
     }
 }
 
-const void *lean_kernel_heston(int fp64, int minb) {
-    if (fp64) return (const void *)&k_lean<double, M_HESTON, 3>;
+template <class Real, int MINB>
+static const void *lean_pick(bool stat) {
+    return stat ? (const void *)&k_lean<Real, M_HESTON, MINB, true> : (const void *)&k_lean<Real, M_HESTON, MINB, false>;
+}
+
+const void *lean_kernel_heston(int fp64, int minb, bool stat) {
+    if (fp64) return lean_pick<double, 3>(stat);
     switch (minb) {
-    case 6: return (const void *)&k_lean<float, M_HESTON, 6>;
-    case 5: return (const void *)&k_lean<float, M_HESTON, 5>;
-    default: return (const void *)&k_lean<float, M_HESTON, 4>;
+    case 6: return lean_pick<float, 6>(stat);
+    case 5: return lean_pick<float, 5>(stat);
+    default: return lean_pick<float, 4>(stat);
     }
 }
 }  // namespace kx

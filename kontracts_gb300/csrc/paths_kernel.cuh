@@ -79,6 +79,7 @@ struct PathArgs {
     const double *z64;   // shared draws (path-major) or null
     const float *z32;
     uint64_t z_dpp;
+    const void *statics; // StaticDev per contract (static-schedule launches of k_lean)
 };
 
 enum { M_GBM = 0, M_HESTON = 1 };
@@ -212,21 +213,6 @@ __device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const Ste
         if (b) bits |= 1u << i;
     }
     return bits;
-}
-
-// Amount of a flow slot with a closed form (KxFastAmount): the operations of
-// the interpreter on its code, in the same order, so the value is identical.
-template <class Real>
-__device__ __forceinline__ Real fast_amount(const KxProgram &P, const KxLeaf &F, Real S) {
-    const Real K = (Real)P.cpool[F.fast_k];
-    Real r;
-    switch (F.fast) {
-    case FA_CALL: r = fmax(S - K, Real(0)); break;
-    case FA_PUT: r = fmax(K - S, Real(0)); break;
-    case FA_SPOT: r = S; break;
-    default: r = K; break;
-    }
-    return F.sign < 0.0 ? -r : r;
 }
 
 // Trigger state of one path and scenario, passed by value to the out-of-line
@@ -562,11 +548,11 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                         if (MODEL == M_GBM) {
                             // log-space exact GBM step (simulator.rs:238-245)
                             if (NS == 1) {
-                                L.y[s] += c0 + c1 * zz[j];
+                                L.y[s] = gbm_step(L.y[s], c0, c1, zz[j]);
                             } else {
                                 const ContractDev &C = A.cons[cur];
-                                L.y[s] += pick<Real>(C.drift[s], C.driftf[s]) * c0 +
-                                          pick<Real>(C.sigma[s], C.sigmaf[s]) * c1 * zz[j];
+                                const Real sc1 = pick<Real>(C.sigma[s], C.sigmaf[s]) * c1;
+                                L.y[s] = gbm_step(L.y[s], pick<Real>(C.drift[s], C.driftf[s]) * c0, sc1, zz[j]);
                             }
                         } else {
                             heston_step<Real>(hr, hk, hth, hsv, hrho, hrp,

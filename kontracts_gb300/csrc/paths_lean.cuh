@@ -136,6 +136,111 @@ __device__ __forceinline__ Trig lean_event(const KxProgram *Pp, const ContractDe
     return on_event<Real>(Pp, Cp, R, thr, D, nullptr, nullptr, KX_BLOCK, s0, y, k, bits, 0u, 0, st);
 }
 
+// ---------------------------------------------------------------------------
+// Static schedules. When every when/anytime condition of a contract reads
+// only the time, every until reads either the time or Spot-cmp-Const, and
+// every flow amount is constant or closed-form, the whole contract is a
+// fixed list of steps at which barriers are armed and flows are paid, plus
+// the barrier knock-outs of each path. The host compiles that list
+// (StaticDev) and the kernel keeps only a few masks per path: the live
+// barriers, the flows still to pay, the next event and the value.
+// Flows are numbered by their flow slot, so the value adds them in the same
+// order as on_event and is the same bit for bit.
+// ---------------------------------------------------------------------------
+constexpr int KX_MAX_SEV = 64;
+
+struct StaticDev {
+    int32_t n_ev;
+    uint32_t up_mask;    // barrier slots that fire upwards (y >= thr); the others downwards (y <= thr)
+    uint32_t all_flows;  // flow slots of the schedule (flows knocked by time-only untils are left out)
+    int32_t pad;
+    int32_t ev_step[KX_MAX_SEV];
+    uint32_t ev_arm[KX_MAX_SEV];  // barrier slots armed at that step (tested at once)
+    uint32_t ev_pay[KX_MAX_SEV];  // flow slots paid at that step unless knocked out
+    uint32_t kill[KX_MAX_TRIG];   // flow slots dropped when barrier slot i knocks
+    float thr32[KX_MAX_TRIG];     // log-spot thresholds, strict comparisons made inclusive
+    double thr64[KX_MAX_TRIG];
+    uint8_t f_fast[KX_MAX_LEAF];  // KxFastAmount of the flow slot (FA_NONE: constant amount)
+    double f_k[KX_MAX_LEAF];      // its constant K
+    double f_sign[KX_MAX_LEAF];   // its sign (the constant amount itself for FA_NONE)
+};
+
+struct SLane {
+    uint32_t live;  // armed barriers not knocked out
+    uint32_t rem;   // flows neither paid nor dropped
+    int e;          // next static event
+    double pv;
+};
+
+template <class Real>
+__device__ __forceinline__ Real sthr(const StaticDev &T, int i) {
+    return sizeof(Real) == 4 ? (Real)T.thr32[i] : (Real)T.thr64[i];
+}
+
+// The contract at step k of a static-schedule path: knock-outs of the live
+// barriers, then the static event of step k (barriers armed and tested at
+// once, flows paid), as on_event orders them (pricer.rs:374-433).
+template <class Real>
+__device__ __forceinline__ void static_event(const StaticDev &T, const double *D, Real s0, Real y, int k, SLane &L) {
+    uint32_t m = L.live;
+    while (m) {
+        const int i = __ffs(m) - 1;
+        m &= m - 1;
+        const Real t = sthr<Real>(T, i);
+        if ((T.up_mask >> i) & 1u ? y >= t : y <= t) {
+            L.live &= ~(1u << i);
+            L.rem &= ~T.kill[i];
+        }
+    }
+    if (L.e < T.n_ev && T.ev_step[L.e] == k) {
+        uint32_t a = T.ev_arm[L.e];
+        while (a) {
+            const int i = __ffs(a) - 1;
+            a &= a - 1;
+            const Real t = sthr<Real>(T, i);
+            if ((T.up_mask >> i) & 1u ? y >= t : y <= t) L.rem &= ~T.kill[i];
+            else L.live |= 1u << i;
+        }
+        uint32_t pay = T.ev_pay[L.e] & L.rem;
+        if (pay) {
+            const Real S = spot_of<Real>(s0, y);
+            while (pay) {
+                const int j = __ffs(pay) - 1;
+                pay &= pay - 1;
+                double amt = T.f_sign[j];
+                if (T.f_fast[j] != FA_NONE) {
+                    const Real K = (Real)T.f_k[j];
+                    Real r;
+                    switch (T.f_fast[j]) {
+                    case FA_CALL: r = fmax(S - K, Real(0)); break;
+                    case FA_PUT: r = fmax(K - S, Real(0)); break;
+                    case FA_SPOT: r = S; break;
+                    default: r = K; break;
+                    }
+                    amt = (double)(T.f_sign[j] < 0.0 ? -r : r);
+                }
+                L.pv = __dadd_rn(L.pv, __dmul_rn(amt, D[k]));
+            }
+        }
+        L.rem &= ~T.ev_pay[L.e];
+        ++L.e;
+    }
+}
+
+template <class Real>
+__device__ __forceinline__ void static_window(const StaticDev &T, uint32_t live, Real &hi, Real &lo) {
+    hi = Real(INFINITY);
+    lo = Real(-INFINITY);
+    uint32_t m = live;
+    while (m) {
+        const int i = __ffs(m) - 1;
+        m &= m - 1;
+        const Real t = sthr<Real>(T, i);
+        if ((T.up_mask >> i) & 1u) hi = fmin(hi, t);
+        else lo = fmax(lo, t);
+    }
+}
+
 template <class Real>
 struct HestonPar {
     Real r, kappa, theta, sigma_v, rho, rho_perp;
@@ -162,7 +267,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 c1 = rec.c1;
             }
             if (MODEL == M_GBM) {
-                y += c0 + c1 * zz[j];  // log-space exact GBM step (simulator.rs:238-245)
+                y = gbm_step(y, c0, c1, zz[j]);  // log-space exact GBM step (simulator.rs:238-245)
             } else {
                 heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
                                   zz[2 * j], zz[2 * j + 1], y, v);
@@ -174,7 +279,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
     return ev;
 }
 
-template <class Real, int MODEL, int MINB>
+template <class Real, int MODEL, int MINB, bool STATIC>
 __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -212,6 +317,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     int k = 0, lim = 0;
     Real y = 0, v = 0, hi = 0, lo = 0;
     Trig st{0, 0, 0, 0, 0, 0, 0, 0, 0.0};
+    SLane sl{0u, 0u, 0, 0.0};
     uint32_t my_steps = 0;
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
@@ -277,7 +383,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 busy = true;
                 y = Real(0);
                 v = fmax(hv0, Real(0));
-                st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
+                if (STATIC) sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
+                else st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
                 k = 0;
             }
             nx += (uint32_t)take;
@@ -327,12 +434,25 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 wait = 0;
                 if (evp) {
                     evp = false;
-                    st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
-                    lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
-                    lim = min(st.nte, nt - 1);
+                    bool done;
+                    double pv;
+                    if (STATIC) {
+                        const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
+                        static_event<Real>(T, D, s0, y, k, sl);
+                        static_window<Real>(T, sl.live, hi, lo);
+                        lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;
+                        done = sl.rem == 0u;
+                        pv = sl.pv;
+                    } else {
+                        st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
+                        lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
+                        lim = min(st.nte, nt - 1);
+                        done = st.done != 0;
+                        pv = st.pv;
+                    }
                     ++k;
-                    if (st.done || k >= nt) {
-                        A.pv[pv_off + path] = st.pv;
+                    if (done || k >= nt) {
+                        A.pv[pv_off + path] = pv;
                         busy = false;
                     }
                 }
@@ -353,7 +473,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
 }
 
 // which: fp64 0/1; returns nullptr for a missing register budget.
-const void *lean_kernel_gbm(int fp64, int minb);
-const void *lean_kernel_heston(int fp64, int minb);
+const void *lean_kernel_gbm(int fp64, int minb, bool stat);
+const void *lean_kernel_heston(int fp64, int minb, bool stat);
 
 }  // namespace kx

@@ -33,7 +33,7 @@ def test_book_equals_individual_prices(prec, tune):
     cs, ms, ns, seeds = _mixed()
     book = kx.Book(cs, ms, ns, seeds, steps_per_year=252, precision=prec, tune=tune)
     info = book.info()
-    assert info["n_contracts"] == len(cs) and info["n_groups"] == 2  # lean and general kernels
+    assert info["n_contracts"] == len(cs) and info["n_groups"] == 3  # static, lean and general kernels
     for rep in range(2):
         res = book.price()
         for c, m, n, s, r in zip(cs, ms, ns, seeds, res):

@@ -1,6 +1,7 @@
-"""The two path kernels value every path identically: k_lean (barrier and
-time-event contracts) against k_paths (every contract), forced through
-KX_PATH_KERNEL, in both precisions and both models, bit for bit."""
+"""The path kernels value every path identically: k_lean on compiled static
+schedules (the default where a contract has one), k_lean with its general
+event handler (KX_PATH_KERNEL=lean) and k_paths (KX_PATH_KERNEL=general), in
+both precisions and both models, bit for bit."""
 import os
 
 import numpy as np
@@ -31,12 +32,15 @@ LEAN = {
 
 def _run(c, model, prec, kernel, n=4000, spy=52):
     old = os.environ.get("KX_PATH_KERNEL")
-    os.environ["KX_PATH_KERNEL"] = kernel
+    if kernel == "auto":
+        os.environ.pop("KX_PATH_KERNEL", None)
+    else:
+        os.environ["KX_PATH_KERNEL"] = kernel
     try:
         return c.price(model, n_paths=n, seed=19, steps_per_year=spy, precision=prec, per_path=True)
     finally:
         if old is None:
-            del os.environ["KX_PATH_KERNEL"]
+            os.environ.pop("KX_PATH_KERNEL", None)
         else:
             os.environ["KX_PATH_KERNEL"] = old
 
@@ -48,8 +52,10 @@ def test_lean_equals_general_gbm(name, prec):
     m = kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X")
     r1, p1 = _run(c, m, prec, "general")
     r2, p2 = _run(c, m, prec, "lean")
+    r3, p3 = _run(c, m, prec, "auto")
     assert np.array_equal(np.asarray(p1), np.asarray(p2)), name
-    assert r1.price == r2.price and r1.std_error == r2.std_error
+    assert np.array_equal(np.asarray(p1), np.asarray(p3)), name
+    assert r1.price == r2.price == r3.price and r1.std_error == r2.std_error == r3.std_error
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
@@ -59,7 +65,9 @@ def test_lean_equals_general_heston(name, prec):
     m = kx.heston(100.0, 0.04, 1.5, 0.04, 0.5, -0.7, 0.03, asset="X")
     _, p1 = _run(c, m, prec, "general", n=2000, spy=100)
     _, p2 = _run(c, m, prec, "lean", n=2000, spy=100)
+    _, p3 = _run(c, m, prec, "auto", n=2000, spy=100)
     assert np.array_equal(np.asarray(p1), np.asarray(p2)), name
+    assert np.array_equal(np.asarray(p1), np.asarray(p3)), name
 
 
 def test_lean_daily_grid_long_paths():
@@ -69,4 +77,17 @@ def test_lean_daily_grid_long_paths():
     m = kx.GBM(s0=180.0, sigma=0.25, r=0.05, asset="X")
     _, p1 = _run(c, m, "fp32", "general", n=100_000, spy=365)
     _, p2 = _run(c, m, "fp32", "lean", n=100_000, spy=365)
+    _, p3 = _run(c, m, "fp32", "auto", n=100_000, spy=365)
     assert np.array_equal(np.asarray(p1), np.asarray(p2))
+    assert np.array_equal(np.asarray(p1), np.asarray(p3))
+
+
+@pytest.mark.parametrize("name,kernel", [("up_and_out", 3), ("double_barrier", 3), ("bermudan_strip", 3),
+                                         ("nested_when", 3), ("late_barrier", 3), ("digital", 2),
+                                         ("knock_in", 2), ("first_touch_pays", 2)])
+def test_kernel_family_selection(name, kernel):
+    """Static schedules serve contracts whose whens read only the time;
+    price-triggered whens (knock-in, first touch) keep the general handler."""
+    m = kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X")
+    _run(LEAN[name](), m, "fp32", "auto", n=1000)
+    assert kx.last_launch_stats()["path_kernel"] == kernel
