@@ -138,24 +138,53 @@ __device__ __forceinline__ void draws4(const AdjArgs &A, uint64_t path, uint64_t
     }
 }
 
+// A contract's parameters in the path precision, converted once per path:
+// GB300's FP64 pipe is a small fraction of its FP32 one, so no double is
+// converted inside the step loops.
+template <class Real>
+struct AdjPar {
+    Real mu, sigma, drift, r, kappa, theta, sigma_v, rho, rho_perp, drp, inv_w, s0;
+    Real thr[ADJ_MAXU];
+};
+
+template <class Real>
+__device__ __forceinline__ AdjPar<Real> adj_par(const AdjArgs &A) {
+    AdjPar<Real> p;
+    p.mu = (Real)A.mu;
+    p.sigma = (Real)A.sigma;
+    p.drift = sub_rn(p.mu, mul_rn(mul_rn(Real(0.5), p.sigma), p.sigma));
+    p.r = (Real)A.r;
+    p.kappa = (Real)A.kappa;
+    p.theta = (Real)A.theta;
+    p.sigma_v = (Real)A.sigma_v;
+    p.rho = (Real)A.rho;
+    p.rho_perp = (Real)A.rho_perp;
+    p.drp = A.rho_perp > 0 ? (Real)(-A.rho / A.rho_perp) : Real(0);
+    p.inv_w = (Real)A.inv_w;
+    p.s0 = (Real)A.s0;
+    for (int u = 0; u < ADJ_MAXU; ++u) p.thr[u] = u < A.n_su ? (Real)A.su[u].thr : Real(0);
+    return p;
+}
+
 // One model step k (from k-1), returning the new (y, v) and the draws used.
 template <class Real, int MODEL>
-__device__ __forceinline__ void model_step(const AdjArgs &A, const StepRec<Real> &rec, Real z1, Real z2, Real &y,
-                                           Real &v) {
+__device__ __forceinline__ void model_step(const AdjPar<Real> &p, int scheme, const StepRec<Real> &rec, Real z1,
+                                           Real z2, Real &y, Real &v) {
     if (MODEL == KX_MODEL_GBM) {
-        const Real dt = rec.c0, sq = rec.c1, sg = (Real)A.sigma;
-        const Real drift = sub_rn((Real)A.mu, mul_rn(mul_rn(Real(0.5), sg), sg));
-        y = gbm_step(y, mul_rn(drift, dt), mul_rn(sg, sq), z1);
+        y = gbm_step(y, mul_rn(p.drift, rec.c0), mul_rn(p.sigma, rec.c1), z1);
     } else {
-        heston_step<Real>((Real)A.r, (Real)A.kappa, (Real)A.theta, (Real)A.sigma_v, (Real)A.rho, (Real)A.rho_perp,
-                          A.scheme, rec.c0, rec.c1, z1, z2, y, v);
+        heston_step<Real>(p.r, p.kappa, p.theta, p.sigma_v, p.rho, p.rho_perp, scheme, rec.c0, rec.c1, z1, z2, y, v);
     }
 }
 
 // One launch covers a list of contracts (each with its own model, grid and
 // path count): the global path index runs over all of them (prefix offsets
 // `off`), so an uneven book is one persistent launch.
-template <class Real, int MODEL>
+//
+// ACC: some contract keeps averages or running extrema. Without them the
+// per-step work is the model step, the smoothed barriers and, only at the
+// steps that pay flows (sorted by step on the host), the amounts.
+template <class Real, int MODEL, bool ACC>
 __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict__ all, const uint64_t *__restrict__ off,
                                                        int n_contracts, uint64_t total, double *__restrict__ out) {
     constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
@@ -173,8 +202,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
         const KxProgram &P = *A.P;
         const int N = A.n_times - 1;  // steps
         const int K = A.K;
-        const Real s0 = (Real)A.s0;
-        const Real inv_w = (Real)A.inv_w;
+        const AdjPar<Real> pp = adj_par<Real>(A);
+        const Real s0 = pp.s0;
+        const Real inv_w = pp.inv_w;
         // ------------------------------ forward ------------------------------
         Real ck_y[ADJ_MAXCK], ck_v[ADJ_MAXCK];
         Real y = Real(0), v = (Real)fmax(A.v0, 0.0);
@@ -197,29 +227,34 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
         Real fcs[ADJ_MAXF], fca[ADJ_MAXF][ADJ_MAXA];
         int farg[ADJ_MAXF][ADJ_MAXA];
         double pv = 0.0, pv_t = 0.0;  // price and sum_f t_f P_f
+        const int nflows = A.n_flows;
+        int nf = 0;                                       // next flow (flows sorted by step)
+        int nft = nflows > 0 ? A.flow[0].t : INT_MAX;     // its step
         Real z[4];
         for (int k = 0; k <= N; ++k) {
             if (k > 0) {
                 const uint64_t d = (uint64_t)(k - 1) * DRAWS;
                 if ((d & 3u) == 0) draws4<Real>(A, path, d, z);
                 const int q = (int)(d & 3u);
-                model_step<Real, MODEL>(A, R[k], z[q], DRAWS == 2 ? z[q + 1] : Real(0), y, v);
+                model_step<Real, MODEL>(pp, A.scheme, R[k], z[q], DRAWS == 2 ? z[q + 1] : Real(0), y, v);
             }
             if (k % K == 0) {
                 ck_y[k / K] = y;
                 ck_v[k / K] = v;
             }
-            const Real S = s0 * fast_exp<Real>(y);
-            for (int a = 0; a < A.n_acc; ++a) {
-                const AdjAcc &Ac = A.acc[a];
-                if (k < Ac.i_from || k > Ac.i_to) continue;
-                if (Ac.kind == ACC_MAX) { if (S > accraw[a]) { accraw[a] = S; argx[a] = k; } }
-                else if (Ac.kind == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
-                else accraw[a] += S;
-            }
+            const bool pays = k == nft;
+            const Real S = (ACC || pays) ? s0 * fast_exp<Real>(y) : Real(0);
+            if (ACC)
+                for (int a = 0; a < A.n_acc; ++a) {
+                    const AdjAcc &Ac = A.acc[a];
+                    if (k < Ac.i_from || k > Ac.i_to) continue;
+                    if (Ac.kind == ACC_MAX) { if (S > accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                    else if (Ac.kind == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                    else accraw[a] += S;
+                }
             for (int u = 0; u < A.n_su; ++u)
                 if (k >= A.su[u].arm) {
-                    const Real thr = (Real)A.su[u].thr;
+                    const Real thr = pp.thr[u];
                     Real x = (y - thr) * inv_w;
                     if (A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT) x = -x;
                     surv[u] *= Real(1) / (Real(1) + fast_exp<Real>(x));
@@ -232,10 +267,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     }
                     if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
-            for (int f = 0; f < A.n_flows; ++f) {
+            if (!pays) continue;
+            for (int f = nf; f < nflows && A.flow[f].t == k; ++f) {
                 const AdjFlow &F = A.flow[f];
-                if (F.t != k) continue;
-                for (int a = 0; a < A.n_acc; ++a)
+                nf = f + 1;
+                if (ACC)
+                    for (int a = 0; a < A.n_acc; ++a)
                     accv[a] = A.acc[a].kind == ACC_SUM ? accraw[a] / (Real)(min(k, A.acc[a].i_to) - A.acc[a].i_from + 1)
                                                        : accraw[a];
                 Dual<Real> amt;
@@ -265,6 +302,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     if (((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
                 if (alive) pv_hard += (double)amt.v * df;
             }
+            nft = nf < nflows ? A.flow[nf].t : INT_MAX;
         }
         // ------------------------------ reverse ------------------------------
         Real sy[ADJ_KMAX + 1], sv[ADJ_KMAX + 1], sz1[ADJ_KMAX + 1], sz2[ADJ_KMAX + 1];
@@ -272,6 +310,8 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
         Real Q[ADJ_MAXU] = {};             // sum of P_f (t_f >= k) under each smoothed until
         Real G[ADJ_MAXA] = {};             // per average: sum of coefficients whose window holds k
         Real g_sig = 0, g_r = 0, g_k = 0, g_th = 0, g_sv = 0, g_rho = 0;
+        int pf = nflows - 1;                              // last flow not yet swept
+        int pft = pf >= 0 ? A.flow[pf].t : -1;            // its step
         const int nseg = (N + K - 1) / K;
         for (int c = nseg - 1; c >= 0; --c) {
             const int k0 = c * K;
@@ -285,7 +325,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 if ((d & 3u) == 0 || k == k0 + 1) draws4<Real>(A, path, d & ~3ull, z);
                 const int q = (int)(d & 3u);
                 const Real a1 = z[q], a2 = DRAWS == 2 ? z[q + 1] : Real(0);
-                model_step<Real, MODEL>(A, R[k], a1, a2, yy, vv);
+                model_step<Real, MODEL>(pp, A.scheme, R[k], a1, a2, yy, vv);
                 sy[k - k0] = yy;
                 sv[k - k0] = vv;
                 sz1[k - k0] = a1;
@@ -300,7 +340,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     const Real dt = rec.c0, sq = rec.c1;
                     const Real z1 = sz1[j + 1], z2 = sz2[j + 1];
                     if (MODEL == KX_MODEL_GBM) {
-                        g_sig += lam * (-(Real)A.sigma * dt + sq * z1);
+                        g_sig += lam * (-pp.sigma * dt + sq * z1);
                         g_r += lam * dt;
                     } else {
                         const Real vk = sv[j];
@@ -309,44 +349,56 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                         const Real dvp = (ft && vk <= Real(0)) ? Real(0) : Real(1);
                         const Real sqv = sqrt(vp);
                         const Real dsq = sqv > Real(0) ? Real(0.5) / sqv : Real(0);  // d sqrt(v)/dv, 0 at v = 0
-                        const Real mix = (Real)A.rho * z1 + (Real)A.rho_perp * z2;
+                        const Real mix = pp.rho * z1 + pp.rho_perp * z2;
                         // v_{k+1} before the floor; the floor passes the adjoint only where it did not bite
-                        const Real vn = vk + (Real)A.kappa * ((Real)A.theta - vp) * dt + (Real)A.sigma_v * sqv * mix * sq;
+                        const Real vn = vk + pp.kappa * (pp.theta - vp) * dt + pp.sigma_v * sqv * mix * sq;
                         const Real m = (ft || vn > Real(0)) ? mu : Real(0);
                         const Real dx_dv = (Real(-0.5) * dt + z1 * sq * dsq) * dvp;
-                        const Real dvn_dv = Real(1) + (-(Real)A.kappa * dt + (Real)A.sigma_v * mix * sq * dsq) * dvp;
+                        const Real dvn_dv = Real(1) + (-pp.kappa * dt + pp.sigma_v * mix * sq * dsq) * dvp;
                         g_r += lam * dt;
-                        g_k += m * ((Real)A.theta - vp) * dt;
-                        g_th += m * (Real)A.kappa * dt;
+                        g_k += m * (pp.theta - vp) * dt;
+                        g_th += m * pp.kappa * dt;
                         g_sv += m * sqv * mix * sq;
-                        const Real drp = A.rho_perp > 0 ? (Real)(-A.rho / A.rho_perp) : Real(0);
-                        g_rho += m * (Real)A.sigma_v * sqv * (z1 + drp * z2) * sq;
+                        g_rho += m * pp.sigma_v * sqv * (z1 + pp.drp * z2) * sq;
                         mu = lam * dx_dv + m * dvn_dv;
                     }
                 }
                 // direct contributions at state k
                 const Real yk = sy[j];
-                const Real Sk = s0 * fast_exp<Real>(yk);
                 Real g = Real(0);
-                for (int f = 0; f < A.n_flows; ++f) {
-                    // an average read at t_f covers [i_from, min(t_f, i_to)]: its coefficient
-                    // joins when the sweep reaches the window's last step
-                    for (int a = 0; a < A.n_acc; ++a)
-                        if (A.acc[a].kind == ACC_SUM && k == min(A.flow[f].t, A.acc[a].i_to)) G[a] += fca[f][a];
-                    if (A.flow[f].t != k) continue;
-                    g += fcs[f] * Sk;
-                    for (int u = 0; u < A.n_su; ++u)
-                        if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
-                }
-                for (int f = 0; f < A.n_flows; ++f)  // running max/min: at the arg-extremum
-                    if (A.flow[f].t >= k)
+                if (ACC) {
+                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    for (int f = 0; f < nflows; ++f) {
+                        // an average read at t_f covers [i_from, min(t_f, i_to)]: its coefficient
+                        // joins when the sweep reaches the window's last step
                         for (int a = 0; a < A.n_acc; ++a)
-                            if (A.acc[a].kind != ACC_SUM && farg[f][a] == k) g += fca[f][a] * Sk;
-                for (int a = 0; a < A.n_acc; ++a)  // averages: inside the window
-                    if (A.acc[a].kind == ACC_SUM && k >= A.acc[a].i_from) g += G[a] * Sk;
+                            if (A.acc[a].kind == ACC_SUM && k == min(A.flow[f].t, A.acc[a].i_to)) G[a] += fca[f][a];
+                        if (A.flow[f].t != k) continue;
+                        g += fcs[f] * Sk;
+                        for (int u = 0; u < A.n_su; ++u)
+                            if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
+                    }
+                    for (int f = 0; f < nflows; ++f)  // running max/min: at the arg-extremum
+                        if (A.flow[f].t >= k)
+                            for (int a = 0; a < A.n_acc; ++a)
+                                if (A.acc[a].kind != ACC_SUM && farg[f][a] == k) g += fca[f][a] * Sk;
+                    for (int a = 0; a < A.n_acc; ++a)  // averages: inside the window
+                        if (A.acc[a].kind == ACC_SUM && k >= A.acc[a].i_from) g += G[a] * Sk;
+                } else if (k == pft) {  // the flows paid at step k, in slot order
+                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    int f0 = pf;
+                    while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
+                    for (int f = f0; f <= pf; ++f) {
+                        g += fcs[f] * Sk;
+                        for (int u = 0; u < A.n_su; ++u)
+                            if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
+                    }
+                    pf = f0 - 1;
+                    pft = pf >= 0 ? A.flow[pf].t : -1;
+                }
                 for (int u = 0; u < A.n_su; ++u)
                     if (k >= A.su[u].arm && Q[u] != Real(0)) {
-                        Real x = (yk - (Real)A.su[u].thr) * inv_w;
+                        Real x = (yk - pp.thr[u]) * inv_w;
                         const bool down = A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT;
                         if (down) x = -x;
                         const Real s = Real(1) / (Real(1) + fast_exp<Real>(x));
@@ -354,8 +406,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                         g += Q[u] * (down ? dls : -dls);
                     }
                 // leaving an average window when walking below its first step
-                for (int a = 0; a < A.n_acc; ++a)
-                    if (A.acc[a].kind == ACC_SUM && k == A.acc[a].i_from) G[a] = Real(0);
+                if (ACC)
+                    for (int a = 0; a < A.n_acc; ++a)
+                        if (A.acc[a].kind == ACC_SUM && k == A.acc[a].i_from) G[a] = Real(0);
                 lam += g;
             }
         }
@@ -464,11 +517,14 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
         fl.sign = F.sign;
         fl.su_mask = mask;
     }
+    // by payment step (slot order within a step): the kernels walk them in order
+    std::stable_sort(a.flow, a.flow + a.n_flows, [](const AdjFlow &x, const AdjFlow &y) { return x.t < y.t; });
 }
 
 template <class Real, int MODEL>
-static const void *adj_kernel() {
-    return reinterpret_cast<const void *>(&k_adjoint<Real, MODEL>);
+static const void *adj_kernel(bool acc) {
+    return acc ? reinterpret_cast<const void *>(&k_adjoint<Real, MODEL, true>)
+               : reinterpret_cast<const void *>(&k_adjoint<Real, MODEL, false>);
 }
 
 // One contract of an adjoint launch (host side).
@@ -587,8 +643,11 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     KX_CUDA(cudaMemcpyAsync(c.items.p, off.data(), (nc + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, c.stream));
     c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + dt.size() * sizeof(double) +
                         nc * sizeof(AdjArgs) + (nc + 1) * sizeof(uint64_t);
-    const void *kfn = model == KX_MODEL_GBM ? (f64 ? adj_kernel<double, KX_MODEL_GBM>() : adj_kernel<float, KX_MODEL_GBM>())
-                                            : (f64 ? adj_kernel<double, KX_MODEL_HESTON>() : adj_kernel<float, KX_MODEL_HESTON>());
+    bool acc = false;
+    for (auto &j : jobs) acc |= j.a.n_acc > 0;
+    const void *kfn = model == KX_MODEL_GBM
+                          ? (f64 ? adj_kernel<double, KX_MODEL_GBM>(acc) : adj_kernel<float, KX_MODEL_GBM>(acc))
+                          : (f64 ? adj_kernel<double, KX_MODEL_HESTON>(acc) : adj_kernel<float, KX_MODEL_HESTON>(acc));
     if (total > 0) {
         const int full = persistent_blocks(kfn, ADJ_BLOCK, 0);
         const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
@@ -649,23 +708,29 @@ static void fill_sens(const std::vector<Stats> &st, int model, double w, kx_sens
 // launch per (model kind, precision) group; prices use the hard barriers.
 void portfolio_adjoint(Ctx &c, size_t n, const kx_program *const *progs, const kx_model *models,
                        const kx_mc_config *cfgs, kx_price_result *out, kx_sens *sens) {
+    std::vector<AdjJob> all;
+    for (size_t i = 0; i < n; ++i) {
+        if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "portfolio pricing uses Philox normals");
+        all.push_back(make_adj_job(program_of(progs[i]), model_from_c(&models[i]), cfgs[i], nullptr));
+    }
+    // one launch per (model kind, precision, averages or extrema present): the
+    // contracts without accumulators get the kernel without their per-step work
     for (int kind = 0; kind < 2; ++kind)
-        for (int prec = 0; prec < 2; ++prec) {
-            std::vector<size_t> idx;
-            for (size_t i = 0; i < n; ++i)
-                if (models[i].kind == kind && cfgs[i].precision == prec) idx.push_back(i);
-            if (idx.empty()) continue;
-            std::vector<AdjJob> jobs;
-            for (size_t i : idx) {
-                if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "portfolio pricing uses Philox normals");
-                jobs.push_back(make_adj_job(program_of(progs[i]), model_from_c(&models[i]), cfgs[i], nullptr));
+        for (int prec = 0; prec < 2; ++prec)
+            for (int acc = 0; acc < 2; ++acc) {
+                std::vector<size_t> idx;
+                for (size_t i = 0; i < n; ++i)
+                    if (models[i].kind == kind && cfgs[i].precision == prec && (all[i].a.n_acc > 0) == (acc == 1))
+                        idx.push_back(i);
+                if (idx.empty()) continue;
+                std::vector<AdjJob> jobs;
+                for (size_t i : idx) jobs.push_back(all[i]);
+                auto st = run_adjoint(c, jobs, prec == KX_PREC_FP64, kind, KX_RNG_PHILOX);
+                for (size_t q = 0; q < idx.size(); ++q) {
+                    out[idx[q]] = finish(st[q][8]);
+                    fill_sens(st[q], kind, jobs[q].w, &sens[idx[q]]);
+                }
             }
-            auto st = run_adjoint(c, jobs, prec == KX_PREC_FP64, kind, KX_RNG_PHILOX);
-            for (size_t q = 0; q < idx.size(); ++q) {
-                out[idx[q]] = finish(st[q][8]);
-                fill_sens(st[q], kind, jobs[q].w, &sens[idx[q]]);
-            }
-        }
 }
 
 }  // namespace kx

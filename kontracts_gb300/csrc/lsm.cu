@@ -70,6 +70,58 @@ __device__ __forceinline__ Real lsm_payoff(const KxProgram &P, Real S, int k) {
     return v;
 }
 
+// The payoff as up to 4 closed-form terms in the path precision, converted
+// once per thread (no double is converted per path on GB300's slow FP64
+// pipe); `ok` is false when some term needs the interpreter.
+template <class Real>
+struct LsmPay {
+    bool ok;
+    int n;
+    uint8_t kind[4];  // FA_NONE: the constant sign[q]
+    Real k[4], sign[4];
+};
+
+template <class Real>
+__device__ __forceinline__ LsmPay<Real> lsm_pay_terms(const KxProgram &P) {
+    LsmPay<Real> t;
+    t.ok = P.n_leaf <= 4;
+    t.n = 0;
+    for (int j = 0; j < P.n_leaf && t.ok; ++j) {
+        const KxLeaf &F = P.leaf[j];
+        if (F.kind != AK_CONST && !F.fast) t.ok = false;
+        t.kind[t.n] = F.kind == AK_CONST ? (uint8_t)FA_NONE : F.fast;
+        t.k[t.n] = F.kind == AK_CONST ? Real(0) : (Real)P.cpool[F.fast_k];
+        t.sign[t.n] = (Real)F.sign;
+        ++t.n;
+    }
+    return t;
+}
+
+// lsm_payoff by the closed-form terms (the same operations as fast_amount).
+template <class Real>
+__device__ __forceinline__ Real lsm_payoff_terms(const LsmPay<Real> &t, Real S) {
+    Real v = Real(0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (q >= t.n) break;
+        Real r;
+        switch (t.kind[q]) {
+        case FA_NONE: v += t.sign[q]; continue;
+        case FA_CALL: r = fmax(S - t.k[q], Real(0)); break;
+        case FA_PUT: r = fmax(t.k[q] - S, Real(0)); break;
+        case FA_SPOT: r = S; break;
+        default: r = t.k[q]; break;
+        }
+        v += t.sign[q] < Real(0) ? -r : r;
+    }
+    return v;
+}
+
+template <class Real>
+__device__ __forceinline__ Real lsm_pay(const LsmPay<Real> &t, const KxProgram &P, Real S, int k) {
+    return t.ok ? lsm_payoff_terms<Real>(t, S) : lsm_payoff<Real>(P, S, k);
+}
+
 template <class Real, int MODEL>
 __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward(const LsmArgs A) {
     constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
@@ -247,7 +299,7 @@ __device__ __forceinline__ double lsm_continuation(const double (&c)[M], double 
 // (upd < 0: initialise them with the payoff at the last date), then
 // accumulate the regression of date `gram` (gram < 0: none).
 template <class Real, int M, int B>
-__global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd, int gram) {
+__global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step(const LsmArgs A, int upd, int gram) {
     constexpr int NA = M * (M + 1) / 2;
     constexpr int NS = NA + M + 1;  // A upper triangle, A^T y, ITM count
     __shared__ double red[32 * 64 + 64];
@@ -275,17 +327,19 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
         }
     }
     const float inv_scale = (float)(1.0 / A.x_scale);
+    const LsmPay<Real> terms = lsm_pay_terms<Real>(P);
     const double disc_u = upd >= 0 ? A.disc[upd] : 0.0;
     const float disc_uf = (float)disc_u;
     const double disc_g = gram >= 0 ? A.disc[gram] : 0.0;
+    const float disc_gf = (float)disc_g;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
          i += (uint64_t)gridDim.x * blockDim.x) {
         Real val;
         if (upd < 0) {
-            val = lsm_payoff<Real>(P, S[(uint64_t)(A.n_ex - 1) * A.n_paths + i], A.n_ex);
+            val = lsm_pay<Real>(terms, P, S[(uint64_t)(A.n_ex - 1) * A.n_paths + i], A.n_ex);
         } else if (F32) {  // the decision in FP32 (FP64 only across threads)
             const float s = (float)S[(uint64_t)upd * A.n_paths + i];
-            const float pay = (float)lsm_payoff<Real>(P, (Real)s, upd + 1);
+            const float pay = (float)lsm_pay<Real>(terms, P, (Real)s, upd + 1);
             const float discounted = (float)V[i] * disc_uf;
             float nv = discounted;
             if (pay > 0.0f) {
@@ -307,7 +361,7 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
             val = (Real)nv;
         } else {
             const Real s = S[(uint64_t)upd * A.n_paths + i];
-            const Real pay = lsm_payoff<Real>(P, s, upd + 1);
+            const Real pay = lsm_pay<Real>(terms, P, s, upd + 1);
             const double discounted = (double)V[i] * disc_u;
             double nv = discounted;
             if (pay > Real(0)) {
@@ -320,9 +374,9 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_step(const LsmArgs A, int upd
         V[i] = val;
         if (gram >= 0) {
             const Real sg = S[(uint64_t)gram * A.n_paths + i];
-            if (lsm_payoff<Real>(P, sg, gram + 1) > Real(0)) {
+            if (lsm_pay<Real>(terms, P, sg, gram + 1) > Real(0)) {
                 if (F32) {
-                    const float yf = (float)val * (float)disc_g;
+                    const float yf = (float)val * disc_gf;
                     float pw[M];
                     lsm_basis_f32<M, B>((float)sg * inv_scale, pw);
                     int q = 0;
