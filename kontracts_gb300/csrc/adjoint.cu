@@ -145,6 +145,9 @@ template <class Real>
 struct AdjPar {
     Real mu, sigma, drift, r, kappa, theta, sigma_v, rho, rho_perp, drp, inv_w, s0;
     Real thr[ADJ_MAXU];
+    // the barrier test of smoothed until u as sgn[u] * y >= hit[u] (strict
+    // comparisons made inclusive at the next representable threshold)
+    Real sgn[ADJ_MAXU], hit[ADJ_MAXU];
 };
 
 template <class Real>
@@ -162,7 +165,16 @@ __device__ __forceinline__ AdjPar<Real> adj_par(const AdjArgs &A) {
     p.drp = A.rho_perp > 0 ? (Real)(-A.rho / A.rho_perp) : Real(0);
     p.inv_w = (Real)A.inv_w;
     p.s0 = (Real)A.s0;
-    for (int u = 0; u < ADJ_MAXU; ++u) p.thr[u] = u < A.n_su ? (Real)A.su[u].thr : Real(0);
+    for (int u = 0; u < ADJ_MAXU; ++u) {
+        const Real t = u < A.n_su ? (Real)A.su[u].thr : Real(0);
+        const int cmp = u < A.n_su ? A.su[u].cmp : CMP_GE;
+        p.thr[u] = t;
+        const bool down = cmp == CMP_LE || cmp == CMP_LT;
+        p.sgn[u] = down ? Real(-1) : Real(1);
+        // y > t  <=>  y >= next_up(t);  y < t  <=>  -y >= -next_down(t)
+        const Real ti = cmp == CMP_GT ? next_up(t) : cmp == CMP_LT ? next_down(t) : t;
+        p.hit[u] = down ? -ti : ti;
+    }
     return p;
 }
 
@@ -228,6 +240,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
         int farg[ADJ_MAXF][ADJ_MAXA];
         double pv = 0.0, pv_t = 0.0;  // price and sum_f t_f P_f
         const int nflows = A.n_flows;
+        const int nsu = A.n_su;
+        int su_arm[ADJ_MAXU];
+        for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
+        int ck = 0, next_ck = 0;                          // next checkpoint slot and its step
         int nf = 0;                                       // next flow (flows sorted by step)
         int nft = nflows > 0 ? A.flow[0].t : INT_MAX;     // its step
         Real z[4];
@@ -238,9 +254,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 const int q = (int)(d & 3u);
                 model_step<Real, MODEL>(pp, A.scheme, R[k], z[q], DRAWS == 2 ? z[q + 1] : Real(0), y, v);
             }
-            if (k % K == 0) {
-                ck_y[k / K] = y;
-                ck_v[k / K] = v;
+            if (k == next_ck) {  // checkpoint every K steps
+                ck_y[ck] = y;
+                ck_v[ck] = v;
+                ++ck;
+                next_ck += K;
             }
             const bool pays = k == nft;
             const Real S = (ACC || pays) ? s0 * fast_exp<Real>(y) : Real(0);
@@ -252,19 +270,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     else if (Ac.kind == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
                     else accraw[a] += S;
                 }
-            for (int u = 0; u < A.n_su; ++u)
-                if (k >= A.su[u].arm) {
-                    const Real thr = pp.thr[u];
-                    Real x = (y - thr) * inv_w;
-                    if (A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT) x = -x;
+            for (int u = 0; u < nsu; ++u)
+                if (k >= su_arm[u]) {
+                    const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;  // > 0 beyond the barrier
                     surv[u] *= Real(1) / (Real(1) + fast_exp<Real>(x));
-                    bool hit;
-                    switch (A.su[u].cmp) {
-                    case CMP_GE: hit = y >= thr; break;
-                    case CMP_GT: hit = y > thr; break;
-                    case CMP_LE: hit = y <= thr; break;
-                    default: hit = y < thr; break;
-                    }
+                    const bool hit = pp.sgn[u] * y >= pp.hit[u];
                     if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
             if (!pays) continue;
@@ -396,14 +406,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     pf = f0 - 1;
                     pft = pf >= 0 ? A.flow[pf].t : -1;
                 }
-                for (int u = 0; u < A.n_su; ++u)
-                    if (k >= A.su[u].arm && Q[u] != Real(0)) {
-                        Real x = (yk - pp.thr[u]) * inv_w;
-                        const bool down = A.su[u].cmp == CMP_LE || A.su[u].cmp == CMP_LT;
-                        if (down) x = -x;
+                for (int u = 0; u < nsu; ++u)
+                    if (k >= su_arm[u] && Q[u] != Real(0)) {
+                        const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
                         const Real s = Real(1) / (Real(1) + fast_exp<Real>(x));
                         const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy|
-                        g += Q[u] * (down ? dls : -dls);
+                        g -= Q[u] * pp.sgn[u] * dls;
                     }
                 // leaving an average window when walking below its first step
                 if (ACC)

@@ -67,6 +67,13 @@ __device__ __forceinline__ float fast_exp<float>(float x) { return __expf(x); }
 template <>
 __device__ __forceinline__ double fast_exp<double>(double x) { return exp(x); }
 
+// Next representable value up / down (a strict comparison with t is the
+// inclusive one with the neighbour of t).
+__device__ __forceinline__ float next_up(float t) { return nextafterf(t, INFINITY); }
+__device__ __forceinline__ double next_up(double t) { return ::nextafter(t, (double)INFINITY); }
+__device__ __forceinline__ float next_down(float t) { return nextafterf(t, -INFINITY); }
+__device__ __forceinline__ double next_down(double t) { return ::nextafter(t, -(double)INFINITY); }
+
 // Separately rounded arithmetic in either precision (never fused into an FMA).
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }

@@ -24,11 +24,6 @@
 
 namespace kx {
 
-__device__ __forceinline__ float next_up(float t) { return nextafterf(t, INFINITY); }
-__device__ __forceinline__ double next_up(double t) { return ::nextafter(t, (double)INFINITY); }
-__device__ __forceinline__ float next_down(float t) { return nextafterf(t, -INFINITY); }
-__device__ __forceinline__ double next_down(double t) { return ::nextafter(t, -(double)INFINITY); }
-
 // Interval test of the live barrier slots: an up slot (>=, >) fires when
 // y >= hi, a down slot (<=, <) when y <= lo. Strict comparisons use the next
 // representable threshold, which gives the same decision for finite y.
