@@ -224,6 +224,24 @@ def _hbm_peak() -> tuple:
         return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
 
 
+def european_fp64(reps=5) -> dict:
+    """Plain European call on GBM: s0 = K = 100, sigma 0.2, r 0.05, T 1, one
+    step, 1,000,000 paths, FP64 paths, seed 42, against Black-Scholes
+    (10.450583572185565)."""
+    import kontracts_gb300 as kx
+    c = kx.european_call("S", 100.0, 1.0)
+    m = kx.GBM(s0=100.0, sigma=0.2, r=0.05, asset="S")
+    best = None
+    for _ in range(reps):
+        r = c.price(m, n_paths=1_000_000, seed=42, steps_per_year=1, precision="fp64")
+        t = _dev_seconds(kx)
+        best = t if best is None or t < best else best
+    bs = 10.450583572185565
+    return {"workload": "European call, 1 step, 1M paths, FP64, seed 42", "seconds": best,
+            "path_steps_per_s": 1_000_000 / best, "price": r.price, "std_error": r.std_error,
+            "black_scholes": bs, "error_in_se": (r.price - bs) / r.std_error}
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -432,7 +450,8 @@ def run_ours(args, ws, rank, local) -> None:
     if greeks is not None:
         line["price_greeks"] = greeks
     if rank == 0 and not args.no_extra:
-        line["other_configs"] = {"heston_book_96": heston_book(), "book_256": book_256(), "lsm_12": lsm_cases()}
+        line["other_configs"] = {"european_fp64": european_fp64(), "heston_book_96": heston_book(),
+                                 "book_256": book_256(), "lsm_12": lsm_cases()}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:

@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;  // > 0 beyond the barrier
-                    surv[u] *= Real(1) / (Real(1) + fast_exp<Real>(x));
+                    surv[u] *= logistic(x);
                     const bool hit = pp.sgn[u] * y >= pp.hit[u];
                     if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real s = Real(1) / (Real(1) + fast_exp<Real>(x));
+                        const Real s = logistic(x);
                         const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy|
                         g -= Q[u] * pp.sgn[u] * dls;
                     }
@@ -527,6 +527,162 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
     }
     // by payment step (slot order within a step): the kernels walk them in order
     std::stable_sort(a.flow, a.flow + a.n_flows, [](const AdjFlow &x, const AdjFlow &y) { return x.t < y.t; });
+}
+
+// GBM contracts without averages or running extrema, checkpoint interval K
+// fixed at compile time: the recomputed segment (K + 1 states and K draws)
+// lives in registers, the segment loops are unrolled, and the GBM step's
+// Jacobian (d y_{k+1} / d y_k = 1) leaves the adjoint unchanged across a
+// step. Same quantities as k_adjoint.
+template <class Real, int K>
+__global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__restrict__ all,
+                                                           const uint64_t *__restrict__ off, int n_contracts,
+                                                           uint64_t total, double *__restrict__ out) {
+    static_assert(K % 4 == 0 && (K & (K - 1)) == 0 && K <= ADJ_KMAX, "K: a power of two, multiple of 4");
+    for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
+         gp += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_contracts - 1;  // contract of global path gp
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= gp) lo = mid;
+            else hi = mid - 1;
+        }
+        const AdjArgs &A = all[lo];
+        const uint64_t path = gp - off[lo];
+        const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+        const KxProgram &P = *A.P;
+        const int N = A.n_times - 1;
+        const AdjPar<Real> pp = adj_par<Real>(A);
+        const Real s0 = pp.s0, inv_w = pp.inv_w;
+        const int nflows = A.n_flows, nsu = A.n_su;
+        int su_arm[ADJ_MAXU];
+        for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
+        // ------------------------------ forward ------------------------------
+        Real ck_y[ADJ_MAXCK];
+        Real y = Real(0);
+        Real surv[ADJ_MAXU];
+        int knock[ADJ_MAXU];
+        for (int u = 0; u < ADJ_MAXU; ++u) {
+            surv[u] = Real(1);
+            knock[u] = INT_MAX;
+        }
+        double pv_hard = 0.0, pv = 0.0, pv_t = 0.0;
+        double fP[ADJ_MAXF];
+        Real fcs[ADJ_MAXF];
+        int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
+        Real z[4];
+        for (int k = 0; k <= N; ++k) {
+            if (k > 0) {
+                const uint64_t d = (uint64_t)(k - 1);
+                if ((d & 3u) == 0) draws4<Real>(A, path, d, z);
+                y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
+            }
+            if (k % K == 0) ck_y[k / K] = y;  // K is a power of two: a mask, not a division
+            for (int u = 0; u < nsu; ++u)
+                if (k >= su_arm[u]) {
+                    const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
+                    surv[u] *= logistic(x);
+                    if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
+                }
+            if (k != nft) continue;
+            const Real S = s0 * fast_exp<Real>(y);
+            for (int f = nf; f < nflows && A.flow[f].t == k; ++f) {
+                const AdjFlow &F = A.flow[f];
+                nf = f + 1;
+                Dual<Real> amt;
+                if (F.kind == AK_CONST) {
+                    amt.v = (Real)F.sign;
+                    for (int q = 0; q < 1 + ADJ_MAXA; ++q) amt.d[q] = Real(0);
+                } else {
+                    Real none[ADJ_MAXA] = {};
+                    amt = eval_dual<Real>(P, F.code_off, F.code_len, S, none);
+                }
+                Real w = Real(1);
+                for (int u = 0; u < nsu; ++u)
+                    if ((F.su_mask >> u) & 1u) w *= surv[u];
+                const double df = A.disc[k];
+                fP[f] = (double)amt.v * (double)w * df;
+                fcs[f] = (Real)((double)(amt.d[0] * w) * df);
+                pv += fP[f];
+                pv_t += A.times[k] * fP[f];
+                bool alive = true;
+                for (int u = 0; u < nsu; ++u)
+                    if (((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
+                if (alive) pv_hard += (double)amt.v * df;
+            }
+            nft = nf < nflows ? A.flow[nf].t : INT_MAX;
+        }
+        // ------------------------------ reverse ------------------------------
+        Real lam = Real(0);  // dPV/dy_{k+1}
+        Real Q[ADJ_MAXU] = {};
+        Real g_sig = Real(0), g_r = Real(0);
+        int pf = nflows - 1, pft = pf >= 0 ? A.flow[pf].t : -1;
+        const int nseg = (N + K - 1) / K;
+        for (int c = nseg - 1; c >= 0; --c) {
+            const int k0 = c * K;
+            const int k1 = min(k0 + K, N);
+            Real sy[K + 1], sz[K + 2];
+            sy[0] = ck_y[c];
+            sz[K + 1] = Real(0);
+#pragma unroll
+            for (int q = 0; q < K / 4; ++q) {  // the draws of steps k0 + 1 .. k0 + K
+                Real w4[4];
+                draws4<Real>(A, path, (uint64_t)(k0 + 4 * q), w4);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) sz[1 + 4 * q + j] = w4[j];
+            }
+#pragma unroll
+            for (int j = 1; j <= K; ++j) {
+                const int k = k0 + j;
+                const StepRec<Real> rec = R[min(k, N)];  // past N: harmless states never read
+                sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
+            }
+            const int jtop = (c == nseg - 1) ? k1 - k0 : k1 - k0 - 1;
+#pragma unroll
+            for (int j = K; j >= 0; --j) {
+                if (j > jtop) continue;
+                const int k = k0 + j;
+                if (k < N) {  // step k -> k + 1: d y_{k+1} / d y_k = 1, so lam carries over
+                    const StepRec<Real> rn = R[k + 1];
+                    g_sig += lam * (-pp.sigma * rn.c0 + rn.c1 * sz[j + 1]);
+                    g_r += lam * rn.c0;
+                }
+                const Real yk = sy[j];
+                Real g = Real(0);
+                if (k == pft) {  // the flows paid at step k, in slot order
+                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    int f0 = pf;
+                    while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
+                    for (int f = f0; f <= pf; ++f) {
+                        g += fcs[f] * Sk;
+                        for (int u = 0; u < nsu; ++u)
+                            if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
+                    }
+                    pf = f0 - 1;
+                    pft = pf >= 0 ? A.flow[pf].t : -1;
+                }
+                for (int u = 0; u < nsu; ++u)
+                    if (k >= su_arm[u] && Q[u] != Real(0)) {
+                        const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
+                        const Real sv = logistic(x);
+                        g -= Q[u] * pp.sgn[u] * (Real(1) - sv) * inv_w;
+                    }
+                lam += g;
+            }
+        }
+        double *o = out + A.out_off + path;
+        const uint64_t n = total;
+        o[8 * n] = pv_hard;
+        o[0 * n] = pv;
+        o[1 * n] = (double)lam / A.s0;
+        o[2 * n] = (double)g_sig;
+        o[3 * n] = (double)g_r - pv_t;
+    }
+}
+
+template <class Real, int K>
+static const void *adj_gbm_kernel() {
+    return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K>);
 }
 
 template <class Real, int MODEL>
@@ -652,26 +808,59 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + dt.size() * sizeof(double) +
                         nc * sizeof(AdjArgs) + (nc + 1) * sizeof(uint64_t);
     bool acc = false;
-    for (auto &j : jobs) acc |= j.a.n_acc > 0;
+    int max_n = 0;
+    for (auto &j : jobs) {
+        acc |= j.a.n_acc > 0;
+        max_n = std::max(max_n, j.a.n_times - 1);
+    }
     const void *kfn = model == KX_MODEL_GBM
                           ? (f64 ? adj_kernel<double, KX_MODEL_GBM>(acc) : adj_kernel<float, KX_MODEL_GBM>(acc))
                           : (f64 ? adj_kernel<double, KX_MODEL_HESTON>(acc) : adj_kernel<float, KX_MODEL_HESTON>(acc));
+    // GBM without accumulators: the register-resident kernel at a tuned
+    // checkpoint interval (results do not depend on it: the recomputation
+    // repeats the forward pass's operations)
+    std::vector<std::pair<int, const void *>> cands;
+    if (model == KX_MODEL_GBM && !acc) {
+        if (max_n / 8 + 1 <= ADJ_MAXCK) cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>() : adj_gbm_kernel<float, 8>()});
+        if (max_n / 16 + 1 <= ADJ_MAXCK)
+            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16>() : adj_gbm_kernel<float, 16>()});
+    }
     if (total > 0) {
-        const int full = persistent_blocks(kfn, ADJ_BLOCK, 0);
-        const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
         const AdjArgs *ap = c.cons.as<AdjArgs>();
         const uint64_t *op = c.items.as<uint64_t>();
         double *outp = c.pv.as<double>();
         void *kargs[] = {&ap, &op, (void *)&nc, (void *)&total, &outp};
-        KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-        KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(ADJ_BLOCK), kargs, 0, c.stream));
-        KX_CUDA(cudaEventRecord(c.ev1, c.stream));
-        KX_CUDA(cudaEventSynchronize(c.ev1));
-        float ms = 0.f;
-        KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        auto launch = [&](const void *fn) {
+            const int full = persistent_blocks(fn, ADJ_BLOCK, 0);
+            const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
+            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+            KX_CUDA(cudaLaunchKernel(fn, dim3(blocks), dim3(ADJ_BLOCK), kargs, 0, c.stream));
+            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+            KX_CUDA(cudaEventSynchronize(c.ev1));
+            float ms = 0.f;
+            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+            c.last.grid_blocks = (uint32_t)blocks;
+            return ms;
+        };
+        if (!cands.empty()) {
+            static int tuned_k[2] = {0, 0};  // per precision; 0: not tuned yet
+            const char *env = getenv("KX_TUNE");
+            const bool tune = !(env && env[0] == '0');
+            int &tk = tuned_k[f64 ? 1 : 0];
+            if (tune && tk == 0 && cands.size() > 1) {
+                float best = 1e30f;
+                for (auto &cd : cands) {
+                    const float ms = launch(cd.second);  // this call's own work: every candidate computes it
+                    if (ms < best) { best = ms; tk = cd.first; }
+                }
+            }
+            kfn = cands[0].second;
+            for (auto &cd : cands)
+                if (cd.first == (tk ? tk : 8)) kfn = cd.second;
+        }
+        const float ms = launch(kfn);
         c.last.kernel_ms += ms;
         c.last.kernel_launches++;
-        c.last.grid_blocks = (uint32_t)blocks;
         c.last.block_threads = ADJ_BLOCK;
     }
     std::vector<StatsJob> sj;

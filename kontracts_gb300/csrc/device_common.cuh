@@ -74,6 +74,11 @@ __device__ __forceinline__ double next_up(double t) { return ::nextafter(t, (dou
 __device__ __forceinline__ float next_down(float t) { return nextafterf(t, -INFINITY); }
 __device__ __forceinline__ double next_down(double t) { return ::nextafter(t, -(double)INFINITY); }
 
+// The logistic 1 / (1 + e^x) of a smoothed barrier (FP32: hardware exp and
+// the approximate divide; every kernel that weighs a path uses this one).
+__device__ __forceinline__ float logistic(float x) { return __fdividef(1.0f, 1.0f + __expf(x)); }
+__device__ __forceinline__ double logistic(double x) { return 1.0 / (1.0 + exp(x)); }
+
 // Separately rounded arithmetic in either precision (never fused into an FMA).
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }

@@ -186,7 +186,7 @@ template <class Real>
 __device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, Real inv_w) {
     Real x = (y - thr) * inv_w;  // > 0 beyond the barrier for >=, >
     if (cmp == CMP_LE || cmp == CMP_LT) x = -x;
-    return Real(1) / (Real(1) + fast_exp<Real>(x));
+    return logistic(x);
 }
 
 // Full condition evaluation of the slots in `mask` at step k: time bits from

@@ -288,6 +288,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     // long enough that waiting costs more than it saves.
     constexpr int EV_BATCH = MODEL == M_GBM ? 8 : 1;
     constexpr int EV_WAIT = 8;
+    // Philox blocks a lane steps through per round of the warp loop: two for
+    // GBM (8 steps) halve the per-round hand-out and event ballots per step.
+    constexpr int BPI = MODEL == M_GBM ? 2 : 1;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
     int cur = -1, pend = -1;
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
         // ---- one Philox block of this lane's path, up to the next event ----
         bool ev = busy && (k == 0 || evp);  // a waiting event or step 0 of a new path
         if (busy && !ev) {
-            {
+            for (int bb = 0; bb < BPI && !ev; ++bb) {
                 const uint32_t km1 = (uint32_t)(k - 1);
                 const uint32_t blk = km1 / SPB;
                 const int off = (int)(km1 % SPB);
