@@ -208,6 +208,25 @@ kx_status kx_price(const kx_program *prog, const kx_model *model,
                    const kx_mc_config *cfg, kx_price_result *out,
                    double *per_path_pv);
 
+/* ---- path ranges (sharding a price over GPUs or calls) --------------------
+ * No reference counterpart. kx_price_chunks prices paths first_path ..
+ * first_path + cfg->n_paths - 1 of the stream `cfg->seed` (the same paths a
+ * kx_price of first_path + n_paths paths would simulate) and returns their
+ * statistics per chunk of KX_STATS_CHUNK paths. first_path must be a multiple
+ * of KX_STATS_CHUNK and first_path + n_paths at most 2^32; Philox only.
+ * kx_merge_chunks merges chunk statistics in the given order (Chan et al.)
+ * into a price: the chunks of consecutive ranges, merged in path order, give
+ * exactly kx_price's result for the whole range. */
+#define KX_STATS_CHUNK 16384u
+typedef struct kx_chunk_stats {
+    double n, mean, m2;  /* paths, mean, sum of squared deviations */
+} kx_chunk_stats;
+kx_status kx_price_chunks(const kx_program *prog, const kx_model *model,
+                          const kx_mc_config *cfg, uint64_t first_path,
+                          kx_chunk_stats *out, size_t cap, size_t *n_out);
+kx_status kx_merge_chunks(const kx_chunk_stats *chunks, size_t n,
+                          kx_price_result *out);
+
 /* kx_price for callers that must not allocate device memory while pricing
  * (no counterpart in the reference). Same arguments and same result as
  * kx_price; every device buffer of the call lives in one static device array

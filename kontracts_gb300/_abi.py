@@ -117,6 +117,11 @@ class KxBookInfo(C.Structure):
 
 
 KX_BOOK_TUNE = 1
+KX_STATS_CHUNK = 16384
+
+
+class KxChunkStats(C.Structure):
+    _fields_ = [("n", C.c_double), ("mean", C.c_double), ("m2", C.c_double)]
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "libkontract_gpu.so")
@@ -155,6 +160,9 @@ SIGNATURES = {
                                               C.POINTER(C.c_double), C.c_size_t, C.c_int32, C.c_int32,
                                               C.POINTER(KxPriceResult)]),
     "kx_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+    "kx_price_chunks": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig), C.c_uint64,
+                                  C.POINTER(KxChunkStats), C.c_size_t, C.POINTER(C.c_size_t)]),
+    "kx_merge_chunks": (C.c_int, [C.POINTER(KxChunkStats), C.c_size_t, C.POINTER(KxPriceResult)]),
     "kx_book_create": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                  C.c_uint32, C.POINTER(_P)]),
     "kx_book_price": (C.c_int, [_P, C.POINTER(KxPriceResult)]),

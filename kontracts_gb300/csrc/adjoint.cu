@@ -534,7 +534,7 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
 // lives in registers, the segment loops are unrolled, and the GBM step's
 // Jacobian (d y_{k+1} / d y_k = 1) leaves the adjoint unchanged across a
 // step. Same quantities as k_adjoint.
-template <class Real, int K>
+template <class Real, int K, int NSU>
 __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__restrict__ all,
                                                            const uint64_t *__restrict__ off, int n_contracts,
                                                            uint64_t total, double *__restrict__ out) {
@@ -554,8 +554,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
         const int N = A.n_times - 1;
         const AdjPar<Real> pp = adj_par<Real>(A);
         const Real s0 = pp.s0, inv_w = pp.inv_w;
-        const int nflows = A.n_flows, nsu = A.n_su;
+        const int nflows = A.n_flows;
+        constexpr int nsu = NSU;
         int su_arm[ADJ_MAXU];
+#pragma unroll
         for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
         // ------------------------------ forward ------------------------------
         Real ck_y[ADJ_MAXCK];
@@ -578,6 +580,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                 y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
             }
             if (k % K == 0) ck_y[k / K] = y;  // K is a power of two: a mask, not a division
+#pragma unroll
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
@@ -598,6 +601,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                     amt = eval_dual<Real>(P, F.code_off, F.code_len, S, none);
                 }
                 Real w = Real(1);
+#pragma unroll
                 for (int u = 0; u < nsu; ++u)
                     if ((F.su_mask >> u) & 1u) w *= surv[u];
                 const double df = A.disc[k];
@@ -606,6 +610,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                 pv += fP[f];
                 pv_t += A.times[k] * fP[f];
                 bool alive = true;
+#pragma unroll
                 for (int u = 0; u < nsu; ++u)
                     if (((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
                 if (alive) pv_hard += (double)amt.v * df;
@@ -655,12 +660,14 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                     while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
                     for (int f = f0; f <= pf; ++f) {
                         g += fcs[f] * Sk;
+#pragma unroll
                         for (int u = 0; u < nsu; ++u)
                             if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
                     }
                     pf = f0 - 1;
                     pft = pf >= 0 ? A.flow[pf].t : -1;
                 }
+#pragma unroll
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
@@ -681,8 +688,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
 }
 
 template <class Real, int K>
-static const void *adj_gbm_kernel() {
-    return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K>);
+static const void *adj_gbm_kernel(int nsu) {
+    switch (nsu) {
+    case 0: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 0>);
+    case 1: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 1>);
+    default: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 2>);
+    }
 }
 
 template <class Real, int MODEL>
@@ -808,10 +819,13 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     c.last.h2d_bytes += progs.size() * sizeof(KxProgram) + steps.size() + dt.size() * sizeof(double) +
                         nc * sizeof(AdjArgs) + (nc + 1) * sizeof(uint64_t);
     bool acc = false;
-    int max_n = 0;
+    int max_n = 0, nsu = -1;
+    bool same_nsu = true;
     for (auto &j : jobs) {
         acc |= j.a.n_acc > 0;
         max_n = std::max(max_n, j.a.n_times - 1);
+        if (nsu >= 0 && j.a.n_su != nsu) same_nsu = false;
+        nsu = j.a.n_su;
     }
     const void *kfn = model == KX_MODEL_GBM
                           ? (f64 ? adj_kernel<double, KX_MODEL_GBM>(acc) : adj_kernel<float, KX_MODEL_GBM>(acc))
@@ -820,10 +834,11 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     // checkpoint interval (results do not depend on it: the recomputation
     // repeats the forward pass's operations)
     std::vector<std::pair<int, const void *>> cands;
-    if (model == KX_MODEL_GBM && !acc) {
-        if (max_n / 8 + 1 <= ADJ_MAXCK) cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>() : adj_gbm_kernel<float, 8>()});
+    if (model == KX_MODEL_GBM && !acc && same_nsu) {
+        if (max_n / 8 + 1 <= ADJ_MAXCK)
+            cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>(nsu) : adj_gbm_kernel<float, 8>(nsu)});
         if (max_n / 16 + 1 <= ADJ_MAXCK)
-            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16>() : adj_gbm_kernel<float, 16>()});
+            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16>(nsu) : adj_gbm_kernel<float, 16>(nsu)});
     }
     if (total > 0) {
         const AdjArgs *ap = c.cons.as<AdjArgs>();
@@ -843,10 +858,10 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             return ms;
         };
         if (!cands.empty()) {
-            static int tuned_k[2] = {0, 0};  // per precision; 0: not tuned yet
+            static int tuned_k[2][ADJ_MAXU + 1] = {};  // per precision and barrier count; 0: not tuned yet
             const char *env = getenv("KX_TUNE");
             const bool tune = !(env && env[0] == '0');
-            int &tk = tuned_k[f64 ? 1 : 0];
+            int &tk = tuned_k[f64 ? 1 : 0][std::min(std::max(nsu, 0), ADJ_MAXU)];
             if (tune && tk == 0 && cands.size() > 1) {
                 float best = 1e30f;
                 for (auto &cd : cands) {
@@ -910,14 +925,16 @@ void portfolio_adjoint(Ctx &c, size_t n, const kx_program *const *progs, const k
         if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "portfolio pricing uses Philox normals");
         all.push_back(make_adj_job(program_of(progs[i]), model_from_c(&models[i]), cfgs[i], nullptr));
     }
-    // one launch per (model kind, precision, averages or extrema present): the
-    // contracts without accumulators get the kernel without their per-step work
+    // one launch per (model kind, precision, averages or extrema present,
+    // smoothed barrier count): each group gets the kernel specialised for it
     for (int kind = 0; kind < 2; ++kind)
         for (int prec = 0; prec < 2; ++prec)
-            for (int acc = 0; acc < 2; ++acc) {
+            for (int acc = 0; acc < 2; ++acc)
+                for (int nsu = 0; nsu <= ADJ_MAXU; ++nsu) {
                 std::vector<size_t> idx;
                 for (size_t i = 0; i < n; ++i)
-                    if (models[i].kind == kind && cfgs[i].precision == prec && (all[i].a.n_acc > 0) == (acc == 1))
+                    if (models[i].kind == kind && cfgs[i].precision == prec && (all[i].a.n_acc > 0) == (acc == 1) &&
+                        all[i].a.n_su == nsu)
                         idx.push_back(i);
                 if (idx.empty()) continue;
                 std::vector<AdjJob> jobs;
@@ -927,7 +944,7 @@ void portfolio_adjoint(Ctx &c, size_t n, const kx_program *const *progs, const k
                     out[idx[q]] = finish(st[q][8]);
                     fill_sens(st[q], kind, jobs[q].w, &sens[idx[q]]);
                 }
-            }
+                }
 }
 
 }  // namespace kx

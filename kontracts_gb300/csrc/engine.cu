@@ -505,7 +505,9 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
         else pack_steps<float>(j.tab, P.steps);
         d.disc_off = (int32_t)P.disc.size();
         P.disc.insert(P.disc.end(), j.tab.disc.begin(), j.tab.disc.end());
-        d.pv_off = P.total;
+        // per-path values of paths path_base .. path_base + n - 1 land at
+        // pv_off .. pv_off + n - 1: the kernels index pv_off + path (mod 2^64)
+        d.pv_off = P.total - (uint64_t)j.path_base;
         j.dev.pv_off = P.total;
         P.total += d.n_paths;
         P.path_steps += d.n_paths * (uint64_t)(d.n_times > 0 ? d.n_times - 1 : 0);
@@ -547,8 +549,8 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     item = (item + 31) / 32 * 32;
     P.item_paths = item;
     for (int ci : order) {
-        const uint64_t n = P.cons[ci].n_paths;
-        for (uint64_t b = 0; b < n; b += item) P.items.push_back(WorkItem{ci, 0, b, std::min(item, n - b)});
+        const uint64_t n = P.cons[ci].n_paths, base = jobs[ci].path_base;
+        for (uint64_t b = 0; b < n; b += item) P.items.push_back(WorkItem{ci, 0, base + b, std::min(item, n - b)});
     }
     P.grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (P.items.size() + 7) / 8 + 1);
     return P;
@@ -857,6 +859,65 @@ kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_co
             c.last.d2h_bytes += cfg->n_paths * sizeof(double);
         }
         end_call(c);
+    });
+}
+
+kx_status kx_price_chunks(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg, uint64_t first_path,
+                          kx_chunk_stats *out, size_t cap, size_t *n_out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        if (!out || !n_out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (cfg->rng != KX_RNG_PHILOX) raise(KX_INVALID_ARGUMENT, "path ranges draw from Philox");
+        if (first_path % KX_STATS_CHUNK != 0) raise(KX_INVALID_ARGUMENT, "first_path must be a multiple of KX_STATS_CHUNK");
+        if (first_path + cfg->n_paths > (1ull << 32)) raise(KX_INVALID_ARGUMENT, "first_path + n_paths must be at most 2^32");
+        const size_t nc = (size_t)((cfg->n_paths + KX_STATS_CHUNK - 1) / KX_STATS_CHUNK);
+        if (cap < nc) raise(KX_INVALID_ARGUMENT, "out holds " + std::to_string(cap) + " chunks, " + std::to_string(nc) +
+                                                     " needed");
+        validate_model(m);
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, m.requires_fine_grid());  // pricer.rs:104
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        std::vector<Job> jobs;
+        jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
+        jobs[0].path_base = (uint32_t)first_path;
+        uint64_t stride = 0;
+        run_paths(c, jobs, *cfg, 1, stride);
+        // the chunks of kx_price's reduction, returned unmerged
+        const uint32_t CH = KX_STATS_CHUNK;
+        std::vector<ChunkDesc> chunks;
+        for (uint64_t b = 0; b < cfg->n_paths; b += CH)
+            chunks.push_back(ChunkDesc{b, (uint32_t)std::min<uint64_t>(CH, cfg->n_paths - b), 0});
+        if (!chunks.empty()) {
+            c.chunks.ensure(chunks.size() * sizeof(ChunkDesc));
+            c.chunk_out.ensure(chunks.size() * sizeof(ChunkOut));
+            c.weights.ensure(8 * sizeof(double));
+            const double w[8] = {1, 0, 0, 0, 0, 0, 0, 0};
+            KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice,
+                                    c.stream));
+            KX_CUDA(cudaMemcpyAsync(c.weights.p, w, sizeof w, cudaMemcpyHostToDevice, c.stream));
+            launch_chunk_stats(c.stream, c.pv.as<double>(), stride, 1, c.weights.as<double>(),
+                               c.chunks.as<ChunkDesc>(), c.chunk_out.as<ChunkOut>(), (unsigned)chunks.size());
+            c.last.kernel_launches++;
+            std::vector<ChunkOut> h(chunks.size());
+            KX_CUDA(cudaMemcpyAsync(h.data(), c.chunk_out.p, h.size() * sizeof(ChunkOut), cudaMemcpyDeviceToHost,
+                                    c.stream));
+            KX_CUDA(cudaStreamSynchronize(c.stream));
+            for (size_t q = 0; q < h.size(); ++q) out[q] = kx_chunk_stats{h[q].n, h[q].mean, h[q].m2};
+        }
+        *n_out = chunks.size();
+        end_call(c);
+    });
+}
+
+kx_status kx_merge_chunks(const kx_chunk_stats *chunks, size_t n, kx_price_result *out) {
+    return guarded([&] {
+        if (!out || (n && !chunks)) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        std::vector<ChunkOut> h(n);
+        for (size_t q = 0; q < n; ++q) h[q] = ChunkOut{chunks[q].n, chunks[q].mean, chunks[q].m2};
+        *out = finish(merge_chunks(h.data(), n));
     });
 }
 

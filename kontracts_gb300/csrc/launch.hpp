@@ -15,6 +15,7 @@ struct Job {  // one contract of a launch
     ContractDev dev;
     Model model;
     std::vector<double> thr;  // [KX_MAX_NS][KX_MAX_SPOT] log(B / s0_s)
+    uint32_t path_base = 0;   // first path index of the stream this launch prices
 };
 
 // Scenario parameters (bump scenarios share the normals of a path).

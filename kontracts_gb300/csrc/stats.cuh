@@ -4,11 +4,13 @@
 #pragma once
 #include <cstdint>
 
+#include "../../include/kontract_gpu.h"
+
 namespace kx {
 
 // Values per chunk: a chunk's statistics do not depend on how many chunks
 // or blocks a launch has, so every launch shape gives the same result.
-constexpr uint32_t KX_STATS_CHUNK = 16384;
+static_assert(KX_STATS_CHUNK == 16384u, "chunk size of the C ABI");
 
 struct ChunkDesc {
     uint64_t begin;

@@ -1,0 +1,76 @@
+"""One price sharded over ranks (one GPU per rank, torch.distributed).
+
+Paths are independent and the Philox counter of a path is its index, so a
+price shards without any exchange on the data path: rank r of w prices a
+contiguous, chunk-aligned range of the paths of one stream (the same paths a
+single GPU would simulate for that range) and keeps its statistics per chunk
+of KX_STATS_CHUNK paths. The only collective is the gather of those chunk
+statistics (three doubles per 16,384 paths); every rank merges them in path
+order, so every rank returns exactly the price one GPU gives for all paths.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Sequence
+
+from . import _abi
+
+CHUNK = _abi.KX_STATS_CHUNK
+
+
+def shard_range(n_paths: int, world: int, rank: int) -> tuple[int, int]:
+    """(first_path, count) of rank `rank`: whole chunks, the first ranks take
+    one chunk more when the chunks do not divide evenly."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    n_chunks = (n_paths + CHUNK - 1) // CHUNK
+    base, extra = divmod(n_chunks, world)
+    c0 = rank * base + min(rank, extra)
+    c1 = c0 + base + (1 if rank < extra else 0)
+    first = min(c0 * CHUNK, n_paths)
+    return first, min(c1 * CHUNK, n_paths) - first
+
+
+def price_chunks(contract, model, first_path: int, n_paths: int, seed: int = 42, steps_per_year: int = 50,
+                 precision: str = "fp32") -> list[tuple[float, float, float]]:
+    """Chunk statistics (n, mean, M2) of paths first_path .. first_path + n_paths - 1."""
+    from . import _cfg, _check, _lib, _lock
+    cm = model._c()
+    cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, False)
+    cap = max(1, (n_paths + CHUNK - 1) // CHUNK)
+    out = (_abi.KxChunkStats * cap)()
+    n_out = C.c_size_t()
+    with _lock:
+        _check(_lib().kx_price_chunks(contract._handle().h, C.byref(cm), C.byref(cfg), int(first_path), out, cap,
+                                      C.byref(n_out)))
+    return [(out[q].n, out[q].mean, out[q].m2) for q in range(n_out.value)]
+
+
+def merge(chunks: Sequence[tuple[float, float, float]]):
+    """The price of chunk statistics merged in the given order (the library's
+    own merge, so the result equals kx_price's bit for bit)."""
+    from . import PriceResult, _check, _lib
+    arr = (_abi.KxChunkStats * max(1, len(chunks)))(*[_abi.KxChunkStats(*c) for c in chunks])
+    out = _abi.KxPriceResult()
+    _check(_lib().kx_merge_chunks(arr, len(chunks), C.byref(out)))
+    return PriceResult(out)
+
+
+def price_sharded(contract, model, n_paths: int, seed: int = 42, steps_per_year: int = 50, precision: str = "fp32",
+                  group=None, chunk_fn: Callable[[int, int], list] | None = None):
+    """Price over the ranks of `group` (the default process group). Every rank
+    returns the same PriceResult, equal to one GPU's. chunk_fn(first, count)
+    replaces the GPU call (it returns that range's chunk statistics)."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    first, count = shard_range(n_paths, world, rank)
+    if chunk_fn is not None:
+        mine = chunk_fn(first, count)
+    elif count:
+        mine = price_chunks(contract, model, first, count, seed, steps_per_year, precision)
+    else:
+        mine = []
+    gathered: list = [None] * world
+    dist.all_gather_object(gathered, mine, group=group)
+    return merge([c for part in gathered for c in part])

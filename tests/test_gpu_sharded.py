@@ -1,0 +1,37 @@
+"""Path ranges on the GPU: the chunk statistics of consecutive chunk-aligned
+ranges of one stream, merged in path order, are kx_price's result for the
+whole range, bit for bit (the ranks of a sharded price each compute one
+range)."""
+import pytest
+
+import kontracts_gb300 as kx
+from kontracts_gb300 import _abi, sharded
+
+pytestmark = pytest.mark.gpu
+
+C = sharded.CHUNK
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", ["up_and_out", "asian", "knock_in"])
+def test_ranges_merge_to_the_whole_price(name, prec):
+    S = kx.S("X")
+    c = {"up_and_out": kx.up_and_out_call("X", 100.0, 130.0, 1.0),
+         "asian": kx.scale((kx.average(S) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+         "knock_in": kx.anytime(S >= 120.0, kx.european_call("X", 100.0, 1.0))}[name]
+    m = kx.GBM(s0=100.0, sigma=0.25, r=0.03, asset="X")
+    n = 5 * C + 123
+    full = c.price(m, n_paths=n, seed=5, steps_per_year=252, precision=prec)
+    parts = []
+    for first, count in (sharded.shard_range(n, 3, r) for r in range(3)):
+        parts += sharded.price_chunks(c, m, first, count, seed=5, steps_per_year=252, precision=prec)
+    r = sharded.merge(parts)
+    assert r.price == full.price and r.std_error == full.std_error and r.n_paths == n
+
+
+def test_ranges_must_start_on_a_chunk():
+    c = kx.european_call("X", 100.0, 1.0)
+    m = kx.GBM(s0=100.0, sigma=0.25, r=0.03, asset="X")
+    with pytest.raises(kx.KontractError) as e:
+        sharded.price_chunks(c, m, 100, 1000)
+    assert e.value.status == "InvalidArgument"

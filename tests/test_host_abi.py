@@ -35,7 +35,7 @@ STRUCTS = {
     "kx_model": _abi.KxModel, "kx_mc_config": _abi.KxMcConfig, "kx_price_result": _abi.KxPriceResult,
     "kx_bumps": _abi.KxBumps, "kx_greeks": _abi.KxGreeks, "kx_adjoint_cfg": _abi.KxAdjointCfg,
     "kx_sens": _abi.KxSens, "kx_launch_stats": _abi.KxLaunchStats, "kx_plan_info": _abi.KxPlanInfo,
-    "kx_book_info": _abi.KxBookInfo,
+    "kx_book_info": _abi.KxBookInfo, "kx_chunk_stats": _abi.KxChunkStats,
 }
 
 
