@@ -70,16 +70,16 @@ std::vector<Job> group_jobs(kx_book &b, const kx_book::Group &g) {
     return jobs;
 }
 
-// Device pointers of a group's tables inside the arena: the table regions are
-// sized for the largest plan the tuner may build (work items of 64 paths).
+// Device pointers of a group's tables inside the arena (the sizes do not
+// depend on the launch shape the tuner tries).
 struct Region {
     size_t progs, steps, disc, cons, thr, items, statics;
 };
 
-Region region_sizes(const PathPlan &P, uint64_t max_items) {
+Region region_sizes(const PathPlan &P) {
     return Region{A256(P.progs.size() * sizeof(KxProgram)), A256(P.steps.size()), A256(P.disc.size() * sizeof(double)),
-                  A256(P.cons.size() * sizeof(ContractDev)), A256(P.thr.size()), A256(max_items * sizeof(WorkItem)),
-                  A256(P.statics.size() * sizeof(StaticDev))};
+                  A256(P.cons.size() * sizeof(ContractDev)), A256(P.thr.size()),
+                  A256(P.item_idx.size() * sizeof(uint32_t)), A256(P.statics.size() * sizeof(StaticDev))};
 }
 
 float time_group(Ctx &c, kx_book &b, kx_book::Group &g, std::vector<Job> &jobs, int minb, uint64_t item) {
@@ -110,7 +110,7 @@ void capture(Ctx &c, kx_book &b) {
     KX_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t err = cudaSuccess;
     for (auto &g : b.groups) {
-        if (g.plan.items.empty()) continue;
+        if (g.plan.n_items == 0) continue;
         if (err == cudaSuccess) err = cudaMemsetAsync(g.B.counters, 0, 64, c.stream);
         PathArgs a = path_args(g.plan, g.B);
         void *args[] = {&a};
@@ -204,9 +204,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
             const bool lean = g.family >= 1;
             const int *vs = variants(b->models[g.members[0]].kind, g.cfg.precision == KX_PREC_FP64, 1, lean, nv);
             g.plan = plan_paths(jobs[q], g.cfg, 1, vs[0], lean, 0, g.family == 2);
-            uint64_t max_items = 0;
-            for (auto &j : jobs[q]) max_items += (j.dev.n_paths + 63) / 64;
-            regs.push_back(region_sizes(g.plan, max_items));
+            regs.push_back(region_sizes(g.plan));
             const Region &r = regs.back();
             bytes += r.progs + r.steps + r.disc + r.cons + r.thr + r.items + r.statics;
             g.pv_base = b->n_paths;
@@ -270,7 +268,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
         const double t0 = now_ms();
         for (size_t q = 0; q < b->groups.size(); ++q) {
             auto &g = b->groups[q];
-            if (g.plan.items.empty()) continue;
+            if (g.plan.n_items == 0) continue;
             int minb = g.plan.minb;
             uint64_t item = g.plan.item_paths;
             if (flags & KX_BOOK_TUNE) {
@@ -319,7 +317,7 @@ kx_status kx_book_price(kx_book *b, kx_price_result *out) {
             memcpy(&sim, hc + 2, sizeof sim);
             c.last.steps_simulated += sim;
             check_err_word(hc[1]);
-            if (!b->groups[q].plan.items.empty()) c.last.kernel_launches++;
+            if (b->groups[q].plan.n_items) c.last.kernel_launches++;
             c.last.path_kernel = b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
         }
         if (b->n_chunks) c.last.kernel_launches++;
@@ -348,12 +346,12 @@ kx_status kx_book_set_models(kx_book *b, const kx_model *models) {
             b->models[i] = ms[i];
         }
         for (auto &g : b->groups) {
-            if (g.plan.items.empty()) continue;
+            if (g.plan.n_items == 0) continue;
             std::vector<Job> jobs = group_jobs(*b, g);
             if (use_lean(jobs, 1) != g.plan.lean || (g.plan.stat && !use_static(jobs, 1)))
                 raise(KX_INVALID_ARGUMENT, "new model parameters change a contract's kernel family");
             PathPlan P = plan_paths(jobs, g.cfg, 1, g.plan.minb, g.plan.lean, g.plan.item_paths, g.plan.stat);
-            if (P.steps.size() != g.plan.steps.size() || P.items.size() != g.plan.items.size() ||
+            if (P.steps.size() != g.plan.steps.size() || P.n_items != g.plan.n_items ||
                 P.statics.size() != g.plan.statics.size() ||
                 P.grid_blocks != g.plan.grid_blocks || P.smem != g.plan.smem)
                 raise(KX_INVALID_ARGUMENT, "new model parameters change the book's layout");

@@ -548,11 +548,22 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     }
     item = (item + 31) / 32 * 32;
     P.item_paths = item;
-    for (int ci : order) {
-        const uint64_t n = P.cons[ci].n_paths, base = jobs[ci].path_base;
-        for (uint64_t b = 0; b < n; b += item) P.items.push_back(WorkItem{ci, 0, base + b, std::min(item, n - b)});
+    // arithmetic items: per contract in launch order, its item count
+    const size_t nc = jobs.size();
+    P.item_idx.assign(2 * nc + 1, 0u);
+    uint64_t n_items = 0;
+    for (size_t q = 0; q < nc; ++q) {
+        const int ci = order[q];
+        P.cons[ci].item_paths = (uint32_t)item;
+        P.cons[ci].path_base = jobs[ci].path_base;
+        P.item_idx[q] = (uint32_t)n_items;
+        P.item_idx[nc + 1 + q] = (uint32_t)ci;
+        n_items += (P.cons[ci].n_paths + item - 1) / item;
     }
-    P.grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (P.items.size() + 7) / 8 + 1);
+    P.item_idx[nc] = (uint32_t)n_items;
+    if (n_items >= (1ull << 31)) raise(KX_INVALID_ARGUMENT, "too many work items in one launch");
+    P.n_items = n_items;
+    P.grid_blocks = (int)std::min<uint64_t>((uint64_t)full, (n_items + 7) / 8 + 1);
     return P;
 }
 
@@ -563,8 +574,11 @@ PathArgs path_args(const PathPlan &P, const PathBuffers &B) {
     a.disc = static_cast<const double *>(B.disc);
     a.cons = static_cast<const ContractDev *>(B.cons);
     a.thr = B.thr;
-    a.items = static_cast<const WorkItem *>(B.items);
-    a.n_items = (uint32_t)P.items.size();
+    a.items = nullptr;  // arithmetic items
+    a.item_start = static_cast<const uint32_t *>(B.items);
+    a.item_order = static_cast<const int32_t *>(B.items) + P.cons.size() + 1;
+    a.n_order = (uint32_t)P.cons.size();
+    a.n_items = (uint32_t)P.n_items;
     a.slots = P.slots;
     a.surv_base = P.surv_base;
     a.item_counter = B.counters;
@@ -582,8 +596,7 @@ void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s) {
     KX_CUDA(cudaMemcpyAsync(B.disc, P.disc.data(), P.disc.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     KX_CUDA(cudaMemcpyAsync(B.cons, P.cons.data(), P.cons.size() * sizeof(ContractDev), cudaMemcpyHostToDevice, s));
     KX_CUDA(cudaMemcpyAsync(B.thr, P.thr.data(), P.thr.size(), cudaMemcpyHostToDevice, s));
-    if (!P.items.empty())
-        KX_CUDA(cudaMemcpyAsync(B.items, P.items.data(), P.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+    KX_CUDA(cudaMemcpyAsync(B.items, P.item_idx.data(), P.item_idx.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     if (P.stat)
         KX_CUDA(cudaMemcpyAsync(B.statics, P.statics.data(), P.statics.size() * sizeof(StaticDev), cudaMemcpyHostToDevice,
                                 s));
@@ -591,7 +604,7 @@ void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s) {
 
 size_t plan_upload_bytes(const PathPlan &P) {
     return P.progs.size() * sizeof(KxProgram) + P.steps.size() + P.disc.size() * sizeof(double) +
-           P.cons.size() * sizeof(ContractDev) + P.thr.size() + P.items.size() * sizeof(WorkItem) +
+           P.cons.size() * sizeof(ContractDev) + P.thr.size() + P.item_idx.size() * sizeof(uint32_t) +
            P.statics.size() * sizeof(StaticDev);
 }
 
@@ -600,13 +613,13 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0, lean && use_static(jobs, ns));
     c.last.path_steps += P.path_steps;
     stride_out = P.total;
-    if (P.items.empty()) return P.total;
+    if (P.n_items == 0) return P.total;
     c.progs.ensure(P.progs.size() * sizeof(KxProgram));
     c.steps.ensure(P.steps.size());
     c.disc.ensure(P.disc.size() * sizeof(double));
     c.cons.ensure(P.cons.size() * sizeof(ContractDev));
     c.thr.ensure(P.thr.size());
-    c.items.ensure(P.items.size() * sizeof(WorkItem));
+    c.items.ensure(P.item_idx.size() * sizeof(uint32_t));
     c.counters.ensure(64);
     c.pv.ensure(std::max<uint64_t>(1, P.total * ns) * sizeof(double));
     c.statics.ensure(std::max<size_t>(1, P.statics.size()) * sizeof(StaticDev));

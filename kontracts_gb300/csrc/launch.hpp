@@ -58,16 +58,17 @@ struct PathPlan {
     std::vector<unsigned char> steps, thr;
     std::vector<double> disc;
     std::vector<ContractDev> cons;
-    std::vector<WorkItem> items;
+    std::vector<uint32_t> item_idx;  // arithmetic items: start of each contract's items (launch order), then order
     std::vector<StaticDev> statics;  // per contract, static-schedule launches
-    uint64_t total = 0, path_steps = 0, item_paths = 0;
+    uint64_t total = 0, path_steps = 0, item_paths = 0, n_items = 0;
     uint32_t slots = 0, surv_base = 0;
     size_t smem = 0;
     const void *kfn = nullptr;
     int grid_blocks = 0;
 };
 
-// Device buffers a plan's tables are uploaded to (counters: 64 zeroed bytes).
+// Device buffers a plan's tables are uploaded to (counters: 64 zeroed bytes;
+// items: the plan's item_idx).
 struct PathBuffers {
     void *progs, *steps, *disc, *cons, *thr, *items;
     uint32_t *counters;

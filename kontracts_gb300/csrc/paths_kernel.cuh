@@ -51,6 +51,8 @@ struct ContractDev {
     float s0f[KX_MAX_NS], driftf[KX_MAX_NS], sigmaf[KX_MAX_NS];
     double v0, kappa, theta, sigma_v, rho, rho_perp, r, inv_w;
     float v0f, kappaf, thetaf, sigma_vf, rhof, rho_perpf, rf, inv_wf;
+    uint32_t item_paths;  // paths per work item of this contract (arithmetic items)
+    uint32_t path_base;   // index of its first path in the stream
 };
 
 struct WorkItem {
@@ -80,7 +82,30 @@ struct PathArgs {
     const float *z32;
     uint64_t z_dpp;
     const void *statics; // StaticDev per contract (static-schedule launches of k_lean)
+    // Arithmetic work items (when `items` is null): the contracts in launch
+    // order `item_order[0..n_order)`, contract item_order[q] owning items
+    // item_start[q] .. item_start[q + 1] - 1 of item_paths paths each.
+    const uint32_t *item_start;
+    const int32_t *item_order;
+    uint32_t n_order;
 };
+
+// Work item `it` of a launch: from the table, or computed from the
+// contract's item size (no per-item table to build or upload).
+__device__ __forceinline__ WorkItem fetch_item(const PathArgs &A, int it) {
+    if (A.items) return A.items[it];
+    int lo = 0, hi = (int)A.n_order - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.item_start[mid] <= (uint32_t)it) lo = mid;
+        else hi = mid - 1;
+    }
+    const int c = A.item_order[lo];
+    const ContractDev &C = A.cons[c];
+    const uint64_t local = (uint64_t)((uint32_t)it - A.item_start[lo]) * C.item_paths;
+    const uint64_t left = C.n_paths - local;
+    return WorkItem{c, 0, (uint64_t)C.path_base + local, left < C.item_paths ? left : (uint64_t)C.item_paths};
+}
 
 enum { M_GBM = 0, M_HESTON = 1 };
 
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                         break;
                     }
                 }
-                const WorkItem w = A.items[it];
+                const WorkItem w = fetch_item(A, it);
                 if (w.contract != cur) {
                     if (cur >= 0 && idle != FULL) {  // finish the current contract first
                         pend = it;

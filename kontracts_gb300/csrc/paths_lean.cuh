@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         break;
                     }
                 }
-                const WorkItem w = A.items[it];
+                const WorkItem w = fetch_item(A, it);
                 if (w.contract != cur) {
                     if (cur >= 0 && idle != FULL) {  // finish the current contract first
                         pend = it;
