@@ -28,9 +28,10 @@ struct FlowRec {
     int kind;       // FlowKind
     int prog;       // program (FK_GENERAL)
     int code_off, code_len;
-    int pad;
+    int only;       // the contract's only flow: its value is stored, not added
     double a;       // strike (FK_CALL / FK_PUT)
     double sign;    // +1 / -1 (FK_CONST: the amount)
+    float af, signf;  // the same in FP32 (no conversion on the FP64 pipe per path)
 };
 
 struct FlowArgs {
@@ -52,20 +53,26 @@ struct FlowArgs {
 };
 
 template <class Real>
+__device__ __forceinline__ Real flow_a(const FlowRec &F) { return sizeof(Real) == 4 ? (Real)F.af : (Real)F.a; }
+template <class Real>
+__device__ __forceinline__ Real flow_sign(const FlowRec &F) { return sizeof(Real) == 4 ? (Real)F.signf : (Real)F.sign; }
+
+template <class Real>
 __device__ __forceinline__ void pay_flows(const FlowArgs &A, int k, Real S, uint64_t path) {
     const double df = A.disc[k];
     for (int f = A.first[k]; f < A.first[k + 1]; ++f) {
         const FlowRec &F = A.flows[f];
         Real amt;
-        if (F.kind == FK_CALL) amt = (Real)F.sign * fmax(S - (Real)F.a, Real(0));
-        else if (F.kind == FK_PUT) amt = (Real)F.sign * fmax((Real)F.a - S, Real(0));
-        else if (F.kind == FK_CONST) amt = (Real)F.sign;
+        if (F.kind == FK_CALL) amt = flow_sign<Real>(F) * fmax(S - flow_a<Real>(F), Real(0));
+        else if (F.kind == FK_PUT) amt = flow_sign<Real>(F) * fmax(flow_a<Real>(F) - S, Real(0));
+        else if (F.kind == FK_CONST) amt = flow_sign<Real>(F);
         else {
             uint32_t e = 0;
             amt = eval_code<Real>(A.progs[F.prog], F.code_off, F.code_len, AccView<Real>{nullptr, 0}, 0u, k, S, e);
         }
         double &dst = A.pv[(uint64_t)F.contract * A.n_paths + path];
-        dst += (double)amt * df;
+        if (F.only) dst = (double)amt * df;
+        else dst += (double)amt * df;
     }
 }
 
@@ -206,6 +213,9 @@ extern "C" kx_status kx_price_batch_shared(size_t n, const kx_program *const *pr
                     FlowRec r = classify(bound[i], f.leaf);
                     r.contract = (int)q;
                     r.prog = (int)q;
+                    r.only = sched[i].flows.size() == 1 ? 1 : 0;
+                    r.af = (float)r.a;
+                    r.signf = (float)r.sign;
                     at[f.step].push_back(r);
                 }
             }

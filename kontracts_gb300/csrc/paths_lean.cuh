@@ -245,13 +245,44 @@ struct HestonPar {
 // The steps of one Philox block from offset `off` on, up to the first step at
 // which the barrier window or the step limit fires (returns true; k is that
 // step) or to the end of the block (k is the next step). UNI: every step has
-// the coefficients (uc0, uc1), so the step table is not read.
+// the coefficients (uc0, uc1), so the step table is not read. The states are
+// the same bit for bit whichever way the block is walked.
 template <class Real, int MODEL, bool UNI>
 __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Real uc1, const HestonPar<Real> &hp,
                                            const Real (&zz)[4], int off, Real hi, Real lo, int lim, Real &y, Real &v,
                                            int &k) {
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;
-    bool ev = false;
+    // GBM: a whole block is stepped first and tested once (min and max of its
+    // states against the window, its last step against the limit); only a
+    // block in which something fires is walked again step by step. A Heston
+    // step is long enough that redoing it costs more than the test saves.
+    if (MODEL == M_GBM && off == 0) {
+        Real yy = y, vv = v, mx = Real(-INFINITY), mn = Real(INFINITY);
+#pragma unroll
+        for (int j = 0; j < SPB; ++j) {
+            Real c0 = uc0, c1 = uc1;
+            if (!UNI) {
+                const StepRec<Real> rec = R[min(k + j, lim)];
+                c0 = rec.c0;
+                c1 = rec.c1;
+            }
+            if (MODEL == M_GBM) {
+                yy = gbm_step(yy, c0, c1, zz[j]);
+            } else {
+                heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
+                                  zz[2 * j], zz[2 * j + 1], yy, vv);
+            }
+            mx = fmax(mx, yy);
+            mn = fmin(mn, yy);
+        }
+        if (mx < hi && mn > lo && k + SPB - 1 < lim) {  // nothing fires inside the block
+            y = yy;
+            v = vv;
+            k += SPB;
+            return false;
+        }
+    }
+    bool ev = false;  // step by step up to the event
 #pragma unroll
     for (int j = 0; j < SPB; ++j) {
         if (j >= off && !ev) {
