@@ -125,11 +125,35 @@ def cpu_baseline(seconds: float = 12.0) -> dict:
     dt = time.perf_counter() - t
     n = int(min(w["n_paths"], max(pilot, pilot * seconds / max(dt, 1e-6))))
     t = time.perf_counter()
-    orc.price(js, m, n_paths=n, seed=42, steps_per_year=w["steps_per_year"])
+    ref = orc.price(js, m, n_paths=n, seed=42, steps_per_year=w["steps_per_year"])
     dt = time.perf_counter() - t
     return {"value": n * steps / dt, "unit": UNIT, "cores": orc.threads(), "kind": "port",
             "sample": f"{n} of {w['n_paths']} paths x {steps} steps, CPU restatement of the reference "
-                      f"pricer (materialised paths + recursive cash-flow walk), {dt:.2f} s"}
+                      f"pricer (materialised paths + recursive cash-flow walk), {dt:.2f} s",
+            "_n": n, "_price": ref.price, "_se": ref.std_error}
+
+
+def accuracy(cb: dict) -> dict:
+    """The GPU's FP32 price against the FP64 CPU run on the same draws (the
+    oracle's Philox paths of the baseline sample) and against the closed form
+    (Reiner-Rubinstein up-and-out with the Broadie-Glasserman-Kou shift for
+    daily monitoring)."""
+    import kontracts_gb300 as kx
+    from oracle import Oracle
+    w = WORKLOAD
+    c = kx.up_and_out_call("S", w["strike"], w["barrier"], w["maturity"])
+    m = kx.GBM(s0=w["s0"], sigma=w["sigma"], r=w["r"], asset="S")
+    n = cb["_n"]
+    g = c.price(m, n_paths=n, seed=42, steps_per_year=w["steps_per_year"], precision="fp32")
+    dt = 1.0 / w["steps_per_year"]
+    bgk = w["barrier"] * math.exp(0.5826 * w["sigma"] * math.sqrt(dt))
+    cf = Oracle().up_and_out_call(w["s0"], w["strike"], bgk, w["r"], w["sigma"], w["maturity"])
+    se = math.sqrt(g.std_error ** 2 + cb["_se"] ** 2)
+    return {"paths": n, "draws": "Philox4x32-10 seed 42, paths 0..n-1 on both",
+            "gpu_fp32_price": g.price, "gpu_std_error": g.std_error, "cpu_fp64_price": cb["_price"],
+            "gpu_minus_cpu": g.price - cb["_price"], "gpu_minus_cpu_rel": (g.price - cb["_price"]) / cb["_price"],
+            "closed_form_bgk": cf, "gpu_minus_closed_form_in_se": (g.price - cf) / g.std_error,
+            "cpu_minus_closed_form_in_combined_se": (cb["_price"] - cf) / se}
 
 
 def run_reference(args, ws, rank) -> None:
@@ -453,7 +477,9 @@ def run_ours(args, ws, rank, local) -> None:
         line["other_configs"] = {"european_fp64": european_fp64(), "heston_book_96": heston_book(),
                                  "book_256": book_256(), "lsm_12": lsm_cases()}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        cb = cpu_baseline(args.cpu_seconds)
+        line["accuracy"] = accuracy(cb)
+        line["cpu_baseline"] = {k: v for k, v in cb.items() if not k.startswith("_")}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
