@@ -465,6 +465,41 @@ class Contract:
         return PriceResult(out)
 
 
+def price_american_batch(cases: Sequence[tuple], n_basis: int = 3, *, precision: str = "fp32",
+                         basis: str = "monomial") -> list[PriceResult]:
+    """Several Longstaff-Schwartz problems in one call (no reference
+    counterpart). Each case is (payoff, model, exercise_dates, n_paths, seed);
+    result i equals payoff_i.price_american(model_i, dates_i, n_paths_i,
+    seed_i, n_basis, precision=..., basis=...) bit for bit."""
+    if basis not in ("monomial", "laguerre"):
+        raise ValueError("basis must be 'monomial' or 'laguerre'")
+    n = len(cases)
+    if n == 0:
+        return []
+    hs = (C.c_void_p * n)()
+    models = (_abi.KxModel * n)()
+    cfgs = (_abi.KxMcConfig * n)()
+    dates = (C.POINTER(C.c_double) * n)()
+    nd = (C.c_size_t * n)()
+    keep = []
+    for i, (payoff, model, ex, n_paths, seed) in enumerate(cases):
+        if not isinstance(model, (GBM, Model)):
+            raise TypeError("expected a GBM or Model")
+        hs[i] = payoff._handle().h.value
+        models[i] = model._c()
+        cfgs[i] = _cfg(n_paths, seed, 50, model.rate, precision, False)
+        d = (C.c_double * max(1, len(ex)))(*[float(x) for x in ex])
+        keep.append(d)
+        dates[i] = C.cast(d, C.POINTER(C.c_double))
+        nd[i] = len(ex)
+    out = (_abi.KxPriceResult * n)()
+    with _lock:
+        _check(_lib().kx_price_american_lsm_batch(n, hs, models, cfgs, dates, nd, int(n_basis),
+                                                  _abi.KX_LSM_LAGUERRE if basis == "laguerre" else _abi.KX_LSM_MONOMIAL,
+                                                  out))
+    return [PriceResult(r) for r in out]
+
+
 def price_batch(contracts: Sequence[Contract], model, n_paths: int = 100_000, seed: int = 42,
                 steps_per_year: int = 50, *, precision: str = "fp32") -> list[PriceResult]:
     """price_batch_gbm (src/pricer.rs:250-294): every contract on the same paths."""
@@ -663,5 +698,6 @@ __all__ = [
     "until", "and_", "or_", "USD", "EUR", "GBP", "JPY", "average", "average_over", "running_max",
     "running_min", "heston", "zero_coupon_bond", "european_call", "european_put", "forward", "straddle",
     "bull_call_spread", "cash_or_nothing_call", "up_and_out_call", "down_and_out_call", "price_batch",
+    "price_american_batch",
     "price_portfolio", "set_shared_draws", "last_launch_stats",
 ]

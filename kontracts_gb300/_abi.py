@@ -159,6 +159,10 @@ SIGNATURES = {
     "kx_price_american_lsm_basis": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                               C.POINTER(C.c_double), C.c_size_t, C.c_int32, C.c_int32,
                                               C.POINTER(KxPriceResult)]),
+    "kx_price_american_lsm_batch": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
+                                              C.POINTER(KxMcConfig), C.POINTER(C.POINTER(C.c_double)),
+                                              C.POINTER(C.c_size_t), C.c_int32, C.c_int32,
+                                              C.POINTER(KxPriceResult)]),
     "kx_measure_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "kx_price_chunks": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig), C.c_uint64,
                                   C.POINTER(KxChunkStats), C.c_size_t, C.POINTER(C.c_size_t)]),

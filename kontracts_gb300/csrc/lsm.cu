@@ -197,33 +197,6 @@ __device__ void block_sums_f32(const float *vals, int n, double *red) {
     __syncthreads();
 }
 
-// numerics.rs:190-236 for m <= LSM_MAXM, on one thread.
-__device__ void solve_gauss(double a[LSM_MAXM][LSM_MAXM], double b[LSM_MAXM], int m, double x[LSM_MAXM]) {
-    for (int col = 0; col < m; ++col) {
-        int piv = col;
-        double best = fabs(a[col][col]);
-        for (int row = col + 1; row < m; ++row) {
-            const double v = fabs(a[row][col]);
-            if (v > best) { best = v; piv = row; }
-        }
-        if (best < 1e-12) {
-            for (int j = 0; j < m; ++j) x[j] = 0.0;
-            return;
-        }
-        for (int c = 0; c < m; ++c) { const double t = a[col][c]; a[col][c] = a[piv][c]; a[piv][c] = t; }
-        { const double t = b[col]; b[col] = b[piv]; b[piv] = t; }
-        for (int row = col + 1; row < m; ++row) {
-            const double factor = __ddiv_rn(a[row][col], a[col][col]);
-            for (int c = col; c < m; ++c) a[row][c] = __dsub_rn(a[row][c], __dmul_rn(factor, a[col][c]));
-            b[row] = __dsub_rn(b[row], __dmul_rn(factor, b[col]));
-        }
-    }
-    for (int row = m - 1; row >= 0; --row) {
-        double sum = b[row];
-        for (int c = row + 1; c < m; ++c) sum = __dsub_rn(sum, __dmul_rn(a[row][c], x[c]));
-        x[row] = __ddiv_rn(sum, a[row][row]);
-    }
-}
 
 // Regression basis at spot s: monomials 1, s, ..., s^(M-1) (lsm.rs:273-278),
 // or weighted Laguerre polynomials e^(-x/2) L_j(x), x = s / x_scale, with
@@ -295,15 +268,93 @@ __device__ __forceinline__ double lsm_continuation(const double (&c)[M], double 
     return cont;
 }
 
+// numerics.rs:190-236 (Gauss elimination with partial pivoting, a pivot below
+// 1e-12 gives zero coefficients) for M <= LSM_MAXM on one warp: lane r < M
+// holds row r of [A | b] in registers. Every element goes through the
+// serial algorithm's operations in its order (each product and difference
+// rounded separately, as on the host), and every lane runs the serial pivot
+// search on the same values; the rows below a pivot are eliminated in
+// parallel. Called by all 32 lanes of a warp.
+template <int M>
+__device__ void solve_gauss_warp(const double *red, int NA, double (&x)[LSM_MAXM]) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    double a[M], b = 0.0;
+#pragma unroll
+    for (int c = 0; c < M; ++c) a[c] = 0.0;
+    if (lane < M) {  // row `lane` of the symmetric matrix from its upper triangle
+        int q = 0;
+#pragma unroll
+        for (int r = 0; r < M; ++r)
+#pragma unroll
+            for (int c = r; c < M; ++c) {
+                if (r == lane) a[c] = red[q];
+                if (c == lane) a[r] = red[q];
+                ++q;
+            }
+        b = red[NA + lane];
+    }
+    bool singular = false;
+#pragma unroll
+    for (int col = 0; col < M; ++col) {
+        // pivot: the first row from col on with the largest |a[row][col]|
+        int piv = col;
+        double best = fabs(__shfl_sync(FULL, a[col], col));
+#pragma unroll
+        for (int row = col + 1; row < M; ++row) {
+            const double v = fabs(__shfl_sync(FULL, a[col], row));
+            if (v > best) { best = v; piv = row; }
+        }
+        if (best < 1e-12) { singular = true; break; }
+        // swap rows col and piv
+        double pr[M];
+#pragma unroll
+        for (int c = 0; c < M; ++c) {
+            const double from_piv = __shfl_sync(FULL, a[c], piv), from_col = __shfl_sync(FULL, a[c], col);
+            if (lane == col) a[c] = from_piv;
+            else if (lane == piv) a[c] = from_col;
+            pr[c] = from_piv;  // the pivot row after the swap
+        }
+        {
+            const double bp = __shfl_sync(FULL, b, piv), bc = __shfl_sync(FULL, b, col);
+            if (lane == col) b = bp;
+            else if (lane == piv) b = bc;
+        }
+        const double bpiv = __shfl_sync(FULL, b, col);
+        if (lane > col && lane < M) {
+            const double factor = __ddiv_rn(a[col], pr[col]);
+#pragma unroll
+            for (int c = col; c < M; ++c) a[c] = __dsub_rn(a[c], __dmul_rn(factor, pr[c]));
+            b = __dsub_rn(b, __dmul_rn(factor, bpiv));
+        }
+    }
+    if (singular) {
+#pragma unroll
+        for (int j = 0; j < M; ++j) x[j] = 0.0;
+        return;
+    }
+    // back substitution from the last row up (the same order of terms)
+#pragma unroll
+    for (int row = M - 1; row >= 0; --row) {
+        double xr = 0.0;
+        if (lane == row) {
+            double sum = b;
+#pragma unroll
+            for (int c = row + 1; c < M; ++c) sum = __dsub_rn(sum, __dmul_rn(a[c], x[c]));
+            xr = __ddiv_rn(sum, a[row]);
+        }
+        x[row] = __shfl_sync(FULL, xr, row);
+    }
+}
+
 // One backward launch: update the values with the decision of date `upd`
 // (upd < 0: initialise them with the payoff at the last date), then
 // accumulate the regression of date `gram` (gram < 0: none).
 template <class Real, int M, int B>
-__global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step(const LsmArgs A, int upd, int gram) {
+__device__ __forceinline__ void lsm_step_block(const LsmArgs &A, int upd, int gram, unsigned blk, unsigned nblk,
+                                               double *red, bool &last) {
     constexpr int NA = M * (M + 1) / 2;
     constexpr int NS = NA + M + 1;  // A upper triangle, A^T y, ITM count
-    __shared__ double red[32 * 64 + 64];
-    __shared__ bool last;
     const KxProgram &P = *A.P;
     const Real *S = reinterpret_cast<const Real *>(A.S);
     Real *V = reinterpret_cast<Real *>(A.value);
@@ -332,8 +383,7 @@ __global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step(const LsmArgs A, int 
     const float disc_uf = (float)disc_u;
     const double disc_g = gram >= 0 ? A.disc[gram] : 0.0;
     const float disc_gf = (float)disc_g;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths;
-         i += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t i = blk * (uint64_t)blockDim.x + threadIdx.x; i < A.n_paths; i += (uint64_t)nblk * blockDim.x) {
         Real val;
         if (upd < 0) {
             val = lsm_pay<Real>(terms, P, S[(uint64_t)(A.n_ex - 1) * A.n_paths + i], A.n_ex);
@@ -407,40 +457,77 @@ __global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step(const LsmArgs A, int 
     if (gram < 0) return;
     if (F32) block_sums_f32(accf, NS, red);
     else block_sums(acc, NS, red);
-    if (threadIdx.x < NS) A.partial[(size_t)blockIdx.x * 64 + threadIdx.x] = red[32 * 64 + threadIdx.x];
+    if (threadIdx.x < NS) A.partial[(size_t)blk * 64 + threadIdx.x] = red[32 * 64 + threadIdx.x];
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(A.ticket, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(A.ticket, 1u) == nblk - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // cross-block sums by the whole block: thread t adds blocks t, t + 256,
-    // ... in that order, then the fixed-order block sum (deterministic)
+    // cross-block sums in a fixed order: 8 threads per sum, thread t of sum q
+    // adds blocks t, t + 8, ... into 4 interleaved FP64 accumulators (the
+    // FP64 pipe is slow; independent chains keep it busy), then the 4 and the
+    // 8 partial sums are added in a fixed tree (deterministic)
+    static_assert(NS * 8 <= LSM_BLOCK, "8 threads per sum");
     {
-        double part[NS];
+        const int q = threadIdx.x >> 3, t = threadIdx.x & 7;
+        double s4[4] = {0.0, 0.0, 0.0, 0.0};
+        if (q < NS) {
+            unsigned b = t;
+            for (; b + 24 < nblk; b += 32) {
 #pragma unroll
-        for (int q = 0; q < NS; ++q) part[q] = 0.0;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-#pragma unroll
-            for (int q = 0; q < NS; ++q) part[q] += __ldcg(A.partial + (size_t)b * 64 + q);
+                for (int u = 0; u < 4; ++u) s4[u] += __ldcg(A.partial + (size_t)(b + 8 * u) * 64 + q);
+            }
+            for (int u = 0; b < nblk; b += 8, u = (u + 1) & 3) s4[u] += __ldcg(A.partial + (size_t)b * 64 + q);
         }
-        block_sums(part, NS, red);
-        if (threadIdx.x < NS) red[threadIdx.x] = red[32 * 64 + threadIdx.x];
+        double v = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);  // within the 8 lanes of sum q
+        if (q < NS && t == 0) red[q] = v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a[LSM_MAXM][LSM_MAXM], b[LSM_MAXM], x[LSM_MAXM];
-        int q = 0;
-        for (int r = 0; r < M; ++r)
-            for (int c = r; c < M; ++c) { a[r][c] = red[q]; a[c][r] = red[q]; ++q; }
-        for (int r = 0; r < M; ++r) b[r] = red[NA + r];
+    if (threadIdx.x < 32) {  // the solve on warp 0
         const double count = red[NS - 1];
         const bool fit = count >= (double)M;  // lsm.rs:190-194
-        if (fit) solve_gauss(a, b, M, x);
-        for (int j = 0; j < M; ++j) A.coef[gram * LSM_COEF + j] = fit ? x[j] : 0.0;
-        A.coef[gram * LSM_COEF + 7] = fit ? 1.0 : 0.0;
-        *A.ticket = 0u;
+        double x[LSM_MAXM];
+        if (fit) solve_gauss_warp<M>(red, NA, x);
+        if (threadIdx.x == 0) {
+            for (int j = 0; j < M; ++j) A.coef[gram * LSM_COEF + j] = fit ? x[j] : 0.0;
+            A.coef[gram * LSM_COEF + 7] = fit ? 1.0 : 0.0;
+            *A.ticket = 0u;
+        }
     }
+}
+
+template <class Real, int M, int B>
+__global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step(const LsmArgs A, int upd, int gram) {
+    __shared__ double red[32 * 64 + 64];
+    __shared__ bool last;
+    lsm_step_block<Real, M, B>(A, upd, gram, blockIdx.x, gridDim.x, red, last);
+}
+
+// One backward step of a batch of independent problems (cases): the cases
+// still active at backward iteration `it` (case q of the launch owns blocks
+// first[q] .. first[q + 1] - 1), each with its own dates, tables, partial
+// sums, ticket and solve. A case's blocks compute exactly what the
+// single-case launch of the same iteration computes.
+template <class Real, int M, int B>
+__global__ void __launch_bounds__(LSM_BLOCK, 4) k_lsm_step_batch(const LsmArgs *__restrict__ cases,
+                                                                  const int *__restrict__ active,
+                                                                  const unsigned *__restrict__ first, int n_active,
+                                                                  int it) {
+    __shared__ double red[32 * 64 + 64];
+    __shared__ bool last;
+    int lo = 0, hi = n_active - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const LsmArgs &A = cases[active[lo]];
+    const int upd = it == 0 ? -1 : A.n_ex - 1 - it;
+    const int gram = A.n_ex - 2 - it;
+    lsm_step_block<Real, M, B>(A, upd, gram, blockIdx.x - first[lo], first[lo + 1] - first[lo], red, last);
 }
 
 template <class Real>
@@ -490,6 +577,130 @@ static void run_lsm(Ctx &c, LsmArgs &a, int m, int model, int basis) {
     c.last.kernel_launches++;
 }
 
+// Host tables of one LSM problem (validation as lsm.rs:87-105).
+struct LsmCase {
+    KxProgram P;
+    std::vector<unsigned char> steps;  // StepRec<Real> of [0, dates...]
+    std::vector<double> disc;
+    LsmArgs a;                         // device pointers filled by the caller
+    Model m;
+    uint64_t np = 0;
+    int n_ex = 0;
+};
+
+static LsmCase lsm_case(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg, const double *dates,
+                        size_t n_dates, int32_t n_basis, int32_t basis) {
+    if (basis != KX_LSM_MONOMIAL && basis != KX_LSM_LAGUERRE) raise(KX_INVALID_ARGUMENT, "unknown LSM basis");
+    const Program &p = program_of(prog);
+    LsmCase L;
+    L.m = model_from_c(model);
+    if (!cfg) raise(KX_INVALID_ARGUMENT, "NULL argument");
+    if (cfg->flags != 0 || (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) ||
+        (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64))
+        raise(KX_INVALID_ARGUMENT, "bad config");
+    if (n_dates == 0 || !dates) raise(KX_MALFORMED_CONTRACT, "LSM: at least one exercise date required");
+    for (size_t i = 1; i < n_dates; ++i)
+        if (!(dates[i] > dates[i - 1])) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
+    if (!(dates[0] > 0.0)) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
+    if (n_basis < 2) raise(KX_MALFORMED_CONTRACT, "LSM: n_basis >= 2 required");
+    if (n_basis > LSM_MAXM) raise(KX_UNSUPPORTED, "LSM: n_basis above 6 is not supported on the device");
+    const KxProgram &Lw = p.low.prog;
+    if (Lw.n_trig != 0 || Lw.n_acc != 0)
+        raise(KX_UNSUPPORTED, "LSM payoff must be an immediate function of the spot "
+                              "(no when/until/anytime, averages or running extrema)");
+    validate_model(L.m);
+    std::vector<double> grid{0.0};
+    grid.insert(grid.end(), dates, dates + n_dates);
+    validate_grid(grid);
+    const bool f64 = cfg->precision == KX_PREC_FP64;
+    L.np = cfg->n_paths;
+    StepTables tab;
+    bind(p.low, grid, L.m, cfg->rate, L.P, tab);
+    L.n_ex = (int)n_dates;
+    L.disc.resize(L.n_ex);
+    for (int d = 0; d + 1 < L.n_ex; ++d) L.disc[d] = std::exp(-cfg->rate * (dates[d + 1] - dates[d]));  // lsm.rs:176
+    L.disc[L.n_ex - 1] = std::exp(-cfg->rate * dates[0]);                                               // lsm.rs:226
+    L.steps.resize(grid.size() * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+    for (size_t k = 0; k < grid.size(); ++k) {
+        if (f64) reinterpret_cast<StepRec<double> *>(L.steps.data())[k] = {tab.c0[k], tab.c1[k], 0u, 0u};
+        else reinterpret_cast<StepRec<float> *>(L.steps.data())[k] = {(float)tab.c0[k], (float)tab.c1[k], 0u, 0u};
+    }
+    LsmArgs &a = L.a;
+    a = LsmArgs{};
+    a.n_times = (int)grid.size();
+    a.n_ex = L.n_ex;
+    a.n_paths = L.np;
+    a.seed = cfg->seed;
+    a.model = L.m.kind;
+    a.scheme = L.m.scheme;
+    a.s0 = L.m.s0;
+    a.v0 = L.m.v0; a.kappa = L.m.kappa; a.theta = L.m.theta; a.sigma_v = L.m.sigma_v; a.rho = L.m.rho;
+    a.rho_perp = std::sqrt(std::max(1.0 - L.m.rho * L.m.rho, 0.0));
+    a.r = L.m.r;
+    a.x_scale = L.m.s0;
+    return L;
+}
+
+template <class Real, int M, int B>
+static void launch_batch_b(Ctx &c, const LsmArgs *cases, const std::vector<int> &n_ex, int blocks, void *idx_dev) {
+    const int n = (int)n_ex.size();
+    const int max_ex = *std::max_element(n_ex.begin(), n_ex.end());
+    const int *act = static_cast<const int *>(idx_dev);
+    // the active cases of every iteration, uploaded once: row `it` = [case ids..., block starts...]
+    std::vector<int> rows((size_t)max_ex * (2 * n + 1), 0);
+    std::vector<int> counts(max_ex, 0);
+    for (int it = 0; it < max_ex; ++it) {
+        int *row = rows.data() + (size_t)it * (2 * n + 1);
+        int q = 0;
+        for (int i = 0; i < n; ++i)
+            if (it <= n_ex[i] - 1) row[q++] = i;
+        for (int j = 0; j <= q; ++j) row[n + j] = j * blocks;
+        counts[it] = q;
+    }
+    KX_CUDA(cudaMemcpyAsync(idx_dev, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    for (int it = 0; it < max_ex; ++it) {
+        const int *row = act + (size_t)it * (2 * n + 1);
+        const unsigned *fst = reinterpret_cast<const unsigned *>(row + n);
+        k_lsm_step_batch<Real, M, B><<<counts[it] * blocks, LSM_BLOCK, 0, c.stream>>>(cases, row, fst, counts[it], it);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    }
+}
+
+template <class Real, int M>
+static void launch_batch(Ctx &c, const LsmArgs *cases, const std::vector<int> &n_ex, int blocks, void *idx, int basis) {
+    if (basis == KX_LSM_LAGUERRE) launch_batch_b<Real, M, KX_LSM_LAGUERRE>(c, cases, n_ex, blocks, idx);
+    else launch_batch_b<Real, M, KX_LSM_MONOMIAL>(c, cases, n_ex, blocks, idx);
+}
+
+template <class Real>
+static void run_lsm_batch(Ctx &c, std::vector<LsmCase> &cs, const LsmArgs *cases_dev, int m, int basis,
+                          void *idx_dev) {
+    const int blocks = c.sm_count * 4;
+    for (auto &L : cs) {  // forward simulations (each writes its own S)
+        if (L.np == 0) continue;
+        if (L.m.kind == KX_MODEL_GBM) k_lsm_forward<Real, KX_MODEL_GBM><<<blocks, LSM_BLOCK, 0, c.stream>>>(L.a);
+        else k_lsm_forward<Real, KX_MODEL_HESTON><<<blocks, LSM_BLOCK, 0, c.stream>>>(L.a);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    }
+    std::vector<int> n_ex;
+    for (auto &L : cs) n_ex.push_back(L.np ? L.n_ex : 0);  // a case without paths is never active
+    switch (m) {
+    case 2: launch_batch<Real, 2>(c, cases_dev, n_ex, blocks, idx_dev, basis); break;
+    case 3: launch_batch<Real, 3>(c, cases_dev, n_ex, blocks, idx_dev, basis); break;
+    case 4: launch_batch<Real, 4>(c, cases_dev, n_ex, blocks, idx_dev, basis); break;
+    case 5: launch_batch<Real, 5>(c, cases_dev, n_ex, blocks, idx_dev, basis); break;
+    default: launch_batch<Real, 6>(c, cases_dev, n_ex, blocks, idx_dev, basis); break;
+    }
+    for (auto &L : cs) {
+        if (L.np == 0) continue;
+        k_lsm_final<Real><<<blocks, LSM_BLOCK, 0, c.stream>>>(L.a);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    }
+}
+
 }  // namespace kx
 
 using namespace kx;
@@ -498,80 +709,39 @@ extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const k
                                                  const kx_mc_config *cfg, const double *dates, size_t n_dates,
                                                  int32_t n_basis, int32_t basis, kx_price_result *out) {
     return guarded([&] {
-        if (basis != KX_LSM_MONOMIAL && basis != KX_LSM_LAGUERRE) raise(KX_INVALID_ARGUMENT, "unknown LSM basis");
-        const Program &p = program_of(prog);
-        Model m = model_from_c(model);
-        if (!cfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
-        if (cfg->flags != 0 || (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) ||
-            (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64))
-            raise(KX_INVALID_ARGUMENT, "bad config");
-        // lsm.rs:87-105
-        if (n_dates == 0 || !dates) raise(KX_MALFORMED_CONTRACT, "LSM: at least one exercise date required");
-        for (size_t i = 1; i < n_dates; ++i)
-            if (!(dates[i] > dates[i - 1])) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
-        if (!(dates[0] > 0.0)) raise(KX_MALFORMED_CONTRACT, "LSM: exercise dates must increase and be > 0");
-        if (n_basis < 2) raise(KX_MALFORMED_CONTRACT, "LSM: n_basis >= 2 required");
-        if (n_basis > LSM_MAXM) raise(KX_UNSUPPORTED, "LSM: n_basis above 6 is not supported on the device");
-        const KxProgram &L = p.low.prog;
-        if (L.n_trig != 0 || L.n_acc != 0)
-            raise(KX_UNSUPPORTED, "LSM payoff must be an immediate function of the spot "
-                                  "(no when/until/anytime, averages or running extrema)");
-        validate_model(m);
-        std::vector<double> grid{0.0};
-        grid.insert(grid.end(), dates, dates + n_dates);
-        validate_grid(grid);
+        if (!out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        LsmCase L = lsm_case(prog, model, cfg, dates, n_dates, n_basis, basis);
         const bool f64 = cfg->precision == KX_PREC_FP64;
-        const uint64_t np = cfg->n_paths;
+        const uint64_t np = L.np;
+        const int n_ex = L.n_ex;
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         memset(&c.last, 0, sizeof c.last);
         c.last.total_ms = -now_ms();
-        KxProgram P;
-        StepTables tab;
-        bind(p.low, grid, m, cfg->rate, P, tab);
-        const int n_ex = (int)n_dates;
-        std::vector<double> disc(n_ex);
-        for (int d = 0; d + 1 < n_ex; ++d) disc[d] = std::exp(-cfg->rate * (dates[d + 1] - dates[d]));  // lsm.rs:176
-        disc[n_ex - 1] = std::exp(-cfg->rate * dates[0]);                                            // lsm.rs:226
-        std::vector<unsigned char> steps(grid.size() * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
-        for (size_t k = 0; k < grid.size(); ++k) {
-            if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {tab.c0[k], tab.c1[k], 0u, 0u};
-            else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)tab.c0[k], (float)tab.c1[k], 0u, 0u};
-        }
         const size_t rs = f64 ? 8 : 4;
         const int blocks = c.sm_count * 4;
         c.progs.ensure(sizeof(KxProgram));
-        c.steps.ensure(steps.size());
-        c.disc.ensure(disc.size() * sizeof(double));
+        c.steps.ensure(L.steps.size());
+        c.disc.ensure(L.disc.size() * sizeof(double));
         c.lsm_paths.ensure(std::max<uint64_t>(1, np * n_ex) * rs);
         c.lsm_value.ensure(std::max<uint64_t>(1, np) * rs);
         c.pv.ensure(std::max<uint64_t>(1, np) * sizeof(double));
         c.lsm_stats.ensure((size_t)blocks * 64 * sizeof(double) + (size_t)n_ex * LSM_COEF * sizeof(double));
         c.counters.ensure(64);
-        KX_CUDA(cudaMemcpyAsync(c.progs.p, &P, sizeof P, cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.disc.p, disc.data(), disc.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.progs.p, &L.P, sizeof L.P, cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.steps.p, L.steps.data(), L.steps.size(), cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.disc.p, L.disc.data(), L.disc.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                c.stream));
         KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
-        c.last.h2d_bytes += sizeof P + steps.size() + disc.size() * sizeof(double);
-        LsmArgs a{};
+        c.last.h2d_bytes += sizeof L.P + L.steps.size() + L.disc.size() * sizeof(double);
+        LsmArgs &a = L.a;
         a.P = c.progs.as<KxProgram>();
         a.steps = c.steps.p;
         a.disc = c.disc.as<double>();
-        a.n_times = (int)grid.size();
-        a.n_ex = n_ex;
-        a.n_paths = np;
-        a.seed = cfg->seed;
-        a.model = m.kind;
-        a.scheme = m.scheme;
-        a.s0 = m.s0;
-        a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
-        a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
-        a.r = m.r;
-        a.x_scale = m.s0;
         if (cfg->rng == KX_RNG_SHARED_DRAWS) {
             DrawStore &ds = c.draws;
             if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
-            if (ds.n_paths < np || ds.dpp < (uint64_t)n_ex * m.draws_per_step())
+            if (ds.n_paths < np || ds.dpp < (uint64_t)n_ex * L.m.draws_per_step())
                 raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
             a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
             a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
@@ -585,8 +755,8 @@ extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const k
         a.ticket = c.counters.as<unsigned>();
         if (np > 0) {
             KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-            if (f64) run_lsm<double>(c, a, n_basis, m.kind, basis);
-            else run_lsm<float>(c, a, n_basis, m.kind, basis);
+            if (f64) run_lsm<double>(c, a, n_basis, L.m.kind, basis);
+            else run_lsm<float>(c, a, n_basis, L.m.kind, basis);
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
@@ -606,4 +776,89 @@ extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_mode
                                            const double *dates, size_t n_dates, int32_t n_basis,
                                            kx_price_result *out) {
     return kx_price_american_lsm_basis(prog, model, cfg, dates, n_dates, n_basis, KX_LSM_MONOMIAL, out);
+}
+
+extern "C" kx_status kx_price_american_lsm_batch(size_t n, const kx_program *const *progs, const kx_model *models,
+                                                 const kx_mc_config *cfgs, const double *const *dates,
+                                                 const size_t *n_dates, int32_t n_basis, int32_t basis,
+                                                 kx_price_result *out) {
+    return guarded([&] {
+        if (n == 0) return;
+        if (!progs || !models || !cfgs || !dates || !n_dates || !out) raise(KX_INVALID_ARGUMENT, "NULL array");
+        std::vector<LsmCase> cs;
+        for (size_t i = 0; i < n; ++i) {
+            cs.push_back(lsm_case(progs[i], &models[i], &cfgs[i], dates[i], n_dates[i], n_basis, basis));
+            if (cfgs[i].rng != KX_RNG_PHILOX) raise(KX_INVALID_ARGUMENT, "an LSM batch draws from Philox");
+            if (cfgs[i].precision != cfgs[0].precision) raise(KX_INVALID_ARGUMENT, "an LSM batch has one precision");
+        }
+        const bool f64 = cfgs[0].precision == KX_PREC_FP64;
+        const size_t rs = f64 ? 8 : 4;
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        memset(&c.last, 0, sizeof c.last);
+        c.last.total_ms = -now_ms();
+        const int blocks = c.sm_count * 4;
+        // one arena: per case its program, steps, discounts, paths, values, per-path results,
+        // partial sums, coefficients and ticket; then the case table and the iteration table
+        auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+        std::vector<size_t> off(n + 1, 0);
+        uint64_t tot_paths = 0;
+        int max_ex = 0;
+        for (size_t i = 0; i < n; ++i) {
+            const LsmCase &L = cs[i];
+            size_t b = al(sizeof(KxProgram)) + al(L.steps.size()) + al(L.disc.size() * sizeof(double)) +
+                       al(std::max<uint64_t>(1, L.np * L.n_ex) * rs) + al(std::max<uint64_t>(1, L.np) * rs) +
+                       al(std::max<uint64_t>(1, L.np) * sizeof(double)) + al((size_t)blocks * 64 * sizeof(double)) +
+                       al((size_t)L.n_ex * LSM_COEF * sizeof(double)) + al(64);
+            off[i + 1] = off[i] + b;
+            tot_paths += L.np;
+            max_ex = std::max(max_ex, L.n_ex);
+        }
+        const size_t off_cases = off[n], off_idx = al(off_cases + n * sizeof(LsmArgs));
+        const size_t total = al(off_idx + (size_t)max_ex * (2 * n + 1) * sizeof(int));
+        c.lsm_paths.ensure(total);
+        unsigned char *base = c.lsm_paths.as<unsigned char>();
+        std::vector<LsmArgs> args(n);
+        std::vector<StatsJob> sj(n);
+        for (size_t i = 0; i < n; ++i) {
+            LsmCase &L = cs[i];
+            unsigned char *q = base + off[i];
+            auto take = [&](size_t bytes) { unsigned char *r = q; q += al(bytes); return r; };
+            L.a.P = reinterpret_cast<const KxProgram *>(take(sizeof(KxProgram)));
+            L.a.steps = take(L.steps.size());
+            L.a.disc = reinterpret_cast<const double *>(take(L.disc.size() * sizeof(double)));
+            L.a.S = take(std::max<uint64_t>(1, L.np * L.n_ex) * rs);
+            L.a.value = take(std::max<uint64_t>(1, L.np) * rs);
+            L.a.pv = reinterpret_cast<double *>(take(std::max<uint64_t>(1, L.np) * sizeof(double)));
+            L.a.partial = reinterpret_cast<double *>(take((size_t)blocks * 64 * sizeof(double)));
+            L.a.coef = reinterpret_cast<double *>(take((size_t)L.n_ex * LSM_COEF * sizeof(double)));
+            L.a.ticket = reinterpret_cast<unsigned *>(take(64));
+            KX_CUDA(cudaMemcpyAsync((void *)L.a.P, &L.P, sizeof(KxProgram), cudaMemcpyHostToDevice, c.stream));
+            KX_CUDA(cudaMemcpyAsync((void *)L.a.steps, L.steps.data(), L.steps.size(), cudaMemcpyHostToDevice, c.stream));
+            KX_CUDA(cudaMemcpyAsync((void *)L.a.disc, L.disc.data(), L.disc.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, c.stream));
+            KX_CUDA(cudaMemsetAsync(L.a.ticket, 0, 64, c.stream));
+            c.last.h2d_bytes += sizeof(KxProgram) + L.steps.size() + L.disc.size() * sizeof(double);
+            args[i] = L.a;
+            sj[i].begin = (uint64_t)(reinterpret_cast<unsigned char *>(L.a.pv) - base) / sizeof(double);
+            sj[i].n = L.np;
+            c.last.path_steps += L.np * (uint64_t)L.n_ex;
+        }
+        LsmArgs *cases_dev = reinterpret_cast<LsmArgs *>(base + off_cases);
+        KX_CUDA(cudaMemcpyAsync(cases_dev, args.data(), n * sizeof(LsmArgs), cudaMemcpyHostToDevice, c.stream));
+        c.last.steps_simulated = c.last.path_steps;
+        if (tot_paths > 0) {
+            KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+            if (f64) run_lsm_batch<double>(c, cs, cases_dev, n_basis, basis, base + off_idx);
+            else run_lsm_batch<float>(c, cs, cases_dev, n_basis, basis, base + off_idx);
+            KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+            KX_CUDA(cudaEventSynchronize(c.ev1));
+            float ms = 0.f;
+            KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+            c.last.kernel_ms += ms;
+        }
+        auto st = device_stats(c, reinterpret_cast<const double *>(base), 0, sj);
+        for (size_t i = 0; i < n; ++i) out[i] = finish(st[i]);
+        c.last.total_ms += now_ms();
+    });
 }

@@ -110,3 +110,28 @@ def test_american_put_laguerre_vs_crr(orc, s0, sigma, t):
                                    basis="laguerre")
     crr = orc.crr_american(s0, 40.0, t, 0.06, sigma, 1000, False)
     assert abs(res.price - crr) < 0.01 * crr + 4 * res.std_error, (res.price, crr)
+
+
+@pytest.mark.parametrize("precision,basis", [("fp32", "monomial"), ("fp32", "laguerre"), ("fp64", "laguerre")])
+def test_lsm_batch_equals_single_calls(precision, basis):
+    """One batched call over cases with different date counts, paths, seeds and
+    models returns each case's single-call result bit for bit."""
+    h = kx.heston(spot=100.0, v0=0.04, kappa=1.5, theta=0.04, sigma_v=0.3, rho=-0.6, r=0.03, asset="X")
+    cases = [
+        (put(40.0), kx.GBM(s0=36.0, sigma=0.2, r=0.06, asset="X"), dates(1.0, 50), 65_536, 1),
+        (put(40.0), kx.GBM(s0=44.0, sigma=0.4, r=0.06, asset="X"), dates(2.0, 100), 40_000, 2),
+        (put(100.0), h, dates(0.5, 12), 30_001, 3),
+        (put(40.0), kx.GBM(s0=40.0, sigma=0.3, r=0.06, asset="X"), dates(1.0, 1), 17, 4),
+    ]
+    got = kx.price_american_batch(cases, n_basis=3, precision=precision, basis=basis)
+    for (c, m, ds, n, seed), g in zip(cases, got):
+        one = c.price_american(m, ds, n_paths=n, seed=seed, n_basis=3, precision=precision, basis=basis)
+        assert (g.price, g.std_error, g.n_paths) == (one.price, one.std_error, one.n_paths)
+
+
+def test_lsm_batch_rejects_a_bad_case():
+    m = kx.GBM(s0=36.0, sigma=0.2, r=0.06, asset="X")
+    c = put(40.0)
+    with pytest.raises(kx.KontractError):
+        kx.price_american_batch([(c, m, dates(1.0, 4), 100, 1)], n_basis=1)
+    assert kx.price_american_batch([]) == []
