@@ -301,9 +301,9 @@ kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *mo
  * call, lsm.rs:80-124). Case i is progs[i] under models[i] with cfgs[i] on
  * the dates dates[i][0 .. n_dates[i]); all cases share n_basis and basis,
  * draw from Philox and have one precision. The backward induction of every
- * case still active at a date runs in one launch, so the per-date launch
- * cost is paid once for the batch; out[i] equals, bit for bit, the result
- * of kx_price_american_lsm_basis on case i alone. */
+ * case still active at a date runs in one launch, and different cases'
+ * dates overlap; out[i] equals, bit for bit, the result of
+ * kx_price_american_lsm_basis on case i alone. At most 1024 cases. */
 kx_status kx_price_american_lsm_batch(size_t n, const kx_program *const *progs,
                                       const kx_model *models, const kx_mc_config *cfgs,
                                       const double *const *dates, const size_t *n_dates,

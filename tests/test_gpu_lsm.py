@@ -134,4 +134,6 @@ def test_lsm_batch_rejects_a_bad_case():
     c = put(40.0)
     with pytest.raises(kx.KontractError):
         kx.price_american_batch([(c, m, dates(1.0, 4), 100, 1)], n_basis=1)
+    with pytest.raises(kx.KontractError):
+        kx.price_american_batch([(c, m, dates(1.0, 4), 100, 1)] * 1025)
     assert kx.price_american_batch([]) == []
