@@ -351,8 +351,9 @@ def lsm_cases(reps=2) -> dict:
     """American puts by Longstaff-Schwartz: s0 in {36, 40, 44}, K = 40,
     sigma in {0.2, 0.4}, r = 0.06, T in {1, 2}, 50 dates a year, 1,000,000
     paths stored FP32, 4 weighted-Laguerre functions. HBM roofline: bytes per
-    path = 4 (store S) + 16 per backward date (read S twice, read and write
-    the FP32 value) + 12 (final value to FP64) per date set."""
+    path and date = 4 (forward store of S) + 16 (backward: read S at the
+    decision and regression dates, read and write the FP32 value), plus 8 per
+    path for the FP64 per-path result."""
     import kontracts_gb300 as kx
     peak, src = _hbm_peak()
     n = 1_000_000
@@ -371,7 +372,7 @@ def lsm_cases(reps=2) -> dict:
                     st = kx.last_launch_stats()
                     ts = st["kernel_ms"] * 1e-3
                     best = ts if best is None or ts < best else best
-                byts = n * (4.0 * nd + 16.0 * nd + 12.0)
+                byts = n * (4.0 * nd + 16.0 * nd + 8.0)
                 cases.append({"s0": s0, "sigma": sig, "T": t, "price": r.price, "se": r.std_error, "seconds": best,
                               "hbm_gbs": byts / best / 1e9})
                 tot_s += best

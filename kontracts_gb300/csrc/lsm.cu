@@ -28,6 +28,9 @@
 namespace kx {
 
 constexpr int LSM_BLOCK = 256;
+// Block reduction scratch (doubles): red[q * 8 + w] the 8 warps' sums of up to
+// 32 quantities q, the block's sums at red[LSM_RED_OUT + q].
+constexpr int LSM_RED_OUT = (LSM_BLOCK / 32) * 32;
 constexpr int LSM_MAXM = 6;
 constexpr int LSM_COEF = 12;  // coef[d * LSM_COEF + j], j < m; [7] = have-fit flag; doubles 8..11 hold
                               // the coefficients and the flag as floats (float index j, 7)
@@ -210,20 +213,22 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward(const LsmArgs A) {
     }
 }
 
-// Block-wide sum of `n` doubles per thread into red[0..n) (fixed order).
+// Block-wide sum of `n` <= 32 doubles per thread into red[LSM_RED_OUT + q]
+// (fixed order).
 __device__ void block_sums(double *vals, int n, double *red) {
+    static_assert(LSM_BLOCK == 256, "8 warps");
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int q = 0; q < n; ++q) {
         double v = vals[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (l == 0) red[q * 32 + w] = v;
+        if (l == 0) red[q * 8 + w] = v;
     }
     __syncthreads();
     if (threadIdx.x < n) {
         double t = 0.0;
-        for (int j = 0; j < nw; ++j) t += red[threadIdx.x * 32 + j];
-        red[32 * 64 + threadIdx.x] = t;
+        for (int j = 0; j < nw; ++j) t += red[threadIdx.x * 8 + j];
+        red[LSM_RED_OUT + threadIdx.x] = t;
     }
     __syncthreads();
 }
@@ -897,14 +902,14 @@ __device__ void lsm_tile(const LsmArgs &A, int it, unsigned tile, double *red, f
     if (gram < 0) return;
     // the tile's partial sums (FP32 paths: float-float, FP64 paths: FP64)
     if (F32) {
-        ff *out = reinterpret_cast<ff *>(red + 32 * 64);
+        ff *out = reinterpret_cast<ff *>(red + LSM_RED_OUT);
         block_sums_ff(accf, NS, red, out);
         if (threadIdx.x < NS)
             __stcg(reinterpret_cast<float2 *>(A.partial) + (size_t)tile * LSM_NSUM + threadIdx.x,
                    make_float2(out[threadIdx.x].hi, out[threadIdx.x].lo));
     } else {
         block_sums(acc, NS, red);
-        if (threadIdx.x < NS) __stcg(A.partial + (size_t)tile * LSM_NSUM + threadIdx.x, red[32 * 64 + threadIdx.x]);
+        if (threadIdx.x < NS) __stcg(A.partial + (size_t)tile * LSM_NSUM + threadIdx.x, red[LSM_RED_OUT + threadIdx.x]);
     }
     __threadfence();
     __syncthreads();
@@ -1010,9 +1015,9 @@ __device__ void lsm_coordinator(const LsmArgs *cases, int n_cases, int k, int n_
 // of the case whose tile it takes next, so different cases' dates overlap and
 // no launch ends between dates.
 template <class Real, int M, int B, bool GEN>
-__global__ void __launch_bounds__(LSM_BLOCK, sizeof(Real) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(LSM_BLOCK, sizeof(Real) == 4 ? 4 : 2)
     k_lsm_backward(const LsmArgs *__restrict__ cases, int n_cases, int max_ex, int n_coord, unsigned *err) {
-    __shared__ double red[32 * 64 + 64];
+    __shared__ double red[LSM_RED_OUT + 32];
     __shared__ int flag;
     const unsigned n_tile_blocks = gridDim.x - (unsigned)n_coord;
     if (blockIdx.x >= n_tile_blocks) {  // the coordinators: the regression solves
