@@ -1,4 +1,4 @@
-"""One price sharded over ranks (one GPU per rank, torch.distributed).
+"""Work sharded over ranks (one GPU per rank, torch.distributed).
 
 Paths are independent and the Philox counter of a path is its index, so a
 price shards without any exchange on the data path: rank r of w prices a
@@ -74,3 +74,40 @@ def price_sharded(contract, model, n_paths: int, seed: int = 42, steps_per_year:
     gathered: list = [None] * world
     dist.all_gather_object(gathered, mine, group=group)
     return merge([c for part in gathered for c in part])
+
+
+def case_shard(n_cases: int, world: int, rank: int) -> list[int]:
+    """The cases of rank `rank`: i = rank, rank + world, ... (every case on
+    exactly one rank)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    return list(range(rank, n_cases, world))
+
+
+def price_american_sharded(cases: Sequence[tuple], n_basis: int = 3, *, precision: str = "fp32",
+                           basis: str = "monomial", group=None, batch_fn: Callable | None = None):
+    """Independent American options (the cases of price_american_batch)
+    sharded over the ranks of `group`: rank r prices cases r, r + w, ... in
+    one batched call on its GPU; the only collective is the gather of the
+    results. Every rank returns all results in case order, each equal to the
+    single-GPU result of its case. batch_fn(cases) replaces the GPU call (it
+    returns one (price, std_error, n_paths) per case)."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    mine = case_shard(len(cases), world, rank)
+    if batch_fn is not None:
+        got = batch_fn([cases[i] for i in mine])
+    elif mine:
+        from . import price_american_batch
+        got = [(r.price, r.std_error, r.n_paths)
+               for r in price_american_batch([cases[i] for i in mine], n_basis, precision=precision, basis=basis)]
+    else:
+        got = []
+    gathered: list = [None] * world
+    dist.all_gather_object(gathered, list(zip(mine, got)), group=group)
+    out: list = [None] * len(cases)
+    for part in gathered:
+        for i, res in part:
+            out[i] = res
+    return out

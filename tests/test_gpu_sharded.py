@@ -35,3 +35,20 @@ def test_ranges_must_start_on_a_chunk():
     with pytest.raises(kx.KontractError) as e:
         sharded.price_chunks(c, m, 100, 1000)
     assert e.value.status == "InvalidArgument"
+
+
+def test_american_case_shards_equal_the_batch():
+    """Each rank's share of a batch of American options priced in its own
+    batched call gives the same results as the whole batch in one call (the
+    cases are independent problems)."""
+    put = kx.scale((kx.const_(40.0) - kx.S("X")).clip(0.0), kx.one())
+    cases = [(put, kx.GBM(s0=s0, sigma=0.25, r=0.06, asset="X"), [i / 20 for i in range(1, 21)], 40_000, 3)
+             for s0 in (34.0, 38.0, 42.0, 46.0, 50.0)]
+    whole = kx.price_american_batch(cases, n_basis=3, basis="laguerre")
+    for world in (2, 3):
+        got = [None] * len(cases)
+        for rank in range(world):
+            mine = sharded.case_shard(len(cases), world, rank)
+            for i, r in zip(mine, kx.price_american_batch([cases[i] for i in mine], n_basis=3, basis="laguerre")):
+                got[i] = r
+        assert [(r.price, r.std_error) for r in got] == [(r.price, r.std_error) for r in whole]

@@ -72,3 +72,44 @@ def test_gloo_two_ranks_give_the_single_process_price(n_paths):
     ref = sharded.merge(_chunks(0, n_paths))
     for _, price, se, n in res:
         assert price == ref.price and se == ref.std_error and n == n_paths
+
+
+def _fake_batch(cases):
+    """Stand-in for the GPU batch: a function of each case alone."""
+    return [(float(c[0]) * 1.5, float(c[0]) * 0.01, int(c[0]) + 7) for c in cases]
+
+
+def _american_worker(rank, world, port, n_cases, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        cases = [(i,) for i in range(n_cases)]
+        q.put((rank, sharded.price_american_sharded(cases, batch_fn=_fake_batch)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_case_shards_cover_every_case_once():
+    for n in (0, 1, 5, 12):
+        for w in (1, 2, 3, 8):
+            got = sorted(i for r in range(w) for i in sharded.case_shard(n, w, r))
+            assert got == list(range(n))
+
+
+@pytest.mark.parametrize("n_cases", [12, 1])
+def test_gloo_two_ranks_price_every_american_case(n_cases):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_american_worker, args=(r, 2, port, n_cases, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    want = _fake_batch([(i,) for i in range(n_cases)])
+    for _, got in res:
+        assert got == want
