@@ -457,9 +457,9 @@ def run_ours(args, ws, rank, local) -> None:
     achieved = sim_steps / (ker_ms * 1e-3) / 1e9
     peak = peaks.get("bare_path_steps", float("nan")) / 1e9
     # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum of the path kernel
-    # on the 1M-path case (profiles/k_lean_static_up_and_out.md: 392,960 + 0 bytes), scaled by the
+    # on the 1M-path case (profiles/k_lean_static_up_and_out.md: 19,968 + 0 bytes), scaled by the
     # number of paths; the per-path values (8 B/path) stay in L2 during the launch.
-    traffic = 19968.0 / 1_000_000 * n_paths  # ncu dram__bytes_read + write of one launch at 1M paths, scaled
+    traffic = 19968.0 / 1_000_000 * n_paths
     kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>", 3: "k_lean<float,GBM,static schedule>"}.get(
         kx.last_launch_stats()["path_kernel"], "?")
     roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
