@@ -587,6 +587,18 @@ PathArgs path_args(const PathPlan &P, const PathBuffers &B) {
     a.pv = B.pv;
     a.pv_stride = P.total;
     a.statics = P.stat ? B.statics : nullptr;
+    bool one_seed = !P.cons.empty();
+    for (const ContractDev &c : P.cons) one_seed = one_seed && c.seed == P.cons[0].seed;
+    if (one_seed) {  // the Philox key schedule of philox4x32_10, once for the launch
+        uint32_t k0 = (uint32_t)P.cons[0].seed, k1 = (uint32_t)(P.cons[0].seed >> 32);
+        for (int r = 0; r < 10; ++r) {
+            a.rk[2 * r] = k0;
+            a.rk[2 * r + 1] = k1;
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        a.rk_ok = 1u;
+    }
     return a;
 }
 

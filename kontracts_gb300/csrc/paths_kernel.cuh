@@ -88,6 +88,10 @@ struct PathArgs {
     const uint32_t *item_start;
     const int32_t *item_order;
     uint32_t n_order;
+    // Philox round keys of the launch's seed when every contract of the
+    // launch has the same seed (rk_ok), read as kernel parameters
+    uint32_t rk_ok;
+    uint32_t rk[20];
 };
 
 // Work item `it` of a launch: from the table, or computed from the

@@ -318,10 +318,10 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     // for GBM, whose blocks are short next to the handler; a Heston block is
     // long enough that waiting costs more than it saves.
     constexpr int EV_BATCH = MODEL == M_GBM ? 8 : 1;
-    constexpr int EV_WAIT = 8;
-    // Philox blocks a lane steps through per round of the warp loop: two for
-    // GBM (8 steps) halve the per-round hand-out and event ballots per step.
-    constexpr int BPI = MODEL == M_GBM ? 2 : 1;
+    constexpr int EV_WAIT = MODEL == M_GBM ? 4 : 8;  // rounds of BPI blocks
+    // Philox blocks a lane steps through per round of the warp loop: four for
+    // GBM (16 steps) cut the per-round hand-out and event ballots per step.
+    constexpr int BPI = MODEL == M_GBM ? 4 : 1;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
     int cur = -1, pend = -1;
@@ -434,8 +434,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 const int off = (int)(km1 % SPB);
                 Real zz[4];
                 if (A.z64 == nullptr && A.z32 == nullptr) {
-                    const uint4 w =
-                        philox4x32_10(make_uint4(blk, path, 0u, stream), (uint32_t)seed, (uint32_t)(seed >> 32));
+                    const uint4 ctr = make_uint4(blk, path, 0u, stream);
+                    const uint4 w = A.rk_ok ? philox4x32_10_rk(ctr, A.rk)
+                                            : philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
                     box_muller(w.x, w.y, zz[0], zz[1]);
                     box_muller(w.z, w.w, zz[2], zz[3]);
                 } else {
