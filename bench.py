@@ -283,6 +283,12 @@ def heston_book(reps=3) -> dict:
         t = _dev_seconds(kx)
         best = t if best is None or t < best else best
     steps = n * 504
+    # roofline: the simulation's steps/s against the bare Heston loop (Philox, Box-Muller, the
+    # full-truncation step; kx_measure_peak(4)) measured in the same process
+    import ctypes as C
+    from kontracts_gb300 import _abi
+    pk = C.c_double()
+    peak = pk.value if _abi.load().kx_measure_peak(4, C.byref(pk)) == 0 else float("nan")
     adj = None
     for _ in range(2):
         a = kx.european_call("S", 100.0, 1.0).adjoint(h, n_paths=n, seed=7, steps_per_year=252, checkpoint_every=16)
@@ -292,6 +298,11 @@ def heston_book(reps=3) -> dict:
     return {"workload": "96 Heston calls (32 strikes x 3 maturities) on one 2M-path simulation, full truncation, "
                         "252 steps/yr, FP32", "seconds": best, "path_steps_per_s": steps / best,
             "contracts_per_s": len(book) / best, "price_T1_K100": res[32 + 15].price,
+            "roofline": {"bound": "issue", "achieved": steps / best / 1e9, "peak": peak / 1e9, "unit": "Gsteps/s",
+                         "frac": steps / best / peak if peak == peak and peak > 0 else None,
+                         "peak_source": "measured in this run: kx_measure_peak(4), the bare Philox4x32-10 + "
+                                        "Box-Muller + Heston full-truncation step loop",
+                         "note": "time includes the 96 payoffs on the shared simulation"},
             "adjoint_T1_K100": {"seconds": ta, "price": a.price, "d_s0": a.d_s0, "d_v0": a.d_v0,
                                 "d_kappa": a.d_kappa, "d_theta": a.d_theta, "d_sigma_v": a.d_sigma_v,
                                 "d_rho": a.d_rho, "se_v0": a.se_v0, "checkpoint_every": 16}}
@@ -413,7 +424,8 @@ def run_ours(args, ws, rank, local) -> None:
     for i in range(args.warmup):
         r = price(seed + i)
     peaks = {}
-    for what, name in ((0, "mufu"), (1, "fp32_fma"), (2, "imad_hi"), (3, "bare_path_steps")):
+    for what, name in ((0, "mufu"), (1, "fp32_fma"), (2, "imad_hi"), (3, "bare_path_steps"),
+                       (4, "bare_heston_steps")):
         v = C.c_double()
         if lib.kx_measure_peak(what, C.byref(v)) == 0:
             peaks[name] = v.value

@@ -347,7 +347,8 @@ void kx_book_free(kx_book *book);
  * 1: FP32 FMA (FMAs/s); 2: 32-bit integer multiply-high (IMAD.HI/s, the
  * Philox multiply); 3: FP32 GBM steps/s of the bare simulation loop (Philox
  * draw, Box-Muller, log-space update; no contract, no scheduling), the
- * ceiling of the path kernels. */
+ * ceiling of the path kernels; 4: the same for FP32 Heston steps/s (2 normals
+ * and the full-truncation Euler step per step). */
 kx_status kx_measure_peak(int32_t what, double *ops_per_s);
 
 /* Counters of the last pricing call (see kx_launch_stats). */

@@ -772,6 +772,31 @@ __global__ void __launch_bounds__(256) k_peak_path(float *out, int paths_per_thr
     if (acc == 12345.f) out[threadIdx.x] = acc;
 }
 
+// The bare Heston loop: Philox4x32-10 + Box-Muller for 2 normals per step and
+// the full-truncation Euler step of the path kernels (log spot and variance),
+// nothing else: the ceiling of a Heston path kernel on this RNG.
+__global__ void __launch_bounds__(256) k_peak_heston(float *out, int paths_per_thread, int n_steps) {
+    float acc = 0.f;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const float dt = 1.0f / 252.0f, sq = sqrtf(dt);
+    for (int q = 0; q < paths_per_thread; ++q) {
+        const uint32_t path = tid * (uint32_t)paths_per_thread + (uint32_t)q;
+        float y = 0.f, v = 0.04f;
+        for (int b = 0; b < n_steps / 2; ++b) {
+            const uint4 w = philox4x32_10(make_uint4((uint32_t)b, path, 0u, 0u), 42u, 0u);
+            float z[4];
+            box_muller(w.x, w.y, z[0], z[1]);
+            box_muller(w.z, w.w, z[2], z[3]);
+            heston_step<float>(0.03f, 2.0f, 0.04f, 0.3f, -0.5f, 0.8660254f, KX_HESTON_FULL_TRUNCATION, dt, sq, z[0],
+                               z[1], y, v);
+            heston_step<float>(0.03f, 2.0f, 0.04f, 0.3f, -0.5f, 0.8660254f, KX_HESTON_FULL_TRUNCATION, dt, sq, z[2],
+                               z[3], y, v);
+        }
+        acc += y + v;
+    }
+    if (acc == 12345.f) out[threadIdx.x] = acc;
+}
+
 }  // namespace kx
 
 using namespace kx;
@@ -780,7 +805,7 @@ extern "C" {
 
 kx_status kx_measure_peak(int32_t what, double *ops_per_s) {
     return guarded([&] {
-        if (!ops_per_s || what < 0 || what > 3) raise(KX_INVALID_ARGUMENT, "bad arguments");
+        if (!ops_per_s || what < 0 || what > 4) raise(KX_INVALID_ARGUMENT, "bad arguments");
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         c.misc.ensure(4096);
@@ -791,13 +816,14 @@ kx_status kx_measure_peak(int32_t what, double *ops_per_s) {
             if (what == 0) k_peak_mufu<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
             else if (what == 1) k_peak_fma<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), iters);
             else if (what == 2) k_peak_imad<<<blocks, threads, 0, c.stream>>>(c.misc.as<unsigned>(), iters);
-            else k_peak_path<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), 4, 256);
+            else if (what == 3) k_peak_path<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), 4, 256);
+            else k_peak_heston<<<blocks, threads, 0, c.stream>>>(c.misc.as<float>(), 4, 256);
             KX_CUDA(cudaGetLastError());
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
             KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
-            const double ops = what == 3 ? (double)blocks * threads * 4 * 256
+            const double ops = what >= 3 ? (double)blocks * threads * 4 * 256
                                          : (double)blocks * threads * iters * 8 * (what == 0 ? 2 : 1);
             best = std::max(best, ops / (ms * 1e-3));
         }

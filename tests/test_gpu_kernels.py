@@ -91,3 +91,19 @@ def test_kernel_family_selection(name, kernel):
     m = kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X")
     _run(LEAN[name](), m, "fp32", "auto", n=1000)
     assert kx.last_launch_stats()["path_kernel"] == kernel
+
+
+def test_calibration_loops_are_positive_and_ordered():
+    """kx_measure_peak: the pipe microbenchmarks and the bare GBM and Heston
+    step loops return positive rates; a Heston step (two normals, a square
+    root) is slower than a GBM step."""
+    import ctypes as C
+    from kontracts_gb300 import _abi
+    lib = _abi.load()
+    got = {}
+    for what in range(5):
+        v = C.c_double()
+        assert lib.kx_measure_peak(what, C.byref(v)) == 0
+        got[what] = v.value
+        assert v.value > 1e9
+    assert got[4] < got[3]

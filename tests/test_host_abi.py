@@ -196,3 +196,11 @@ def test_pricing_without_device_fails_loudly():
     with pytest.raises(kx.KontractError) as e:
         kx.european_call("X", 100.0, 1.0).price(kx.GBM(100, 0.2, 0.05, asset="X"), n_paths=10)
     assert e.value.status == "NoDevice"
+
+
+def test_measure_peak_rejects_unknown_loops():
+    import ctypes as C
+    lib = _abi.load()
+    v = C.c_double()
+    assert lib.kx_measure_peak(5, C.byref(v)) == _abi.KX_INVALID_ARGUMENT
+    assert lib.kx_measure_peak(-1, C.byref(v)) == _abi.KX_INVALID_ARGUMENT
