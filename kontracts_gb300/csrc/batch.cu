@@ -90,29 +90,33 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
             pay_flows<Real>(A, 0, s0, path);
             nf = A.next[1];
         }
-        Real z[4];
-        for (int k = 1; k < A.n_times; ++k) {
+        // one Philox block (4 normals) per SPB steps, walked with compile-time indices
+        constexpr int SPB = 4 / DRAWS;
+        for (int k = 1; k < A.n_times; k += SPB) {
             const uint64_t d = (uint64_t)(k - 1) * DRAWS;
-            if ((d & 3u) == 0) {
-                if (A.z64 == nullptr && A.z32 == nullptr) {
-                    const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
-                                                  (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
-                    box_muller(w.x, w.y, z[0], z[1]);
-                    box_muller(w.z, w.w, z[2], z[3]);
-                } else {
+            Real z[4];
+            if (A.z64 == nullptr && A.z32 == nullptr) {
+                const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
+                                              (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+                box_muller(w.x, w.y, z[0], z[1]);
+                box_muller(w.z, w.w, z[2], z[3]);
+            } else {
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        z[j] = d + j < A.z_dpp ? (A.z64 ? (Real)A.z64[path * A.z_dpp + d + j] : (Real)A.z32[path * A.z_dpp + d + j])
-                                               : Real(0);
-                }
+                for (int j = 0; j < 4; ++j)
+                    z[j] = d + j < A.z_dpp ? (A.z64 ? (Real)A.z64[path * A.z_dpp + d + j] : (Real)A.z32[path * A.z_dpp + d + j])
+                                           : Real(0);
             }
-            const StepRec<Real> rec = R[k];
-            const int q = (int)(d & 3u);
-            if (MODEL == KX_MODEL_GBM) y = gbm_step(y, rec.c0, rec.c1, z[q]);
-            else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[q], z[q + 1], y, v);
-            if (k == nf) {
-                pay_flows<Real>(A, k, spot_of<Real>(s0, y), path);
-                nf = A.next[k + 1];
+#pragma unroll
+            for (int j = 0; j < SPB; ++j) {
+                const int kk = k + j;
+                if (kk >= A.n_times) break;
+                const StepRec<Real> rec = R[kk];
+                if (MODEL == KX_MODEL_GBM) y = gbm_step(y, rec.c0, rec.c1, z[j]);
+                else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[2 * j], z[2 * j + 1], y, v);
+                if (kk == nf) {
+                    pay_flows<Real>(A, kk, spot_of<Real>(s0, y), path);
+                    nf = A.next[kk + 1];
+                }
             }
         }
     }
@@ -247,7 +251,12 @@ extern "C" kx_status kx_price_batch_shared(size_t n, const kx_program *const *pr
             KX_CUDA(cudaMemcpyAsync(c.misc.as<int>() + nt + 1, next.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
             KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
             KX_CUDA(cudaMemcpyAsync(c.disc.p, tabs[stat[0]].disc.data(), nt * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-            KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np * ns) * sizeof(double), c.stream));
+            // rows of contracts with several flows (or none) are added to: zero them; a contract
+            // with a single flow has it stored on every path (every path walks every step)
+            bool all_single = true;
+            for (size_t q = 0; q < stat.size(); ++q) all_single = all_single && sched[stat[q]].flows.size() == 1;
+            if (!all_single)
+                KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np * ns) * sizeof(double), c.stream));
             FlowArgs a{};
             a.progs = c.progs.as<KxProgram>();
             a.flows = c.items.as<FlowRec>();
