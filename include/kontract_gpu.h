@@ -151,7 +151,8 @@ typedef struct kx_launch_stats {
     uint32_t block_threads;
     uint32_t path_kernel;      /* last path kernel: 0 none, 1 k_paths (every
                                   contract), 2 k_lean (barrier/time contracts),
-                                  3 k_lean on compiled static schedules */
+                                  3 k_lean on compiled static schedules, 4 the
+                                  same with a running average of the spot */
     uint64_t h2d_bytes, d2h_bytes;
 } kx_launch_stats;
 
@@ -325,7 +326,7 @@ typedef struct kx_book_info {
     uint32_t n_contracts, n_groups;
     uint64_t n_paths, path_steps;  /* totals over the book */
     double tune_ms;                /* time spent tuning at creation */
-    uint32_t group_kernel[4];      /* first 4 groups: 1 k_paths, 2 k_lean, 3 static */
+    uint32_t group_kernel[4];      /* first 4 groups: 1 k_paths, 2 k_lean, 3 static, 4 static + average */
     uint32_t group_minb[4];        /* tuned register budget */
     uint32_t group_item_paths[4];  /* tuned paths per work item */
     uint32_t group_contracts[4];

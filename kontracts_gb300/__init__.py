@@ -586,7 +586,7 @@ class Book:
         g = i.n_groups
         return {"n_contracts": i.n_contracts, "n_groups": g, "n_paths": i.n_paths, "path_steps": i.path_steps,
                 "tune_ms": i.tune_ms,
-                "groups": [{"kernel": {1: "k_paths", 2: "k_lean", 3: "k_lean/static"}.get(i.group_kernel[q], "?"),
+                "groups": [{"kernel": {1: "k_paths", 2: "k_lean", 3: "k_lean/static", 4: "k_lean/static+average"}.get(i.group_kernel[q], "?"),
                             "minb": i.group_minb[q], "item_paths": i.group_item_paths[q],
                             "contracts": i.group_contracts[q]} for q in range(min(g, 4))]}
 

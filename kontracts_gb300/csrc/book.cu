@@ -175,16 +175,17 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
         Ctx &c = ctx();
         std::lock_guard<std::mutex> lk(c.mu);
         begin_call(c);
-        // groups: (model kind, precision, kernel family)
+        // groups: (model kind, precision, kernel family: 3 static with a running average,
+        // 2 static, 1 lean with the general handler, 0 k_paths)
         std::vector<int> fam(n);
         for (size_t i = 0; i < n; ++i) {
             std::vector<Job> one;
             one.push_back(make_job(*b->progs[i], b->models[i], b->cfgs[i], b->grids[i], {}, 0, 0.0));
-            fam[i] = use_static(one, 1) ? 2 : use_lean(one, 1) ? 1 : 0;
+            fam[i] = use_static(one, 1) ? (lean_has_average(one) ? 3 : 2) : use_lean(one, 1) ? 1 : 0;
         }
         for (int kind = 0; kind < 2; ++kind)
             for (int prec = 0; prec < 2; ++prec)
-                for (int f = 2; f >= 0; --f) {
+                for (int f = 3; f >= 0; --f) {
                     kx_book::Group g;
                     for (size_t i = 0; i < n; ++i)
                         if (b->models[i].kind == kind && b->cfgs[i].precision == prec && fam[i] == f) g.members.push_back(i);
@@ -203,7 +204,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
             int nv = 0;
             const bool lean = g.family >= 1;
             const int *vs = variants(b->models[g.members[0]].kind, g.cfg.precision == KX_PREC_FP64, 1, lean, nv);
-            g.plan = plan_paths(jobs[q], g.cfg, 1, vs[0], lean, 0, g.family == 2);
+            g.plan = plan_paths(jobs[q], g.cfg, 1, vs[0], lean, 0, g.family >= 2);
             regs.push_back(region_sizes(g.plan));
             const Region &r = regs.back();
             bytes += r.progs + r.steps + r.disc + r.cons + r.thr + r.items + r.statics;
@@ -318,7 +319,7 @@ kx_status kx_book_price(kx_book *b, kx_price_result *out) {
             c.last.steps_simulated += sim;
             check_err_word(hc[1]);
             if (b->groups[q].plan.n_items) c.last.kernel_launches++;
-            c.last.path_kernel = b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
+            c.last.path_kernel = b->groups[q].plan.acc ? 4u : b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
         }
         if (b->n_chunks) c.last.kernel_launches++;
         const size_t n = b->progs.size();
@@ -372,7 +373,7 @@ kx_status kx_book_get_info(const kx_book *b, kx_book_info *info) {
         info->path_steps = b->path_steps;
         info->tune_ms = b->tune_ms;
         for (size_t q = 0; q < b->groups.size() && q < 4; ++q) {
-            info->group_kernel[q] = b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
+            info->group_kernel[q] = b->groups[q].plan.acc ? 4u : b->groups[q].plan.stat ? 3u : b->groups[q].plan.lean ? 2u : 1u;
             info->group_minb[q] = (uint32_t)b->groups[q].plan.minb;
             info->group_item_paths[q] = (uint32_t)b->groups[q].plan.item_paths;
             info->group_contracts[q] = (uint32_t)b->groups[q].members.size();

@@ -302,8 +302,9 @@ template void pack_steps<double>(const StepTables &, std::vector<unsigned char> 
 // Launch the fused path kernel over `jobs` (all of one model kind, one
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
-const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat) {
-    if (lean) return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat) : lean_kernel_heston(f64, minb, stat);
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat, bool acc) {
+    if (lean)
+        return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc) : lean_kernel_heston(f64, minb, stat, acc);
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
     if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
     return paths_kernel_heston(f64, minb);
@@ -313,19 +314,43 @@ const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool
 // Spot-cmp-Const conditions and keep no averages or extrema (one scenario,
 // no smoothing). Both kernels value every path identically; KX_PATH_KERNEL
 // = "general" or "lean" forces one of them (the lean one only where it applies).
+// A contract's one running average of the spot that the static family of
+// k_lean keeps in registers (average(S) over a window, no nesting).
+static bool lean_average(const KxProgram &P) {
+    return P.n_acc == 1 && P.acc[0].kind == ACC_SUM && P.acc[0].inner == IK_SPOT && !P.acc[0].static_err;
+}
+
 static bool lean_applies(const std::vector<Job> &jobs, int ns) {
     if (ns != 1) return false;
+    bool avg = false;
     for (auto &j : jobs) {
-        if (j.dev.smooth || j.prog.n_acc || j.prog.spot_each_step) return false;
+        if (j.dev.smooth) return false;
+        if (j.prog.n_acc && !lean_average(j.prog)) return false;
+        // the spot each step: for the average (kept by k_lean) or a general condition (not served)
+        if (j.prog.spot_each_step && !j.prog.n_acc) return false;
+        avg = avg || j.prog.n_acc;
         for (int i = 0; i < j.prog.n_trig; ++i)
             if (j.prog.trig[i].cond_kind == CK_GENERAL) return false;
     }
+    if (avg) {  // averages only on static schedules
+        StaticDev T;
+        for (auto &j : jobs)
+            if (!build_static(j, T)) return false;
+    }
     return true;
+}
+
+bool lean_has_average(const std::vector<Job> &jobs) {
+    for (auto &j : jobs)
+        if (j.prog.n_acc) return true;
+    return false;
 }
 
 bool use_lean(const std::vector<Job> &jobs, int ns) {
     const char *env = getenv("KX_PATH_KERNEL");
     if (env && strcmp(env, "general") == 0) return false;
+    // "lean" forces the general event handler, which keeps no averages
+    if (env && strcmp(env, "lean") == 0 && lean_has_average(jobs)) return false;
     return lean_applies(jobs, ns);
 }
 
@@ -334,9 +359,16 @@ bool use_lean(const std::vector<Job> &jobs, int ns) {
 // an error-capable evaluation, or more than KX_MAX_SEV event steps.
 bool build_static(const Job &j, StaticDev &T) {
     const KxProgram &P = j.prog;
-    if (P.err_capable || (P.all_leaves & ~P.simple_leaves) != 0u || P.n_acc) return false;
+    if (P.n_acc > 1 || (P.n_acc == 1 && !lean_average(P))) return false;
+    // amounts without a closed form only when they read the average (the interpreter evaluates them)
+    if (!P.n_acc && (P.err_capable || (P.all_leaves & ~P.simple_leaves) != 0u)) return false;
     const StaticSchedule S = static_schedule(P, j.tab);
     if (!S.static_ok) return false;
+    // an average can only fail when read too early (acc_value): every flow that reads it pays at a
+    // known step, so the schedule is error-free when each such step is at or after its first valid one
+    if (P.n_acc)
+        for (auto &f : S.flows)
+            if (P.leaf[f.leaf].err_capable && f.step < P.acc[0].e_min) return false;
     memset(&T, 0, sizeof T);
     std::map<int, std::pair<uint32_t, uint32_t>> at;  // step -> (armed barriers, paid flows)
     for (auto &f : S.flows) {
@@ -371,9 +403,16 @@ bool build_static(const Job &j, StaticDev &T) {
     }
     for (int q = 0; q < P.n_leaf; ++q) {
         const KxLeaf &F = P.leaf[q];
-        T.f_fast[q] = F.kind == AK_CONST ? (uint8_t)FA_NONE : F.fast;
-        T.f_k[q] = F.kind == AK_CONST ? 0.0 : P.cpool[F.fast_k];
+        const bool simple = (P.simple_leaves >> q) & 1u;
+        T.f_fast[q] = F.kind == AK_CONST || !simple ? (uint8_t)FA_NONE : F.fast;
+        T.f_k[q] = F.kind == AK_CONST || !simple ? 0.0 : P.cpool[F.fast_k];
         T.f_sign[q] = F.sign;
+        if (F.kind != AK_CONST && !simple) T.gen_flows |= 1u << q;
+    }
+    if (P.n_acc) {
+        T.acc_on = 1;
+        T.acc_from = P.acc[0].i_from;
+        T.acc_to = P.acc[0].i_to;
     }
     return true;
 }
@@ -486,6 +525,8 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.f64 = cfg.precision == KX_PREC_FP64;
     P.lean = lean;
     P.stat = lean && stat;
+    P.acc = P.stat && lean_has_average(jobs);
+    if (lean && !P.stat && lean_has_average(jobs)) raise(KX_CUDA_ERROR, "averages need the static family");
     if (P.stat) {
         P.statics.resize(jobs.size());
         for (size_t q = 0; q < jobs.size(); ++q)
@@ -534,8 +575,8 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     const bool smooth = jobs[0].dev.smooth != 0;
     P.surv_base = 2u * (uint32_t)max_acc;
     P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
-    P.smem = (size_t)ns * P.slots * block * (f64 ? 8 : 4);
-    P.kfn = select_kernel(P.model, f64, ns, minb, lean, P.stat);
+    P.smem = lean ? 0 : (size_t)ns * P.slots * block * (f64 ? 8 : 4);  // k_lean keeps its average in registers
+    P.kfn = select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc);
     if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (P.smem > 48 * 1024)
         KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
@@ -661,7 +702,7 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.last.kernel_launches++;
     c.last.grid_blocks = (uint32_t)P.grid_blocks;
     c.last.block_threads = (uint32_t)KX_BLOCK;
-    c.last.path_kernel = P.stat ? 3u : lean ? 2u : 1u;
+    c.last.path_kernel = P.acc ? 4u : P.stat ? 3u : lean ? 2u : 1u;
     uint32_t hc[4] = {0, 0, 0, 0};
     KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));

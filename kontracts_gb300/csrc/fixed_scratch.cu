@@ -151,7 +151,7 @@ extern "C" kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_mod
             float *t = reinterpret_cast<float *>(thr.data());
             for (size_t q = 0; q < j.thr.size(); ++q) t[q] = (float)j.thr[q];
         }
-        const bool lean = use_lean(jobs, 1);
+        const bool lean = use_lean(jobs, 1) && !lean_has_average(jobs);  // this entry runs no static schedules
         int nv = 0;
         const int minb = variants(j.model.kind, f64, 1, lean, nv)[0];
         const void *kfn = select_kernel(j.model.kind, f64, 1, minb, lean);

@@ -9,14 +9,19 @@ template __global__ void k_paths<double, M_GBM, 1, 4>(const PathArgs);
 template __global__ void k_paths<double, M_GBM, 1, 2>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 6, false>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 6, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 6, true, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, false>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 5, true, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 4, false>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 4, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 4, true, true>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 4, false>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 4, true>(const PathArgs);
+template __global__ void k_lean<double, M_GBM, 4, true, true>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 3, false>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 3, true>(const PathArgs);
+template __global__ void k_lean<double, M_GBM, 3, true, true>(const PathArgs);
 
 const void *paths_kernel_gbm(int fp64, int minb) {
     if (fp64) return minb >= 4 ? (const void *)&k_paths<double, M_GBM, 1, 4> : (const void *)&k_paths<double, M_GBM, 1, 2>;
@@ -28,16 +33,17 @@ const void *paths_kernel_gbm(int fp64, int minb) {
 }
 
 template <class Real, int MINB>
-static const void *lean_pick(bool stat) {
+static const void *lean_pick(bool stat, bool acc) {
+    if (acc) return (const void *)&k_lean<Real, M_GBM, MINB, true, true>;
     return stat ? (const void *)&k_lean<Real, M_GBM, MINB, true> : (const void *)&k_lean<Real, M_GBM, MINB, false>;
 }
 
-const void *lean_kernel_gbm(int fp64, int minb, bool stat) {
-    if (fp64) return minb >= 4 ? lean_pick<double, 4>(stat) : lean_pick<double, 3>(stat);
+const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc) {
+    if (fp64) return minb >= 4 ? lean_pick<double, 4>(stat, acc) : lean_pick<double, 3>(stat, acc);
     switch (minb) {
-    case 6: return lean_pick<float, 6>(stat);
-    case 5: return lean_pick<float, 5>(stat);
-    default: return lean_pick<float, 4>(stat);
+    case 6: return lean_pick<float, 6>(stat, acc);
+    case 5: return lean_pick<float, 5>(stat, acc);
+    default: return lean_pick<float, 4>(stat, acc);
     }
 }
 }  // namespace kx

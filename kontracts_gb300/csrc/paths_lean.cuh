@@ -148,6 +148,10 @@ struct StaticDev {
     int32_t n_ev;
     uint32_t up_mask;    // barrier slots that fire upwards (y >= thr); the others downwards (y <= thr)
     uint32_t all_flows;  // flow slots of the schedule (flows knocked by time-only untils are left out)
+    uint32_t gen_flows;  // flow slots whose amount reads the average: evaluated by the interpreter
+    int32_t acc_on;      // the contract keeps one running average of the spot (accumulator slot 0)
+    int32_t acc_from;    // its window: steps acc_from .. acc_to
+    int32_t acc_to;
     int32_t pad;
     int32_t ev_step[KX_MAX_SEV];
     uint32_t ev_arm[KX_MAX_SEV];  // barrier slots armed at that step (tested at once)
@@ -172,11 +176,28 @@ __device__ __forceinline__ Real sthr(const StaticDev &T, int i) {
     return sizeof(Real) == 4 ? (Real)T.thr32[i] : (Real)T.thr64[i];
 }
 
+// One spot added to the running sum of an average, as the general kernel
+// adds it (contract_step): compensated (Kahan) in FP32, plain in FP64.
+template <class Real>
+__device__ __forceinline__ void acc_add(Real &v, Real &c, Real x) {
+    if (sizeof(Real) == 8) {
+        v = v + x;
+    } else {
+        const Real yk = x - c;
+        const Real t = v + yk;
+        c = (t - v) - yk;
+        v = t;
+    }
+}
+
 // The contract at step k of a static-schedule path: knock-outs of the live
 // barriers, then the static event of step k (barriers armed and tested at
-// once, flows paid), as on_event orders them (pricer.rs:374-433).
-template <class Real>
-__device__ __forceinline__ void static_event(const StaticDev &T, const double *D, Real s0, Real y, int k, SLane &L) {
+// once, flows paid), as on_event orders them (pricer.rs:374-433). ACC: flows
+// in gen_flows read the running average (av, ac: its sum and compensation),
+// evaluated by the interpreter as on_event evaluates them.
+template <class Real, bool ACC = false>
+__device__ __forceinline__ void static_event(const StaticDev &T, const double *D, Real s0, Real y, int k, SLane &L,
+                                             const KxProgram *P = nullptr, Real av = Real(0), Real ac = Real(0)) {
     uint32_t m = L.live;
     while (m) {
         const int i = __ffs(m) - 1;
@@ -203,7 +224,12 @@ __device__ __forceinline__ void static_event(const StaticDev &T, const double *D
                 const int j = __ffs(pay) - 1;
                 pay &= pay - 1;
                 double amt = T.f_sign[j];
-                if (T.f_fast[j] != FA_NONE) {
+                if (ACC && ((T.gen_flows >> j) & 1u)) {
+                    Real accbuf[2] = {av, ac};
+                    uint32_t e = 0;
+                    amt = (double)eval_code<Real>(*P, P->leaf[j].code_off, P->leaf[j].code_len,
+                                                  AccView<Real>{accbuf, 1}, 0u, k, S, e);
+                } else if (T.f_fast[j] != FA_NONE) {
                     const Real K = (Real)T.f_k[j];
                     Real r;
                     switch (T.f_fast[j]) {
@@ -246,11 +272,12 @@ struct HestonPar {
 // which the barrier window or the step limit fires (returns true; k is that
 // step) or to the end of the block (k is the next step). UNI: every step has
 // the coefficients (uc0, uc1), so the step table is not read. The states are
-// the same bit for bit whichever way the block is walked.
-template <class Real, int MODEL, bool UNI>
+// the same bit for bit whichever way the block is walked. ACC: the spot of
+// every step in af .. at is added to the running average (av, ac).
+template <class Real, int MODEL, bool UNI, bool ACC>
 __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Real uc1, const HestonPar<Real> &hp,
                                            const Real (&zz)[4], int off, Real hi, Real lo, int lim, Real &y, Real &v,
-                                           int &k) {
+                                           int &k, Real s0, int af, int at, Real &av, Real &ac) {
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;
     // GBM: a whole block is stepped first and tested once (min and max of its
     // states against the window, its last step against the limit); only a
@@ -258,6 +285,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
     // step is long enough that redoing it costs more than the test saves.
     if (MODEL == M_GBM && off == 0) {
         Real yy = y, vv = v, mx = Real(-INFINITY), mn = Real(INFINITY);
+        Real av2 = av, ac2 = ac;
 #pragma unroll
         for (int j = 0; j < SPB; ++j) {
             Real c0 = uc0, c1 = uc1;
@@ -272,12 +300,17 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
                                   zz[2 * j], zz[2 * j + 1], yy, vv);
             }
+            if (ACC && k + j >= af && k + j <= at) acc_add<Real>(av2, ac2, spot_of<Real>(s0, yy));
             mx = fmax(mx, yy);
             mn = fmin(mn, yy);
         }
         if (mx < hi && mn > lo && k + SPB - 1 < lim) {  // nothing fires inside the block
             y = yy;
             v = vv;
+            if (ACC) {
+                av = av2;
+                ac = ac2;
+            }
             k += SPB;
             return false;
         }
@@ -298,6 +331,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
                                   zz[2 * j], zz[2 * j + 1], y, v);
             }
+            if (ACC && k >= af && k <= at) acc_add<Real>(av, ac, spot_of<Real>(s0, y));
             if (y >= hi || y <= lo || k >= lim) ev = true;
             else ++k;
         }
@@ -305,8 +339,11 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
     return ev;
 }
 
-template <class Real, int MODEL, int MINB, bool STATIC>
+// ACC (static schedules only): the contracts may keep one running average
+// of the spot (accumulator slot 0), summed in registers.
+template <class Real, int MODEL, int MINB, bool STATIC, bool ACC = false>
 __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
+    static_assert(!ACC || STATIC, "averages need a static schedule");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -348,6 +385,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     Trig st{0, 0, 0, 0, 0, 0, 0, 0, 0.0};
     SLane sl{0u, 0u, 0, 0.0};
     uint32_t my_steps = 0;
+    Real av = 0, ac = 0;      // running average: sum and compensation
+    int acc_f = 1, acc_t = 0; // warp-uniform: the contract's average window (empty: none)
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
 
@@ -396,6 +435,11 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         hv0 = pick<Real>(C->v0, C->v0f);
                         scheme = C->heston_scheme;
                     }
+                    if (ACC) {
+                        const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
+                        acc_f = T.acc_on ? T.acc_from : 1;
+                        acc_t = T.acc_on ? T.acc_to : 0;
+                    }
                 }
                 pend = -1;
                 nx = (uint32_t)w.first;
@@ -412,6 +456,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 busy = true;
                 y = Real(0);
                 v = fmax(hv0, Real(0));
+                av = ac = Real(0);
                 if (STATIC) sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
                 else st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
                 k = 0;
@@ -448,8 +493,12 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 }
                 const int k_in = k;
                 const HestonPar<Real> hp{hr, hk, hth, hsv, hrho, hrp, scheme};
-                if (uniform) ev = lean_steps<Real, MODEL, true>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k);
-                else ev = lean_steps<Real, MODEL, false>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k);
+                if (uniform)
+                    ev = lean_steps<Real, MODEL, true, ACC>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, acc_f,
+                                                            acc_t, av, ac);
+                else
+                    ev = lean_steps<Real, MODEL, false, ACC>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, acc_f,
+                                                             acc_t, av, ac);
                 my_steps += (uint32_t)(k - k_in) + (ev ? 1u : 0u);
             }
         }
@@ -468,7 +517,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                     double pv;
                     if (STATIC) {
                         const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
-                        static_event<Real>(T, D, s0, y, k, sl);
+                        if (ACC && k == 0 && acc_f <= 0 && 0 <= acc_t)  // the spot at t = 0 (steps >= 1: lean_steps)
+                            acc_add<Real>(av, ac, spot_of<Real>(s0, y));
+                        static_event<Real, ACC>(T, D, s0, y, k, sl, P, av, ac);
                         static_window<Real>(T, sl.live, hi, lo);
                         lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;
                         done = sl.rem == 0u;
@@ -503,7 +554,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
 }
 
 // which: fp64 0/1; returns nullptr for a missing register budget.
-const void *lean_kernel_gbm(int fp64, int minb, bool stat);
-const void *lean_kernel_heston(int fp64, int minb, bool stat);
+// acc: the static family with a running average (stat must be set).
+const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc);
+const void *lean_kernel_heston(int fp64, int minb, bool stat, bool acc);
 
 }  // namespace kx

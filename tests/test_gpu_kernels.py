@@ -82,6 +82,42 @@ def test_lean_daily_grid_long_paths():
     assert np.array_equal(np.asarray(p1), np.asarray(p3))
 
 
+AVERAGES = {
+    "asian": lambda: kx.scale((kx.average(S) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "asian_window": lambda: kx.scale((kx.average_over(S, 0.25, 0.75) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "asian_put_early": lambda: kx.scale((100.0 - kx.average(S)).clip(0.0), kx.one()) @ kx.at(0.6),
+    "knock_out_asian": lambda: kx.until(S >= 135.0, kx.scale((kx.average(S) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0)),
+    "asian_plus_call": lambda: kx.scale((kx.average(S) - 95.0).clip(0.0), kx.one()) @ kx.at(1.0)
+    + kx.european_call("X", 110.0, 0.5),
+}
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", sorted(AVERAGES))
+def test_lean_average_equals_general(name, prec):
+    """Averages of the spot on a static schedule: k_lean keeps the running sum
+    in registers (compensated in FP32, as k_paths sums it) and values every
+    path as k_paths does, bit for bit, in both models."""
+    c = AVERAGES[name]()
+    for m, n, spy in ((kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X"), 4000, 52),
+                      (kx.heston(100.0, 0.04, 1.5, 0.04, 0.5, -0.7, 0.03, asset="X"), 2000, 100)):
+        r1, p1 = _run(c, m, prec, "general", n=n, spy=spy)
+        r3, p3 = _run(c, m, prec, "auto", n=n, spy=spy)
+        assert kx.last_launch_stats()["path_kernel"] == 4, name
+        assert np.array_equal(np.asarray(p1), np.asarray(p3)), name
+        assert r1.price == r3.price and r1.std_error == r3.std_error
+
+
+def test_lean_average_daily_grid():
+    """An Asian call on a daily grid at a size where lanes hold paths of very
+    different ages (the book's Asian shape)."""
+    c = AVERAGES["asian"]()
+    m = kx.GBM(s0=100.0, sigma=0.25, r=0.03, asset="X")
+    _, p1 = _run(c, m, "fp32", "general", n=100_000, spy=252)
+    _, p3 = _run(c, m, "fp32", "auto", n=100_000, spy=252)
+    assert np.array_equal(np.asarray(p1), np.asarray(p3))
+
+
 @pytest.mark.parametrize("name,kernel", [("up_and_out", 3), ("double_barrier", 3), ("bermudan_strip", 3),
                                          ("nested_when", 3), ("late_barrier", 3), ("digital", 2),
                                          ("knock_in", 2), ("first_touch_pays", 2)])
