@@ -314,10 +314,11 @@ const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool
 // Spot-cmp-Const conditions and keep no averages or extrema (one scenario,
 // no smoothing). Both kernels value every path identically; KX_PATH_KERNEL
 // = "general" or "lean" forces one of them (the lean one only where it applies).
-// A contract's one running average of the spot that the static family of
-// k_lean keeps in registers (average(S) over a window, no nesting).
+// A contract's one accumulator of the spot that the static family of k_lean
+// keeps in registers: an average over a window, a running max or min (no
+// nesting).
 static bool lean_average(const KxProgram &P) {
-    return P.n_acc == 1 && P.acc[0].kind == ACC_SUM && P.acc[0].inner == IK_SPOT && !P.acc[0].static_err;
+    return P.n_acc == 1 && P.acc[0].inner == IK_SPOT && !P.acc[0].static_err;
 }
 
 static bool lean_applies(const std::vector<Job> &jobs, int ns) {
@@ -413,6 +414,7 @@ bool build_static(const Job &j, StaticDev &T) {
         T.acc_on = 1;
         T.acc_from = P.acc[0].i_from;
         T.acc_to = P.acc[0].i_to;
+        T.acc_kind = P.acc[0].kind;
     }
     return true;
 }

@@ -148,11 +148,11 @@ struct StaticDev {
     int32_t n_ev;
     uint32_t up_mask;    // barrier slots that fire upwards (y >= thr); the others downwards (y <= thr)
     uint32_t all_flows;  // flow slots of the schedule (flows knocked by time-only untils are left out)
-    uint32_t gen_flows;  // flow slots whose amount reads the average: evaluated by the interpreter
-    int32_t acc_on;      // the contract keeps one running average of the spot (accumulator slot 0)
+    uint32_t gen_flows;  // flow slots whose amount reads the accumulator: evaluated by the interpreter
+    int32_t acc_on;      // the contract keeps one accumulator of the spot (slot 0): average, max or min
     int32_t acc_from;    // its window: steps acc_from .. acc_to
     int32_t acc_to;
-    int32_t pad;
+    int32_t acc_kind;    // KxAccKind
     int32_t ev_step[KX_MAX_SEV];
     uint32_t ev_arm[KX_MAX_SEV];  // barrier slots armed at that step (tested at once)
     uint32_t ev_pay[KX_MAX_SEV];  // flow slots paid at that step unless knocked out
@@ -176,11 +176,18 @@ __device__ __forceinline__ Real sthr(const StaticDev &T, int i) {
     return sizeof(Real) == 4 ? (Real)T.thr32[i] : (Real)T.thr64[i];
 }
 
-// One spot added to the running sum of an average, as the general kernel
-// adds it (contract_step): compensated (Kahan) in FP32, plain in FP64.
-template <class Real>
-__device__ __forceinline__ void acc_add(Real &v, Real &c, Real x) {
-    if (sizeof(Real) == 8) {
+// One spot added to the accumulator, as the general kernel adds it
+// (contract_step): a running max or min, or the sum of an average,
+// compensated (Kahan) in FP32 and plain in FP64. AK: the kind (KxAccKind)
+// when known at compile time, -1 to read `kind`.
+template <class Real, int AK = -1>
+__device__ __forceinline__ void acc_add(int kind, Real &v, Real &c, Real x) {
+    if (AK >= 0) kind = AK;
+    if (kind == ACC_MAX) {
+        v = fmax(v, x);
+    } else if (kind == ACC_MIN) {
+        v = fmin(v, x);
+    } else if (sizeof(Real) == 8) {
         v = v + x;
     } else {
         const Real yk = x - c;
@@ -273,11 +280,13 @@ struct HestonPar {
 // step) or to the end of the block (k is the next step). UNI: every step has
 // the coefficients (uc0, uc1), so the step table is not read. The states are
 // the same bit for bit whichever way the block is walked. ACC: the spot of
-// every step in af .. at is added to the running average (av, ac).
-template <class Real, int MODEL, bool UNI, bool ACC>
+// every step in af .. at is added to the accumulator of kind AK (av, ac;
+// AK < 0: none).
+template <class Real, int MODEL, bool UNI, int AK>
 __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Real uc1, const HestonPar<Real> &hp,
                                            const Real (&zz)[4], int off, Real hi, Real lo, int lim, Real &y, Real &v,
                                            int &k, Real s0, int af, int at, Real &av, Real &ac) {
+    constexpr bool ACC = AK >= 0;
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;
     // GBM: a whole block is stepped first and tested once (min and max of its
     // states against the window, its last step against the limit); only a
@@ -300,7 +309,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
                                   zz[2 * j], zz[2 * j + 1], yy, vv);
             }
-            if (ACC && k + j >= af && k + j <= at) acc_add<Real>(av2, ac2, spot_of<Real>(s0, yy));
+            if (ACC && k + j >= af && k + j <= at) acc_add<Real, AK>(AK, av2, ac2, spot_of<Real>(s0, yy));
             mx = fmax(mx, yy);
             mn = fmin(mn, yy);
         }
@@ -331,7 +340,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
                                   zz[2 * j], zz[2 * j + 1], y, v);
             }
-            if (ACC && k >= af && k <= at) acc_add<Real>(av, ac, spot_of<Real>(s0, y));
+            if (ACC && k >= af && k <= at) acc_add<Real, AK>(AK, av, ac, spot_of<Real>(s0, y));
             if (y >= hi || y <= lo || k >= lim) ev = true;
             else ++k;
         }
@@ -339,8 +348,8 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
     return ev;
 }
 
-// ACC (static schedules only): the contracts may keep one running average
-// of the spot (accumulator slot 0), summed in registers.
+// ACC (static schedules only): the contracts may keep one accumulator of the
+// spot (slot 0: an average, a running max or min), in registers.
 template <class Real, int MODEL, int MINB, bool STATIC, bool ACC = false>
 __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     static_assert(!ACC || STATIC, "averages need a static schedule");
@@ -385,8 +394,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     Trig st{0, 0, 0, 0, 0, 0, 0, 0, 0.0};
     SLane sl{0u, 0u, 0, 0.0};
     uint32_t my_steps = 0;
-    Real av = 0, ac = 0;      // running average: sum and compensation
-    int acc_f = 1, acc_t = 0; // warp-uniform: the contract's average window (empty: none)
+    Real av = 0, ac = 0;      // accumulator: value (sum, max or min) and compensation
+    int acc_f = 1, acc_t = 0; // warp-uniform: the contract's accumulator window (empty: none)
+    int acc_k = ACC_SUM;      // and its kind
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
 
@@ -439,6 +449,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
                         acc_f = T.acc_on ? T.acc_from : 1;
                         acc_t = T.acc_on ? T.acc_to : 0;
+                        acc_k = T.acc_kind;
                     }
                 }
                 pend = -1;
@@ -456,7 +467,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 busy = true;
                 y = Real(0);
                 v = fmax(hv0, Real(0));
-                av = ac = Real(0);
+                // as k_paths starts an accumulator
+                av = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
+                ac = Real(0);
                 if (STATIC) sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
                 else st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
                 k = 0;
@@ -493,12 +506,27 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 }
                 const int k_in = k;
                 const HestonPar<Real> hp{hr, hk, hth, hsv, hrho, hrp, scheme};
-                if (uniform)
-                    ev = lean_steps<Real, MODEL, true, ACC>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, acc_f,
-                                                            acc_t, av, ac);
-                else
-                    ev = lean_steps<Real, MODEL, false, ACC>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, acc_f,
-                                                             acc_t, av, ac);
+                if (!ACC) {
+                    if (uniform)
+                        ev = lean_steps<Real, MODEL, true, -1>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, 0, -1,
+                                                               av, ac);
+                    else
+                        ev = lean_steps<Real, MODEL, false, -1>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, 0,
+                                                                -1, av, ac);
+                } else if (acc_k == ACC_SUM) {  // the kind is warp-uniform: one branch per block, none per step
+                    if (uniform)
+                        ev = lean_steps<Real, MODEL, true, ACC_SUM>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0,
+                                                                    acc_f, acc_t, av, ac);
+                    else
+                        ev = lean_steps<Real, MODEL, false, ACC_SUM>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0,
+                                                                     acc_f, acc_t, av, ac);
+                } else if (acc_k == ACC_MAX) {
+                    ev = lean_steps<Real, MODEL, false, ACC_MAX>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0,
+                                                                 acc_f, acc_t, av, ac);
+                } else {
+                    ev = lean_steps<Real, MODEL, false, ACC_MIN>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0,
+                                                                 acc_f, acc_t, av, ac);
+                }
                 my_steps += (uint32_t)(k - k_in) + (ev ? 1u : 0u);
             }
         }
@@ -518,7 +546,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                     if (STATIC) {
                         const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
                         if (ACC && k == 0 && acc_f <= 0 && 0 <= acc_t)  // the spot at t = 0 (steps >= 1: lean_steps)
-                            acc_add<Real>(av, ac, spot_of<Real>(s0, y));
+                            acc_add<Real>(acc_k, av, ac, spot_of<Real>(s0, y));
                         static_event<Real, ACC>(T, D, s0, y, k, sl, P, av, ac);
                         static_window<Real>(T, sl.live, hi, lo);
                         lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;

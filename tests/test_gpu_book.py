@@ -33,8 +33,8 @@ def test_book_equals_individual_prices(prec, tune):
     cs, ms, ns, seeds = _mixed()
     book = kx.Book(cs, ms, ns, seeds, steps_per_year=252, precision=prec, tune=tune)
     info = book.info()
-    # static, static with the Asian's running average, lean (knock-in), general (running max)
-    assert info["n_contracts"] == len(cs) and info["n_groups"] == 4
+    # static, static with an accumulator (the Asian and the lookback), lean (knock-in)
+    assert info["n_contracts"] == len(cs) and info["n_groups"] == 3
     for rep in range(2):
         res = book.price()
         for c, m, n, s, r in zip(cs, ms, ns, seeds, res):

@@ -89,15 +89,20 @@ AVERAGES = {
     "knock_out_asian": lambda: kx.until(S >= 135.0, kx.scale((kx.average(S) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0)),
     "asian_plus_call": lambda: kx.scale((kx.average(S) - 95.0).clip(0.0), kx.one()) @ kx.at(1.0)
     + kx.european_call("X", 110.0, 0.5),
+    "lookback_call": lambda: kx.scale((kx.running_max(S) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "lookback_put": lambda: kx.scale((105.0 - kx.running_min(S)).clip(0.0), kx.one()) @ kx.at(0.8),
+    "knock_out_lookback": lambda: kx.until(S <= 70.0, kx.scale((kx.running_max(S) - 100.0).clip(0.0), kx.one())
+                                           @ kx.at(1.0)),
 }
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 @pytest.mark.parametrize("name", sorted(AVERAGES))
 def test_lean_average_equals_general(name, prec):
-    """Averages of the spot on a static schedule: k_lean keeps the running sum
-    in registers (compensated in FP32, as k_paths sums it) and values every
-    path as k_paths does, bit for bit, in both models."""
+    """An average, running max or running min of the spot on a static
+    schedule: k_lean keeps the accumulator in registers (an average's sum
+    compensated in FP32, as k_paths sums it) and values every path as
+    k_paths does, bit for bit, in both models."""
     c = AVERAGES[name]()
     for m, n, spy in ((kx.GBM(s0=100.0, sigma=0.3, r=0.04, asset="X"), 4000, 52),
                       (kx.heston(100.0, 0.04, 1.5, 0.04, 0.5, -0.7, 0.03, asset="X"), 2000, 100)):
