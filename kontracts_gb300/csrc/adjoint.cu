@@ -123,11 +123,14 @@ __device__ Dual<Real> eval_dual(const KxProgram &P, int off, int len, Real S, co
     return st[0];
 }
 
+// keys: the launch's Philox round keys when every contract has one seed.
 template <class Real>
-__device__ __forceinline__ void draws4(const AdjArgs &A, uint64_t path, uint64_t d, Real z[4]) {
+__device__ __forceinline__ void draws4(const AdjArgs &A, const PhiloxKeys &keys, uint64_t path, uint64_t d,
+                                       Real z[4]) {
     if (A.z64 == nullptr && A.z32 == nullptr) {
-        const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
-                                      (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+        const uint4 ctr = make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u);
+        const uint4 w = keys.ok ? philox4x32_10_rk(ctr, keys.rk)
+                                : philox4x32_10(ctr, (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
         box_muller(w.x, w.y, z[0], z[1]);
         box_muller(w.z, w.w, z[2], z[3]);
     } else {
@@ -198,7 +201,8 @@ __device__ __forceinline__ void model_step(const AdjPar<Real> &p, int scheme, co
 // steps that pay flows (sorted by step on the host), the amounts.
 template <class Real, int MODEL, bool ACC>
 __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict__ all, const uint64_t *__restrict__ off,
-                                                       int n_contracts, uint64_t total, double *__restrict__ out) {
+                                                       int n_contracts, uint64_t total, double *__restrict__ out,
+                                                       const PhiloxKeys keys) {
     constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
     for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
          gp += (uint64_t)gridDim.x * blockDim.x) {
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
         for (int k = 0; k <= N; ++k) {
             if (k > 0) {
                 const uint64_t d = (uint64_t)(k - 1) * DRAWS;
-                if ((d & 3u) == 0) draws4<Real>(A, path, d, z);
+                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
                 const int q = (int)(d & 3u);
                 model_step<Real, MODEL>(pp, A.scheme, R[k], z[q], DRAWS == 2 ? z[q + 1] : Real(0), y, v);
             }
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
             sv[0] = vv;
             for (int k = k0 + 1; k <= k1; ++k) {
                 const uint64_t d = (uint64_t)(k - 1) * DRAWS;
-                if ((d & 3u) == 0 || k == k0 + 1) draws4<Real>(A, path, d & ~3ull, z);
+                if ((d & 3u) == 0 || k == k0 + 1) draws4<Real>(A, keys, path, d & ~3ull, z);
                 const int q = (int)(d & 3u);
                 const Real a1 = z[q], a2 = DRAWS == 2 ? z[q + 1] : Real(0);
                 model_step<Real, MODEL>(pp, A.scheme, R[k], a1, a2, yy, vv);
@@ -537,7 +541,8 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
 template <class Real, int K, int NSU>
 __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__restrict__ all,
                                                            const uint64_t *__restrict__ off, int n_contracts,
-                                                           uint64_t total, double *__restrict__ out) {
+                                                           uint64_t total, double *__restrict__ out,
+                                                           const PhiloxKeys keys) {
     static_assert(K % 4 == 0 && (K & (K - 1)) == 0 && K <= ADJ_KMAX, "K: a power of two, multiple of 4");
     for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
          gp += (uint64_t)gridDim.x * blockDim.x) {
@@ -576,7 +581,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
         for (int k = 0; k <= N; ++k) {
             if (k > 0) {
                 const uint64_t d = (uint64_t)(k - 1);
-                if ((d & 3u) == 0) draws4<Real>(A, path, d, z);
+                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
                 y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
             }
             if (k % K == 0) ck_y[k / K] = y;  // K is a power of two: a mask, not a division
@@ -632,7 +637,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
 #pragma unroll
             for (int q = 0; q < K / 4; ++q) {  // the draws of steps k0 + 1 .. k0 + K
                 Real w4[4];
-                draws4<Real>(A, path, (uint64_t)(k0 + 4 * q), w4);
+                draws4<Real>(A, keys, path, (uint64_t)(k0 + 4 * q), w4);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) sz[1 + 4 * q + j] = w4[j];
             }
@@ -844,7 +849,11 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
         const AdjArgs *ap = c.cons.as<AdjArgs>();
         const uint64_t *op = c.items.as<uint64_t>();
         double *outp = c.pv.as<double>();
-        void *kargs[] = {&ap, &op, (void *)&nc, (void *)&total, &outp};
+        PhiloxKeys keys{};
+        bool one_seed = true;
+        for (int i = 0; i < nc; ++i) one_seed = one_seed && args[i].seed == args[0].seed;
+        if (one_seed) keys = philox_keys(args[0].seed);
+        void *kargs[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys};
         auto launch = [&](const void *fn) {
             const int full = persistent_blocks(fn, ADJ_BLOCK, 0);
             const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);

@@ -47,6 +47,26 @@ __device__ __forceinline__ uint4 philox4x32_10_rk(uint4 c, const uint32_t (&rk)[
     return c;
 }
 
+// The round keys of one seed for philox4x32_10_rk, passed to a kernel as a
+// parameter when every path of the launch draws from that seed (ok = 1).
+struct PhiloxKeys {
+    uint32_t ok;
+    uint32_t rk[20];
+};
+
+inline PhiloxKeys philox_keys(uint64_t seed) {
+    PhiloxKeys K{};
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        K.rk[2 * r] = k0;
+        K.rk[2 * r + 1] = k1;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    K.ok = 1u;
+    return K;
+}
+
 __device__ __forceinline__ float sqrt_approx(float x) {
     float r;
     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
