@@ -88,9 +88,23 @@ typedef struct kx_mc_config {
                                 registered with kx_set_shared_draws */
     int32_t precision;       /* KX_PREC_*: path arithmetic type; payoff sums are
                                 always FP64 */
-    int32_t flags;           /* reserved, must be 0 */
+    int32_t flags;           /* KX_VR_* bits (kx_price only), else 0 */
     double rate;             /* deterministic discount rate */
 } kx_mc_config;
+
+/* Variance reduction of kx_price (McConfig.variance_reduction,
+ * src/pricer.rs:108-230, src/variance_reduction.rs:60-235):
+ * KX_VR_ANTITHETIC: GBM models price n_paths / 2 pairs (the paths of the
+ * stream and their mirrors with negated normals), each pair valued at the mean
+ * of its two PVs; other models price the plain paths.
+ * KX_VR_CONTROL_VARIATE: the at-the-money call on the model's asset paid at
+ * the grid's last date is the control, its Black-Scholes value (s0, sigma of
+ * a GBM model; 100 and 0.2 otherwise, as the reference) known: per path
+ * pv - (pv_call - bs); with KX_VR_ANTITHETIC the correction is applied to the
+ * pair-averaged prices, and the standard error is the target's sample std over
+ * sqrt(2 n_half) (pricer.rs:185-219). */
+#define KX_VR_ANTITHETIC 1
+#define KX_VR_CONTROL_VARIATE 2
 
 /* Mirrors PriceResult (src/pricer.rs:58-71). */
 typedef struct kx_price_result {

@@ -393,13 +393,15 @@ class Contract:
               shared_draws: bool = False, per_path: bool = False):
         """Price under `model` (GBM or Model), as Contract.price of the
         reference. Returns a PriceResult (and the per-path discounted values
-        as a list when per_path=True)."""
-        if antithetic or control_variate:
-            raise KontractError(_abi.KX_UNSUPPORTED, "variance reduction is not part of this engine yet")
+        as a list when per_path=True). antithetic / control_variate: the
+        reference's variance reduction (pricer.rs:108-230): antithetic pairs
+        for GBM models, the at-the-money call as a control (no per-path
+        values then)."""
         if not isinstance(model, (GBM, Model)):
             raise TypeError("expected a GBM or Model")
         cm = model._c()
         cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, shared_draws)
+        cfg.flags = (_abi.KX_VR_ANTITHETIC if antithetic else 0) | (_abi.KX_VR_CONTROL_VARIATE if control_variate else 0)
         res = _abi.KxPriceResult()
         pp = (C.c_double * max(1, int(n_paths)))() if per_path else None
         with _lock:

@@ -18,6 +18,8 @@ KX_MALFORMED_CONTRACT = 6
 KX_UNSUPPORTED = 7
 KX_INVALID_ARGUMENT = 8
 KX_LSM_MONOMIAL = 0
+KX_VR_ANTITHETIC = 1
+KX_VR_CONTROL_VARIATE = 2
 KX_LSM_LAGUERRE = 1
 KX_CUDA_ERROR = 9
 KX_DEVICE_TIMEOUT = 10

@@ -815,6 +815,151 @@ __global__ void __launch_bounds__(256) k_peak_path(float *out, int paths_per_thr
     if (acc == 12345.f) out[threadIdx.x] = acc;
 }
 
+// Variance reduction (variance_reduction.rs:186-235): the antithetic pair
+// estimator 0.5 (b + a) and the control-variate correction t - 1 (c - bs),
+// per path, in the reference's operation order.
+__global__ void k_vr_pairs(const double *__restrict__ b, const double *__restrict__ a, uint64_t n,
+                           double *__restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = 0.5 * (b[i] + a[i]);
+}
+__global__ void k_vr_control(const double *__restrict__ t, const double *__restrict__ c, double bs, uint64_t n,
+                             double *__restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = t[i] - 1.0 * (c[i] - bs);
+}
+
+// norm_cdf and black_scholes_call of numerics.rs:22-71: the Abramowitz-Stegun
+// 7.1.26 rational approximation of erfc, as the reference evaluates it (its
+// value enters the control-variate price).
+static double norm_cdf_as(double x) {
+    const double z = x / 1.4142135623730951;  // x / sqrt(2)
+    const double sign = z < 0.0 ? -1.0 : 1.0;
+    const double a = std::fabs(z);
+    const double t = 1.0 / (1.0 + 0.3275911 * a);
+    const double poly = ((((1.061405429 * t - 1.453152027) * t) + 1.421413741) * t - 0.284496736) * t + 0.254829592;
+    const double erf_abs = 1.0 - poly * t * std::exp(-a * a);
+    return 0.5 * (1.0 + sign * erf_abs);
+}
+static double bs_call_as(double s, double k, double t, double r, double sigma) {
+    if (t <= 0.0 || sigma <= 0.0) return std::max(s - k * std::exp(-r * t), 0.0);
+    const double vst = sigma * std::sqrt(t);
+    const double d1 = (std::log(s / k) + (r + 0.5 * sigma * sigma) * t) / vst;
+    const double d2 = d1 - vst;
+    return s * norm_cdf_as(d1) - k * std::exp(-r * t) * norm_cdf_as(d2);
+}
+
+// A job on the mirrored paths: the diffusion coefficient of every step
+// negated, so every normal enters with the opposite sign (the GBM update is
+// y + fma(c1, z, c0); -c1 * z = c1 * -z exactly).
+static void mirror_job(Job &j) {
+    for (auto &c1 : j.tab.c1) c1 = -c1;
+    j.dev.uc1 = -j.dev.uc1;
+    j.dev.uc1f = -j.dev.uc1f;
+}
+
+// price_gbm with variance reduction (pricer.rs:108-230): the target (and the
+// control call) valued on the same grid and stream, combined per path on the
+// device, summarised with the deterministic chunk statistics.
+static kx_price_result price_vr(Ctx &c, const Program &p, const Model &m, const kx_mc_config &cfg,
+                                const std::vector<double> &grid, int vr) {
+    const bool gbm = m.kind == KX_MODEL_GBM;
+    const bool anti = (vr & KX_VR_ANTITHETIC) && gbm;  // other simulators have no antithetic paths
+    const bool cv = (vr & KX_VR_CONTROL_VARIATE) != 0;
+    const double cs0 = gbm ? m.s0 : 100.0, csig = gbm ? m.sigma : 0.2;  // gbm_params().unwrap_or
+    const double t_mat = grid.back();
+    Program ctrl;
+    double bs = 0.0;
+    if (cv) {  // when(at(t_mat), scale(max(spot(asset) - s0, 0), one("USD")))
+        char buf[96];
+        std::string js = "{\"When\":[{\"At\":";
+        snprintf(buf, sizeof buf, "%.17g", t_mat);
+        js += buf;
+        js += "},{\"Scale\":[{\"Max\":[{\"Sub\":[{\"Spot\":";
+        std::string a;  // the asset name as a JSON string
+        for (char ch : m.asset) {
+            if (ch == '"' || ch == '\\') a += '\\';
+            a += ch;
+        }
+        js += "\"" + a + "\"},{\"Const\":";
+        snprintf(buf, sizeof buf, "%.17g", cs0);
+        js += buf;
+        js += "}]},{\"Const\":0.0}]},{\"One\":\"USD\"}]}]}";
+        ctrl.json = js;
+        ctrl.ast = parse_contract_json(js.c_str());
+        ctrl.plan = compile_plan(*ctrl.ast);
+        lower(ctrl);
+        bs = bs_call_as(cs0, cs0, t_mat, cfg.rate, csig);
+    }
+    const uint64_t n = anti ? cfg.n_paths / 2 : cfg.n_paths;
+    kx_mc_config c2 = cfg;
+    c2.n_paths = n;
+    std::vector<Job> jobs;
+    jobs.push_back(make_job(p, m, c2, grid, {}, 0, 0.0));  // target
+    if (anti) {
+        jobs.push_back(jobs[0]);
+        mirror_job(jobs.back());
+    }
+    if (cv) {
+        jobs.push_back(make_job(ctrl, m, c2, grid, {}, 0, 0.0));
+        if (anti) {
+            jobs.push_back(jobs.back());
+            mirror_job(jobs.back());
+        }
+    }
+    uint64_t stride = 0;
+    run_paths(c, jobs, c2, 1, stride);
+    std::vector<StatsJob> sj(1);
+    sj[0].n = n;
+    // jobs: [target] (plain), [target, mirror] (anti), [target, control] (cv),
+    // [target, mirror, control, control mirror] (anti and cv)
+    const size_t want = 1 + (anti ? 1 : 0) + (cv ? (anti ? 2 : 1) : 0);
+    if (jobs.size() != want) raise(KX_CUDA_ERROR, "variance reduction: unexpected job layout");
+    if ((!anti && !cv) || (n == 0 && !(anti && cv)))  // plain paths (no antithetic paths for this model)
+        return finish(device_stats(c, c.pv.as<double>(), stride, sj)[0]);
+    const double *pv = c.pv.as<double>();
+    const int blocks = c.sm_count * 4;
+    auto pairs = [&](size_t jb, size_t ja, double *out) {
+        k_vr_pairs<<<blocks, 256, 0, c.stream>>>(pv + jobs[jb].dev.pv_off, pv + jobs[ja].dev.pv_off, n, out);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+    };
+    c.vr.ensure(std::max<uint64_t>(1, 2 * n) * sizeof(double));
+    double *v0 = c.vr.as<double>(), *v1 = v0 + n;
+    if (anti && !cv) {  // price_antithetic_on_paths
+        pairs(0, 1, v0);
+        return finish(device_stats(c, v0, n, sj)[0]);
+    }
+    if (!anti && cv) {  // cv only: price_control_variate_on_paths
+        k_vr_control<<<blocks, 256, 0, c.stream>>>(pv + jobs[0].dev.pv_off, pv + jobs[1].dev.pv_off, bs, n, v0);
+        KX_CUDA(cudaGetLastError());
+        c.last.kernel_launches++;
+        return finish(device_stats(c, v0, n, sj)[0]);
+    }
+    // antithetic + control variate: price_antithetic_with_cv (pricer.rs:185-219); with no pair the
+    // reference's formula gives the Black-Scholes value and a 0 / 0 standard error
+    if (n) {
+        pairs(0, 1, v0);
+        pairs(2, 3, v1);
+    }
+    std::vector<StatsJob> two(2);
+    two[0].begin = 0;
+    two[0].n = n;
+    two[1].begin = n;
+    two[1].n = n;
+    const std::vector<Stats> st = device_stats(c, v0, 2 * n, two);
+    const kx_price_result target = finish(st[0]), control = finish(st[1]);
+    kx_price_result r{};
+    r.price = target.price - 1.0 * (control.price - bs);
+    const uint64_t n_all = 2 * n;
+    r.sample_std = target.sample_std;
+    r.std_error = target.sample_std / std::sqrt((double)n_all);
+    r.ci95_low = r.price - 1.959963984540054 * r.std_error;
+    r.ci95_high = r.price + 1.959963984540054 * r.std_error;
+    r.n_paths = n_all;
+    return r;
+}
+
 // The bare Heston loop: Philox4x32-10 + Box-Muller for 2 normals per step and
 // the full-truncation Euler step of the path kernels (log spot and variance),
 // nothing else: the ceiling of a Heston path kernel on this RNG.
@@ -927,18 +1072,29 @@ kx_status kx_clear_shared_draws(void) {
     });
 }
 
-kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg, kx_price_result *out,
+kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg_in, kx_price_result *out,
                    double *per_path_pv) {
     return guarded([&] {
         const Program &p = program_of(prog);
         Model m = model_from_c(model);
+        if (!cfg_in) raise(KX_INVALID_ARGUMENT, "config is NULL");
+        const int vr = cfg_in->flags & (KX_VR_ANTITHETIC | KX_VR_CONTROL_VARIATE);
+        kx_mc_config cfg_v = *cfg_in;
+        cfg_v.flags &= ~vr;
+        const kx_mc_config *cfg = &cfg_v;
         check_cfg(cfg);
         if (!out) raise(KX_INVALID_ARGUMENT, "out is NULL");
+        if (vr && per_path_pv) raise(KX_INVALID_ARGUMENT, "per-path values are not defined with variance reduction");
         validate_model(m);
         auto grid = time_grid_forced(p.plan, cfg->steps_per_year, m.requires_fine_grid());  // pricer.rs:104
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         begin_call(c);
+        if (vr) {  // pricer.rs:108-110
+            *out = price_vr(c, p, m, *cfg, grid, vr);
+            end_call(c);
+            return;
+        }
         std::vector<Job> jobs;
         jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
         uint64_t stride = 0;

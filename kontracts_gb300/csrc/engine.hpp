@@ -39,7 +39,7 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scratch owned by the context
-    DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, weights, misc, lsm_paths, lsm_value,
+    DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, weights, misc, vr, lsm_paths, lsm_value,
         lsm_stats, statics;
     DrawStore draws;
     kx_launch_stats last{};

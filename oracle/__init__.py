@@ -68,6 +68,7 @@ class Oracle:
         L.ko_simulate.argtypes = [P(_abi.KxModel), P(D), C.c_size_t, C.c_uint64, P(_abi.KxMcConfig), P(D)]
         L.ko_normals.argtypes = [C.c_uint64, C.c_uint64, C.c_size_t, P(D)]
         L.ko_price.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(_abi.KxPriceResult), P(D)]
+        L.ko_price_vr.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), C.c_int, P(_abi.KxPriceResult)]
         L.ko_price_on_grid.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                        P(_abi.KxPriceResult)]
         L.ko_price_batch.argtypes = [C.c_size_t, P(C.c_char_p), P(_abi.KxModel), P(_abi.KxMcConfig),
@@ -155,6 +156,16 @@ class Oracle:
         self._chk(self.L.ko_price(js.encode(), C.byref(cm), C.byref(cfg), C.byref(r),
                                   pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
         return (Result(r), pp[:n_paths]) if per_path else Result(r)
+
+    def price_vr(self, js: str, model, n_paths=100_000, seed=42, steps_per_year=50, antithetic=False,
+                 control_variate=False, rate=None, shared=False) -> Result:
+        """price_gbm with variance reduction (pricer.rs:108-230)."""
+        cm = _model_c(model)
+        cfg = self.cfg(n_paths, seed, steps_per_year, _rate(model, rate), shared)
+        r = _abi.KxPriceResult()
+        flags = (1 if antithetic else 0) | (2 if control_variate else 0)
+        self._chk(self.L.ko_price_vr(js.encode(), C.byref(cm), C.byref(cfg), flags, C.byref(r)))
+        return Result(r)
 
     def price_on_grid(self, js: str, model, grid, n_paths, seed, rate=None, shared=False) -> Result:
         cm = _model_c(model)

@@ -743,8 +743,11 @@ NormalSource make_source(const kx_mc_config &cfg) {
 // Value `n_paths` paths of `model` on `grid` with each contract in `cons`;
 // pvs[c][i]. Paths are materialised chunk by chunk (the reference keeps all of
 // them; values per path are the same).
+// negate: the antithetic paths (simulate_antithetic_gbm, variance_reduction.rs:76-129,
+// whose anti path steps with drift - diff_scale * z, i.e. the normals negated).
 void value_paths(const std::vector<const Con *> &cons, const Model &m, const std::vector<double> &grid,
-                 uint64_t n_paths, const NormalSource &ns, double rate, std::vector<std::vector<double>> &pvs) {
+                 uint64_t n_paths, const NormalSource &ns, double rate, std::vector<std::vector<double>> &pvs,
+                 bool negate = false) {
     validate_model(m);
     validate_grid(grid);
     pvs.assign(cons.size(), std::vector<double>(n_paths));
@@ -764,6 +767,8 @@ void value_paths(const std::vector<const Con *> &cons, const Model &m, const std
                 // simulate (materialise) the chunk
                 for (uint64_t i = (uint64_t)c0; i < c1; ++i) {
                     ns.fill(i, nd, z.data());
+                    if (negate)
+                        for (size_t q = 0; q < nd; ++q) z[q] = -z[q];
                     simulate_path(m, grid, z.data(), &rows[(i - c0) * grid.size()]);
                 }
                 // then value every path of the chunk
@@ -999,6 +1004,71 @@ int ko_price(const char *json, const kx_model *model, const kx_mc_config *cfg, k
         value_paths({c.get()}, m, grid, mc.n_paths, make_source(mc), mc.rate, pvs);
         *out = summarize(pvs[0]);
         if (per_path) memcpy(per_path, pvs[0].data(), pvs[0].size() * sizeof(double));
+    });
+}
+
+double ko_bs_call(double s, double k, double t, double r, double sigma);
+
+// price_gbm with variance reduction (pricer.rs:108-230, variance_reduction.rs:60-235).
+// flags: 1 antithetic, 2 control variate (the ATM call at the grid's last date).
+int ko_price_vr(const char *json, const kx_model *model, const kx_mc_config *cfg, int flags, kx_price_result *out) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        Model m = to_model(model);
+        kx_mc_config mc = check_cfg(cfg);
+        Plan p = compile(*c);
+        auto grid = time_grid_forced(p, mc.steps_per_year, m.requires_fine());
+        const bool gbm = m.kind == KX_MODEL_GBM;
+        const bool anti = (flags & 1) && gbm;  // Simulator::simulate_antithetic_paths: None unless GBM
+        const bool cv = (flags & 2) != 0;
+        const double s0 = gbm ? m.s0 : 100.0, sigma = gbm ? m.sigma : 0.2;  // gbm_params().unwrap_or
+        const double t_mat = grid.empty() ? 1.0 : grid.back();
+        ConP ctrl;
+        double bs = 0.0;
+        if (cv) {  // pricer.rs:160-167
+            char buf[512];
+            snprintf(buf, sizeof buf,
+                     "{\"When\":[{\"At\":%.17g},{\"Scale\":[{\"Max\":[{\"Sub\":[{\"Spot\":\"%s\"},{\"Const\":%.17g}]},"
+                     "{\"Const\":0.0}]},{\"One\":\"USD\"}]}]}",
+                     t_mat, m.asset.c_str(), s0);
+            ctrl = parse_contract(buf);
+            bs = ko_bs_call(s0, s0, t_mat, mc.rate, sigma);
+        }
+        const NormalSource ns = make_source(mc);
+        std::vector<const Con *> cons{c.get()};
+        if (cv) cons.push_back(ctrl.get());
+        if (anti) {
+            const uint64_t n_half = mc.n_paths / 2;
+            std::vector<std::vector<double>> b, a;
+            value_paths(cons, m, grid, n_half, ns, mc.rate, b);
+            value_paths(cons, m, grid, n_half, ns, mc.rate, a, true);
+            auto pairs = [&](size_t q) {  // price_antithetic_on_paths
+                std::vector<double> v(n_half);
+                for (uint64_t i = 0; i < n_half; ++i) v[i] = 0.5 * (b[q][i] + a[q][i]);
+                return summarize(v);
+            };
+            if (!cv) {
+                *out = pairs(0);
+                return;
+            }
+            const kx_price_result res = pairs(0), ctl = pairs(1);  // price_antithetic_with_cv
+            kx_price_result r{};
+            r.price = res.price - 1.0 * (ctl.price - bs);
+            const uint64_t n = 2 * n_half;
+            r.sample_std = res.sample_std;
+            r.std_error = res.sample_std / std::sqrt((double)n);
+            r.ci95_low = r.price - 1.959963984540054 * r.std_error;
+            r.ci95_high = r.price + 1.959963984540054 * r.std_error;
+            r.n_paths = n;
+            *out = r;
+            return;
+        }
+        std::vector<std::vector<double>> pvs;
+        value_paths(cons, m, grid, mc.n_paths, ns, mc.rate, pvs);
+        if (cv) {  // price_control_variate_on_paths with beta = 1
+            for (uint64_t i = 0; i < mc.n_paths; ++i) pvs[0][i] = pvs[0][i] - 1.0 * (pvs[1][i] - bs);
+        }
+        *out = summarize(pvs[0]);
     });
 }
 
