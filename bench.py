@@ -266,6 +266,33 @@ def european_fp64(reps=5) -> dict:
             "black_scholes": bs, "error_in_se": (r.price - bs) / r.std_error}
 
 
+def variance_reduction(reps=3) -> dict:
+    """The benchmark's up-and-out call (4,000,000 paths, daily grid, FP32)
+    priced plain and with the reference's variance reduction (antithetic
+    pairs, the at-the-money call as a control, both): device time, standard
+    error, and the gain at equal standard error over plain pricing
+    (time x SE^2, plain / mode)."""
+    import kontracts_gb300 as kx
+    c = kx.up_and_out_call("S", 100.0, 200.0, 1.0)
+    m = kx.GBM(s0=180.0, sigma=0.25, r=0.05, asset="S")
+    out = {"workload": "up-and-out call, s0 180, K 100, B 200, sigma 0.25, r 0.05, T 1, 365 steps/yr, 4M paths, FP32"}
+    base = None
+    for name, anti, cv in (("plain", False, False), ("antithetic", True, False), ("control_variate", False, True),
+                           ("antithetic_control_variate", True, True)):
+        best = None
+        for _ in range(reps):
+            r = c.price(m, n_paths=4_000_000, seed=42, steps_per_year=365, antithetic=anti, control_variate=cv)
+            t = _dev_seconds(kx)
+            best = t if best is None or t < best else best
+        row = {"seconds": best, "price": r.price, "std_error": r.std_error, "n_paths": r.n_paths}
+        if base is None:
+            base = (best, r.std_error)
+        else:
+            row["equal_se_gain"] = (base[0] * base[1] ** 2) / (best * r.std_error ** 2)
+        out[name] = row
+    return out
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -497,7 +524,8 @@ def run_ours(args, ws, rank, local) -> None:
         line["price_greeks"] = greeks
     if rank == 0 and not args.no_extra:
         line["other_configs"] = {"european_fp64": european_fp64(), "heston_book_96": heston_book(),
-                                 "book_256": book_256(), "lsm_12": lsm_cases()}
+                                 "book_256": book_256(), "lsm_12": lsm_cases(),
+                                 "variance_reduction": variance_reduction()}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.cpu_seconds)
         line["accuracy"] = accuracy(cb)
