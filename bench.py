@@ -293,6 +293,56 @@ def variance_reduction(reps=3) -> dict:
     return out
 
 
+def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
+    """A trader's spot x vol surface (greek_surface, surface.rs:104-137):
+    11 spots (80..120) x 9 vols (0.10..0.42) of an up-and-out call (K 100,
+    B 130, T 1) on a daily grid (252 steps a year), 100,000 paths per cell,
+    FP32 paths, default bumps (1e-2, 1e-2, 1e-4), seed 42. Each cell is seven
+    CRN reprices; the 99 cells x 7 scenarios run as one path launch. The
+    oracle (the reference's cell loop restated, all host threads) prices a
+    bounded sample of the same cells for the CPU rate."""
+    import kontracts_gb300 as kx
+    from oracle import Oracle
+    c = kx.up_and_out_call("S", 100.0, 130.0, 1.0)
+    spots = [80.0 + 4.0 * i for i in range(11)]
+    vols = [0.10 + 0.04 * j for j in range(9)]
+    n, spy = 100_000, 252
+    steps = len(c.time_grid(spy)) - 1
+    best, launches = None, 0
+    for _ in range(reps):
+        s = kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05)
+        t = _dev_seconds(kx)
+        launches = kx.last_launch_stats()["kernel_launches"]
+        best = t if best is None or t < best else best
+    t0 = time.perf_counter()
+    kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05)
+    wall = time.perf_counter() - t0
+    cells = len(spots) * len(vols)
+    scen_steps = cells * 7 * n * steps
+    # CPU: the oracle on a sample of cells and paths, scaled to cells/s at n paths
+    orc = Oracle()
+    pn = 20_000
+    t0 = time.perf_counter()
+    orc.greek_surface(c.to_json(), "S", spots[5:6], vols[3:4], n_paths=pn, seed=42, steps_per_year=spy, rate=0.05)
+    dt = time.perf_counter() - t0
+    k = max(1, min(cells, int(cpu_seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    orc.greek_surface(c.to_json(), "S", spots[:1], vols[:k] if k <= len(vols) else vols, n_paths=pn, seed=42,
+                      steps_per_year=spy, rate=0.05)
+    cdt = time.perf_counter() - t0
+    kc = min(k, len(vols))
+    cpu_cells_per_s = kc * pn / n / cdt
+    return {"workload": "greek surface, 11 spots x 9 vols, up-and-out call K 100 B 130 T 1, 252 steps/yr, "
+                        "100k paths per cell, FP32, default bumps", "cells": cells,
+            "seconds": best, "wall_seconds_e2e": wall, "gpu_launches": launches,
+            "cells_per_s": cells / best, "scenario_path_steps_per_s": scen_steps / best,
+            "delta_atm_0.26": float(s.delta[5, 4]), "gamma_atm_0.26": float(s.gamma[5, 4]),
+            "vega_atm_0.26": float(s.vega[5, 4]),
+            "cpu_baseline": {"cells_per_s": cpu_cells_per_s, "cores": orc.threads(), "kind": "port",
+                             "sample": f"{kc} cells x {pn} paths x {steps} steps x 7 reprices, {cdt:.2f} s"},
+            "gpu_over_cpu_cells_per_s": cells / best / cpu_cells_per_s}
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -525,7 +575,8 @@ def run_ours(args, ws, rank, local) -> None:
     if rank == 0 and not args.no_extra:
         line["other_configs"] = {"european_fp64": european_fp64(), "heston_book_96": heston_book(),
                                  "book_256": book_256(), "lsm_12": lsm_cases(),
-                                 "variance_reduction": variance_reduction()}
+                                 "variance_reduction": variance_reduction(),
+                                 "greek_surface_99": greek_surface_grid()}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.cpu_seconds)
         line["accuracy"] = accuracy(cb)

@@ -274,13 +274,28 @@ kx_status kx_price_portfolio(size_t n, const kx_program *const *progs,
                              const kx_model *models, const kx_mc_config *cfgs,
                              kx_price_result *out, kx_sens *sens);
 
-/* greeks_gbm (src/greeks.rs:60-98): CRN bump-and-reprice. All bumped
- * scenarios reuse each path's normals inside one launch. GBM only (model->kind
- * must be KX_MODEL_GBM); drift = rate, as the reference rebuilds the model
- * with Gbm::new(asset, s0, rate, sigma) (greeks.rs:70). */
+/* greeks_gbm (src/greeks.rs:60-98): CRN bump-and-reprice. The seven
+ * reprices are plain jobs of one path launch, each priced as kx_price prices
+ * the bumped model (the lean kernels), all on the seed's normals; the
+ * estimators are means of per-path central differences. With bumps->smooth
+ * one job carries the seven scenarios of the barrier-smoothed payoff. GBM
+ * only (model->kind must be KX_MODEL_GBM); drift = rate, as the reference
+ * rebuilds the model with Gbm::new(asset, s0, rate, sigma) (greeks.rs:70). */
 kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model,
                          const kx_mc_config *cfg, const kx_bumps *bumps,
                          kx_greeks *out);
+
+/* greek_surface (src/surface.rs:104-137): greeks_gbm at every cell of the
+ * grid spots x vols, out[i * n_vols + j] for spots[i], vols[j] (row-major as
+ * GreekSurface, surface.rs:17-35; rho and the standard errors come along).
+ * Every cell reprices with the same seed, so all cells and their seven bump
+ * reprices value the same normals: the 7 x n_spots x n_vols reprices run as
+ * the plain jobs of one path launch (several when the per-path values would
+ * exceed 8 GiB), each cell bitwise equal to kx_greeks_bump at that cell. An
+ * empty grid is KX_INCONSISTENT_PATH (surface.rs:113-117). */
+kx_status kx_greek_surface(const kx_program *prog, const char *asset, const double *spots, size_t n_spots,
+                           const double *vols, size_t n_vols, const kx_mc_config *cfg, const kx_bumps *bumps,
+                           kx_greeks *out);
 
 /* Pathwise adjoint: one reverse sweep per path recomputing the path from its
  * Philox counters with a checkpoint every `checkpoint_every` steps; the

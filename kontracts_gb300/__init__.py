@@ -502,6 +502,102 @@ def price_american_batch(cases: Sequence[tuple], n_basis: int = 3, *, precision:
     return [PriceResult(r) for r in out]
 
 
+def _fmt_display(x: float) -> str:
+    """Rust's `{}` of an f64: the shortest round-trip digits in plain decimal
+    notation (no exponent), no fractional part for integral values, and NaN /
+    inf / -inf for the non-finite ones."""
+    x = float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "inf" if x > 0 else "-inf"
+    import decimal
+    t = format(decimal.Decimal(repr(x)), "f")
+    if "." in t:
+        t = t.rstrip("0").rstrip(".")
+    return t
+
+
+def _rust_round(x: float) -> int:
+    """f64::round (half away from zero) followed by `as i32` (NaN -> 0,
+    saturating)."""
+    if math.isnan(x):
+        return 0
+    if math.isinf(x):
+        return 2**31 - 1 if x > 0 else -(2**31)
+    a = abs(x)
+    r = math.floor(a)
+    if a - r >= 0.5:
+        r += 1
+    r = int(r) if x >= 0 else -int(r)
+    return max(-(2**31), min(2**31 - 1, r))
+
+
+class GreekSurface:
+    """Mirror of GreekSurface (src/surface.rs:17-35): the axes `spots` and
+    `vols` and the matrices price, delta, gamma, vega of shape
+    [len(spots), len(vols)] (row i = spots[i], column j = vols[j]), plus rho
+    and each estimator's standard error (`<name>_se`), as numpy arrays."""
+
+    QUANTITIES = ("price", "delta", "gamma", "vega", "rho",
+                  "price_se", "delta_se", "gamma_se", "vega_se", "rho_se")
+
+    def __init__(self, spots: Sequence[float], vols: Sequence[float], cells: Sequence[Any]):
+        import numpy as np
+        self.spots = [float(s) for s in spots]
+        self.vols = [float(v) for v in vols]
+        shape = (len(self.spots), len(self.vols))
+        for q in self.QUANTITIES:
+            setattr(self, q, np.array([getattr(g, q) for g in cells], dtype=np.float64).reshape(shape))
+
+    def to_csv(self, quantity) -> str:
+        """surface.rs:38-62: header `spot\\vol,<vols>`, then one row per spot."""
+        head = "spot\\vol" + "".join("," + _fmt_display(v) for v in self.vols) + "\n"
+        rows = "".join(_fmt_display(s) + "".join("," + _fmt_display(quantity[i][j]) for j in range(len(self.vols)))
+                       + "\n" for i, s in enumerate(self.spots))
+        return head + rows
+
+    def to_pgm(self, quantity) -> str:
+        """surface.rs:64-97: P2 (ASCII) grayscale, min -> 0 and max -> 255."""
+        rows, cols = len(quantity), (len(quantity[0]) if len(quantity) else 0)
+        lo, hi = math.inf, -math.inf
+        for i in range(rows):
+            for j in range(cols):
+                x = float(quantity[i][j])
+                if not math.isnan(x):  # f64::min / f64::max ignore NaN
+                    lo, hi = min(lo, x), max(hi, x)
+        span = 1.0 if abs(hi - lo) < 1e-300 else hi - lo
+        out = [f"P2\n{cols} {rows}\n255\n"]
+        for i in range(rows):
+            out.append("".join(f"{max(0, min(255, _rust_round((float(quantity[i][j]) - lo) / span * 255.0)))} "
+                               for j in range(cols)) + "\n")
+        return "".join(out)
+
+    def __repr__(self):
+        return f"GreekSurface({len(self.spots)} spots x {len(self.vols)} vols)"
+
+
+def greek_surface(contract: Contract, asset: str, spots: Sequence[float], vols: Sequence[float],
+                  n_paths: int = 100_000, seed: int = 42, steps_per_year: int = 50, rate: float = 0.0, *,
+                  bumps: tuple | None = None, relative: bool = False, precision: str = "fp32") -> GreekSurface:
+    """greek_surface (src/surface.rs:104-137): bump-and-reprice Greeks
+    (greeks_gbm) at every cell of spots x vols, all cells on the same seed.
+    The arguments after `vols` are McConfig's fields (default McConfig,
+    pricer.rs:44-54) and BumpSizes (default (1e-2, 1e-2, 1e-4)). One path
+    launch values every cell and its seven scenarios."""
+    hs, hv, hr = bumps if bumps is not None else (1e-2, 1e-2, 1e-4)
+    b = _abi.KxBumps(spot=hs, vol=hv, rate=hr, relative=int(relative), smooth=0, smoothing_width=0.0)
+    cfg = _cfg(n_paths, seed, steps_per_year, rate, precision, False)
+    ns, nv = len(spots), len(vols)
+    sp = (C.c_double * max(1, ns))(*[float(x) for x in spots])
+    vo = (C.c_double * max(1, nv))(*[float(x) for x in vols])
+    out = (_abi.KxGreeks * max(1, ns * nv))()
+    with _lock:
+        _check(_lib().kx_greek_surface(contract._handle().h, asset.encode(), sp, ns, vo, nv, C.byref(cfg),
+                                       C.byref(b), out))
+    return GreekSurface(spots, vols, [Greeks(g) for g in out[: ns * nv]])
+
+
 def price_batch(contracts: Sequence[Contract], model, n_paths: int = 100_000, seed: int = 42,
                 steps_per_year: int = 50, *, precision: str = "fp32") -> list[PriceResult]:
     """price_batch_gbm (src/pricer.rs:250-294): every contract on the same paths."""
@@ -700,6 +796,6 @@ __all__ = [
     "until", "and_", "or_", "USD", "EUR", "GBP", "JPY", "average", "average_over", "running_max",
     "running_min", "heston", "zero_coupon_bond", "european_call", "european_put", "forward", "straddle",
     "bull_call_spread", "cash_or_nothing_call", "up_and_out_call", "down_and_out_call", "price_batch",
-    "price_american_batch",
+    "price_american_batch", "GreekSurface", "greek_surface",
     "price_portfolio", "set_shared_draws", "last_launch_stats",
 ]

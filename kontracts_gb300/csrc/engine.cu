@@ -15,6 +15,7 @@
 // lane idle. Path-to-lane assignment depends only on the data, and per-path
 // values are written to fixed slots, so results do not depend on timing.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -1221,6 +1222,78 @@ kx_status kx_price_portfolio(size_t n, const kx_program *const *progs, const kx_
     });
 }
 
+}  // extern "C"
+
+// The seven CRN scenarios of greeks_gbm (greeks.rs:65-97) at spot s0 and
+// volatility sigma: base, spot up / down, vol up / down, rate up / down, all
+// with drift = rate as Gbm::new(asset, s0, rate, sigma) (greeks.rs:70). The
+// bump sizes (relative ones scaled by the bumped parameter) land in h[3].
+static std::vector<Scenario> bump_scenarios(double s0, double sigma, double r, const kx_bumps &b, double h[3]) {
+    const double hs = b.relative ? b.spot * s0 : b.spot;
+    const double hv = b.relative ? b.vol * sigma : b.vol;
+    const double hr = b.relative ? b.rate * r : b.rate;
+    if (!(hs > 0) || !(hv > 0) || !(hr > 0)) raise(KX_INVALID_ARGUMENT, "bump sizes must be positive");
+    if (sigma - hv < 0) raise(KX_MALFORMED_CONTRACT, "GBM sigma must be non-negative (vol bump too large)");
+    h[0] = hs;
+    h[1] = hv;
+    h[2] = hr;
+    return {{s0, r, sigma, r},      {s0 + hs, r, sigma, r}, {s0 - hs, r, sigma, r},    {s0, r, sigma + hv, r},
+            {s0, r, sigma - hv, r}, {s0, r + hr, sigma, r + hr}, {s0, r - hr, sigma, r - hr}};
+}
+
+// Statistics of the five estimators of one bumped job whose seven scenario
+// values per path start at `begin`: price, then delta, gamma, vega and rho as
+// per-path central differences (greeks.rs:85-89), in the order of kx_greeks.
+static void greek_stats(uint64_t begin, uint64_t n, const double h[3], StatsJob out[5]) {
+    const double hs = h[0], hv = h[1], hr = h[2];
+    for (int q = 0; q < 5; ++q) {
+        out[q] = StatsJob{};
+        out[q].begin = begin;
+        out[q].n = n;
+        out[q].ns = KX_MAX_NS;
+        std::fill(out[q].w, out[q].w + 8, 0.0);
+    }
+    out[0].w[0] = 1.0;                                                                        // price
+    out[1].w[1] = 1.0 / (2 * hs); out[1].w[2] = -1.0 / (2 * hs);                              // delta
+    out[2].w[1] = 1.0 / (hs * hs); out[2].w[0] = -2.0 / (hs * hs); out[2].w[2] = 1.0 / (hs * hs);  // gamma
+    out[3].w[3] = 1.0 / (2 * hv); out[3].w[4] = -1.0 / (2 * hv);                              // vega
+    out[4].w[5] = 1.0 / (2 * hr); out[4].w[6] = -1.0 / (2 * hr);                              // rho
+}
+
+// The seven reprices of greeks_gbm as plain single-scenario jobs, appended in
+// scenario order: each prices Gbm::new(asset, s0, rate, sigma) under McConfig
+// {rate, ..cfg} (greeks.rs:69-76) like kx_price, on the same seed and
+// therefore the same normals. The lean kernels value each job at the speed
+// of a plain price; the seven values of a path sit n_paths apart.
+static void append_reprices(std::vector<Job> &jobs, const Program &p, const Model &base, const kx_mc_config &cfg,
+                            const std::vector<double> &grid, const std::vector<Scenario> &sc) {
+    for (const Scenario &s : sc) {
+        Model m = base;
+        m.s0 = s.s0;
+        m.mu = s.mu;
+        m.sigma = s.sigma;
+        kx_mc_config c2 = cfg;
+        c2.rate = s.rate;
+        jobs.push_back(make_job(p, m, c2, grid, {}, 0, 0.0));
+    }
+}
+
+static void fill_greeks(const Stats *st5, kx_greeks *out) {
+    const kx_price_result r0 = finish(st5[0]), r1 = finish(st5[1]), r2 = finish(st5[2]), r3 = finish(st5[3]),
+                          r4 = finish(st5[4]);
+    out->price = r0.price; out->price_se = r0.std_error;
+    out->delta = r1.price; out->delta_se = r1.std_error;
+    out->gamma = r2.price; out->gamma_se = r2.std_error;
+    out->vega = r3.price; out->vega_se = r3.std_error;
+    out->rho = r4.price; out->rho_se = r4.std_error;
+}
+
+// Upper bound of the per-path values one surface launch keeps in HBM (seven
+// doubles per path and cell); larger surfaces run as several launches.
+static constexpr uint64_t SURFACE_PV_BYTES = 8ull << 30;
+
+extern "C" {
+
 kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
                          const kx_bumps *bumps, kx_greeks *out) {
     return guarded([&] {
@@ -1230,17 +1303,10 @@ kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model, const kx
         if (!out) raise(KX_INVALID_ARGUMENT, "out is NULL");
         if (m.kind != KX_MODEL_GBM) raise(KX_UNSUPPORTED, "bump-and-reprice Greeks need a GBM model (greeks.rs:60)");
         validate_model(m);
-        kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
+        const kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
         const double r = cfg->rate;
-        const double hs = b.relative ? b.spot * m.s0 : b.spot;
-        const double hv = b.relative ? b.vol * m.sigma : b.vol;
-        const double hr = b.relative ? b.rate * r : b.rate;
-        if (!(hs > 0) || !(hv > 0) || !(hr > 0)) raise(KX_INVALID_ARGUMENT, "bump sizes must be positive");
-        // greeks.rs:65-97: drift = rate, seven reprices sharing the normals
-        std::vector<Scenario> sc = {{m.s0, r, m.sigma, r},      {m.s0 + hs, r, m.sigma, r}, {m.s0 - hs, r, m.sigma, r},
-                                    {m.s0, r, m.sigma + hv, r}, {m.s0, r, m.sigma - hv, r}, {m.s0, r + hr, m.sigma, r + hr},
-                                    {m.s0, r - hr, m.sigma, r - hr}};
-        if (m.sigma - hv < 0) raise(KX_MALFORMED_CONTRACT, "GBM sigma must be non-negative (vol bump too large)");
+        double h[3];
+        std::vector<Scenario> sc = bump_scenarios(m.s0, m.sigma, r, b, h);
         auto grid = time_grid_forced(p.plan, cfg->steps_per_year, false);
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
@@ -1248,29 +1314,80 @@ kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model, const kx
         Model mb = m;
         mb.mu = r;
         std::vector<Job> jobs;
-        double w = b.smoothing_width;
-        jobs.push_back(make_job(p, mb, *cfg, grid, sc, b.smooth ? 1 : 0, w > 0 ? w : 1.0));
-        uint64_t stride = 0;
-        run_paths(c, jobs, *cfg, KX_MAX_NS, stride);
         std::vector<StatsJob> sj(5);
-        for (auto &j : sj) {
-            j.begin = 0;
-            j.n = cfg->n_paths;
-            j.ns = KX_MAX_NS;
-            std::fill(j.w, j.w + 8, 0.0);
+        uint64_t stride = 0;
+        if (b.smooth) {  // the smoothed payoff: one job whose seven scenarios share each path's draws
+            const double w = b.smoothing_width;
+            jobs.push_back(make_job(p, mb, *cfg, grid, sc, 1, w > 0 ? w : 1.0));
+            run_paths(c, jobs, *cfg, KX_MAX_NS, stride);
+        } else {
+            append_reprices(jobs, p, mb, *cfg, grid, sc);
+            run_paths(c, jobs, *cfg, 1, stride);
+            stride = cfg->n_paths;
         }
-        sj[0].w[0] = 1.0;                                                           // price
-        sj[1].w[1] = 1.0 / (2 * hs); sj[1].w[2] = -1.0 / (2 * hs);                 // delta
-        sj[2].w[1] = 1.0 / (hs * hs); sj[2].w[0] = -2.0 / (hs * hs); sj[2].w[2] = 1.0 / (hs * hs);  // gamma
-        sj[3].w[3] = 1.0 / (2 * hv); sj[3].w[4] = -1.0 / (2 * hv);                 // vega
-        sj[4].w[5] = 1.0 / (2 * hr); sj[4].w[6] = -1.0 / (2 * hr);                 // rho
+        greek_stats(0, cfg->n_paths, h, sj.data());
         auto st = device_stats(c, c.pv.as<double>(), stride, sj);
-        kx_price_result r0 = finish(st[0]), r1 = finish(st[1]), r2 = finish(st[2]), r3 = finish(st[3]), r4 = finish(st[4]);
-        out->price = r0.price; out->price_se = r0.std_error;
-        out->delta = r1.price; out->delta_se = r1.std_error;
-        out->gamma = r2.price; out->gamma_se = r2.std_error;
-        out->vega = r3.price; out->vega_se = r3.std_error;
-        out->rho = r4.price; out->rho_se = r4.std_error;
+        fill_greeks(st.data(), out);
+        end_call(c);
+    });
+}
+
+kx_status kx_greek_surface(const kx_program *prog, const char *asset, const double *spots, size_t n_spots,
+                           const double *vols, size_t n_vols, const kx_mc_config *cfg, const kx_bumps *bumps,
+                           kx_greeks *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        check_cfg(cfg);
+        if (n_spots == 0 || n_vols == 0) raise(KX_INCONSISTENT_PATH, "empty surface grid");  // surface.rs:113-117
+        if (!spots || !vols || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        const kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
+        const double r = cfg->rate;
+        const size_t n_cells = n_spots * n_vols;
+        // cell (i, j) = spots[i] x vols[j], row-major (surface.rs:120-124); every
+        // cell is greeks_gbm on the same seed, so all cells share each path's normals
+        std::vector<std::vector<Scenario>> sc(n_cells);
+        std::vector<std::array<double, 3>> h(n_cells);
+        for (size_t q = 0; q < n_cells; ++q) {
+            Model m{};
+            m.kind = KX_MODEL_GBM;
+            m.s0 = spots[q / n_vols];
+            m.mu = r;
+            m.sigma = vols[q % n_vols];
+            validate_model(m);
+            sc[q] = bump_scenarios(m.s0, m.sigma, r, b, h[q].data());
+        }
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, false);
+        kx_model cm{};
+        cm.kind = KX_MODEL_GBM;
+        cm.s0 = spots[0];
+        cm.mu = r;
+        cm.sigma = vols[0];
+        cm.asset = asset;
+        const Model base = model_from_c(&cm);
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        const uint64_t per_cell = std::max<uint64_t>(1, cfg->n_paths) * KX_MAX_NS * sizeof(double);
+        const size_t cells_per_launch = (size_t)std::max<uint64_t>(1, SURFACE_PV_BYTES / per_cell);
+        for (size_t c0 = 0; c0 < n_cells; c0 += cells_per_launch) {
+            const size_t c1 = std::min(n_cells, c0 + cells_per_launch);
+            std::vector<Job> jobs;
+            for (size_t q = c0; q < c1; ++q) append_reprices(jobs, p, base, *cfg, grid, sc[q]);
+            uint64_t stride = 0;
+            run_paths(c, jobs, *cfg, 1, stride);
+            // estimator-major, so that cells with equal bump sizes share a statistics launch
+            const size_t nj = c1 - c0;
+            std::vector<StatsJob> tmp(5), sj(5 * nj);
+            for (size_t q = 0; q < nj; ++q) {
+                greek_stats(jobs[KX_MAX_NS * q].dev.pv_off, cfg->n_paths, h[c0 + q].data(), tmp.data());
+                for (int e = 0; e < 5; ++e) sj[e * nj + q] = tmp[e];
+            }
+            auto st = device_stats(c, c.pv.as<double>(), cfg->n_paths, sj);
+            for (size_t q = 0; q < nj; ++q) {
+                const Stats st5[5] = {st[q], st[nj + q], st[2 * nj + q], st[3 * nj + q], st[4 * nj + q]};
+                fill_greeks(st5, &out[c0 + q]);
+            }
+        }
         end_call(c);
     });
 }

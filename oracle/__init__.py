@@ -75,6 +75,8 @@ class Oracle:
                                      P(_abi.KxPriceResult)]
         L.ko_greeks.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(_abi.KxBumps),
                                 P(_abi.KxGreeks)]
+        L.ko_greek_surface.argtypes = [C.c_char_p, C.c_char_p, P(D), C.c_size_t, P(D), C.c_size_t,
+                                       P(_abi.KxMcConfig), P(_abi.KxBumps), P(_abi.KxGreeks)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
         L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
@@ -193,6 +195,20 @@ class Oracle:
         g = _abi.KxGreeks()
         self._chk(self.L.ko_greeks(js.encode(), C.byref(cm), C.byref(cfg), C.byref(b), C.byref(g)))
         return {k: getattr(g, k) for k, _ in g._fields_}
+
+    def greek_surface(self, js: str, asset: str, spots, vols, n_paths=100_000, seed=42, steps_per_year=50,
+                      rate=0.0, bumps=(1e-2, 1e-2, 1e-4), relative=False) -> list:
+        """greek_surface (surface.rs:104-137): a row-major list of greeks dicts,
+        cell i * len(vols) + j for spots[i], vols[j]."""
+        sp = (C.c_double * max(1, len(spots)))(*spots)
+        vo = (C.c_double * max(1, len(vols)))(*vols)
+        cfg = self.cfg(n_paths, seed, steps_per_year, rate)
+        b = _abi.KxBumps(spot=bumps[0], vol=bumps[1], rate=bumps[2], relative=int(relative), smooth=0,
+                         smoothing_width=0.0)
+        out = (_abi.KxGreeks * max(1, len(spots) * len(vols)))()
+        self._chk(self.L.ko_greek_surface(js.encode(), asset.encode(), sp, len(spots), vo, len(vols), C.byref(cfg),
+                                          C.byref(b), out))
+        return [{k: getattr(g, k) for k, _ in g._fields_} for g in out[: len(spots) * len(vols)]]
 
     def price_american(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
                        per_path=False, basis="monomial"):

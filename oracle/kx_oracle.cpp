@@ -1114,6 +1114,51 @@ int ko_price_batch(size_t n, const char *const *jsons, const kx_model *model, co
 
 // greeks_gbm (greeks.rs:60-98): 7 reprices with the same normals. Bumps are
 // absolute, or relative to the bumped value when bumps->relative != 0.
+// greeks_gbm (greeks.rs:60-98) of contract c at spot s0 and volatility sigma:
+// seven reprices on the same normals, price / delta / gamma from the spot
+// reprices, vega and rho from the vol and rate ones, each a difference of
+// means; the standard errors are those of the per-path differences.
+static void greeks_at(const ConP &c, const Model &base, const kx_mc_config &mc, const kx_bumps &b, double s0,
+                      double sigma, kx_greeks *out) {
+    double r = mc.rate;
+    double hs = b.relative ? b.spot * s0 : b.spot;
+    double hv = b.relative ? b.vol * sigma : b.vol;
+    double hr = b.relative ? b.rate * r : b.rate;
+    Plan p = compile(*c);
+    auto grid = time_grid_forced(p, mc.steps_per_year, false);
+    NormalSource ns = make_source(mc);
+    auto reprice = [&](double s, double sg, double rate, std::vector<double> &pv) {
+        Model m = base;
+        m.s0 = s; m.mu = rate; m.sigma = sg;  // Gbm::new(asset, s0, rate, sigma), greeks.rs:70
+        std::vector<std::vector<double>> pvs;
+        value_paths({c.get()}, m, grid, mc.n_paths, ns, rate, pvs);
+        pv = std::move(pvs[0]);
+    };
+    std::vector<double> p0, psu, psd, pvu, pvd, pru, prd;
+    reprice(s0, sigma, r, p0);
+    reprice(s0 + hs, sigma, r, psu);
+    reprice(s0 - hs, sigma, r, psd);
+    reprice(s0, sigma + hv, r, pvu);
+    reprice(s0, sigma - hv, r, pvd);
+    reprice(s0, sigma, r + hr, pru);
+    reprice(s0, sigma, r - hr, prd);
+    auto mean = [](const std::vector<double> &v) { return summarize(v).price; };
+    double price = mean(p0), su = mean(psu), sd = mean(psd);
+    out->price = price;
+    out->delta = (su - sd) / (2.0 * hs);
+    out->gamma = (su - 2.0 * price + sd) / (hs * hs);
+    out->vega = (mean(pvu) - mean(pvd)) / (2.0 * hv);
+    out->rho = (mean(pru) - mean(prd)) / (2.0 * hr);
+    size_t n = p0.size();
+    std::vector<double> e(n);
+    auto se_of = [&](auto f) { for (size_t i = 0; i < n; ++i) e[i] = f(i); return summarize(e).std_error; };
+    out->price_se = summarize(p0).std_error;
+    out->delta_se = se_of([&](size_t i) { return (psu[i] - psd[i]) / (2.0 * hs); });
+    out->gamma_se = se_of([&](size_t i) { return (psu[i] - 2.0 * p0[i] + psd[i]) / (hs * hs); });
+    out->vega_se = se_of([&](size_t i) { return (pvu[i] - pvd[i]) / (2.0 * hv); });
+    out->rho_se = se_of([&](size_t i) { return (pru[i] - prd[i]) / (2.0 * hr); });
+}
+
 int ko_greeks(const char *json, const kx_model *model, const kx_mc_config *cfg, const kx_bumps *bumps,
               kx_greeks *out) {
     return run([&] {
@@ -1122,48 +1167,31 @@ int ko_greeks(const char *json, const kx_model *model, const kx_mc_config *cfg, 
         if (base.kind != KX_MODEL_GBM) fail(KX_UNSUPPORTED, "greeks need a GBM model");
         kx_mc_config mc = check_cfg(cfg);
         kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
-        double r = mc.rate;
-        double hs = b.relative ? b.spot * base.s0 : b.spot;
-        double hv = b.relative ? b.vol * base.sigma : b.vol;
-        double hr = b.relative ? b.rate * r : b.rate;
-        Plan p = compile(*c);
-        auto grid = time_grid_forced(p, mc.steps_per_year, false);
-        NormalSource ns = make_source(mc);
-        auto reprice = [&](double s0, double sigma, double rate, std::vector<double> &pv) {
-            Model m = base;
-            m.s0 = s0; m.mu = rate; m.sigma = sigma;  // Gbm::new(asset, s0, rate, sigma), greeks.rs:70
-            std::vector<std::vector<double>> pvs;
-            value_paths({c.get()}, m, grid, mc.n_paths, ns, rate, pvs);
-            pv = std::move(pvs[0]);
-        };
-        std::vector<double> p0, psu, psd, pvu, pvd, pru, prd;
-        reprice(base.s0, base.sigma, r, p0);
-        reprice(base.s0 + hs, base.sigma, r, psu);
-        reprice(base.s0 - hs, base.sigma, r, psd);
-        reprice(base.s0, base.sigma + hv, r, pvu);
-        reprice(base.s0, base.sigma - hv, r, pvd);
-        reprice(base.s0, base.sigma, r + hr, pru);
-        reprice(base.s0, base.sigma, r - hr, prd);
-        auto mean = [](const std::vector<double> &v) { return summarize(v).price; };
-        double price = mean(p0), su = mean(psu), sd = mean(psd);
-        out->price = price;
-        out->delta = (su - sd) / (2.0 * hs);
-        out->gamma = (su - 2.0 * price + sd) / (hs * hs);
-        out->vega = (mean(pvu) - mean(pvd)) / (2.0 * hv);
-        out->rho = (mean(pru) - mean(prd)) / (2.0 * hr);
-        size_t n = p0.size();
-        std::vector<double> e(n);
-        auto se_of = [&](auto f) { for (size_t i = 0; i < n; ++i) e[i] = f(i); return summarize(e).std_error; };
-        out->price_se = summarize(p0).std_error;
-        out->delta_se = se_of([&](size_t i) { return (psu[i] - psd[i]) / (2.0 * hs); });
-        out->gamma_se = se_of([&](size_t i) { return (psu[i] - 2.0 * p0[i] + psd[i]) / (hs * hs); });
-        out->vega_se = se_of([&](size_t i) { return (pvu[i] - pvd[i]) / (2.0 * hv); });
-        out->rho_se = se_of([&](size_t i) { return (pru[i] - prd[i]) / (2.0 * hr); });
+        greeks_at(c, base, mc, b, base.s0, base.sigma, out);
     });
 }
 
-// price_american_lsm (lsm.rs:80-229). per_path (nullable) gets the value of
-// every path discounted to t = 0.
+// greek_surface (surface.rs:104-137): greeks_gbm at every (spots[i], vols[j]),
+// out[i * n_vols + j]; an empty grid is InconsistentPath (surface.rs:113-117).
+int ko_greek_surface(const char *json, const char *asset, const double *spots, size_t n_spots, const double *vols,
+                     size_t n_vols, const kx_mc_config *cfg, const kx_bumps *bumps, kx_greeks *out) {
+    return run([&] {
+        if (n_spots == 0 || n_vols == 0) fail(KX_INCONSISTENT_PATH, "empty surface grid");
+        ConP c = parse_contract(json);
+        kx_mc_config mc = check_cfg(cfg);
+        kx_bumps b = bumps ? *bumps : kx_bumps{1e-2, 1e-2, 1e-4, 0, 0, 0.0};
+        kx_model cm{};
+        cm.kind = KX_MODEL_GBM;
+        cm.s0 = spots[0];
+        cm.mu = mc.rate;
+        cm.sigma = vols[0];
+        cm.asset = asset;
+        Model base = to_model(&cm);
+        for (size_t i = 0; i < n_spots; ++i)
+            for (size_t j = 0; j < n_vols; ++j) greeks_at(c, base, mc, b, spots[i], vols[j], &out[i * n_vols + j]);
+    });
+}
+
 int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
                             size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
     return run([&] {
