@@ -298,9 +298,12 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
     11 spots (80..120) x 9 vols (0.10..0.42) of an up-and-out call (K 100,
     B 130, T 1) on a daily grid (252 steps a year), 100,000 paths per cell,
     FP32 paths, default bumps (1e-2, 1e-2, 1e-4), seed 42. Each cell is seven
-    CRN reprices; the 99 cells x 7 scenarios run as one path launch. The
+    CRN reprices; the 99 cells x 7 reprices run as one path launch. The
     oracle (the reference's cell loop restated, all host threads) prices a
-    bounded sample of the same cells for the CPU rate."""
+    bounded sample of the same cells for the CPU rate. `adjoint`: the same
+    grid by one pathwise-adjoint portfolio launch (no gamma), at equal
+    standard error against the bump surface (median over cells of
+    (SE_bump / SE_adjoint)^2, the worse of delta and vega)."""
     import kontracts_gb300 as kx
     from oracle import Oracle
     c = kx.up_and_out_call("S", 100.0, 130.0, 1.0)
@@ -317,6 +320,15 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
     t0 = time.perf_counter()
     kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05)
     wall = time.perf_counter() - t0
+    # the same grid as one pathwise-adjoint portfolio launch (delta / vega / rho of the smoothed payoff)
+    best_a = None
+    for _ in range(reps):
+        a = kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05,
+                             method="adjoint")
+        t = _dev_seconds(kx)
+        best_a = t if best_a is None or t < best_a else best_a
+    import numpy as np
+    se_ratio = {q: float(np.median((getattr(s, q + "_se") / getattr(a, q + "_se")) ** 2)) for q in ("delta", "vega")}
     cells = len(spots) * len(vols)
     scen_steps = cells * 7 * n * steps
     # CPU: the oracle on a sample of cells and paths, scaled to cells/s at n paths
@@ -340,7 +352,11 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
             "vega_atm_0.26": float(s.vega[5, 4]),
             "cpu_baseline": {"cells_per_s": cpu_cells_per_s, "cores": orc.threads(), "kind": "port",
                              "sample": f"{kc} cells x {pn} paths x {steps} steps x 7 reprices, {cdt:.2f} s"},
-            "gpu_over_cpu_cells_per_s": cells / best / cpu_cells_per_s}
+            "gpu_over_cpu_cells_per_s": cells / best / cpu_cells_per_s,
+            "adjoint": {"seconds": best_a, "cells_per_s": cells / best_a,
+                        "median_se2_ratio_bump_over_adjoint": se_ratio,
+                        "equal_se_speedup_vs_bump": best * max(se_ratio.values()) / best_a,
+                        "delta_atm_0.26": float(a.delta[5, 4]), "vega_atm_0.26": float(a.vega[5, 4])}}
 
 
 def heston_book(reps=3) -> dict:

@@ -577,14 +577,47 @@ class GreekSurface:
         return f"GreekSurface({len(self.spots)} spots x {len(self.vols)} vols)"
 
 
+def _adjoint_surface(contract, asset, spots, vols, n_paths, seed, steps_per_year, rate, precision) -> GreekSurface:
+    if not spots or not vols:
+        raise KontractError(_abi.KX_INCONSISTENT_PATH, "empty surface grid")  # surface.rs:113-117
+    cells = [(float(s), float(v)) for s in spots for v in vols]
+    models = [GBM(s0=s, sigma=v, r=rate, asset=asset) for s, v in cells]
+    res, sens = price_portfolio([contract] * len(cells), models, [n_paths] * len(cells), seed, steps_per_year,
+                                precision=precision, greeks=True)
+    nan = float("nan")
+
+    class _Cell:
+        pass
+    out = []
+    for r, g in zip(res, sens):
+        c = _Cell()
+        c.price, c.price_se = r.price, r.std_error
+        c.delta, c.delta_se = g.d_s0, g.se_s0
+        c.vega, c.vega_se = g.d_sigma, g.se_sigma
+        c.rho, c.rho_se = g.d_r, g.se_r
+        c.gamma = c.gamma_se = nan
+        out.append(c)
+    return GreekSurface(spots, vols, out)
+
+
 def greek_surface(contract: Contract, asset: str, spots: Sequence[float], vols: Sequence[float],
                   n_paths: int = 100_000, seed: int = 42, steps_per_year: int = 50, rate: float = 0.0, *,
-                  bumps: tuple | None = None, relative: bool = False, precision: str = "fp32") -> GreekSurface:
+                  bumps: tuple | None = None, relative: bool = False, precision: str = "fp32",
+                  method: str = "bump") -> GreekSurface:
     """greek_surface (src/surface.rs:104-137): bump-and-reprice Greeks
     (greeks_gbm) at every cell of spots x vols, all cells on the same seed.
     The arguments after `vols` are McConfig's fields (default McConfig,
     pricer.rs:44-54) and BumpSizes (default (1e-2, 1e-2, 1e-4)). One path
-    launch values every cell and its seven scenarios."""
+    launch values every cell and its seven reprices.
+
+    method="adjoint" (no reference counterpart): every cell is a contract of
+    one pathwise-adjoint portfolio launch (kx_price_portfolio with
+    sensitivities): price with the hard barriers, delta / vega / rho of the
+    barrier-smoothed payoff, gamma NaN (a pathwise first derivative only)."""
+    if method == "adjoint":
+        return _adjoint_surface(contract, asset, spots, vols, n_paths, seed, steps_per_year, rate, precision)
+    if method != "bump":
+        raise ValueError("method must be 'bump' or 'adjoint'")
     hs, hv, hr = bumps if bumps is not None else (1e-2, 1e-2, 1e-4)
     b = _abi.KxBumps(spot=hs, vol=hv, rate=hr, relative=int(relative), smooth=0, smoothing_width=0.0)
     cfg = _cfg(n_paths, seed, steps_per_year, rate, precision, False)
