@@ -297,6 +297,27 @@ kx_status kx_greek_surface(const kx_program *prog, const char *asset, const doub
                            const double *vols, size_t n_vols, const kx_mc_config *cfg, const kx_bumps *bumps,
                            kx_greeks *out);
 
+/* gbm_prices (src/calibration.rs:72-90) for several volatilities at once:
+ * out[k * n_quotes + i] = price_gbm of the contract under
+ * Gbm::new(asset, spots[i], cfg->rate, sigmas[k]) with cfg, NaN where that
+ * price fails (calibration.rs:86). All n_sigmas x n_quotes prices come from
+ * one path launch on the seed's normals (the common random numbers of the
+ * reference's calibration, seed 42). Philox only. */
+kx_status kx_calib_gbm_prices(const kx_program *prog, const char *asset, const double *spots, size_t n_quotes,
+                              const double *sigmas, size_t n_sigmas, const kx_mc_config *cfg, double *out);
+
+/* eval_obj_heston (src/calibration.rs:103-126) for a population of parameter
+ * vectors params[k] = (v0, kappa, theta, sigma_v, rho) (5 doubles each):
+ * obj[k] = sum over the quotes whose price succeeds of (price - quote)^2,
+ * divided by n_quotes, with quotes[i] = (spot, market price) and the model
+ * HestonSimulator::new(asset, spot, v0, kappa, theta, sigma_v, rho,
+ * cfg->rate) (reference floor scheme). `prices` (nullable) receives the
+ * n_params x n_quotes prices, NaN where one fails. One path launch prices the
+ * whole population (a CMA-ES generation) on the seed's normals. */
+kx_status kx_calib_heston_objective(const kx_program *prog, const char *asset, const double *quotes, size_t n_quotes,
+                                    const double *params, size_t n_params, const kx_mc_config *cfg, double *obj,
+                                    double *prices);
+
 /* Pathwise adjoint: one reverse sweep per path recomputing the path from its
  * Philox counters with a checkpoint every `checkpoint_every` steps; the
  * barrier indicator of until-conditions is a logistic of the stated width.

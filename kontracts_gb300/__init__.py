@@ -631,6 +631,16 @@ def greek_surface(contract: Contract, asset: str, spots: Sequence[float], vols: 
     return GreekSurface(spots, vols, [Greeks(g) for g in out[: ns * nv]])
 
 
+def fit_gbm_volatility(contract: Contract, maturities: Sequence[float], market_prices: Sequence[tuple], rate: float,
+                       n_paths: int = 2000) -> float:
+    """The reference binding's fit_gbm_volatility (src/bindings.rs:1014-1038):
+    the fitted GBM volatility for (spot, price) quotes
+    (kontracts_gb300.calibration.fit_gbm_volatility with n_paths)."""
+    from . import calibration
+    cfg = calibration.FastCalibrationConfig(n_paths=int(n_paths))
+    return calibration.fit_gbm_volatility(contract, maturities, market_prices, rate, cfg).parameters[0]
+
+
 def price_batch(contracts: Sequence[Contract], model, n_paths: int = 100_000, seed: int = 42,
                 steps_per_year: int = 50, *, precision: str = "fp32") -> list[PriceResult]:
     """price_batch_gbm (src/pricer.rs:250-294): every contract on the same paths."""
@@ -829,6 +839,6 @@ __all__ = [
     "until", "and_", "or_", "USD", "EUR", "GBP", "JPY", "average", "average_over", "running_max",
     "running_min", "heston", "zero_coupon_bond", "european_call", "european_put", "forward", "straddle",
     "bull_call_spread", "cash_or_nothing_call", "up_and_out_call", "down_and_out_call", "price_batch",
-    "price_american_batch", "GreekSurface", "greek_surface",
+    "price_american_batch", "GreekSurface", "greek_surface", "fit_gbm_volatility",
     "price_portfolio", "set_shared_draws", "last_launch_stats",
 ]

@@ -155,6 +155,11 @@ SIGNATURES = {
                                  C.POINTER(KxBumps), C.POINTER(KxGreeks)]),
     "kx_greek_surface": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_double),
                                    C.c_size_t, C.POINTER(KxMcConfig), C.POINTER(KxBumps), C.POINTER(KxGreeks)]),
+    "kx_calib_gbm_prices": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_double),
+                                      C.c_size_t, C.POINTER(KxMcConfig), C.POINTER(C.c_double)]),
+    "kx_calib_heston_objective": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_double), C.c_size_t,
+                                            C.POINTER(C.c_double), C.c_size_t, C.POINTER(KxMcConfig),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "kx_greeks_adjoint": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                     C.POINTER(KxAdjointCfg), C.POINTER(KxSens)]),
     "kx_price_american_lsm": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),

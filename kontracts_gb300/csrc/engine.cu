@@ -1288,6 +1288,43 @@ static void fill_greeks(const Stats *st5, kx_greeks *out) {
     out->rho = r4.price; out->rho_se = r4.std_error;
 }
 
+// Prices of one contract under many models of one kind with one config, as
+// the calibration objectives price their quotes (calibration.rs:72-90,
+// 103-126): one path launch for every entry whose price can be formed; an
+// entry whose job cannot be built (the reference's price_gbm returns an
+// error: an unknown asset, an invalid parameter) is reported in ok[] as 0
+// and left out of the launch.
+static void calib_prices(Ctx &c, const Program &p, const std::vector<Model> &models, const kx_mc_config &cfg,
+                         std::vector<double> &price, std::vector<char> &ok) {
+    const size_t n = models.size();
+    price.assign(n, std::nan(""));
+    ok.assign(n, 0);
+    if (n == 0) return;
+    auto grid = time_grid_forced(p.plan, cfg.steps_per_year, models[0].requires_fine_grid());
+    std::vector<Job> jobs;
+    std::vector<size_t> idx;
+    for (size_t q = 0; q < n; ++q) {
+        try {
+            jobs.push_back(make_job(p, models[q], cfg, grid, {}, 0, 0.0));
+            idx.push_back(q);
+        } catch (const Error &) {
+        }
+    }
+    if (jobs.empty()) return;
+    uint64_t stride = 0;
+    run_paths(c, jobs, cfg, 1, stride);
+    std::vector<StatsJob> sj(jobs.size());
+    for (size_t q = 0; q < jobs.size(); ++q) {
+        sj[q].begin = jobs[q].dev.pv_off;
+        sj[q].n = jobs[q].dev.n_paths;
+    }
+    auto st = device_stats(c, c.pv.as<double>(), stride, sj);
+    for (size_t q = 0; q < jobs.size(); ++q) {
+        price[idx[q]] = finish(st[q]).price;
+        ok[idx[q]] = 1;
+    }
+}
+
 // Upper bound of the per-path values one surface launch keeps in HBM (seven
 // doubles per path and cell); larger surfaces run as several launches.
 static constexpr uint64_t SURFACE_PV_BYTES = 8ull << 30;
@@ -1387,6 +1424,85 @@ kx_status kx_greek_surface(const kx_program *prog, const char *asset, const doub
                 const Stats st5[5] = {st[q], st[nj + q], st[2 * nj + q], st[3 * nj + q], st[4 * nj + q]};
                 fill_greeks(st5, &out[c0 + q]);
             }
+        }
+        end_call(c);
+    });
+}
+
+kx_status kx_calib_gbm_prices(const kx_program *prog, const char *asset, const double *spots, size_t n_quotes,
+                              const double *sigmas, size_t n_sigmas, const kx_mc_config *cfg, double *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        check_cfg(cfg);
+        if (cfg->rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "calibration pricing uses Philox normals");
+        if ((n_quotes && !spots) || (n_sigmas && !sigmas) || (n_quotes * n_sigmas && !out))
+            raise(KX_INVALID_ARGUMENT, "NULL argument");
+        // Gbm::new(asset, spot, rate, sigma) per quote and volatility (calibration.rs:83)
+        std::vector<Model> models;
+        for (size_t k = 0; k < n_sigmas; ++k)
+            for (size_t i = 0; i < n_quotes; ++i) {
+                kx_model cm{};
+                cm.kind = KX_MODEL_GBM;
+                cm.s0 = spots[i];
+                cm.mu = cfg->rate;
+                cm.sigma = sigmas[k];
+                cm.asset = asset;
+                models.push_back(model_from_c(&cm));
+            }
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        std::vector<double> price;
+        std::vector<char> ok;
+        calib_prices(c, p, models, *cfg, price, ok);
+        for (size_t q = 0; q < models.size(); ++q) out[q] = price[q];  // NaN where the price fails (:86)
+        end_call(c);
+    });
+}
+
+kx_status kx_calib_heston_objective(const kx_program *prog, const char *asset, const double *quotes, size_t n_quotes,
+                                    const double *params, size_t n_params, const kx_mc_config *cfg, double *obj,
+                                    double *prices) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        check_cfg(cfg);
+        if (cfg->rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "calibration pricing uses Philox normals");
+        if ((n_quotes && !quotes) || (n_params && (!params || !obj))) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        // HestonSimulator::new(asset, spot, v0, kappa, theta, sigma_v, rho, rate) (calibration.rs:114-115)
+        std::vector<Model> models;
+        for (size_t k = 0; k < n_params; ++k)
+            for (size_t i = 0; i < n_quotes; ++i) {
+                kx_model cm{};
+                cm.kind = KX_MODEL_HESTON;
+                cm.heston_scheme = KX_HESTON_REFERENCE_FLOOR;
+                cm.s0 = quotes[2 * i];
+                cm.v0 = params[5 * k];
+                cm.kappa = params[5 * k + 1];
+                cm.theta = params[5 * k + 2];
+                cm.sigma_v = params[5 * k + 3];
+                cm.rho = params[5 * k + 4];
+                cm.r = cfg->rate;
+                cm.asset = asset;
+                models.push_back(model_from_c(&cm));
+            }
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        std::vector<double> price;
+        std::vector<char> ok;
+        calib_prices(c, p, models, *cfg, price, ok);
+        // the squared errors of the quotes that priced, in quote order, over n_quotes (:111-125)
+        for (size_t k = 0; k < n_params; ++k) {
+            double sum = 0.0;
+            for (size_t i = 0; i < n_quotes; ++i) {
+                const size_t q = k * n_quotes + i;
+                if (!ok[q]) continue;
+                const double d = price[q] - quotes[2 * i + 1];
+                sum += d * d;
+            }
+            obj[k] = sum / (double)n_quotes;
+            if (prices)
+                for (size_t i = 0; i < n_quotes; ++i) prices[k * n_quotes + i] = price[k * n_quotes + i];
         }
         end_call(c);
     });

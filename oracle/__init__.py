@@ -77,6 +77,10 @@ class Oracle:
                                 P(_abi.KxGreeks)]
         L.ko_greek_surface.argtypes = [C.c_char_p, C.c_char_p, P(D), C.c_size_t, P(D), C.c_size_t,
                                        P(_abi.KxMcConfig), P(_abi.KxBumps), P(_abi.KxGreeks)]
+        L.ko_calib_gbm_prices.argtypes = [C.c_char_p, C.c_char_p, P(D), C.c_size_t, P(D), C.c_size_t,
+                                          P(_abi.KxMcConfig), P(D)]
+        L.ko_calib_heston_objective.argtypes = [C.c_char_p, C.c_char_p, P(D), C.c_size_t, P(D), C.c_size_t,
+                                                P(_abi.KxMcConfig), P(D)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
         L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
@@ -209,6 +213,31 @@ class Oracle:
         self._chk(self.L.ko_greek_surface(js.encode(), asset.encode(), sp, len(spots), vo, len(vols), C.byref(cfg),
                                           C.byref(b), out))
         return [{k: getattr(g, k) for k, _ in g._fields_} for g in out[: len(spots) * len(vols)]]
+
+    def calib_gbm_prices(self, js: str, asset: str, spots, sigmas, n_paths=1000, seed=42, steps_per_year=252,
+                         rate=0.0) -> np.ndarray:
+        """gbm_prices (calibration.rs:72-90) per volatility: [len(sigmas), len(spots)]."""
+        sp = np.ascontiguousarray(spots, dtype=np.float64)
+        sg = np.ascontiguousarray(sigmas, dtype=np.float64)
+        out = np.zeros(max(1, len(sp) * len(sg)))
+        cfg = self.cfg(n_paths, seed, steps_per_year, rate)
+        self._chk(self.L.ko_calib_gbm_prices(js.encode(), asset.encode(), sp.ctypes.data_as(C.POINTER(C.c_double)),
+                                             len(sp), sg.ctypes.data_as(C.POINTER(C.c_double)), len(sg),
+                                             C.byref(cfg), out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[: len(sp) * len(sg)].reshape(len(sg), len(sp))
+
+    def calib_heston_objective(self, js: str, asset: str, quotes, params, n_paths=1000, seed=42,
+                               steps_per_year=252, rate=0.0) -> np.ndarray:
+        """eval_obj_heston (calibration.rs:103-126) for each row of params."""
+        q = np.ascontiguousarray(quotes, dtype=np.float64).reshape(-1, 2)
+        p = np.ascontiguousarray(params, dtype=np.float64).reshape(-1, 5)
+        obj = np.zeros(max(1, len(p)))
+        cfg = self.cfg(n_paths, seed, steps_per_year, rate)
+        self._chk(self.L.ko_calib_heston_objective(js.encode(), asset.encode(),
+                                                   q.ctypes.data_as(C.POINTER(C.c_double)), len(q),
+                                                   p.ctypes.data_as(C.POINTER(C.c_double)), len(p), C.byref(cfg),
+                                                   obj.ctypes.data_as(C.POINTER(C.c_double))))
+        return obj[: len(p)]
 
     def price_american(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
                        per_path=False, basis="monomial"):

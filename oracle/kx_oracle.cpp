@@ -1192,6 +1192,74 @@ int ko_greek_surface(const char *json, const char *asset, const double *spots, s
     });
 }
 
+// price_gbm of one contract under `m`, or false where the reference's
+// price_gbm returns an error (the calibration objectives skip those quotes).
+static bool try_price(const ConP &c, const Model &m, const kx_mc_config &mc, double &price) {
+    try {
+        Plan p = compile(*c);
+        auto grid = time_grid_forced(p, mc.steps_per_year, m.requires_fine());
+        std::vector<std::vector<double>> pvs;
+        value_paths({c.get()}, m, grid, mc.n_paths, make_source(mc), mc.rate, pvs);
+        price = summarize(pvs[0]).price;
+        return true;
+    } catch (const KxError &) {
+        return false;
+    }
+}
+
+// gbm_prices (calibration.rs:72-90) for several volatilities:
+// out[k * n_quotes + i] under Gbm::new(asset, spots[i], rate, sigmas[k]), NaN on error.
+int ko_calib_gbm_prices(const char *json, const char *asset, const double *spots, size_t n_quotes,
+                        const double *sigmas, size_t n_sigmas, const kx_mc_config *cfg, double *out) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        kx_mc_config mc = check_cfg(cfg);
+        for (size_t k = 0; k < n_sigmas; ++k)
+            for (size_t i = 0; i < n_quotes; ++i) {
+                kx_model cm{};
+                cm.kind = KX_MODEL_GBM;
+                cm.s0 = spots[i];
+                cm.mu = mc.rate;
+                cm.sigma = sigmas[k];
+                cm.asset = asset;
+                double p = 0.0;
+                out[k * n_quotes + i] = try_price(c, to_model(&cm), mc, p) ? p : std::nan("");
+            }
+    });
+}
+
+// eval_obj_heston (calibration.rs:103-126) for each parameter vector
+// (v0, kappa, theta, sigma_v, rho): the squared errors of the quotes that
+// price, summed in quote order, over the number of quotes.
+int ko_calib_heston_objective(const char *json, const char *asset, const double *quotes, size_t n_quotes,
+                              const double *params, size_t n_params, const kx_mc_config *cfg, double *obj) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        kx_mc_config mc = check_cfg(cfg);
+        for (size_t k = 0; k < n_params; ++k) {
+            double sum = 0.0;
+            for (size_t i = 0; i < n_quotes; ++i) {
+                kx_model cm{};
+                cm.kind = KX_MODEL_HESTON;
+                cm.heston_scheme = KX_HESTON_REFERENCE_FLOOR;
+                cm.s0 = quotes[2 * i];
+                cm.v0 = params[5 * k];
+                cm.kappa = params[5 * k + 1];
+                cm.theta = params[5 * k + 2];
+                cm.sigma_v = params[5 * k + 3];
+                cm.rho = params[5 * k + 4];
+                cm.r = mc.rate;
+                cm.asset = asset;
+                double p = 0.0;
+                if (!try_price(c, to_model(&cm), mc, p)) continue;
+                const double d = p - quotes[2 * i + 1];
+                sum += d * d;
+            }
+            obj[k] = sum / (double)n_quotes;
+        }
+    });
+}
+
 int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
                             size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
     return run([&] {
