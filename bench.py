@@ -359,6 +359,58 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
                         "delta_atm_0.26": float(a.delta[5, 4]), "vega_atm_0.26": float(a.vega[5, 4])}}
 
 
+def heston_calibration(cpu_seconds=6.0) -> dict:
+    """calibrate_heston_cmaes (calibration.rs:441-465) as the reference tests
+    it: three call quotes (spots 90 / 100 / 110, K 100, T 1, r 0.05) priced
+    under (v0, kappa, theta, sigma_v, rho) = (0.04, 2, 0.04, 0.3, -0.5) on the
+    calibration's own paths (3,000 paths, seed 42, 252 steps a year), 40
+    generations of 40 candidates. Each generation's 120 Heston prices are one
+    path launch. FP64 paths (the reference's precision) and FP32. CPU: the
+    oracle's eval_obj_heston over one generation's population, all host
+    threads, scaled to the 40 generations."""
+    import numpy as np
+
+    import kontracts_gb300 as kx
+    from kontracts_gb300 import calibration as cal
+    from oracle import Oracle
+    c = kx.european_call("underlying", 100.0, 1.0)
+    hp = [0.04, 2.0, 0.04, 0.3, -0.5]
+    quotes = [(s, c.price(kx.heston(s, *hp, 0.05, asset="underlying"), n_paths=3000, seed=42, steps_per_year=252,
+                          precision="fp64").price) for s in (90.0, 100.0, 110.0)]
+    out = {"workload": "Heston CMA-ES calibration, 3 call quotes, 3000 paths x 252 steps, 40 generations x 40 "
+                       "candidates (the reference's calibrate_heston_reproduces_prices)"}
+    for prec in ("fp64", "fp32"):
+        cfg = cal.FastCalibrationConfig(n_paths=3000, max_iterations=40, precision=prec)
+        cal.calibrate_heston_cmaes(c, quotes, 0.05, cal.FastCalibrationConfig(n_paths=3000, max_iterations=2,
+                                                                             precision=prec))  # tune + warm
+        t0 = time.perf_counter()
+        res = cal.calibrate_heston_cmaes(c, quotes, 0.05, cfg)
+        wall = time.perf_counter() - t0
+        err = max(abs(c.price(kx.heston(s, *res.parameters, 0.05, asset="underlying"), n_paths=3000, seed=42,
+                              steps_per_year=252, precision="fp64").price - q) / q for s, q in quotes)
+        out[prec] = {"wall_seconds": wall, "generations": res.iterations, "objective": res.objective,
+                     "parameters": res.parameters, "max_rel_price_error": err,
+                     "generations_per_s": res.iterations / wall}
+    # the oracle on one generation (40 candidates x 3 quotes), repeated to ~cpu_seconds
+    orc = Oracle()
+    rng = np.random.default_rng(1)
+    pop = [[float(rng.uniform(lo, hi)) for lo, hi in zip(cal.HESTON_LOWER, cal.HESTON_UPPER)] for _ in range(40)]
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        orc.calib_heston_objective(c.to_json(), "underlying", quotes, pop, n_paths=3000, steps_per_year=252,
+                                   rate=0.05)
+        k += 1
+        if time.perf_counter() - t0 > cpu_seconds or k >= 40:
+            break
+    per_gen = (time.perf_counter() - t0) / k
+    out["cpu_baseline"] = {"seconds_per_generation": per_gen, "generations_per_s": 1.0 / per_gen,
+                           "cores": orc.threads(), "kind": "port",
+                           "sample": f"{k} generations of 40 candidates x 3 quotes x 3000 paths x 252 steps"}
+    out["gpu_fp64_over_cpu_generations_per_s"] = out["fp64"]["generations_per_s"] * per_gen
+    return out
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -592,7 +644,8 @@ def run_ours(args, ws, rank, local) -> None:
         line["other_configs"] = {"european_fp64": european_fp64(), "heston_book_96": heston_book(),
                                  "book_256": book_256(), "lsm_12": lsm_cases(),
                                  "variance_reduction": variance_reduction(),
-                                 "greek_surface_99": greek_surface_grid()}
+                                 "greek_surface_99": greek_surface_grid(),
+                                 "heston_calibration": heston_calibration()}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.cpu_seconds)
         line["accuracy"] = accuracy(cb)
