@@ -318,6 +318,51 @@ kx_status kx_calib_heston_objective(const kx_program *prog, const char *asset, c
                                     const double *params, size_t n_params, const kx_mc_config *cfg, double *obj,
                                     double *prices);
 
+/* ---- multilevel Monte Carlo ----------------------------------------------
+ * Mirrors MlmcConfig (src/mlmc.rs:50-72; defaults n_levels 6, pilot_paths
+ * 2000, target_variance 1e-4, cost_per_step 1) and MlmcResult (:75-96). */
+#define KX_MLMC_MAX_LEVELS 20
+typedef struct kx_mlmc_cfg {
+    uint32_t n_levels;       /* finest level L: levels 0..L, level l has 2^l steps */
+    uint32_t cost_per_step;
+    uint64_t pilot_paths;
+    double target_variance;
+} kx_mlmc_cfg;
+
+typedef struct kx_mlmc_result {
+    kx_price_result price;
+    uint32_t n_levels;       /* levels 0..n_levels are filled */
+    uint32_t reserved;
+    double level_means[KX_MLMC_MAX_LEVELS + 1];
+    double level_variances[KX_MLMC_MAX_LEVELS + 1];
+    uint64_t level_costs[KX_MLMC_MAX_LEVELS + 1];
+    uint64_t level_paths[KX_MLMC_MAX_LEVELS + 1];
+    uint64_t total_cost;
+} kx_mlmc_result;
+
+/* price_mlmc_detailed (src/mlmc.rs:107-215): the telescoping sum of level
+ * means E[P_l - P_(l-1)] over uniform grids of 2^l steps on [0, horizon],
+ * GBM or Heston (simulate_level_pair, simulator.rs:321-409 and 592-690: the
+ * coarse path of a pair steps with the summed normals of two fine steps).
+ * A pilot of pilot_paths per level, then optimal_allocation's extra paths
+ * with the seed XOR 0xA5A55A5ADEADBEEF (mlmc.rs:142-166). Each phase is two
+ * path launches (all levels' fine paths, then all coarse paths) and one
+ * statistics launch of the per-path differences. Path i of level l draws the
+ * Philox stream keyed by mix(mix(seed, l), l + 1) (mix: simulator.rs:431). */
+kx_status kx_price_mlmc(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                        const kx_mlmc_cfg *mcfg, kx_mlmc_result *out);
+
+/* estimate_variance_at_level (mlmc.rs:218-229): the sample variance of
+ * P_l - P_(l-1) over n_pilot coupled paths of level `level`. */
+kx_status kx_mlmc_level_variance(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                                 uint32_t level, uint64_t n_pilot, double *variance);
+
+/* optimal_allocation (mlmc.rs:231-258): paths per level
+ * ceil(sum_k sqrt(V_k C_k) sqrt(V_l / C_l) / target), at least 1; all zero when
+ * n is 0 or target <= 0. Host arithmetic only. */
+kx_status kx_mlmc_optimal_allocation(const double *variances, const uint64_t *costs, size_t n, double target_var,
+                                     uint64_t *out);
+
 /* Pathwise adjoint: one reverse sweep per path recomputing the path from its
  * Philox counters with a checkpoint every `checkpoint_every` steps; the
  * barrier indicator of until-conditions is a logistic of the stated width.

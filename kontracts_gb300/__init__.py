@@ -842,3 +842,9 @@ __all__ = [
     "price_american_batch", "GreekSurface", "greek_surface", "fit_gbm_volatility",
     "price_portfolio", "set_shared_draws", "last_launch_stats",
 ]
+
+from .mlmc import (MlmcConfig, MlmcResult, estimate_variance_at_level, optimal_allocation,  # noqa: E402
+                   price_mlmc, price_mlmc_detailed)
+
+__all__ += ["MlmcConfig", "MlmcResult", "price_mlmc", "price_mlmc_detailed", "estimate_variance_at_level",
+            "optimal_allocation"]

@@ -73,10 +73,27 @@ class KxBumps(C.Structure):
     ]
 
 
+KX_MLMC_MAX_LEVELS = 20
+
+
+class KxMlmcCfg(C.Structure):
+    _fields_ = [("n_levels", C.c_uint32), ("cost_per_step", C.c_uint32), ("pilot_paths", C.c_uint64),
+                ("target_variance", C.c_double)]
+
+
 class KxGreeks(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "price", "delta", "gamma", "vega", "rho",
         "price_se", "delta_se", "gamma_se", "vega_se", "rho_se")]
+
+
+class KxMlmcResult(C.Structure):
+    _fields_ = [("price", KxPriceResult), ("n_levels", C.c_uint32), ("reserved", C.c_uint32),
+                ("level_means", C.c_double * (KX_MLMC_MAX_LEVELS + 1)),
+                ("level_variances", C.c_double * (KX_MLMC_MAX_LEVELS + 1)),
+                ("level_costs", C.c_uint64 * (KX_MLMC_MAX_LEVELS + 1)),
+                ("level_paths", C.c_uint64 * (KX_MLMC_MAX_LEVELS + 1)),
+                ("total_cost", C.c_uint64)]
 
 
 class KxAdjointCfg(C.Structure):
@@ -160,6 +177,12 @@ SIGNATURES = {
     "kx_calib_heston_objective": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_double), C.c_size_t,
                                             C.POINTER(C.c_double), C.c_size_t, C.POINTER(KxMcConfig),
                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "kx_price_mlmc": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig), C.POINTER(KxMlmcCfg),
+                                C.POINTER(KxMlmcResult)]),
+    "kx_mlmc_level_variance": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig), C.c_uint32, C.c_uint64,
+                                         C.POINTER(C.c_double)]),
+    "kx_mlmc_optimal_allocation": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t, C.c_double,
+                                             C.POINTER(C.c_uint64)]),
     "kx_greeks_adjoint": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                     C.POINTER(KxAdjointCfg), C.POINTER(KxSens)]),
     "kx_price_american_lsm": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),

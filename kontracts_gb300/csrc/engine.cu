@@ -433,7 +433,7 @@ bool use_static(const std::vector<Job> &jobs, int ns) {
 }
 
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
-                            int minb, bool lean);
+                            int minb, bool lean, bool pair = false);
 
 // Project autotuner: the path kernel exists at a few register budgets
 // (minimum resident blocks per SM). The first launch of each kind (model,
@@ -523,7 +523,7 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
 }
 
 PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
-                    uint64_t item_paths, bool stat) {
+                    uint64_t item_paths, bool stat, bool pair) {
     PathPlan P;
     P.f64 = cfg.precision == KX_PREC_FP64;
     P.lean = lean;
@@ -579,7 +579,7 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.surv_base = 2u * (uint32_t)max_acc;
     P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
     P.smem = lean ? 0 : (size_t)ns * P.slots * block * (f64 ? 8 : 4);  // k_lean keeps its average in registers
-    P.kfn = select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc);
+    P.kfn = pair ? paths_kernel_pair(P.model, f64) : select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc);
     if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (P.smem > 48 * 1024)
         KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
@@ -665,8 +665,8 @@ size_t plan_upload_bytes(const PathPlan &P) {
 }
 
 static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out,
-                            int minb, bool lean) {
-    PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0, lean && use_static(jobs, ns));
+                            int minb, bool lean, bool pair) {
+    PathPlan P = plan_paths(jobs, cfg, ns, minb, lean, 0, lean && use_static(jobs, ns), pair);
     c.last.path_steps += P.path_steps;
     stride_out = P.total;
     if (P.n_items == 0) return P.total;
@@ -1325,6 +1325,118 @@ static void calib_prices(Ctx &c, const Program &p, const std::vector<Model> &mod
     }
 }
 
+// ---------------------------------------------------------------------------
+// multilevel Monte Carlo (mlmc.rs, simulate_level_pair)
+// ---------------------------------------------------------------------------
+static std::vector<double> uniform_grid(double t_max, uint64_t n_steps) {  // simulator.rs:181-184
+    const uint64_t n = std::max<uint64_t>(n_steps, 1);
+    std::vector<double> g(n + 1);
+    for (uint64_t k = 0; k <= n; ++k) g[k] = t_max * (double)k / (double)n;
+    return g;
+}
+
+static uint64_t mix_seed(uint64_t seed, uint64_t index) {  // simulator.rs:431-433
+    return seed ^ (index * 0x9E3779B97F4A7C15ull);
+}
+
+static uint64_t mlmc_level_cost(uint32_t l) {  // mlmc.rs:266-272
+    return l == 0 ? 1 : (1ull << l) + (1ull << (l - 1));
+}
+
+// Every step of a level-pair path has the same coefficients, formed as the
+// reference forms them from dt = t_max / n (simulator.rs:328-343, 610-616):
+// GBM (mu - sigma^2 / 2) dt and sigma sqrt(dt_f) (the coarse path's normal is
+// the sum of two fine ones, so its diffusion keeps sqrt(dt_f)); Heston dt and
+// sqrt(dt).
+static void set_level_steps(Job &j, const Model &m, double dt, double dt_f) {
+    double c0, c1;
+    if (m.kind == KX_MODEL_GBM) {
+        c0 = (m.mu - 0.5 * m.sigma * m.sigma) * dt;
+        c1 = m.sigma * std::sqrt(dt_f);
+    } else {
+        c0 = dt;
+        c1 = std::sqrt(dt);
+    }
+    for (size_t k = 1; k < j.tab.c0.size(); ++k) {
+        j.tab.c0[k] = c0;
+        j.tab.c1[k] = c1;
+    }
+    ContractDev &d = j.dev;
+    d.uniform = j.tab.c0.size() > 1 ? 1 : 0;
+    d.uc0 = c0;
+    d.uc1 = c1;
+    d.uc0f = (float)c0;
+    d.uc1f = (float)c1;
+}
+
+struct LevelRun {
+    uint32_t level;
+    uint64_t n;
+};
+
+// Statistics of Y_l = P_l - P_(l-1) (P_(-1) = 0) on n coupled paths per run
+// (mlmc.rs:276-305), runs in increasing level order. The fine paths of all
+// runs are one launch, the coarse paths (the _PAIR kernels, reading the same
+// Philox streams two fine steps per step) another; both per-path value arrays
+// are copied side by side so that a run's coarse value sits at a fixed
+// distance from its fine one, and one statistics launch forms fine - coarse.
+static std::vector<Stats> mlmc_level_stats(Ctx &c, const Program &p, const Model &m, const kx_mc_config &cfg,
+                                           double t_max, uint64_t seed, const std::vector<LevelRun> &runs) {
+    std::vector<Job> fine, coarse;
+    uint64_t n0 = 0;
+    for (const LevelRun &r : runs) {
+        const uint32_t l = r.level;
+        kx_mc_config c2 = cfg;
+        c2.n_paths = r.n;
+        c2.seed = mix_seed(mix_seed(seed, l), (uint64_t)l + 1);  // mlmc.rs:288, simulator.rs:345
+        const uint64_t nf = 1ull << l;
+        const double dt_f = t_max / (double)nf;
+        Job jf = make_job(p, m, c2, uniform_grid(t_max, nf), {}, 0, 0.0);
+        set_level_steps(jf, m, dt_f, dt_f);
+        fine.push_back(std::move(jf));
+        if (l == 0) {
+            n0 = r.n;
+            continue;
+        }
+        const double dt_c = t_max / (double)(nf / 2);
+        Job jc = make_job(p, m, c2, uniform_grid(t_max, nf / 2), {}, 0, 0.0);
+        set_level_steps(jc, m, dt_c, dt_f);
+        coarse.push_back(std::move(jc));
+    }
+    uint64_t nfine = 0, ncoarse = 0;
+    run_paths(c, fine, cfg, 1, nfine);
+    c.mlmc.ensure(std::max<uint64_t>(1, 2 * nfine) * sizeof(double));
+    if (nfine)
+        KX_CUDA(cudaMemcpyAsync(c.mlmc.p, c.pv.p, nfine * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    if (!coarse.empty()) {
+        run_paths_v(c, coarse, cfg, 1, ncoarse, 2, false, true);
+        KX_CUDA(cudaMemcpyAsync(c.mlmc.as<double>() + nfine, c.pv.p, ncoarse * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c.stream));
+    }
+    // run q >= 1 (level >= 1): fine at f_q, coarse at nfine + f_q - n0, i.e. (nfine - n0) further on
+    std::vector<StatsJob> sj(runs.size());
+    size_t qc = 0;
+    for (size_t q = 0; q < runs.size(); ++q) {
+        sj[q].begin = fine[q].dev.pv_off;
+        sj[q].n = runs[q].n;
+        if (runs[q].level > 0) {
+            if (coarse[qc].dev.pv_off + n0 != fine[q].dev.pv_off) raise(KX_CUDA_ERROR, "level pair layout");
+            ++qc;
+            sj[q].ns = 2;
+            sj[q].w[0] = 1.0;
+            sj[q].w[1] = -1.0;
+        }
+    }
+    return device_stats(c, c.mlmc.as<double>(), nfine - n0, sj);
+}
+
+static void check_mlmc_model(const Model &m) {
+    if (m.kind != KX_MODEL_GBM && m.kind != KX_MODEL_HESTON)
+        raise(KX_UNSUPPORTED, "this model has no level pairs (simulate_level_pair)");
+    if (m.kind == KX_MODEL_HESTON && m.scheme != KX_HESTON_REFERENCE_FLOOR)
+        raise(KX_UNSUPPORTED, "level pairs follow the reference Heston scheme (floor after the step)");
+}
+
 // Upper bound of the per-path values one surface launch keeps in HBM (seven
 // doubles per path and cell); larger surfaces run as several launches.
 static constexpr uint64_t SURFACE_PV_BYTES = 8ull << 30;
@@ -1504,6 +1616,136 @@ kx_status kx_calib_heston_objective(const kx_program *prog, const char *asset, c
             if (prices)
                 for (size_t i = 0; i < n_quotes; ++i) prices[k * n_quotes + i] = price[k * n_quotes + i];
         }
+        end_call(c);
+    });
+}
+
+kx_status kx_mlmc_optimal_allocation(const double *variances, const uint64_t *costs, size_t n, double target_var,
+                                     uint64_t *out) {
+    return guarded([&] {
+        if (n && (!variances || !costs || !out)) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (n == 0) return;
+        if (target_var <= 0.0) {  // mlmc.rs:238-240
+            for (size_t k = 0; k < n; ++k) out[k] = 0;
+            return;
+        }
+        double sum_sqrt_vc = 0.0;  // mlmc.rs:241-243
+        for (size_t k = 0; k < n; ++k) sum_sqrt_vc += std::sqrt(std::max(variances[k], 0.0) * (double)std::max<uint64_t>(costs[k], 1));
+        for (size_t k = 0; k < n; ++k) {
+            const double v = std::max(variances[k], 0.0);
+            const double cst = (double)std::max<uint64_t>(costs[k], 1);
+            if (v <= 0.0) {
+                out[k] = 1;
+                continue;
+            }
+            const double nk = (sum_sqrt_vc * std::sqrt(v / cst)) / target_var;
+            const double up = std::ceil(nk);
+            out[k] = std::max<uint64_t>(up >= 1.8446744073709552e19 ? UINT64_MAX : (uint64_t)up, 1);
+        }
+    });
+}
+
+kx_status kx_mlmc_level_variance(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                                 uint32_t level, uint64_t n_pilot, double *variance) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        check_mlmc_model(m);
+        validate_model(m);
+        if (!variance) raise(KX_INVALID_ARGUMENT, "variance is NULL");
+        if (level > KX_MLMC_MAX_LEVELS) raise(KX_INVALID_ARGUMENT, "level above KX_MLMC_MAX_LEVELS");
+        if (cfg->rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "level pairs draw from Philox");
+        if (n_pilot >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_pilot must be below 2^32");
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        *variance = 0.0;
+        if (n_pilot) {
+            auto st = mlmc_level_stats(c, p, m, *cfg, p.plan.horizon, cfg->seed, {{level, n_pilot}});
+            *variance = st[0].n > 1 ? st[0].m2 / (st[0].n - 1.0) : 0.0;  // mean_var, mlmc.rs:318-332
+        }
+        end_call(c);
+    });
+}
+
+kx_status kx_price_mlmc(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,
+                        const kx_mlmc_cfg *mcfg, kx_mlmc_result *out) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        Model m = model_from_c(model);
+        check_cfg(cfg);
+        check_mlmc_model(m);
+        validate_model(m);
+        if (!mcfg || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (cfg->rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "level pairs draw from Philox");
+        const uint32_t L = mcfg->n_levels;
+        if (L > KX_MLMC_MAX_LEVELS) raise(KX_INVALID_ARGUMENT, "n_levels above KX_MLMC_MAX_LEVELS");
+        if (mcfg->pilot_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "pilot_paths must be below 2^32");
+        const double t_max = p.plan.horizon;  // mlmc.rs:309-312
+        std::vector<uint64_t> costs(L + 1);
+        for (uint32_t l = 0; l <= L; ++l) costs[l] = mlmc_level_cost(l) * std::max<uint32_t>(mcfg->cost_per_step, 1);
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        // pilot: pilot_paths per level, one pair of launches for all levels (mlmc.rs:126-138)
+        std::vector<double> sums(L + 1, 0.0), sumsq(L + 1, 0.0), var(L + 1, 0.0);
+        std::vector<uint64_t> counts(L + 1, 0);
+        auto absorb = [&](uint32_t l, const Stats &st) {  // the running sums of mlmc.rs:133-135 and :150-152
+            sums[l] += st.n * st.mean;
+            sumsq[l] += st.m2 + st.n * st.mean * st.mean;
+            counts[l] += (uint64_t)st.n;
+        };
+        if (mcfg->pilot_paths) {
+            std::vector<LevelRun> runs;
+            for (uint32_t l = 0; l <= L; ++l) runs.push_back({l, mcfg->pilot_paths});
+            auto st = mlmc_level_stats(c, p, m, *cfg, t_max, cfg->seed, runs);
+            for (uint32_t l = 0; l <= L; ++l) {
+                var[l] = st[l].n > 1 ? st[l].m2 / (st[l].n - 1.0) : 0.0;
+                absorb(l, st[l]);
+            }
+        }
+        // optimal allocation and the extra paths on a second seed (mlmc.rs:140-166)
+        std::vector<uint64_t> extra(L + 1, 0);
+        if (kx_mlmc_optimal_allocation(var.data(), costs.data(), L + 1, mcfg->target_variance, extra.data()) != KX_OK)
+            raise(KX_INVALID_ARGUMENT, "optimal allocation failed");
+        std::vector<LevelRun> runs;
+        for (uint32_t l = 0; l <= L; ++l)
+            if (extra[l] > 0) {
+                if (extra[l] >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "a level needs 2^32 or more paths");
+                runs.push_back({l, extra[l]});
+            }
+        if (!runs.empty()) {
+            auto st = mlmc_level_stats(c, p, m, *cfg, t_max, cfg->seed ^ 0xA5A55A5ADEADBEEFull, runs);
+            for (size_t q = 0; q < runs.size(); ++q) absorb(runs[q].level, st[q]);
+        }
+        // level means and variances, the estimator and its standard error (mlmc.rs:168-214)
+        memset(out, 0, sizeof *out);
+        out->n_levels = L;
+        double price = 0.0, var_q = 0.0;
+        uint64_t n_total = 0, total_cost = 0;
+        for (uint32_t l = 0; l <= L; ++l) {
+            const double n = (double)std::max<uint64_t>(counts[l], 1);
+            const double mean = sums[l] / n;
+            const double v = counts[l] > 1 ? std::max((sumsq[l] - n * mean * mean) / (n - 1.0), 0.0) : 0.0;
+            out->level_means[l] = mean;
+            out->level_variances[l] = v;
+            out->level_costs[l] = costs[l];
+            out->level_paths[l] = counts[l];
+            price += mean;
+            var_q += v / n;
+            n_total += counts[l];
+            total_cost += counts[l] * costs[l];
+        }
+        const double se = std::sqrt(std::max(var_q, 0.0));
+        const double Z95 = 1.959963984540054;
+        out->price.price = price;
+        out->price.std_error = se;
+        out->price.sample_std = se * std::sqrt((double)std::max<uint64_t>(n_total, 1));
+        out->price.ci95_low = price - Z95 * se;
+        out->price.ci95_high = price + Z95 * se;
+        out->price.n_paths = n_total;
+        out->total_cost = total_cost;
         end_call(c);
     });
 }

@@ -40,7 +40,7 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scratch owned by the context
     DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, weights, misc, vr, lsm_paths, lsm_value,
-        lsm_stats, statics;
+        lsm_stats, statics, mlmc;
     DrawStore draws;
     kx_launch_stats last{};
     std::mutex mu;

@@ -79,9 +79,10 @@ struct PathBuffers {
 };
 
 // Lays out the tables of `jobs` (sets each job's pv offset) and the launch
-// geometry; item_paths = 0 picks the default work-item size.
+// geometry; item_paths = 0 picks the default work-item size; pair = true
+// launches the coarse kernels of multilevel pairs (k_paths, _PAIR models).
 PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int minb, bool lean,
-                    uint64_t item_paths, bool stat);
+                    uint64_t item_paths, bool stat, bool pair = false);
 PathArgs path_args(const PathPlan &P, const PathBuffers &B);
 void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s);
 size_t plan_upload_bytes(const PathPlan &P);

@@ -111,7 +111,11 @@ __device__ __forceinline__ WorkItem fetch_item(const PathArgs &A, int it) {
     return WorkItem{c, 0, (uint64_t)C.path_base + local, left < C.item_paths ? left : (uint64_t)C.item_paths};
 }
 
-enum { M_GBM = 0, M_HESTON = 1 };
+// Path models of k_paths. The _PAIR models are the coarse paths of a
+// multilevel Monte-Carlo pair (simulator.rs:321-409, 592-690): every coarse
+// step consumes the normals of two fine steps of the same Philox stream, so a
+// coarse job on the seed and path indices of its fine job is coupled to it.
+enum { M_GBM = 0, M_HESTON = 1, M_GBM_PAIR = 2, M_HESTON_PAIR = 3 };
 
 // Per-contract values a warp keeps in registers: only what the per-step hot
 // path reads. Everything else is read from the (L1-resident) program table
@@ -439,8 +443,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
-    constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
+    constexpr bool HESTON = MODEL == M_HESTON || MODEL == M_HESTON_PAIR;
+    constexpr int DRAWS = MODEL == M_GBM ? 1 : MODEL == M_HESTON_PAIR ? 4 : 2;  // normals per grid step
+    constexpr int SPB = 4 / DRAWS;                                             // grid steps per Philox block
     constexpr uint32_t ALL = (1u << NS) - 1u;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
@@ -481,7 +486,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                     }
                     cur = w.contract;
                     load_hot<Real, NS>(H, A, cur);
-                    if (MODEL == M_HESTON) {
+                    if (HESTON) {
                         const ContractDev &C = A.cons[cur];
                         hr = pick<Real>(C.r, C.rf);
                         hk = pick<Real>(C.kappa, C.kappaf);
@@ -574,20 +579,28 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         if ((done >> s) & 1u) continue;
-                        if (MODEL == M_GBM) {
-                            // log-space exact GBM step (simulator.rs:238-245)
+                        if (!HESTON) {
+                            // log-space exact GBM step (simulator.rs:238-245); a coarse step of a
+                            // multilevel pair adds its two fine normals (simulator.rs:373-377)
+                            const Real z = MODEL == M_GBM_PAIR ? zz[2 * j] + zz[2 * j + 1] : zz[j];
                             if (NS == 1) {
-                                L.y[s] = gbm_step(L.y[s], c0, c1, zz[j]);
+                                L.y[s] = gbm_step(L.y[s], c0, c1, z);
                             } else {
                                 const ContractDev &C = A.cons[cur];
                                 const Real sc1 = pick<Real>(C.sigma[s], C.sigmaf[s]) * c1;
-                                L.y[s] = gbm_step(L.y[s], pick<Real>(C.drift[s], C.driftf[s]) * c0, sc1, zz[j]);
+                                L.y[s] = gbm_step(L.y[s], pick<Real>(C.drift[s], C.driftf[s]) * c0, sc1, z);
                             }
                         } else {
+                            Real z1 = zz[2 * j], z2 = zz[2 * j + 1];
+                            if (MODEL == M_HESTON_PAIR) {  // the two fine (z1, z2) pairs, summed over sqrt 2 (:656-661)
+                                const Real inv_sqrt2 = Real(0.70710678118654752440);
+                                z1 = (zz[0] + zz[2]) * inv_sqrt2;
+                                z2 = (zz[1] + zz[3]) * inv_sqrt2;
+                            }
                             heston_step<Real>(hr, hk, hth, hsv, hrho, hrp,
                                               (H.flags & HF_FULLTRUNC) ? KX_HESTON_FULL_TRUNCATION
                                                                        : KX_HESTON_REFERENCE_FLOOR,
-                                              c0, c1, zz[2 * j], zz[2 * j + 1], L.y[s], L.v[s]);
+                                              c0, c1, z1, z2, L.y[s], L.v[s]);
                         }
                         if (contract_step<Real, NS>(H, A, cur, L, s, kk, smem)) done |= 1u << s;
                     }
@@ -615,6 +628,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
 }
 
 // Kernel variants, one function per translation unit.
+// paths_kernel_pair: the coarse kernels of multilevel pairs (model 0 GBM, 1 Heston).
+const void *paths_kernel_pair(int model, int fp64);
 // which: 0 GBM FP32, 1 GBM FP64, 2 Heston FP32, 3 Heston FP64, 4 GBM FP32 x7
 // scenarios, 5 GBM FP64 x7 scenarios. Returns nullptr for a missing variant.
 const void *paths_kernel_gbm(int fp64, int minb);

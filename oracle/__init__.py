@@ -81,6 +81,11 @@ class Oracle:
                                           P(_abi.KxMcConfig), P(D)]
         L.ko_calib_heston_objective.argtypes = [C.c_char_p, C.c_char_p, P(D), C.c_size_t, P(D), C.c_size_t,
                                                 P(_abi.KxMcConfig), P(D)]
+        L.ko_mlmc_level_values.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), C.c_uint32, C.c_uint64,
+                                           P(D)]
+        L.ko_mlmc_optimal_allocation.argtypes = [P(D), P(C.c_uint64), C.c_size_t, C.c_double, P(C.c_uint64)]
+        L.ko_price_mlmc.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(_abi.KxMlmcCfg),
+                                    P(_abi.KxMlmcResult)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
         L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
@@ -238,6 +243,37 @@ class Oracle:
                                                    p.ctypes.data_as(C.POINTER(C.c_double)), len(p), C.byref(cfg),
                                                    obj.ctypes.data_as(C.POINTER(C.c_double))))
         return obj[: len(p)]
+
+    def mlmc_level_values(self, js: str, model, level: int, n: int, seed=42, rate=None) -> np.ndarray:
+        """level_samples (mlmc.rs:276-305): P_l - P_(l-1) per coupled path."""
+        cm = _model_c(model)
+        cfg = self.cfg(0, seed, 0, _rate(model, rate))
+        out = np.zeros(max(1, n))
+        self._chk(self.L.ko_mlmc_level_values(js.encode(), C.byref(cm), C.byref(cfg), int(level), int(n),
+                                              out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[:n]
+
+    def mlmc_optimal_allocation(self, variances, costs, target) -> list:
+        n = min(len(variances), len(costs))
+        v = (C.c_double * max(1, n))(*variances[:n])
+        c = (C.c_uint64 * max(1, n))(*costs[:n])
+        out = (C.c_uint64 * max(1, n))()
+        self._chk(self.L.ko_mlmc_optimal_allocation(v, c, n, float(target), out))
+        return list(out[:n])
+
+    def price_mlmc(self, js: str, model, n_levels=6, pilot_paths=2000, target_variance=1e-4, cost_per_step=1,
+                   seed=42, rate=None) -> dict:
+        """price_mlmc_detailed (mlmc.rs:107-215)."""
+        cm = _model_c(model)
+        cfg = self.cfg(0, seed, 0, _rate(model, rate))
+        mc = _abi.KxMlmcCfg(n_levels=n_levels, cost_per_step=cost_per_step, pilot_paths=pilot_paths,
+                            target_variance=target_variance)
+        out = _abi.KxMlmcResult()
+        self._chk(self.L.ko_price_mlmc(js.encode(), C.byref(cm), C.byref(cfg), C.byref(mc), C.byref(out)))
+        k = out.n_levels + 1
+        return {"price": Result(out.price), "level_means": list(out.level_means[:k]),
+                "level_variances": list(out.level_variances[:k]), "level_costs": list(out.level_costs[:k]),
+                "level_paths": list(out.level_paths[:k]), "total_cost": out.total_cost}
 
     def price_american(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
                        per_path=False, basis="monomial"):

@@ -1260,6 +1260,233 @@ int ko_calib_heston_objective(const char *json, const char *asset, const double 
     });
 }
 
+// ---- multilevel Monte Carlo (mlmc.rs) ---------------------------------------
+static uint64_t mix(uint64_t seed, uint64_t index) { return seed ^ (index * 0x9E3779B97F4A7C15ull); }  // simulator.rs:431
+
+static std::vector<double> uniform_grid(double t_max, uint64_t n_steps) {  // simulator.rs:181-184
+    uint64_t n = std::max<uint64_t>(n_steps, 1);
+    std::vector<double> g(n + 1);
+    for (uint64_t k = 0; k <= n; ++k) g[k] = t_max * (double)k / (double)n;
+    return g;
+}
+
+// simulate_level_pair (simulator.rs:321-409 GBM, 592-690 Heston) then
+// level_samples (mlmc.rs:276-305): ys[i] = PV(fine path i) - PV(coarse path i),
+// the coarse path stepping with the sum of two fine normals. `seed` is the
+// level's seed mix(cfg.seed, level) (mlmc.rs:288); path i draws the Philox
+// stream keyed by mix(seed, level + 1), where the reference seeds its path
+// generator with mix(mix(seed, level + 1), i) (simulator.rs:345).
+static void level_values(const Con &con, const Model &m, double t_max, uint32_t level, uint64_t n, uint64_t seed,
+                         double rate, std::vector<double> &ys) {
+    const uint64_t nf = 1ull << level;
+    const bool coarse = level > 0;
+    const uint64_t nc = coarse ? nf / 2 : 0;
+    const std::vector<double> gf = uniform_grid(t_max, nf);
+    const std::vector<double> gc = coarse ? uniform_grid(t_max, nc) : std::vector<double>();
+    const double dt_f = t_max / (double)nf;
+    const double sqrt_dt_f = std::sqrt(dt_f);
+    NormalSource ns;
+    ns.seed = mix(seed, (uint64_t)level + 1);
+    const bool gbm = m.kind == KX_MODEL_GBM;
+    const size_t dpp = (gbm ? 1 : 2) * nf;
+    ys.assign(n, 0.0);
+    const double rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
+    // Heston Euler step with the floor on v (simulator.rs:615-633)
+    auto heston_row = [&](const std::vector<std::pair<double, double>> &incs, double dt, double *row) {
+        const double sqrt_dt = std::sqrt(dt);
+        double sp = m.s0, v = std::max(m.v0, 0.0);
+        row[0] = sp;
+        for (size_t k = 0; k < incs.size(); ++k) {
+            const double sqrt_v = std::sqrt(v);
+            const double dw_s = incs[k].first * sqrt_dt;
+            const double dw_v = (m.rho * incs[k].first + rho_perp * incs[k].second) * sqrt_dt;
+            sp *= std::exp(m.r * dt - 0.5 * v * dt + sqrt_v * dw_s);
+            v = std::max(v + m.kappa * (m.theta - v) * dt + m.sigma_v * sqrt_v * dw_v, 0.0);
+            row[k + 1] = sp;
+        }
+    };
+    int err_code = 0;
+    std::string err_msg;
+#pragma omp parallel num_threads(g_threads > 0 ? g_threads : omp_get_max_threads())
+    {
+        std::vector<double> z(std::max<size_t>(dpp, 1)), rf(gf.size()), rc(std::max<size_t>(gc.size(), 1));
+        std::vector<std::pair<double, double>> inc;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t i = 0; i < (int64_t)n; ++i) {
+            if (err_code) continue;
+            try {
+                ns.fill((uint64_t)i, dpp, z.data());
+                if (gbm) {
+                    const double drift_f = (m.mu - 0.5 * m.sigma * m.sigma) * dt_f;
+                    double sp = m.s0;
+                    rf[0] = sp;
+                    for (uint64_t k = 0; k < nf; ++k) {
+                        sp *= std::exp(drift_f + m.sigma * sqrt_dt_f * z[k]);
+                        rf[k + 1] = sp;
+                    }
+                    if (coarse) {
+                        const double dt_c = t_max / (double)nc;
+                        const double drift_c = (m.mu - 0.5 * m.sigma * m.sigma) * dt_c;
+                        sp = m.s0;
+                        rc[0] = sp;
+                        for (uint64_t j = 0; j < nc; ++j) {
+                            const double dw = z[2 * j] + z[2 * j + 1];
+                            sp *= std::exp(drift_c + m.sigma * sqrt_dt_f * dw);
+                            rc[j + 1] = sp;
+                        }
+                    }
+                } else {
+                    inc.resize(nf);
+                    for (uint64_t k = 0; k < nf; ++k) inc[k] = {z[2 * k], z[2 * k + 1]};
+                    heston_row(inc, dt_f, rf.data());
+                    if (coarse) {
+                        const double inv_sqrt2 = 0.70710678118654752440;
+                        std::vector<std::pair<double, double>> ic(nc);
+                        for (uint64_t j = 0; j < nc; ++j)
+                            ic[j] = {(inc[2 * j].first + inc[2 * j + 1].first) * inv_sqrt2,
+                                     (inc[2 * j].second + inc[2 * j + 1].second) * inv_sqrt2};
+                        heston_row(ic, t_max / (double)nc, rc.data());
+                    }
+                }
+                PathView pf{&gf, rf.data(), &m.asset};
+                const double vf = present_value(con, pf, gf, rate);
+                double vc = 0.0;
+                if (coarse) {
+                    PathView pc{&gc, rc.data(), &m.asset};
+                    vc = present_value(con, pc, gc, rate);
+                }
+                ys[(size_t)i] = vf - vc;
+            } catch (const KxError &e) {
+#pragma omp critical
+                if (!err_code) { err_code = e.code; err_msg = e.msg; }
+            }
+        }
+    }
+    if (err_code) fail(err_code, err_msg);
+}
+
+// mean_var (mlmc.rs:318-332): two-pass mean and unbiased variance
+static void mean_var(const std::vector<double> &xs, double &mean, double &var) {
+    const size_t n = xs.size();
+    mean = var = 0.0;
+    if (n == 0) return;
+    double s = 0.0;
+    for (double x : xs) s += x;
+    mean = s / (double)n;
+    if (n > 1) {
+        double q = 0.0;
+        for (double x : xs) q += (x - mean) * (x - mean);
+        var = q / ((double)n - 1.0);
+    }
+}
+
+int ko_mlmc_level_values(const char *json, const kx_model *model, const kx_mc_config *cfg, uint32_t level,
+                         uint64_t n, double *ys) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        Model m = to_model(model);
+        kx_mc_config mc = check_cfg(cfg);
+        validate_model(m);
+        Plan p = compile(*c);
+        std::vector<double> v;
+        level_values(*c, m, p.horizon, level, n, mix(mc.seed, level), mc.rate, v);  // mlmc.rs:288
+        memcpy(ys, v.data(), n * sizeof(double));
+    });
+}
+
+// optimal_allocation (mlmc.rs:231-258)
+static std::vector<uint64_t> optimal_allocation(const std::vector<double> &v, const std::vector<uint64_t> &c,
+                                                double target) {
+    const size_t l = std::min(v.size(), c.size());
+    std::vector<uint64_t> out(l, 0);
+    if (l == 0 || target <= 0.0) return out;
+    double sum = 0.0;
+    for (size_t k = 0; k < l; ++k) sum += std::sqrt(std::max(v[k], 0.0) * (double)std::max<uint64_t>(c[k], 1));
+    for (size_t k = 0; k < l; ++k) {
+        const double vk = std::max(v[k], 0.0), ck = (double)std::max<uint64_t>(c[k], 1);
+        if (vk <= 0.0) {
+            out[k] = 1;
+            continue;
+        }
+        out[k] = std::max<uint64_t>((uint64_t)std::ceil((sum * std::sqrt(vk / ck)) / target), 1);
+    }
+    return out;
+}
+
+int ko_mlmc_optimal_allocation(const double *v, const uint64_t *c, size_t n, double target, uint64_t *out) {
+    return run([&] {
+        auto r = optimal_allocation(std::vector<double>(v, v + n), std::vector<uint64_t>(c, c + n), target);
+        for (size_t k = 0; k < n; ++k) out[k] = r[k];
+    });
+}
+
+// price_mlmc_detailed (mlmc.rs:107-215)
+int ko_price_mlmc(const char *json, const kx_model *model, const kx_mc_config *cfg, const kx_mlmc_cfg *mcfg,
+                  kx_mlmc_result *out) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        Model m = to_model(model);
+        kx_mc_config mc = check_cfg(cfg);
+        validate_model(m);
+        const uint32_t L = mcfg->n_levels;
+        if (L > KX_MLMC_MAX_LEVELS) fail(KX_INVALID_ARGUMENT, "too many levels");
+        Plan p = compile(*c);
+        const double t_max = p.horizon;
+        std::vector<uint64_t> costs(L + 1);
+        for (uint32_t l = 0; l <= L; ++l)
+            costs[l] = (l == 0 ? 1 : (1ull << l) + (1ull << (l - 1))) * std::max<uint32_t>(mcfg->cost_per_step, 1);
+        std::vector<double> means(L + 1, 0.0), var(L + 1, 0.0), sums(L + 1, 0.0), sumsq(L + 1, 0.0);
+        std::vector<uint64_t> counts(L + 1, 0);
+        std::vector<double> ys;
+        for (uint32_t l = 0; l <= L; ++l) {
+            ys.clear();
+            if (mcfg->pilot_paths) level_values(*c, m, t_max, l, mcfg->pilot_paths, mix(mc.seed, l), mc.rate, ys);
+            mean_var(ys, means[l], var[l]);
+            for (double y : ys) sums[l] += y;
+            for (double y : ys) sumsq[l] += y * y;
+            counts[l] = ys.size();
+        }
+        auto extra = optimal_allocation(var, costs, mcfg->target_variance);
+        const uint64_t seed_main = mc.seed ^ 0xA5A55A5ADEADBEEFull;
+        for (uint32_t l = 0; l <= L; ++l) {
+            if (extra[l] == 0) continue;
+            level_values(*c, m, t_max, l, extra[l], mix(seed_main, l), mc.rate, ys);
+            double s = 0.0, q = 0.0;
+            for (double y : ys) s += y;
+            for (double y : ys) q += y * y;
+            sums[l] += s;
+            sumsq[l] += q;
+            counts[l] += ys.size();
+        }
+        memset(out, 0, sizeof *out);
+        out->n_levels = L;
+        double price = 0.0, var_q = 0.0;
+        uint64_t n_total = 0, total_cost = 0;
+        for (uint32_t l = 0; l <= L; ++l) {
+            const double n = (double)std::max<uint64_t>(counts[l], 1);
+            const double mean = sums[l] / n;
+            const double v = counts[l] > 1 ? std::max((sumsq[l] - n * mean * mean) / (n - 1.0), 0.0) : 0.0;
+            out->level_means[l] = mean;
+            out->level_variances[l] = v;
+            out->level_costs[l] = costs[l];
+            out->level_paths[l] = counts[l];
+            price += mean;
+            var_q += v / n;
+            n_total += counts[l];
+            total_cost += counts[l] * costs[l];
+        }
+        const double se = std::sqrt(std::max(var_q, 0.0));
+        const double Z95 = 1.959963984540054;
+        out->price.price = price;
+        out->price.std_error = se;
+        out->price.sample_std = se * std::sqrt((double)std::max<uint64_t>(n_total, 1));
+        out->price.ci95_low = price - Z95 * se;
+        out->price.ci95_high = price + Z95 * se;
+        out->price.n_paths = n_total;
+        out->total_cost = total_cost;
+    });
+}
+
 int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
                             size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
     return run([&] {
