@@ -411,6 +411,50 @@ def heston_calibration(cpu_seconds=6.0) -> dict:
     return out
 
 
+def mlmc_heston() -> dict:
+    """price_mlmc_detailed (mlmc.rs:107-215) on a European call under Heston
+    (s0 100, v0 0.04, kappa 1.5, theta 0.04, sigma_v 0.3, rho -0.7, r 0.05,
+    T 1): 9 levels (2^0 .. 2^8 steps), 2,000 pilot paths, target standard
+    error 0.005, seed 11; per phase one fine and one coarse path launch for
+    all levels. Against the oracle (the reference's level loop restated, all
+    host threads) on the same configuration, and against plain Monte Carlo on
+    the GPU at the finest grid and the same standard error (the reference's
+    mlmc_cheaper_than_standard_mc comparison)."""
+    import kontracts_gb300 as kx
+    from oracle import Oracle
+    c = kx.european_call("S", 100.0, 1.0)
+    h = kx.heston(100.0, 0.04, 1.5, 0.04, 0.3, -0.7, 0.05, asset="S")
+    cfg = kx.MlmcConfig(n_levels=8, pilot_paths=2000, target_variance=0.005 ** 2)
+    out = {"workload": "Heston call MLMC, levels 0..8, pilot 2000, target SE 0.005, seed 11"}
+    for prec in ("fp64", "fp32"):
+        kx.price_mlmc_detailed(c, h, kx.MlmcConfig(n_levels=8, pilot_paths=2000, target_variance=0.05 ** 2),
+                               seed=11, precision=prec)  # tune + warm
+        t0 = time.perf_counter()
+        d = kx.price_mlmc_detailed(c, h, cfg, seed=11, precision=prec)
+        wall = time.perf_counter() - t0
+        out[prec] = {"wall_seconds": wall, "price": d.price.price, "std_error": d.price.std_error,
+                     "level_paths": d.level_paths, "total_cost_steps": d.total_cost,
+                     "path_steps_per_s": d.total_cost / wall}
+    orc = Oracle()
+    t0 = time.perf_counter()
+    r = orc.price_mlmc(c.to_json(), h, n_levels=8, pilot_paths=2000, target_variance=0.005 ** 2, seed=11)
+    cpu = time.perf_counter() - t0
+    out["cpu_baseline"] = {"wall_seconds": cpu, "price": r["price"].price, "cores": orc.threads(), "kind": "port",
+                           "path_steps_per_s": r["total_cost"] / cpu, "sample": "the whole configuration"}
+    out["gpu_fp64_vs_cpu_price_diff"] = out["fp64"]["price"] - r["price"].price
+    out["gpu_fp64_over_cpu_wall"] = cpu / out["fp64"]["wall_seconds"]
+    # plain Monte Carlo on the 2^8-step grid at the same standard error, on the GPU (FP64)
+    pilot = c.price(h, n_paths=30_000, seed=99, steps_per_year=256, precision="fp64")
+    n_std = int((pilot.sample_std / 0.005) ** 2) + 1
+    t0 = time.perf_counter()
+    std = c.price(h, n_paths=n_std, seed=99, steps_per_year=256, precision="fp64")
+    t_std = time.perf_counter() - t0
+    out["plain_mc_same_se_fp64"] = {"n_paths": n_std, "wall_seconds": t_std, "price": std.price,
+                                    "std_error": std.std_error, "cost_steps": n_std * 256}
+    out["mlmc_speedup_over_plain_mc_fp64"] = t_std / out["fp64"]["wall_seconds"]
+    return out
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -645,7 +689,7 @@ def run_ours(args, ws, rank, local) -> None:
                                  "book_256": book_256(), "lsm_12": lsm_cases(),
                                  "variance_reduction": variance_reduction(),
                                  "greek_surface_99": greek_surface_grid(),
-                                 "heston_calibration": heston_calibration()}
+                                 "heston_calibration": heston_calibration(), "mlmc_heston": mlmc_heston()}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.cpu_seconds)
         line["accuracy"] = accuracy(cb)
