@@ -54,7 +54,7 @@ typedef struct kx_program kx_program; /* compiled + lowered contract (opaque) */
  * Mirrors Gbm (src/simulator.rs:188-199) and HestonSimulator
  * (src/simulator.rs:453-471). `asset` is the name the contract's Spot(...)
  * observables must use (Simulator::asset_name, simulator.rs:98). */
-enum { KX_MODEL_GBM = 0, KX_MODEL_HESTON = 1 };
+enum { KX_MODEL_GBM = 0, KX_MODEL_HESTON = 1, KX_MODEL_MULTI_GBM = 2 /* kx_multi_gbm only */ };
 
 /* Heston discretisation. REFERENCE_FLOOR is the reference's scheme
  * (Euler step, then v = max(v, 0); simulator.rs:517-534) and is the default.
@@ -317,6 +317,28 @@ kx_status kx_calib_gbm_prices(const kx_program *prog, const char *asset, const d
 kx_status kx_calib_heston_objective(const kx_program *prog, const char *asset, const double *quotes, size_t n_quotes,
                                     const double *params, size_t n_params, const kx_mc_config *cfg, double *obj,
                                     double *prices);
+
+/* ---- correlated multi-factor GBM ------------------------------------------
+ * Mirrors CorrelatedGbmN (src/multi_asset.rs:49-105) with its GbmFactor list
+ * (src/fx.rs:149-169): n_assets >= 2 named factors (s0, mu, sigma) and their
+ * n x n correlation, row-major in corr[i * n_assets + j]. */
+#define KX_MAX_ASSETS 7
+typedef struct kx_multi_gbm {
+    uint32_t n_assets;
+    uint32_t reserved;
+    const char *names[KX_MAX_ASSETS];
+    double s0[KX_MAX_ASSETS], mu[KX_MAX_ASSETS], sigma[KX_MAX_ASSETS];
+    double corr[KX_MAX_ASSETS * KX_MAX_ASSETS];
+} kx_multi_gbm;
+
+/* price_gbm (src/pricer.rs:97) under a CorrelatedGbmN: every Spot(name) of the
+ * contract reads its factor; each grid step draws n_assets normals, correlates
+ * them with the lower Cholesky factor (numerics.rs:158-183) and steps every
+ * factor exactly in log space (multi_asset.rs:85-170). The general path kernel
+ * (M_MULTI). Fewer than 2 factors or a negative volatility is
+ * KX_MALFORMED_CONTRACT, a spot of no factor KX_UNKNOWN_ASSET. */
+kx_status kx_price_multi(const kx_program *prog, const kx_multi_gbm *model, const kx_mc_config *cfg,
+                         kx_price_result *out, double *per_path_pv);
 
 /* ---- multilevel Monte Carlo ----------------------------------------------
  * Mirrors MlmcConfig (src/mlmc.rs:50-72; defaults n_levels 6, pilot_paths

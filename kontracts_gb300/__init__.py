@@ -283,6 +283,34 @@ class Model:
         return f"Model({self.label}, rate={self.rate})"
 
 
+class CorrelatedGbmN:
+    """Correlated GBM factors (src/multi_asset.rs:49-105): `factors` is a list
+    of (name, s0, mu, sigma) as GbmFactor::new (src/fx.rs:160-169) and `corr`
+    their n x n correlation. `rate` discounts the flows (McConfig.rate)."""
+
+    def __init__(self, factors: Sequence[tuple], corr: Sequence[Sequence[float]], rate: float = 0.0):
+        self.factors = [(str(n), float(s0), float(mu), float(sg)) for n, s0, mu, sg in factors]
+        self.corr = [[float(x) for x in row] for row in corr]
+        self.rate = float(rate)
+        k = len(self.factors)
+        if k > _abi.KX_MAX_ASSETS:
+            raise ValueError(f"at most {_abi.KX_MAX_ASSETS} factors")
+        if len(self.corr) != k or any(len(r) != k for r in self.corr):
+            raise KontractError(_abi.KX_MALFORMED_CONTRACT,
+                                f"CorrelatedGbmN: the correlation matrix must be {k}x{k}")  # multi_asset.rs:69-73
+
+    def _c(self) -> _abi.KxMultiGbm:
+        k = len(self.factors)
+        m = _abi.KxMultiGbm(n_assets=k)
+        self._names = [n.encode() for n, _, _, _ in self.factors]  # keep the bytes alive
+        for i, (n, s0, mu, sg) in enumerate(self.factors):
+            m.names[i] = self._names[i]
+            m.s0[i], m.mu[i], m.sigma[i] = s0, mu, sg
+            for j in range(k):
+                m.corr[i * k + j] = self.corr[i][j]
+        return m
+
+
 def heston(spot: float, v0: float, kappa: float, theta: float, sigma_v: float, rho: float, r: float,
            asset: str = "ASSET", scheme: str = "reference") -> Model:
     """Heston model (src/bindings.rs:547-567). `scheme`: "reference" (Euler
@@ -397,8 +425,20 @@ class Contract:
         reference's variance reduction (pricer.rs:108-230): antithetic pairs
         for GBM models, the at-the-money call as a control (no per-path
         values then)."""
+        if isinstance(model, CorrelatedGbmN):
+            if antithetic or control_variate:
+                raise KontractError(_abi.KX_UNSUPPORTED, "variance reduction needs a one-asset model")
+            mm = model._c()
+            cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, shared_draws)
+            res = _abi.KxPriceResult()
+            pp = (C.c_double * max(1, int(n_paths)))() if per_path else None
+            with _lock:
+                _check(_lib().kx_price_multi(self._handle().h, C.byref(mm), C.byref(cfg), C.byref(res), pp))
+            if per_path:
+                return PriceResult(res), list(pp[: int(n_paths)])
+            return PriceResult(res)
         if not isinstance(model, (GBM, Model)):
-            raise TypeError("expected a GBM or Model")
+            raise TypeError("expected a GBM, Model or CorrelatedGbmN")
         cm = model._c()
         cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, shared_draws)
         cfg.flags = (_abi.KX_VR_ANTITHETIC if antithetic else 0) | (_abi.KX_VR_CONTROL_VARIATE if control_variate else 0)
@@ -839,7 +879,7 @@ __all__ = [
     "until", "and_", "or_", "USD", "EUR", "GBP", "JPY", "average", "average_over", "running_max",
     "running_min", "heston", "zero_coupon_bond", "european_call", "european_put", "forward", "straddle",
     "bull_call_spread", "cash_or_nothing_call", "up_and_out_call", "down_and_out_call", "price_batch",
-    "price_american_batch", "GreekSurface", "greek_surface", "fit_gbm_volatility",
+    "price_american_batch", "GreekSurface", "greek_surface", "fit_gbm_volatility", "CorrelatedGbmN",
     "price_portfolio", "set_shared_draws", "last_launch_stats",
 ]
 

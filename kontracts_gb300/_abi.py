@@ -73,6 +73,15 @@ class KxBumps(C.Structure):
     ]
 
 
+KX_MAX_ASSETS = 7
+
+
+class KxMultiGbm(C.Structure):
+    _fields_ = [("n_assets", C.c_uint32), ("reserved", C.c_uint32), ("names", C.c_char_p * KX_MAX_ASSETS),
+                ("s0", C.c_double * KX_MAX_ASSETS), ("mu", C.c_double * KX_MAX_ASSETS),
+                ("sigma", C.c_double * KX_MAX_ASSETS), ("corr", C.c_double * (KX_MAX_ASSETS * KX_MAX_ASSETS))]
+
+
 KX_MLMC_MAX_LEVELS = 20
 
 
@@ -183,6 +192,8 @@ SIGNATURES = {
                                          C.POINTER(C.c_double)]),
     "kx_mlmc_optimal_allocation": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t, C.c_double,
                                              C.POINTER(C.c_uint64)]),
+    "kx_price_multi": (C.c_int, [_P, C.POINTER(KxMultiGbm), C.POINTER(KxMcConfig), C.POINTER(KxPriceResult),
+                                 C.POINTER(C.c_double)]),
     "kx_greeks_adjoint": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                     C.POINTER(KxAdjointCfg), C.POINTER(KxSens)]),
     "kx_price_american_lsm": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),

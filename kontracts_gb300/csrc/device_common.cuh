@@ -195,7 +195,8 @@ struct EvalOut {
 
 template <class Real>
 __device__ __noinline__ EvalOut<Real> eval_code_impl(const KxProgram *__restrict__ Pp, int off, int len, Real *acc_base,
-                                                     int acc_stride, uint32_t poisoned, int k, Real S) {
+                                                     int acc_stride, uint32_t poisoned, int k, Real S,
+                                                     const Real *Sx) {
     const KxProgram &P = *Pp;
     const AccView<Real> acc{acc_base, acc_stride};
     Real st[KX_MAX_STACK];
@@ -205,7 +206,7 @@ __device__ __noinline__ EvalOut<Real> eval_code_impl(const KxProgram *__restrict
         const KxIns ins = P.code[pc];
         switch (ins.op) {
         case OP_CONST: st[sp] = (Real)P.cpool[ins.arg]; eb[sp++] = 0; break;
-        case OP_SPOT: st[sp] = S; eb[sp++] = 0; break;
+        case OP_SPOT: st[sp] = Sx ? Sx[ins.arg] : S; eb[sp++] = 0; break;  // Sx: the spots of a multi-asset path
         case OP_ACC: {
             uint32_t e = 0;
             st[sp] = acc_value<Real>(P, ins.arg, acc, poisoned, k, e);
@@ -251,8 +252,8 @@ __device__ __noinline__ EvalOut<Real> eval_code_impl(const KxProgram *__restrict
 // the per-step path that calls it.
 template <class Real>
 __device__ __forceinline__ Real eval_code(const KxProgram &P, int off, int len, AccView<Real> acc, uint32_t poisoned,
-                                          int k, Real S, uint32_t &err) {
-    const EvalOut<Real> o = eval_code_impl<Real>(&P, off, len, acc.base, acc.stride, poisoned, k, S);
+                                          int k, Real S, uint32_t &err, const Real *Sx = nullptr) {
+    const EvalOut<Real> o = eval_code_impl<Real>(&P, off, len, acc.base, acc.stride, poisoned, k, S, Sx);
     err |= o.err;
     return o.v;
 }

@@ -34,7 +34,7 @@
 // expression opcodes (postfix, one stack of reals and booleans)
 enum KxOp : uint8_t {
     OP_CONST = 0,  // push cpool[arg]
-    OP_SPOT,       // push S at the current step
+    OP_SPOT,       // push S of asset arg at the current step (arg 0 on one-asset models)
     OP_ACC,        // push value of accumulator arg
     OP_NEG,
     OP_ADD,
@@ -107,7 +107,7 @@ struct KxAcc {
     uint8_t kind;       // KxAccKind
     uint8_t inner;      // KxInnerKind
     uint8_t fixed;      // ACC_SUM: window end given (to_year = Some)
-    uint8_t pad;
+    uint8_t pad;        // IK_SPOT: the asset it reads (0 on one-asset models)
     uint16_t code_off;  // IK_GENERAL inner program
     uint16_t code_len;
     // bound to a grid (host fills these per launch):

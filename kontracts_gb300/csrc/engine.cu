@@ -217,6 +217,10 @@ Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, const st
     validate_model(m);
     validate_grid(grid);
     std::vector<Scenario> scen = scen_in;
+    if (m.kind == KX_MODEL_MULTI_GBM) {  // factor i in the per-scenario slots i (M_MULTI)
+        scen.clear();
+        for (size_t i = 0; i < m.assets.size(); ++i) scen.push_back(Scenario{m.a_s0[i], m.a_mu[i], m.a_sigma[i], cfg.rate});
+    }
     if (scen.empty()) scen.push_back(Scenario{m.s0, m.mu, m.sigma, cfg.rate});
     const int ns = (int)scen.size();
     Model m0 = m;
@@ -266,6 +270,13 @@ Job make_job(const Program &p, const Model &m, const kx_mc_config &cfg, const st
         d.driftf[s] = (float)d.drift[s];
         d.sigmaf[s] = (float)d.sigma[s];
     }
+    if (m.kind == KX_MODEL_MULTI_GBM) {
+        d.n_assets = (int32_t)m.assets.size();
+        for (size_t q = 0; q < m.chol.size(); ++q) {
+            d.chol[q] = m.chol[q];
+            d.cholf[q] = (float)m.chol[q];
+        }
+    }
     d.v0 = m.v0; d.kappa = m.kappa; d.theta = m.theta; d.sigma_v = m.sigma_v; d.rho = m.rho;
     d.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));  // simulator.rs:510
     d.r = m.r;
@@ -304,6 +315,7 @@ template void pack_steps<double>(const StepTables &, std::vector<unsigned char> 
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
 const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat, bool acc) {
+    if (model == KX_MODEL_MULTI_GBM) return paths_kernel_multi(f64);  // general handler, one budget
     if (lean)
         return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc) : lean_kernel_heston(f64, minb, stat, acc);
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
@@ -326,6 +338,7 @@ static bool lean_applies(const std::vector<Job> &jobs, int ns) {
     if (ns != 1) return false;
     bool avg = false;
     for (auto &j : jobs) {
+        if (j.model.kind == KX_MODEL_MULTI_GBM) return false;
         if (j.dev.smooth) return false;
         if (j.prog.n_acc && !lean_average(j.prog)) return false;
         // the spot each step: for the average (kept by k_lean) or a general condition (not served)
@@ -1437,6 +1450,45 @@ static void check_mlmc_model(const Model &m) {
         raise(KX_UNSUPPORTED, "level pairs follow the reference Heston scheme (floor after the step)");
 }
 
+// CorrelatedGbmN::new (multi_asset.rs:62-83): at least two factors, a
+// correlation of their size (implied by the struct), no negative volatility;
+// its lower Cholesky factor as numerics::cholesky_lower (numerics.rs:158-183),
+// diagonal pivots floored at 0 and columns under a zero pivot set to 0.
+static Model multi_model(const kx_multi_gbm &mm) {
+    const uint32_t n = mm.n_assets;
+    if (n < 2) raise(KX_MALFORMED_CONTRACT, "CorrelatedGbmN: at least 2 assets required");
+    if (n > KX_MAX_ASSETS) raise(KX_INVALID_ARGUMENT, "more than KX_MAX_ASSETS factors");
+    Model m;
+    m.kind = KX_MODEL_MULTI_GBM;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!mm.names[i]) raise(KX_INVALID_ARGUMENT, "factor name is NULL");
+        if (mm.sigma[i] < 0.0) raise(KX_MALFORMED_CONTRACT, "CorrelatedGbmN: every volatility must be >= 0");
+        m.assets.push_back(mm.names[i]);
+        m.a_s0.push_back(mm.s0[i]);
+        m.a_mu.push_back(mm.mu[i]);
+        m.a_sigma.push_back(mm.sigma[i]);
+    }
+    std::vector<double> l(n * n, 0.0);
+    for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t j = 0; j <= i; ++j) {
+            double sum = mm.corr[i * n + j];
+            for (uint32_t k = 0; k < j; ++k) sum -= l[i * n + k] * l[j * n + k];
+            if (i == j) {
+                l[i * n + j] = std::sqrt(std::max(sum, 0.0));
+            } else {
+                const double pivot = l[j * n + j];
+                l[i * n + j] = pivot > 0.0 ? sum / pivot : 0.0;
+            }
+        }
+    for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t j = 0; j <= i; ++j) m.chol.push_back(l[i * n + j]);
+    m.asset = m.assets[0];
+    m.s0 = m.a_s0[0];
+    m.mu = m.a_mu[0];
+    m.sigma = m.a_sigma[0];
+    return m;
+}
+
 // Upper bound of the per-path values one surface launch keeps in HBM (seven
 // doubles per path and cell); larger surfaces run as several launches.
 static constexpr uint64_t SURFACE_PV_BYTES = 8ull << 30;
@@ -1746,6 +1798,33 @@ kx_status kx_price_mlmc(const kx_program *prog, const kx_model *model, const kx_
         out->price.ci95_high = price + Z95 * se;
         out->price.n_paths = n_total;
         out->total_cost = total_cost;
+        end_call(c);
+    });
+}
+
+kx_status kx_price_multi(const kx_program *prog, const kx_multi_gbm *model, const kx_mc_config *cfg,
+                         kx_price_result *out, double *per_path_pv) {
+    return guarded([&] {
+        const Program &p = program_of(prog);
+        if (!model || !out) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        check_cfg(cfg);
+        const Model m = multi_model(*model);
+        auto grid = time_grid_forced(p.plan, cfg->steps_per_year, false);
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        begin_call(c);
+        std::vector<Job> jobs;
+        jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
+        uint64_t stride = 0;
+        run_paths(c, jobs, *cfg, 1, stride);
+        std::vector<StatsJob> sj(1);
+        sj[0].n = cfg->n_paths;
+        *out = finish(device_stats(c, c.pv.as<double>(), stride, sj)[0]);
+        if (per_path_pv && cfg->n_paths) {
+            KX_CUDA(cudaMemcpyAsync(per_path_pv, c.pv.p, cfg->n_paths * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            KX_CUDA(cudaStreamSynchronize(c.stream));
+            c.last.d2h_bytes += cfg->n_paths * sizeof(double);
+        }
         end_call(c);
     });
 }

@@ -403,7 +403,7 @@ struct Lowerer {
         a.kind = n.k == NK::RunningMax ? ACC_MAX : n.k == NK::RunningMin ? ACC_MIN : ACC_SUM;
         if (inner.k == NK::Spot) {
             a.inner = IK_SPOT;
-            note_spot(inner);
+            a.pad = (uint8_t)note_spot(inner);  // the asset it reads
         } else {
             a.inner = IK_GENERAL;
             int start = P.n_code;
@@ -428,16 +428,19 @@ struct Lowerer {
         acc_nodes.emplace_back(&n, slot);
         return slot;
     }
-    void note_spot(const Node &n) {
-        if (std::find(L.spot_assets.begin(), L.spot_assets.end(), n.text) == L.spot_assets.end())
-            L.spot_assets.push_back(n.text);
+    // Index of the spot's asset in the program's asset list (order of appearance).
+    int note_spot(const Node &n) {
+        auto it = std::find(L.spot_assets.begin(), L.spot_assets.end(), n.text);
+        if (it != L.spot_assets.end()) return (int)(it - L.spot_assets.begin());
+        L.spot_assets.push_back(n.text);
+        return (int)L.spot_assets.size() - 1;
     }
 
     // Observable -> postfix code; returns the stack depth it needs.
     int obs(const Node &n) {
         switch (n.k) {
         case NK::Const: emit(OP_CONST, konst(n.num)); return 1;
-        case NK::Spot: note_spot(n); emit(OP_SPOT); return 1;
+        case NK::Spot: emit(OP_SPOT, (uint16_t)note_spot(n)); return 1;
         case NK::Neg: { int d = obs(*n.kid[0]); emit(OP_NEG); return d; }
         case NK::Add: case NK::Sub: case NK::Mul: case NK::Div: case NK::Max: case NK::Min: {
             int a = obs(*n.kid[0]);
@@ -720,7 +723,10 @@ Model model_from_c(const kx_model *m) {
 }
 
 void validate_model(const Model &m) {
-    if (m.kind == KX_MODEL_GBM) {
+    if (m.kind == KX_MODEL_MULTI_GBM) {
+        for (double sg : m.a_sigma)
+            if (sg < 0.0) raise(KX_MALFORMED_CONTRACT, "CorrelatedGbmN: every volatility must be >= 0");
+    } else if (m.kind == KX_MODEL_GBM) {
         if (m.sigma < 0.0) raise(KX_MALFORMED_CONTRACT, "GBM sigma must be non-negative");  // simulator.rs:221-225
     } else {                                                                               // simulator.rs:556-580
         if (!(m.rho >= -1.0 && m.rho <= 1.0)) raise(KX_MALFORMED_CONTRACT, "Heston rho must be in [-1, 1]");
@@ -764,8 +770,29 @@ void bind(const Lowered &low, const std::vector<double> &grid, const Model &m, d
     P = low.prog;
     const int n = (int)grid.size();
     P.n_times = n;
-    for (auto &a : low.spot_assets)
-        if (a != m.asset) raise(KX_UNKNOWN_ASSET, a);  // observable.rs:78-87
+    if (m.kind == KX_MODEL_MULTI_GBM) {
+        // the program's assets -> the model's factors (observable.rs:78-87): OP_SPOT and
+        // spot accumulators read the factor's index; every price condition and amount goes
+        // through the interpreter (the closed forms read one spot)
+        std::vector<int> idx;
+        for (auto &a : low.spot_assets) {
+            auto it = std::find(m.assets.begin(), m.assets.end(), a);
+            if (it == m.assets.end()) raise(KX_UNKNOWN_ASSET, a);
+            idx.push_back((int)(it - m.assets.begin()));
+        }
+        for (int c = 0; c < P.n_code; ++c)
+            if (P.code[c].op == OP_SPOT) P.code[c].arg = (uint16_t)idx[P.code[c].arg];
+        for (int a = 0; a < P.n_acc; ++a)
+            if (P.acc[a].inner == IK_SPOT) P.acc[a].pad = (uint8_t)idx[P.acc[a].pad];
+        for (int i = 0; i < P.n_leaf; ++i) P.leaf[i].fast = FA_NONE;
+        P.simple_leaves = 0;
+        for (int i = 0; i < P.n_trig; ++i)
+            if (P.trig[i].cond_kind == CK_SPOT_CMP) P.trig[i].cond_kind = CK_GENERAL;
+        P.spot_each_step = 1;
+    } else {
+        for (auto &a : low.spot_assets)
+            if (a != m.asset) raise(KX_UNKNOWN_ASSET, a);  // observable.rs:78-87
+    }
     if (low.has_running_average)
         for (int e = 0; e + 1 < n; ++e)
             if (grid[e + 1] <= grid[e] + 1e-12)

@@ -96,8 +96,15 @@ struct Model {
     double s0 = 100, mu = 0, sigma = 0.2;
     double v0 = 0.04, kappa = 1, theta = 0.04, sigma_v = 0, rho = 0, r = 0;
     std::string asset = "ASSET";
+    // KX_MODEL_MULTI_GBM (CorrelatedGbmN, multi_asset.rs:49-105): the factors'
+    // names, spots, drifts and volatilities, and the packed lower Cholesky
+    // factor of their correlation (row i: chol[i (i + 1) / 2 + j], j <= i)
+    std::vector<std::string> assets;
+    std::vector<double> a_s0, a_mu, a_sigma, chol;
     bool requires_fine_grid() const { return kind == KX_MODEL_HESTON; }
-    int draws_per_step() const { return kind == KX_MODEL_HESTON ? 2 : 1; }
+    int draws_per_step() const {
+        return kind == KX_MODEL_HESTON ? 2 : kind == KX_MODEL_MULTI_GBM ? (int)assets.size() : 1;
+    }
 };
 Model model_from_c(const kx_model *m);
 void validate_model(const Model &m);

@@ -53,6 +53,12 @@ struct ContractDev {
     float v0f, kappaf, thetaf, sigma_vf, rhof, rho_perpf, rf, inv_wf;
     uint32_t item_paths;  // paths per work item of this contract (arithmetic items)
     uint32_t path_base;   // index of its first path in the stream
+    // M_MULTI: factors (s0 / drift / sigma above hold factor i at index i) and the
+    // packed lower Cholesky factor of their correlation, row i at i (i + 1) / 2
+    int32_t n_assets;
+    int32_t pad_assets;
+    double chol[KX_MAX_NS * (KX_MAX_NS + 1) / 2];
+    float cholf[KX_MAX_NS * (KX_MAX_NS + 1) / 2];
 };
 
 struct WorkItem {
@@ -115,7 +121,10 @@ __device__ __forceinline__ WorkItem fetch_item(const PathArgs &A, int it) {
 // multilevel Monte-Carlo pair (simulator.rs:321-409, 592-690): every coarse
 // step consumes the normals of two fine steps of the same Philox stream, so a
 // coarse job on the seed and path indices of its fine job is coupled to it.
-enum { M_GBM = 0, M_HESTON = 1, M_GBM_PAIR = 2, M_HESTON_PAIR = 3 };
+enum { M_GBM = 0, M_HESTON = 1, M_GBM_PAIR = 2, M_HESTON_PAIR = 3, M_MULTI = 4 };
+// M_MULTI: n_assets correlated GBM factors (CorrelatedGbmN, multi_asset.rs:107-170):
+// each step draws n_assets normals z, correlates them with the lower Cholesky
+// factor (w = L z) and steps factor i with its own drift and volatility.
 
 // Per-contract values a warp keeps in registers: only what the per-step hot
 // path reads. Everything else is read from the (L1-resident) program table
@@ -228,7 +237,7 @@ __device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, R
 template <class Real>
 __device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const StepRec<Real> *R, const Real *thr,
                                                    bool smooth, Real y, Real S, uint32_t poisoned, uint32_t mask, int k,
-                                                   AccView<Real> acc, uint32_t &err) {
+                                                   AccView<Real> acc, uint32_t &err, const Real *Sx) {
     uint32_t bits = mask & P.time_mask;
     if (bits) bits &= R[k].tt;
     uint32_t pm = mask & ~P.time_mask;
@@ -241,7 +250,7 @@ __device__ __forceinline__ uint32_t cond_bits_full(const KxProgram &P, const Ste
             if (smooth && T.kind == TK_UNTIL) continue;  // weighted instead of knocked
             b = cmp_y<Real>(T.cmp, y, thr[T.spot_slot]);
         } else {
-            b = eval_code<Real>(P, T.code_off, T.code_len, acc, poisoned, k, S, err) != Real(0);
+            b = eval_code<Real>(P, T.code_off, T.code_len, acc, poisoned, k, S, err, Sx) != Real(0);
         }
         if (b) bits |= 1u << i;
     }
@@ -263,14 +272,16 @@ struct Trig {
 template <class Real>
 __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp, const StepRec<Real> *R,
                                       const Real *thr, const double *D, Real *acc_base, Real *surv_base, int stride,
-                                      Real s0, Real y, int k, uint32_t bits, uint32_t gen_mask, int smooth, Trig st) {
+                                      Real s0, Real y, int k, uint32_t bits, uint32_t gen_mask, int smooth, Trig st,
+                                      const Real *Sx) {
     const KxProgram &P = *Pp;
     const AccView<Real> acc{acc_base, stride};
     const AccView<Real> surv{surv_base, stride};
     const Real inv_w = pick<Real>(Cp->inv_w, Cp->inv_wf);
     const Real S = spot_of<Real>(s0, y);
     const uint32_t live = st.armed & ~st.resolved;
-    if (live & gen_mask) bits |= cond_bits_full<Real>(P, R, thr, smooth, y, S, st.poisoned, live & gen_mask, k, acc, st.err);
+    if (live & gen_mask)
+        bits |= cond_bits_full<Real>(P, R, thr, smooth, y, S, st.poisoned, live & gen_mask, k, acc, st.err, Sx);
     if (smooth) {  // smoothed until weights of the slots armed before this step
         uint32_t sm = st.armed & P.until_mask & ~P.time_mask;
         while (sm) {
@@ -301,7 +312,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
         }
         arm &= ~st.armed;
         st.armed |= arm;
-        newly = arm ? cond_bits_full<Real>(P, R, thr, smooth, y, S, st.poisoned, arm, k, acc, st.err) : 0u;
+        newly = arm ? cond_bits_full<Real>(P, R, thr, smooth, y, S, st.poisoned, arm, k, acc, st.err, Sx) : 0u;
         if (smooth && arm) {  // smoothed slots armed now weigh this step too
             uint32_t sm = arm & P.until_mask & ~P.time_mask;
             while (sm) {
@@ -328,7 +339,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
         if (is_dead && !F.err_capable) continue;
         double amt = F.kind == AK_CONST ? F.sign
                      : F.fast           ? (double)fast_amount<Real>(P, F, S)
-                                        : (double)eval_code<Real>(P, F.code_off, F.code_len, acc, st.poisoned, k, S, st.err);
+                                        : (double)eval_code<Real>(P, F.code_off, F.code_len, acc, st.poisoned, k, S, st.err, Sx);
         if (is_dead) continue;
         if (smooth) {
             uint32_t us = P.until_mask & ~P.time_mask & st.armed;
@@ -364,7 +375,7 @@ __device__ __noinline__ Trig on_event(const KxProgram *Pp, const ContractDev *Cp
 // model moved to step k. Returns true when no flow can change any more.
 template <class Real, int NS>
 __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const PathArgs &A, int cur, Lane<Real, NS> &L,
-                                              int s, int k, Real *smem) {
+                                              int s, int k, Real *smem, const Real *Sx = nullptr) {
     const AccView<Real> acc{smem + (s * (int)A.slots) * KX_BLOCK + threadIdx.x, KX_BLOCK};
     if (H.n_acc) {  // accumulators (observable.rs:120-140), inner ones first (slot order)
         const KxProgram &P = *H.P;
@@ -374,10 +385,10 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const Path
             if (k < Ac.i_from || k > Ac.i_to) continue;
             Real x;
             if (Ac.inner == IK_SPOT) {
-                x = S;
+                x = Sx ? Sx[Ac.pad] : S;
             } else {
                 uint32_t e = 0;
-                x = eval_code<Real>(P, Ac.code_off, Ac.code_len, acc, L.poisoned[s], k, S, e);
+                x = eval_code<Real>(P, Ac.code_off, Ac.code_len, acc, L.poisoned[s], k, S, e, Sx);
                 if (e) L.poisoned[s] |= 1u << a;
             }
             Real &v = acc[2 * a];
@@ -417,7 +428,7 @@ __device__ __forceinline__ bool contract_step(const Hot<Real, NS> &H, const Path
     st = on_event<Real>(H.P, C, H.R, reinterpret_cast<const Real *>(A.thr) + ((size_t)cur * KX_MAX_NS + s) * KX_MAX_SPOT,
                         A.disc + C->disc_off + (size_t)s * H.n_times, acc.base,
                         smem + (s * (int)A.slots + (int)A.surv_base) * KX_BLOCK + threadIdx.x, KX_BLOCK, H.s0[s],
-                        L.y[s], k, bits, H.gen_mask, (H.flags & HF_SMOOTH) ? 1 : 0, st);
+                        L.y[s], k, bits, H.gen_mask, (H.flags & HF_SMOOTH) ? 1 : 0, st, Sx);
     L.armed[s] = st.armed;
     L.resolved[s] = st.resolved;
     L.dead[s] = st.dead;
@@ -444,8 +455,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     constexpr bool HESTON = MODEL == M_HESTON || MODEL == M_HESTON_PAIR;
-    constexpr int DRAWS = MODEL == M_GBM ? 1 : MODEL == M_HESTON_PAIR ? 4 : 2;  // normals per grid step
-    constexpr int SPB = 4 / DRAWS;                                             // grid steps per Philox block
+    constexpr bool MULTI = MODEL == M_MULTI;  // one step per round, n_assets normals per step
+    constexpr int DRAWS = MODEL == M_GBM ? 1 : MODEL == M_HESTON_PAIR || MULTI ? 4 : 2;  // normals per grid step
+    constexpr int SPB = 4 / DRAWS;                                                       // grid steps per Philox block
     constexpr uint32_t ALL = (1u << NS) - 1u;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
@@ -462,6 +474,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
     Lane<Real, NS> L;
     L.err = 0;
     uint32_t my_steps = 0;
+    int n_assets = 1;                      // warp-uniform (M_MULTI)
+    Real ym[MULTI ? KX_MAX_NS : 1];        // M_MULTI: log(S_i / s0_i) of every factor
+    Real sx[MULTI ? KX_MAX_NS : 1];        // M_MULTI: the factors' spots at the current step
 
     while (true) {
         // ---- hand paths to idle lanes (warp-uniform control) ----
@@ -486,6 +501,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                     }
                     cur = w.contract;
                     load_hot<Real, NS>(H, A, cur);
+                    if (MULTI) n_assets = A.cons[cur].n_assets;
                     if (HESTON) {
                         const ContractDev &C = A.cons[cur];
                         hr = pick<Real>(C.r, C.rf);
@@ -528,7 +544,14 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                     }
                     if (H.flags & HF_SMOOTH)
                         for (int q = 0; q < P.n_spot_cmp; ++q) av[(int)A.surv_base + q] = Real(1);
-                    if (contract_step<Real, NS>(H, A, cur, L, s, 0, smem)) done |= 1u << s;
+                    if (MULTI) {
+                        const ContractDev &C = A.cons[cur];
+                        for (int i = 0; i < n_assets; ++i) {
+                            ym[i] = Real(0);
+                            sx[i] = pick<Real>(C.s0[i], C.s0f[i]);
+                        }
+                    }
+                    if (contract_step<Real, NS>(H, A, cur, L, s, 0, smem, MULTI ? sx : nullptr)) done |= 1u << s;
                 }
                 k = 1;
                 if (H.n_times <= 1 || done == ALL) {
@@ -545,8 +568,61 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
             continue;
         }
 
+        // ---- M_MULTI: advance busy lanes by one grid step of every factor ----
+        if (MULTI && path >= 0) {
+            const ContractDev &C = A.cons[cur];
+            const int kk = k;
+            Real c0, c1;
+            if (H.flags & HF_UNIFORM) {
+                c0 = H.uc0;
+                c1 = H.uc1;
+            } else {
+                const StepRec<Real> rec = H.R[kk];
+                c0 = rec.c0;
+                c1 = rec.c1;
+            }
+            // the step's normals are draws (kk - 1) n .. (kk - 1) n + n - 1 of the path's stream
+            Real z[MULTI ? KX_MAX_NS : 1];
+            const uint64_t d0 = (uint64_t)(kk - 1) * (uint64_t)n_assets;
+            uint32_t blk = 0xffffffffu;
+            Real zz[4] = {Real(0), Real(0), Real(0), Real(0)};
+            for (int i = 0; i < n_assets; ++i) {
+                const uint64_t d = d0 + (uint64_t)i;
+                if (A.z64 == nullptr && A.z32 == nullptr) {
+                    if ((uint32_t)(d >> 2) != blk) {
+                        blk = (uint32_t)(d >> 2);
+                        const uint4 w = philox4x32_10(make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32),
+                                                                 C.stream),
+                                                      (uint32_t)C.seed, (uint32_t)(C.seed >> 32));
+                        box_muller(w.x, w.y, zz[0], zz[1]);
+                        box_muller(w.z, w.w, zz[2], zz[3]);
+                    }
+                    z[i] = zz[d & 3];
+                } else {
+                    const uint64_t base = (uint64_t)path * A.z_dpp;
+                    z[i] = d < A.z_dpp ? (A.z64 ? (Real)A.z64[base + d] : (Real)A.z32[base + d]) : Real(0);
+                }
+            }
+            // w = L z (multi_asset.rs:146-156), then each factor's exact log step
+            for (int i = 0; i < n_assets; ++i) {
+                Real wi = Real(0);
+                const int row = i * (i + 1) / 2;
+                for (int j = 0; j <= i; ++j) wi = wi + pick<Real>(C.chol[row + j], C.cholf[row + j]) * z[j];
+                ym[i] = gbm_step(ym[i], pick<Real>(C.drift[i], C.driftf[i]) * c0, pick<Real>(C.sigma[i], C.sigmaf[i]) * c1,
+                                 wi);
+                sx[i] = spot_of<Real>(pick<Real>(C.s0[i], C.s0f[i]), ym[i]);
+            }
+            L.y[0] = ym[0];
+            if (contract_step<Real, NS>(H, A, cur, L, 0, kk, smem, sx)) done = ALL;
+            ++my_steps;
+            k += 1;
+            if (k >= H.n_times || done == ALL) {
+                write_path<Real, NS>(A, cur, path, L);
+                path = -1;
+            }
+        }
         // ---- advance busy lanes by one Philox block of grid steps ----
-        if (path >= 0) {
+        if (!MULTI && path >= 0) {
             const int nt = H.n_times;
             Real zz[4];
             if (A.z64 == nullptr && A.z32 == nullptr) {
@@ -630,6 +706,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
 // Kernel variants, one function per translation unit.
 // paths_kernel_pair: the coarse kernels of multilevel pairs (model 0 GBM, 1 Heston).
 const void *paths_kernel_pair(int model, int fp64);
+// paths_kernel_multi: correlated multi-factor GBM (M_MULTI).
+const void *paths_kernel_multi(int fp64);
 // which: 0 GBM FP32, 1 GBM FP64, 2 Heston FP32, 3 Heston FP64, 4 GBM FP32 x7
 // scenarios, 5 GBM FP64 x7 scenarios. Returns nullptr for a missing variant.
 const void *paths_kernel_gbm(int fp64, int minb);

@@ -128,7 +128,7 @@ __device__ __forceinline__ Trig lean_event(const KxProgram *Pp, const ContractDe
         st.done = (P.all_leaves & ~(st.emitted | st.dead)) == 0u;
         return st;
     }
-    return on_event<Real>(Pp, Cp, R, thr, D, nullptr, nullptr, KX_BLOCK, s0, y, k, bits, 0u, 0, st);
+    return on_event<Real>(Pp, Cp, R, thr, D, nullptr, nullptr, KX_BLOCK, s0, y, k, bits, 0u, 0, st, nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -86,6 +86,7 @@ class Oracle:
         L.ko_mlmc_optimal_allocation.argtypes = [P(D), P(C.c_uint64), C.c_size_t, C.c_double, P(C.c_uint64)]
         L.ko_price_mlmc.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(_abi.KxMlmcCfg),
                                     P(_abi.KxMlmcResult)]
+        L.ko_price_multi.argtypes = [C.c_char_p, P(_abi.KxMultiGbm), P(_abi.KxMcConfig), P(_abi.KxPriceResult), P(D)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
         L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
@@ -274,6 +275,16 @@ class Oracle:
         return {"price": Result(out.price), "level_means": list(out.level_means[:k]),
                 "level_variances": list(out.level_variances[:k]), "level_costs": list(out.level_costs[:k]),
                 "level_paths": list(out.level_paths[:k]), "total_cost": out.total_cost}
+
+    def price_multi(self, js: str, model, n_paths=100_000, seed=42, steps_per_year=50, per_path=False):
+        """price_gbm under CorrelatedGbmN (multi_asset.rs:107-170)."""
+        mm = model._c()
+        cfg = self.cfg(n_paths, seed, steps_per_year, model.rate)
+        r = _abi.KxPriceResult()
+        pp = np.zeros(max(1, n_paths)) if per_path else None
+        self._chk(self.L.ko_price_multi(js.encode(), C.byref(mm), C.byref(cfg), C.byref(r),
+                                        pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
+        return (Result(r), pp[:n_paths]) if per_path else Result(r)
 
     def price_american(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
                        per_path=False, basis="monomial"):

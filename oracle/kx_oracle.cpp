@@ -567,6 +567,9 @@ struct PathView {
     const std::vector<double> *times;
     const double *spots;
     const std::string *asset;
+    // a multi-asset path (Path::with_asset per factor): names[i]'s spots in rows[i]
+    const std::vector<std::string> *names = nullptr;
+    const double *const *rows = nullptr;
     size_t len() const { return times->size(); }
 };
 
@@ -579,6 +582,13 @@ double eval_obs(const Obs &o, const PathView &p, size_t t) {
     switch (o.k) {
     case O_CONST: return o.c;
     case O_SPOT:  // observable.rs:79-87
+        if (p.names) {
+            size_t i = 0;
+            while (i < p.names->size() && (*p.names)[i] != o.name) ++i;
+            if (i == p.names->size()) fail(KX_UNKNOWN_ASSET, o.name);
+            if (t >= p.len()) fail(KX_STEP_OUT_OF_RANGE, std::to_string(t));
+            return p.rows[i][t];
+        }
         if (o.name != *p.asset) fail(KX_UNKNOWN_ASSET, o.name);
         if (t >= p.len()) fail(KX_STEP_OUT_OF_RANGE, std::to_string(t));
         return p.spots[t];
@@ -1484,6 +1494,92 @@ int ko_price_mlmc(const char *json, const kx_model *model, const kx_mc_config *c
         out->price.ci95_high = price + Z95 * se;
         out->price.n_paths = n_total;
         out->total_cost = total_cost;
+    });
+}
+
+// ---- correlated multi-factor GBM (multi_asset.rs) ---------------------------
+// numerics::cholesky_lower (numerics.rs:158-183)
+static std::vector<std::vector<double>> cholesky_lower(const std::vector<std::vector<double>> &a) {
+    const size_t n = a.size();
+    std::vector<std::vector<double>> l(n, std::vector<double>(n, 0.0));
+    for (size_t i = 0; i < n; ++i)
+        for (size_t j = 0; j <= i; ++j) {
+            double sum = a[i][j];
+            for (size_t k = 0; k < j; ++k) sum -= l[i][k] * l[j][k];
+            if (i == j) {
+                l[i][j] = std::sqrt(std::max(sum, 0.0));
+            } else {
+                const double pivot = l[j][j];
+                l[i][j] = pivot > 0.0 ? sum / pivot : 0.0;
+            }
+        }
+    return l;
+}
+
+// price_gbm under CorrelatedGbmN::simulate_paths (multi_asset.rs:127-170): per
+// grid step k >= 1 the normals (k - 1) n .. (k - 1) n + n - 1 of the path's
+// Philox stream, w = L z, and every factor's exact step (evolve, :85-104).
+int ko_price_multi(const char *json, const kx_multi_gbm *mm, const kx_mc_config *cfg, kx_price_result *out,
+                   double *per_path) {
+    return run([&] {
+        ConP c = parse_contract(json);
+        kx_mc_config mc = check_cfg(cfg);
+        const size_t n = mm->n_assets;
+        if (n < 2) fail(KX_MALFORMED_CONTRACT, "CorrelatedGbmN: at least 2 assets required");
+        std::vector<std::string> names;
+        std::vector<std::vector<double>> corr(n, std::vector<double>(n));
+        for (size_t i = 0; i < n; ++i) {
+            if (mm->sigma[i] < 0.0) fail(KX_MALFORMED_CONTRACT, "CorrelatedGbmN: every volatility must be >= 0");
+            names.push_back(mm->names[i]);
+            for (size_t j = 0; j < n; ++j) corr[i][j] = mm->corr[i * n + j];
+        }
+        const auto L = cholesky_lower(corr);
+        Plan p = compile(*c);
+        const auto grid = time_grid_forced(p, mc.steps_per_year, false);
+        const size_t G = grid.size();
+        NormalSource ns = make_source(mc);
+        std::vector<double> pvs(mc.n_paths);
+        int err_code = 0;
+        std::string err_msg;
+#pragma omp parallel num_threads(g_threads > 0 ? g_threads : omp_get_max_threads())
+        {
+            std::vector<double> z(std::max<size_t>((G - 1) * n, 1)), rows(n * G), w(n);
+            std::vector<const double *> rp(n);
+#pragma omp for schedule(dynamic, 256)
+            for (int64_t i = 0; i < (int64_t)mc.n_paths; ++i) {
+                if (err_code) continue;
+                try {
+                    ns.fill((uint64_t)i, (G - 1) * n, z.data());
+                    std::vector<double> sp(mm->s0, mm->s0 + n);
+                    for (size_t a = 0; a < n; ++a) rows[a * G] = sp[a];
+                    double prev_t = grid[0];
+                    for (size_t k = 1; k < G; ++k) {
+                        const double dt = grid[k] - prev_t;
+                        for (size_t a = 0; a < n; ++a) {
+                            double acc = 0.0;
+                            for (size_t j = 0; j <= a; ++j) acc += L[a][j] * z[(k - 1) * n + j];
+                            w[a] = acc;
+                        }
+                        for (size_t a = 0; a < n; ++a) {
+                            if (dt > 0.0)
+                                sp[a] *= std::exp((mm->mu[a] - 0.5 * mm->sigma[a] * mm->sigma[a]) * dt +
+                                                  mm->sigma[a] * std::sqrt(dt) * w[a]);
+                            rows[a * G + k] = sp[a];
+                        }
+                        prev_t = grid[k];
+                    }
+                    for (size_t a = 0; a < n; ++a) rp[a] = &rows[a * G];
+                    PathView pv{&grid, rows.data(), &names[0], &names, rp.data()};
+                    pvs[(size_t)i] = present_value(*c, pv, grid, mc.rate);
+                } catch (const KxError &e) {
+#pragma omp critical
+                    if (!err_code) { err_code = e.code; err_msg = e.msg; }
+                }
+            }
+        }
+        if (err_code) fail(err_code, err_msg);
+        *out = summarize(pvs);
+        if (per_path) memcpy(per_path, pvs.data(), pvs.size() * sizeof(double));
     });
 }
 
