@@ -455,6 +455,46 @@ def mlmc_heston() -> dict:
     return out
 
 
+def multi_asset_basket(reps=3) -> dict:
+    """A knock-out basket call on 5 correlated GBM factors (CorrelatedGbmN,
+    multi_asset.rs): s0 100, sigma 0.15..0.35, pairwise correlation 0.4, r
+    0.03; payoff max(basket - 100, 0) at T 1 unless the equally weighted
+    basket reaches 130 on the daily grid (252 steps); 1,000,000 paths, FP32
+    and FP64. CPU: the oracle on a bounded sample."""
+    import kontracts_gb300 as kx
+    from oracle import Oracle
+    S = kx.S
+    n_f = 5
+    fac = [(f"S{i}", 100.0, 0.03, 0.15 + 0.05 * i) for i in range(n_f)]
+    corr = [[1.0 if i == j else 0.4 for j in range(n_f)] for i in range(n_f)]
+    m = kx.CorrelatedGbmN(fac, corr, rate=0.03)
+    basket = (S("S0") + S("S1") + S("S2") + S("S3") + S("S4")) / 5.0
+    c = kx.until(basket >= 130.0, kx.scale((basket - 100.0).clip(0.0), kx.one()) @ kx.at(1.0))
+    n, spy = 1_000_000, 252
+    steps = len(c.time_grid(spy)) - 1
+    out = {"workload": "knock-out basket call, 5 correlated GBM factors, daily grid, 1M paths"}
+    for prec in ("fp32", "fp64"):
+        c.price(m, n_paths=n, seed=42, steps_per_year=spy, precision=prec)  # tune + warm
+        best = None
+        for _ in range(reps):
+            r = c.price(m, n_paths=n, seed=42, steps_per_year=spy, precision=prec)
+            t = _dev_seconds(kx)
+            best = t if best is None or t < best else best
+        sim = kx.last_launch_stats()["steps_simulated"]
+        out[prec] = {"seconds": best, "price": r.price, "std_error": r.std_error,
+                     "nominal_path_steps_per_s": n * steps / best, "simulated_path_steps_per_s": sim / best,
+                     "factor_steps_per_s": sim * n_f / best}
+    orc = Oracle()
+    ns = 200_000
+    t0 = time.perf_counter()
+    o = orc.price_multi(c.to_json(), m, n_paths=ns, seed=42, steps_per_year=spy)
+    cpu = time.perf_counter() - t0
+    out["cpu_baseline"] = {"nominal_path_steps_per_s": ns * steps / cpu, "cores": orc.threads(), "kind": "port",
+                           "sample": f"{ns} paths x {steps} steps, {cpu:.2f} s", "price": o.price}
+    out["gpu_fp32_over_cpu"] = out["fp32"]["nominal_path_steps_per_s"] / out["cpu_baseline"]["nominal_path_steps_per_s"]
+    return out
+
+
 def heston_book(reps=3) -> dict:
     """Heston benchmark shape: 32 strikes (evenly spaced in [80, 120]) x T in
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
@@ -689,7 +729,8 @@ def run_ours(args, ws, rank, local) -> None:
                                  "book_256": book_256(), "lsm_12": lsm_cases(),
                                  "variance_reduction": variance_reduction(),
                                  "greek_surface_99": greek_surface_grid(),
-                                 "heston_calibration": heston_calibration(), "mlmc_heston": mlmc_heston()}
+                                 "heston_calibration": heston_calibration(), "mlmc_heston": mlmc_heston(),
+                                 "multi_asset_basket": multi_asset_basket()}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.cpu_seconds)
         line["accuracy"] = accuracy(cb)
