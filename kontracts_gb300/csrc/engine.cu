@@ -475,6 +475,11 @@ static std::string tune_key(const std::vector<Job> &jobs, const kx_mc_config &cf
 }
 
 const int *variants(int model, bool f64, int ns, bool lean, int &n) {
+    static const int vm[] = {2};
+    if (model == KX_MODEL_MULTI_GBM) {  // one register budget (paths_multi.cu)
+        n = 1;
+        return vm;
+    }
     static const int v1[] = {4, 3, 2};
     static const int v7[] = {2, 1};
     static const int l32[] = {4, 5, 6};
@@ -499,7 +504,7 @@ static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cf
     const bool tune = !(env && env[0] == '0');
     const std::string key = tune_key(jobs, cfg, ns);
     auto it = g_tune.find(key);
-    if (tune && it == g_tune.end()) {
+    if (tune && nv > 1 && it == g_tune.end()) {
         // calibration batch: the same contracts with fewer paths
         uint64_t total = 0;
         for (auto &j : jobs) total += j.dev.n_paths;
