@@ -546,9 +546,10 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                         for (int q = 0; q < P.n_spot_cmp; ++q) av[(int)A.surv_base + q] = Real(1);
                     if (MULTI) {
                         const ContractDev &C = A.cons[cur];
-                        for (int i = 0; i < n_assets; ++i) {
+#pragma unroll
+                        for (int i = 0; i < (MULTI ? KX_MAX_NS : 1); ++i) {
                             ym[i] = Real(0);
-                            sx[i] = pick<Real>(C.s0[i], C.s0f[i]);
+                            sx[i] = i < n_assets ? pick<Real>(C.s0[i], C.s0f[i]) : Real(0);
                         }
                     }
                     if (contract_step<Real, NS>(H, A, cur, L, s, 0, smem, MULTI ? sx : nullptr)) done |= 1u << s;
@@ -581,36 +582,46 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
                 c0 = rec.c0;
                 c1 = rec.c1;
             }
-            // the step's normals are draws (kk - 1) n .. (kk - 1) n + n - 1 of the path's stream
+            // the step's normals are draws (kk - 1) n .. (kk - 1) n + n - 1 of the path's stream;
+            // the factor loops are unrolled over the largest count so the state stays in registers
             Real z[MULTI ? KX_MAX_NS : 1];
             const uint64_t d0 = (uint64_t)(kk - 1) * (uint64_t)n_assets;
             uint32_t blk = 0xffffffffu;
             Real zz[4] = {Real(0), Real(0), Real(0), Real(0)};
-            for (int i = 0; i < n_assets; ++i) {
-                const uint64_t d = d0 + (uint64_t)i;
-                if (A.z64 == nullptr && A.z32 == nullptr) {
-                    if ((uint32_t)(d >> 2) != blk) {
-                        blk = (uint32_t)(d >> 2);
-                        const uint4 w = philox4x32_10(make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32),
-                                                                 C.stream),
-                                                      (uint32_t)C.seed, (uint32_t)(C.seed >> 32));
-                        box_muller(w.x, w.y, zz[0], zz[1]);
-                        box_muller(w.z, w.w, zz[2], zz[3]);
+#pragma unroll
+            for (int i = 0; i < (MULTI ? KX_MAX_NS : 1); ++i) {
+                z[i] = Real(0);
+                if (i < n_assets) {
+                    const uint64_t d = d0 + (uint64_t)i;
+                    if (A.z64 == nullptr && A.z32 == nullptr) {
+                        if ((uint32_t)(d >> 2) != blk) {
+                            blk = (uint32_t)(d >> 2);
+                            const uint4 w = philox4x32_10(
+                                make_uint4(blk, (uint32_t)path, (uint32_t)((uint64_t)path >> 32), C.stream),
+                                (uint32_t)C.seed, (uint32_t)(C.seed >> 32));
+                            box_muller(w.x, w.y, zz[0], zz[1]);
+                            box_muller(w.z, w.w, zz[2], zz[3]);
+                        }
+                        const uint32_t q = (uint32_t)(d & 3);
+                        z[i] = q == 0 ? zz[0] : q == 1 ? zz[1] : q == 2 ? zz[2] : zz[3];
+                    } else {
+                        const uint64_t base = (uint64_t)path * A.z_dpp;
+                        z[i] = d < A.z_dpp ? (A.z64 ? (Real)A.z64[base + d] : (Real)A.z32[base + d]) : Real(0);
                     }
-                    z[i] = zz[d & 3];
-                } else {
-                    const uint64_t base = (uint64_t)path * A.z_dpp;
-                    z[i] = d < A.z_dpp ? (A.z64 ? (Real)A.z64[base + d] : (Real)A.z32[base + d]) : Real(0);
                 }
             }
             // w = L z (multi_asset.rs:146-156), then each factor's exact log step
-            for (int i = 0; i < n_assets; ++i) {
-                Real wi = Real(0);
-                const int row = i * (i + 1) / 2;
-                for (int j = 0; j <= i; ++j) wi = wi + pick<Real>(C.chol[row + j], C.cholf[row + j]) * z[j];
-                ym[i] = gbm_step(ym[i], pick<Real>(C.drift[i], C.driftf[i]) * c0, pick<Real>(C.sigma[i], C.sigmaf[i]) * c1,
-                                 wi);
-                sx[i] = spot_of<Real>(pick<Real>(C.s0[i], C.s0f[i]), ym[i]);
+#pragma unroll
+            for (int i = 0; i < (MULTI ? KX_MAX_NS : 1); ++i) {
+                if (i < n_assets) {
+                    Real wi = Real(0);
+                    const int row = i * (i + 1) / 2;
+#pragma unroll
+                    for (int j = 0; j <= i; ++j) wi = wi + pick<Real>(C.chol[row + j], C.cholf[row + j]) * z[j];
+                    ym[i] = gbm_step(ym[i], pick<Real>(C.drift[i], C.driftf[i]) * c0,
+                                     pick<Real>(C.sigma[i], C.sigmaf[i]) * c1, wi);
+                    sx[i] = spot_of<Real>(pick<Real>(C.s0[i], C.s0f[i]), ym[i]);
+                }
             }
             L.y[0] = ym[0];
             if (contract_step<Real, NS>(H, A, cur, L, 0, kk, smem, sx)) done = ALL;
