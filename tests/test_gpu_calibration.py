@@ -120,3 +120,15 @@ def test_calibrate_heston_cmaes_reproduces_prices():
     assert err < 0.005, (err, res.parameters)
     for v, lo, hi in zip(res.parameters, cal.HESTON_LOWER, cal.HESTON_UPPER):
         assert lo <= v <= hi
+
+
+def test_empty_quotes_and_single_cell_surface(orc):
+    """No quotes: the objective is 0 / 0 = NaN as eval_obj_heston computes it;
+    a one-cell surface is greeks_gbm at that cell."""
+    c = kx.european_call("underlying", 100.0, 1.0)
+    assert math.isnan(cal.heston_objective(c, [], [HP], R, 100)[0])
+    assert math.isnan(orc.calib_heston_objective(c.to_json(), "underlying", np.zeros((0, 2)), [HP], n_paths=100,
+                                                 rate=R)[0])
+    s = kx.greek_surface(c, "underlying", [100.0], [0.2], n_paths=10_000, seed=4, steps_per_year=4, rate=R)
+    g = c.greeks(kx.GBM(s0=100.0, sigma=0.2, r=R, asset="underlying"), n_paths=10_000, seed=4, steps_per_year=4)
+    assert s.delta[0, 0] == g.delta and s.price[0, 0] == g.price and s.gamma[0, 0] == g.gamma

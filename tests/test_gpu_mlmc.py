@@ -94,3 +94,13 @@ def test_rejections():
     with pytest.raises(kx.KontractError) as e:
         kx.price_mlmc(c, kx.heston(S0, 0.04, 1.5, 0.04, 0.3, -0.7, R, asset="S", scheme="full_truncation"))
     assert e.value.status == "Unsupported"
+
+
+def test_no_pilot_allocates_one_path_per_level(orc):
+    """pilot_paths = 0: every level's variance is 0, optimal_allocation gives
+    one path per level (mlmc.rs:250-252), all on the second seed."""
+    c, m = CONTRACTS["call"](), MODELS["gbm"]()
+    g = kx.price_mlmc_detailed(c, m, kx.MlmcConfig(n_levels=3, pilot_paths=0, target_variance=1e-4), seed=2)
+    o = orc.price_mlmc(c.to_json(), m, n_levels=3, pilot_paths=0, target_variance=1e-4, seed=2)
+    assert g.level_paths == o["level_paths"] == [1, 1, 1, 1]
+    assert abs(g.price.price - o["price"].price) <= 1e-10 * max(1.0, abs(o["price"].price))

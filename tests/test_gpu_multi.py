@@ -78,3 +78,20 @@ def test_rejections():
     with pytest.raises(kx.KontractError) as e:
         kx.european_call("S1", 100.0, 1.0).price(kx.CorrelatedGbmN([("S1", 100.0, R, 0.2)], [[1.0]]), n_paths=100)
     assert e.value.status == "MalformedContract"
+
+
+def test_seven_factors_equal_oracle_and_eight_rejected(orc):
+    """The largest factor count (KX_MAX_ASSETS = 7) in FP64 against the oracle;
+    an eighth factor is refused on the host."""
+    fac = [(f"A{i}", 90.0 + 3 * i, 0.02, 0.1 + 0.03 * i) for i in range(7)]
+    corr = [[1.0 if i == j else 0.3 - 0.02 * abs(i - j) for j in range(7)] for i in range(7)]
+    m = kx.CorrelatedGbmN(fac, corr, rate=R)
+    tot = S("A0")
+    for i in range(1, 7):
+        tot = tot + S(f"A{i}")
+    c = kx.until(S("A6") >= 150.0, kx.scale((tot / 7.0 - 100.0).clip(0.0), kx.one()) @ kx.at(1.0))
+    r, pp = c.price(m, n_paths=3000, seed=21, steps_per_year=24, precision="fp64", per_path=True)
+    o, op = orc.price_multi(c.to_json(), m, n_paths=3000, seed=21, steps_per_year=24, per_path=True)
+    assert np.allclose(np.asarray(pp), op, rtol=1e-11, atol=1e-11)
+    with pytest.raises(ValueError):
+        kx.CorrelatedGbmN(fac + [("A7", 100.0, 0.0, 0.2)], [[1.0] * 8] * 8)
