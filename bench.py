@@ -240,6 +240,30 @@ def _dev_seconds(kx) -> float:
     return (st["kernel_ms"] + st["reduce_ms"]) * 1e-3
 
 
+_BARE = {}
+
+
+def _bare_loop(what: int) -> float:
+    """kx_measure_peak: 3 the bare Philox + Box-Muller + GBM step loop, 4 the
+    Heston one (FP32 steps/s on this GPU, measured once per process)."""
+    if what not in _BARE:
+        import ctypes as C
+        from kontracts_gb300 import _abi
+        v = C.c_double()
+        _BARE[what] = v.value if _abi.load().kx_measure_peak(what, C.byref(v)) == 0 else float("nan")
+    return _BARE[what]
+
+
+def _issue_roofline(sim_steps: float, kernel_s: float, what: int, unit_note: str) -> dict:
+    """Simulated steps/s of the path kernel(s) against the bare step loop of the
+    same model: the issue-bound roofline of the path kernels."""
+    achieved = sim_steps / kernel_s / 1e9
+    peak = _bare_loop(what) / 1e9
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
+            "frac": achieved / peak if peak == peak and peak > 0 else None,
+            "peak_source": f"kx_measure_peak({what}) in this run", "note": unit_note}
+
+
 def _hbm_peak() -> tuple:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -311,12 +335,16 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
     vols = [0.10 + 0.04 * j for j in range(9)]
     n, spy = 100_000, 252
     steps = len(c.time_grid(spy)) - 1
-    best, launches = None, 0
+    best, launches, roof = None, 0, None
     for _ in range(reps):
         s = kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05)
         t = _dev_seconds(kx)
-        launches = kx.last_launch_stats()["kernel_launches"]
-        best = t if best is None or t < best else best
+        st = kx.last_launch_stats()
+        launches = st["kernel_launches"]
+        if best is None or t < best:
+            best = t
+            roof = _issue_roofline(st["steps_simulated"], st["kernel_ms"] * 1e-3, 3,
+                                   "simulated scenario-steps of the 693 reprices (knocked-out paths stop)")
     t0 = time.perf_counter()
     kx.greek_surface(c, "S", spots, vols, n_paths=n, seed=42, steps_per_year=spy, rate=0.05)
     wall = time.perf_counter() - t0
@@ -347,7 +375,7 @@ def greek_surface_grid(reps=3, cpu_seconds=4.0) -> dict:
     return {"workload": "greek surface, 11 spots x 9 vols, up-and-out call K 100 B 130 T 1, 252 steps/yr, "
                         "100k paths per cell, FP32, default bumps", "cells": cells,
             "seconds": best, "wall_seconds_e2e": wall, "gpu_launches": launches,
-            "cells_per_s": cells / best, "scenario_path_steps_per_s": scen_steps / best,
+            "cells_per_s": cells / best, "scenario_path_steps_per_s": scen_steps / best, "roofline": roof,
             "delta_atm_0.26": float(s.delta[5, 4]), "gamma_atm_0.26": float(s.gamma[5, 4]),
             "vega_atm_0.26": float(s.vega[5, 4]),
             "cpu_baseline": {"cells_per_s": cpu_cells_per_s, "cores": orc.threads(), "kind": "port",
@@ -432,6 +460,10 @@ def mlmc_heston() -> dict:
         t0 = time.perf_counter()
         d = kx.price_mlmc_detailed(c, h, cfg, seed=11, precision=prec)
         wall = time.perf_counter() - t0
+        if prec == "fp32":
+            st = kx.last_launch_stats()
+            out["roofline"] = _issue_roofline(st["steps_simulated"], st["kernel_ms"] * 1e-3, 4,
+                                              "simulated Heston steps of both phases' fine and coarse launches")
         out[prec] = {"wall_seconds": wall, "price": d.price.price, "std_error": d.price.std_error,
                      "level_paths": d.level_paths, "total_cost_steps": d.total_cost,
                      "path_steps_per_s": d.total_cost / wall}
@@ -480,7 +512,12 @@ def multi_asset_basket(reps=3) -> dict:
             r = c.price(m, n_paths=n, seed=42, steps_per_year=spy, precision=prec)
             t = _dev_seconds(kx)
             best = t if best is None or t < best else best
-        sim = kx.last_launch_stats()["steps_simulated"]
+        st = kx.last_launch_stats()
+        sim = st["steps_simulated"]
+        if prec == "fp32":
+            out["roofline"] = _issue_roofline(sim * n_f, st["kernel_ms"] * 1e-3, 3,
+                                              "factor-steps (each one normal and one GBM step, as the bare loop) "
+                                              "of the last run")
         out[prec] = {"seconds": best, "price": r.price, "std_error": r.std_error,
                      "nominal_path_steps_per_s": n * steps / best, "simulated_path_steps_per_s": sim / best,
                      "factor_steps_per_s": sim * n_f / best}
