@@ -315,7 +315,7 @@ template void pack_steps<double>(const StepTables &, std::vector<unsigned char> 
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
 const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat, bool acc) {
-    if (model == KX_MODEL_MULTI_GBM) return paths_kernel_multi(f64);  // general handler, one budget
+    if (model == KX_MODEL_MULTI_GBM) return paths_kernel_multi(f64, minb);  // general handler
     if (lean)
         return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc) : lean_kernel_heston(f64, minb, stat, acc);
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
@@ -475,10 +475,11 @@ static std::string tune_key(const std::vector<Job> &jobs, const kx_mc_config &cf
 }
 
 const int *variants(int model, bool f64, int ns, bool lean, int &n) {
-    static const int vm[] = {2};
-    if (model == KX_MODEL_MULTI_GBM) {  // one register budget (paths_multi.cu)
-        n = 1;
-        return vm;
+    static const int vm32[] = {4, 3, 2};
+    static const int vm64[] = {2};
+    if (model == KX_MODEL_MULTI_GBM) {  // the budgets of paths_multi.cu
+        n = f64 ? 1 : 3;
+        return f64 ? vm64 : vm32;
     }
     static const int v1[] = {4, 3, 2};
     static const int v7[] = {2, 1};
