@@ -111,3 +111,65 @@ def price_american_sharded(cases: Sequence[tuple], n_basis: int = 3, *, precisio
         for i, res in part:
             out[i] = res
     return out
+
+
+def greek_surface_sharded(contract, asset: str, spots: Sequence[float], vols: Sequence[float], *, group=None,
+                          surface_fn: Callable | None = None, **kw):
+    """greek_surface (surface.rs:104-137) sharded over the ranks of `group`:
+    rank r computes the rows of spots r, r + w, ... (all vols) in one
+    kx_greek_surface call on its GPU, all on the same seed as the
+    single-GPU surface; the only collective is the gather of the rows. Every
+    rank returns the whole GreekSurface, cell for cell the single-GPU one.
+    surface_fn(spots_subset) -> GreekSurface replaces the GPU call."""
+    import torch.distributed as dist
+    from . import GreekSurface, KontractError, greek_surface
+    if not spots or not vols:
+        raise KontractError(_abi.KX_INCONSISTENT_PATH, "empty surface grid")  # surface.rs:113-117
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    mine = case_shard(len(spots), world, rank)
+    rows = []
+    if mine:
+        sub = [spots[i] for i in mine]
+        s = surface_fn(sub) if surface_fn is not None else greek_surface(contract, asset, sub, vols, **kw)
+        for q, i in enumerate(mine):
+            rows.append((i, {f: [float(x) for x in getattr(s, f)[q]] for f in GreekSurface.QUANTITIES}))
+    gathered: list = [None] * world
+    dist.all_gather_object(gathered, rows, group=group)
+    by_row = {i: r for part in gathered for i, r in part}
+
+    class _Cell:
+        pass
+    cells = []
+    for i in range(len(spots)):
+        for j in range(len(vols)):
+            c = _Cell()
+            for f in GreekSurface.QUANTITIES:
+                setattr(c, f, by_row[i][f][j])
+            cells.append(c)
+    return GreekSurface(spots, vols, cells)
+
+
+def population_sharded(objective_batch: Callable, *, group=None) -> Callable:
+    """A batched calibration objective (for instance a CMA-ES generation, as
+    kontracts_gb300.calibration.heston_objective evaluates one) sharded over
+    the ranks of `group`: every rank calls the returned function with the
+    same population, evaluates candidates r, r + w, ... on its GPU and
+    all-gathers the objectives, so every rank's optimizer sees the same
+    values and takes the same steps."""
+    import torch.distributed as dist
+
+    def sharded(points):
+        world = dist.get_world_size(group)
+        rank = dist.get_rank(group)
+        mine = case_shard(len(points), world, rank)
+        vals = list(objective_batch([points[i] for i in mine])) if mine else []
+        gathered: list = [None] * world
+        dist.all_gather_object(gathered, [(i, float(v)) for i, v in zip(mine, vals)], group=group)
+        out = [0.0] * len(points)
+        for part in gathered:
+            for i, v in part:
+                out[i] = v
+        return out
+
+    return sharded

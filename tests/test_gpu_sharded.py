@@ -52,3 +52,20 @@ def test_american_case_shards_equal_the_batch():
             for i, r in zip(mine, kx.price_american_batch([cases[i] for i in mine], n_basis=3, basis="laguerre")):
                 got[i] = r
         assert [(r.price, r.std_error) for r in got] == [(r.price, r.std_error) for r in whole]
+
+
+def test_surface_row_shards_equal_the_whole_surface():
+    """Each rank's spot rows of a Greek surface, computed in its own
+    kx_greek_surface call, are the whole surface's rows bit for bit (every
+    cell reprices on the same seed whichever rows share its launch)."""
+    c = kx.up_and_out_call("X", 100.0, 130.0, 1.0)
+    spots, vols = [85.0, 95.0, 105.0, 115.0, 125.0], [0.15, 0.3]
+    kw = dict(n_paths=20_000, seed=6, steps_per_year=52, rate=0.04)
+    whole = kx.greek_surface(c, "X", spots, vols, **kw)
+    for world in (2, 3):
+        for rank in range(world):
+            mine = sharded.case_shard(len(spots), world, rank)
+            part = kx.greek_surface(c, "X", [spots[i] for i in mine], vols, **kw)
+            for q, i in enumerate(mine):
+                for f in kx.GreekSurface.QUANTITIES:
+                    assert (getattr(part, f)[q] == getattr(whole, f)[i]).all(), (world, rank, f)

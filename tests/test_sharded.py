@@ -113,3 +113,51 @@ def test_gloo_two_ranks_price_every_american_case(n_cases):
     want = _fake_batch([(i,) for i in range(n_cases)])
     for _, got in res:
         assert got == want
+
+
+def _fake_surface(spots, vols):
+    """A deterministic stand-in for one GPU's surface of the given spot rows."""
+    import kontracts_gb300 as kx
+
+    class _G:
+        def __init__(self, s, v):
+            for k, f in enumerate(kx.GreekSurface.QUANTITIES):
+                setattr(self, f, s * 1000.0 + v * 10.0 + k)
+    return kx.GreekSurface(spots, vols, [_G(s, v) for s in spots for v in vols])
+
+
+def _surface_worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        spots, vols = [80.0, 90.0, 100.0, 110.0, 120.0], [0.1, 0.2, 0.3]
+        s = sharded.greek_surface_sharded(None, "S", spots, vols, surface_fn=lambda sub: _fake_surface(sub, vols))
+        f = sharded.population_sharded(lambda pts: [sum(x * x for x in p) for p in pts])
+        pop = [[float(i), 1.0, -float(i)] for i in range(7)]
+        q.put((rank, {k: getattr(s, k).tolist() for k in ("price", "delta", "rho_se")}, f(pop)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gloo_two_ranks_shard_surface_rows_and_populations():
+    """Surface rows and calibration candidates split over two gloo ranks: every
+    rank assembles the whole surface and every objective, equal to one process."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_surface_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    vols = [0.1, 0.2, 0.3]
+    want = _fake_surface([80.0, 90.0, 100.0, 110.0, 120.0], vols)
+    pop = [[float(i), 1.0, -float(i)] for i in range(7)]
+    for _, surf, objs in res:
+        for k in ("price", "delta", "rho_se"):
+            assert surf[k] == getattr(want, k).tolist()
+        assert objs == [sum(x * x for x in p) for p in pop]
