@@ -21,9 +21,13 @@ call over that batch.
 
 `--impl reference` times that CPU restatement alone (all host threads), the
 reference's own CPU pricer being Rust that cannot be built here.
-Multi-GPU (torchrun, N > 1): every rank prices its own batch on its own GPU
-with its own Philox stream (weak scaling, no collective on the data path);
-value = all ranks' path-steps / the slowest rank's time.
+Multi-GPU: `--gpus N` starts N ranks under torch.distributed.run (or runs
+as one rank of an outer torchrun). Weak scaling (default): every rank prices
+its own batch on its own GPU with its own Philox stream, no collective on the
+data path. Strong scaling (`--scaling strong`): one price of `--paths` paths,
+each rank a chunk-aligned range of the same stream, the per-chunk statistics
+gathered and merged (the single-GPU result). value = all ranks' path-steps /
+the slowest rank's device time.
 """
 from __future__ import annotations
 
@@ -156,34 +160,52 @@ def accuracy(cb: dict) -> dict:
             "cpu_minus_closed_form_in_combined_se": (cb["_price"] - cf) / se}
 
 
+# The workload's contract, call.until(S >= 200) on the call max(S - 100, 0) at
+# T = 1, as the reference's serde JSON (Contract::to_json, src/ast.rs:210-217).
+WORKLOAD_JSON = ('{"Until":[{"Ge":[{"Spot":"S"},{"Const":200.0}]},{"When":[{"At":1.0},{"Scale":[{"Max":'
+                 '[{"Sub":[{"Spot":"S"},{"Const":100.0}]},{"Const":0.0}]},{"One":"USD"}]}]}]}')
+
+
+def _config(n_paths: int, ws: int) -> dict:
+    """The `config` of both arms' lines (identical for the same workload)."""
+    return dict(WORKLOAD, n_paths=n_paths, l2="flushed between timed steps (256 MB write) on the GPU arm",
+                parallelism=f"paths sharded over {ws} GPU(s), no collective" if ws > 1 else "1 GPU")
+
+
 def run_reference(args, ws, rank) -> None:
+    """The CPU restatement of the reference pricer (the reference is Rust and
+    cannot be built here) on the same workload as the GPU arm: the same
+    contract, model, grid and number of paths per step. It loads no engine
+    code: the contract is its serde JSON, the grid the oracle's own."""
     if rank != 0:
         return
-    import kontracts_gb300 as kx
-    from oracle import Oracle
+    from oracle import Oracle, _abi
     orc = Oracle()
     w = WORKLOAD
-    c = kx.up_and_out_call("S", w["strike"], w["barrier"], w["maturity"])
-    m = kx.GBM(s0=w["s0"], sigma=w["sigma"], r=w["r"], asset="S")
-    js = c.to_json()
-    steps = len(c.time_grid(w["steps_per_year"])) - 1
-    n = args.ref_paths
-    for _ in range(args.warmup):
-        orc.price(js, m, n_paths=max(1000, n // 10), seed=42, steps_per_year=w["steps_per_year"])
+    m = _abi.KxModel(kind=_abi.KX_MODEL_GBM, heston_scheme=0, s0=w["s0"], mu=w["r"], sigma=w["sigma"],
+                     asset=b"S")
+    js = WORKLOAD_JSON
+    spy = w["steps_per_year"]
+    steps = len(orc.time_grid(js, spy)) - 1
+    n = args.paths
+    for i in range(args.warmup):
+        orc.price(js, m, n_paths=n, seed=42 + 1000 + i, steps_per_year=spy, rate=w["r"])
     times = []
     for k in range(args.steps):
         t = time.perf_counter()
-        orc.price(js, m, n_paths=n, seed=42 + k, steps_per_year=w["steps_per_year"])
+        orc.price(js, m, n_paths=n, seed=42 + 100 + k, steps_per_year=spy, rate=w["r"])
         times.append(time.perf_counter() - t)
     tot = sum(times)
     value = n * steps * args.steps / tot
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox normals)",
-        "config": dict(WORKLOAD, sample_paths=n),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 normals)",
+        "config": _config(n, ws),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.threads(), "kind": "port",
-                         "sample": f"{n} of {w['n_paths']} paths x {steps} steps per step"},
+                         "sample": f"the whole workload per step: {n} paths x {steps} steps, CPU restatement of "
+                                   f"the reference pricer (materialised paths + recursive cash-flow walk), "
+                                   f"OpenMP over paths; rank 0 only"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -681,9 +703,20 @@ def run_ours(args, ws, rank, local) -> None:
     n_paths = args.paths
     c = kx.up_and_out_call("S", w["strike"], w["barrier"], w["maturity"])
     m = kx.GBM(s0=w["s0"], sigma=w["sigma"], r=w["r"], asset="S")
-    seed = 42 + 1000003 * rank
     steps_per_path = len(c.time_grid(w["steps_per_year"])) - 1
-    price = lambda s: c.price(m, n_paths=n_paths, seed=s, steps_per_year=w["steps_per_year"], precision="fp32")
+    if args.scaling == "strong":
+        # one price of n_paths paths over the ranks: each prices its chunk-aligned range of the
+        # same stream, the chunk statistics are gathered and merged (the single-GPU result)
+        from kontracts_gb300 import sharded
+        seed = 42
+        price = lambda s: sharded.price_sharded(c, m, n_paths, seed=s, steps_per_year=w["steps_per_year"],
+                                                precision="fp32")
+        job_paths = n_paths
+    else:
+        seed = 42 + 1000003 * rank
+        price = lambda s: c.price(m, n_paths=n_paths, seed=s, steps_per_year=w["steps_per_year"],
+                                  precision="fp32")
+        job_paths = ws * n_paths
     dev = torch.device("cuda", 0)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
@@ -699,7 +732,7 @@ def run_ours(args, ws, rank, local) -> None:
     clocks = Clocks(local)
     _barrier(ws)
     torch.cuda.synchronize()
-    dev_ms, ker_ms, sim_steps, launches = 0.0, 0.0, 0, 0
+    dev_ms, ker_ms, sim_steps, launches, rank_steps = 0.0, 0.0, 0, 0, 0
     results = []
     for k in range(args.steps):
         flush.zero_()
@@ -709,14 +742,15 @@ def run_ours(args, ws, rank, local) -> None:
         dev_ms += st["kernel_ms"] + st["reduce_ms"]
         ker_ms += st["kernel_ms"]
         sim_steps += st["steps_simulated"]
+        rank_steps += st["path_steps"]  # this rank's nominal path-steps
         launches += st["kernel_launches"]
         results.append(r)
     torch.cuda.synchronize()
     _barrier(ws)
     clk = clocks.stop()
     dev_ms_max = _barrier_max(dev_ms, ws)
-    nominal = n_paths * steps_per_path
-    value = ws * nominal * args.steps / (dev_ms_max * 1e-3)
+    nominal = job_paths * steps_per_path  # all ranks' path-steps of one step
+    value = nominal * args.steps / (dev_ms_max * 1e-3)
     # ---- e2e: the C-ABI call from the host, wall clock ----
     _barrier(ws)
     torch.cuda.synchronize()
@@ -728,7 +762,7 @@ def run_ours(args, ws, rank, local) -> None:
         h2d += st["h2d_bytes"]
         d2h += st["d2h_bytes"]
     e2e_s = _barrier_max(time.perf_counter() - t0, ws)
-    e2e = {"value": ws * nominal * args.steps / e2e_s, "unit": UNIT,
+    e2e = {"value": nominal * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
            "ms_per_step": 1e3 * e2e_s / args.steps}
     # ---- roofline of the path kernel: simulated steps/s against the bare simulation loop ----
@@ -737,7 +771,8 @@ def run_ours(args, ws, rank, local) -> None:
     # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum of the path kernel
     # on the 1M-path case (profiles/k_lean_static_up_and_out.md: 19,968 + 0 bytes), scaled by the
     # number of paths; the per-path values (8 B/path) stay in L2 during the launch.
-    traffic = 19968.0 / 1_000_000 * n_paths
+    rank_paths = rank_steps // max(1, steps_per_path * args.steps)  # paths of one launch on this rank
+    traffic = 19968.0 / 1_000_000 * rank_paths
     kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>", 3: "k_lean<float,GBM,static schedule>"}.get(
         kx.last_launch_stats()["path_kernel"], "?")
     roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
@@ -745,17 +780,17 @@ def run_ours(args, ws, rank, local) -> None:
                 "peak_source": "measured in this run: kx_measure_peak(3), the bare Philox4x32-10 + Box-Muller "
                                "+ GBM step loop (no contract, no scheduling) on this GPU",
                 "kernel": kname, "algorithmic_bytes_per_path": 8,
-                "achieved_hbm_gbs": 8.0 * n_paths * args.steps / (ker_ms * 1e-3) / 1e9,
-                "steps_simulated_fraction": sim_steps / (nominal * args.steps),
+                "achieved_hbm_gbs": 8.0 * rank_paths * args.steps / (ker_ms * 1e-3) / 1e9,
+                "steps_simulated_fraction": sim_steps / max(1, rank_steps),
                 "mufu_results_per_s_share": 2.0 * sim_steps / (ker_ms * 1e-3) / peaks.get("mufu", float("nan")),
                 "measured_peaks_per_s": dict(peaks)}
     greeks = None if args.no_greeks else price_greeks(c, m, n_paths, seed, w["steps_per_year"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": args.scaling,
+        "vs_baseline": None,
         "dtype": "f32 paths / f64 sums", "data": "synthetic (Philox4x32-10 normals generated in registers)",
-        "config": dict(WORKLOAD, n_paths=n_paths, l2="flushed between timed steps (256 MB write)",
-                       parallelism=f"paths sharded over {ws} GPU(s), no collective"),
+        "config": _config(n_paths, ws),
         "price": results[-1].price, "std_error": results[-1].std_error,
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
     }
@@ -776,14 +811,36 @@ def run_ours(args, ws, rank, local) -> None:
         print(json.dumps(line), flush=True)
 
 
+def _launch(n: int) -> int:
+    """Start n ranks of this command under torch.distributed.run (one node,
+    rendezvous on 127.0.0.1); rank 0 prints the line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def _pin_device(local: int) -> None:
+    """Give rank `local` its own GPU: the library prices on device 0 of the
+    process, so the rank sees only the local-th device of the visible list."""
+    vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
+    os.environ["CUDA_VISIBLE_DEVICES"] = vis[local % len(vis)] if vis else str(local)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--paths", type=int, default=WORKLOAD["n_paths"])
-    ap.add_argument("--ref-paths", type=int, default=400_000)
+    ap.add_argument("--paths", type=int, default=WORKLOAD["n_paths"],
+                    help="paths per rank (weak scaling) or in all (strong)")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: every rank prices its own batch; strong: one price split over the ranks "
+                         "(chunk statistics gathered, the single-GPU result)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-greeks", action="store_true")
@@ -792,8 +849,10 @@ def main() -> None:
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = _dist()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(_launch(args.gpus))
     if ws > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        _pin_device(local)
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("gloo")

@@ -250,9 +250,11 @@ kx_status kx_merge_chunks(const kx_chunk_stats *chunks, size_t n,
  * points, cfg->rng == KX_RNG_PHILOX; otherwise KX_INVALID_ARGUMENT and nothing
  * runs. The first call of a process does the set-up (device made current,
  * address of the array looked up, library stream created): make it before
- * any stream capture. The array is shared by all calls of the process, so
- * calls are serialised by the library lock; the call returns when its
- * results are on the host. */
+ * any stream capture. The address looked up is that of the array's copy on
+ * the library's device (device 0 of the process, as for every entry point
+ * here); it stays bound to that device for the life of the process. The
+ * array is shared by all calls of the process, so calls are serialised by
+ * the library lock; the call returns when its results are on the host. */
 #define KX_FIXED_MAX_PATHS 1048576u
 #define KX_FIXED_MAX_POINTS 8192u
 kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_model *model,

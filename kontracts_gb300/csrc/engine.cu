@@ -53,7 +53,10 @@ void DevBuf::ensure(size_t bytes) {
 
 Ctx &ctx() {
     static Ctx c;
-    if (c.ready) return c;
+    static std::mutex setup_mu;
+    if (c.ready.load(std::memory_order_acquire)) return c;
+    std::lock_guard<std::mutex> g(setup_mu);
+    if (c.ready.load(std::memory_order_relaxed)) return c;  // another thread finished the set-up
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || n <= 0) {
@@ -67,10 +70,11 @@ Ctx &ctx() {
     c.cc_major = prop.major;
     c.cc_minor = prop.minor;
     c.name = prop.name;
-    KX_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    KX_CUDA(cudaEventCreate(&c.ev0));
-    KX_CUDA(cudaEventCreate(&c.ev1));
-    c.ready = true;
+    // a set-up that failed half way is retried by the next call: keep what exists
+    if (!c.stream) KX_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    if (!c.ev0) KX_CUDA(cudaEventCreate(&c.ev0));
+    if (!c.ev1) KX_CUDA(cudaEventCreate(&c.ev1));
+    c.ready.store(true, std::memory_order_release);
     return c;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -31,7 +32,7 @@ struct DrawStore {  // host normals for KX_RNG_SHARED_DRAWS
 };
 
 struct Ctx {
-    bool ready = false;
+    std::atomic<bool> ready{false};  // set once, after every field below is valid
     int device = 0;
     int sm_count = 0;
     int cc_major = 0, cc_minor = 0;
@@ -47,6 +48,8 @@ struct Ctx {
 };
 
 // Lazily initialised process context; throws KX_NO_DEVICE without a GPU.
+// Thread-safe: the first callers race only for a set-up mutex, one of them
+// creates the stream and events, the others wait and then see the result.
 Ctx &ctx();
 
 // Persistent grid size for a kernel with `block` threads and `smem` bytes.

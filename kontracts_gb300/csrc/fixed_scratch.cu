@@ -19,7 +19,11 @@
 // Set-up: the first call of a process makes the device current and looks up
 // the array's address once (cudaGetSymbolAddress); that first call also
 // creates the library's stream and events. Make the first call before any
-// stream capture or other phase in which set-up work is unwelcome.
+// stream capture or other phase in which set-up work is unwelcome. The
+// address is the array's copy on the library's device (device 0 of the
+// process, the one device every entry point of this library uses); the
+// array exists on every device that loads the library, but only that copy
+// is used.
 //
 // Zeroing: the work-queue counter, the error word and the step counter at
 // the start of the array must be zero when the path kernel starts; every call
@@ -158,7 +162,7 @@ extern "C" kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_mod
         if (!kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
         const int block = KX_BLOCK;
         const uint32_t slots = 2u * (uint32_t)j.prog.n_acc;
-        const size_t smem = (size_t)slots * block * (f64 ? 8 : 4);
+        const size_t smem = lean ? 0 : (size_t)slots * block * (f64 ? 8 : 4);  // lean kernels keep no state in shared memory
         const int full = persistent_blocks(kfn, block, smem);
         const uint64_t warps_total = (uint64_t)full * (block / 32);
         uint64_t item = n / std::max<uint64_t>(1, warps_total * 8);

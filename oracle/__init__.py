@@ -7,15 +7,45 @@ this package; the engine (kontracts_gb300/) never does.
 from __future__ import annotations
 
 import ctypes as C
+import importlib.util
 import os
 import subprocess
+import sys
 
 import numpy as np
 
-from kontracts_gb300 import _abi
-
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libkx_oracle.so")
+
+
+def _load_abi():
+    """The ctypes mirror of the C structures (kontracts_gb300/_abi.py). When the
+    engine package is already imported (the tests), its module is shared, so
+    that its model objects pass straight through; otherwise that one file is
+    loaded on its own, without the engine package or its library, so that a
+    CPU-only run of the oracle loads no engine code."""
+    mod = sys.modules.get("kontracts_gb300._abi")
+    if mod is not None:
+        return mod
+    path = os.path.join(os.path.dirname(HERE), "kontracts_gb300", "_abi.py")
+    spec = importlib.util.spec_from_file_location("_kx_oracle_abi", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+_abi = _load_abi()
+
+
+def _as_struct(obj, cls):
+    """obj as an instance of cls: a structure of the same layout from another
+    copy of the mirror module is copied field by field."""
+    if isinstance(obj, cls):
+        return obj
+    out = cls()
+    for f, _ in cls._fields_:
+        setattr(out, f, getattr(obj, f))
+    return out
 
 
 class OracleError(ValueError):
@@ -42,7 +72,7 @@ def build() -> None:
 
 
 def _model_c(model) -> _abi.KxModel:
-    return model._c() if hasattr(model, "_c") else model
+    return _as_struct(model._c() if hasattr(model, "_c") else model, _abi.KxModel)
 
 
 def _rate(model, rate):
@@ -278,7 +308,7 @@ class Oracle:
 
     def price_multi(self, js: str, model, n_paths=100_000, seed=42, steps_per_year=50, per_path=False):
         """price_gbm under CorrelatedGbmN (multi_asset.rs:107-170)."""
-        mm = model._c()
+        mm = _as_struct(model._c(), _abi.KxMultiGbm)
         cfg = self.cfg(n_paths, seed, steps_per_year, model.rate)
         r = _abi.KxPriceResult()
         pp = np.zeros(max(1, n_paths)) if per_path else None

@@ -63,6 +63,27 @@ def test_fixed_scratch_per_path_values():
         assert np.allclose(pv2, np.asarray(pv), rtol=TOL, atol=TOL)
 
 
+def test_fixed_scratch_call_leaves_free_device_memory_unchanged():
+    # the property the entry point exists for: after a first call (set-up),
+    # a call takes no device memory, so the device's free memory is the same
+    # before and after it, even for a launch kx_price has not sized its
+    # buffers for yet
+    torch = pytest.importorskip("torch")
+    c = kx.up_and_out_call("X", 100.0, 150.0, 1.0)
+    m = kx.GBM(s0=100.0, sigma=0.3, r=0.02, asset="X")
+    for prec in ("fp32", "fp64"):  # set-up, and the lazy loading of both kernels' code
+        st, _, _ = _fixed(c, m, 1000, 5, 52, prec)
+        assert st == 0, kx._lib().kx_last_error_message()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for n, prec in ((1 << 20, "fp32"), (300_000, "fp64")):
+        st, r, _ = _fixed(c, m, n, 9, 252, prec)
+        assert st == 0 and r.n_paths == n
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
+
+
 def test_fixed_scratch_rejects_sizes_beyond_its_limits():
     c = kx.european_call("X", 100.0, 1.0)
     m = kx.GBM(s0=100.0, sigma=0.2, r=0.01, asset="X")
