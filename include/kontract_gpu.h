@@ -189,6 +189,13 @@ int32_t kx_abi_version(void);
 /* Message of the last failing call on this thread ("" if none). */
 const char *kx_last_error_message(void);
 
+/* Payload of the last failing call on this thread, so that a binding can
+ * rebuild KontractError::TimeOutOfRange(f64) and StepOutOfRange(usize)
+ * (src/error.rs:11-15) without parsing the message: *time receives the date
+ * of KX_TIME_OUT_OF_RANGE (NaN for any other outcome), *step the index of
+ * KX_STEP_OUT_OF_RANGE (UINT64_MAX otherwise). Either pointer may be NULL. */
+kx_status kx_last_error_payload(double *time, uint64_t *step);
+
 /* Parse the serde JSON of a Contract (Contract::from_json, src/ast.rs:215),
  * run the compiler (compile, src/compiler.rs:69) and lower the AST to the
  * flat trigger/flow/accumulator table the kernels interpret. Replaces the
@@ -415,6 +422,15 @@ kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *mo
                                       const kx_mc_config *cfg, const double *dates,
                                       size_t n_dates, int32_t n_basis, int32_t basis,
                                       kx_price_result *out);
+
+/* kx_price_american_lsm_basis with every path's discounted realised value
+ * (lsm.rs:226) in per_path_pv (nullable, cfg->n_paths doubles): the value of
+ * the payoff at the date the path is exercised, discounted to t = 0, so a
+ * caller can compare exercise decisions path by path. */
+kx_status kx_price_american_lsm_paths(const kx_program *prog, const kx_model *model,
+                                      const kx_mc_config *cfg, const double *dates,
+                                      size_t n_dates, int32_t n_basis, int32_t basis,
+                                      kx_price_result *out, double *per_path_pv);
 
 /* n independent kx_price_american_lsm_basis problems in one call (no
  * reference counterpart; the reference prices one American option per

@@ -29,11 +29,14 @@ USD, EUR, GBP, JPY = "USD", "EUR", "GBP", "JPY"
 
 class KontractError(ValueError):
     """Raised for every engine error (the reference raises ValueError,
-    src/bindings.rs:50-52). `.status` is the kx_status name."""
+    src/bindings.rs:50-52). `.status` is the kx_status name; `.payload` the
+    date of TimeOutOfRange or the index of StepOutOfRange (error.rs:11-15),
+    else None."""
 
-    def __init__(self, status: int, message: str):
+    def __init__(self, status: int, message: str, payload=None):
         self.code = status
         self.status = _abi.STATUS_NAMES.get(status, str(status))
+        self.payload = payload
         super().__init__(f"{self.status}: {message}")
 
 
@@ -46,8 +49,12 @@ def _lib():
 
 def _check(st: int) -> None:
     if st != _abi.KX_OK:
-        msg = _lib().kx_last_error_message().decode("utf-8", "replace")
-        raise KontractError(st, msg)
+        lib = _lib()
+        msg = lib.kx_last_error_message().decode("utf-8", "replace")
+        t, k = C.c_double(), C.c_uint64()
+        lib.kx_last_error_payload(C.byref(t), C.byref(k))
+        payload = t.value if st == _abi.KX_TIME_OUT_OF_RANGE else k.value if st == _abi.KX_STEP_OUT_OF_RANGE else None
+        raise KontractError(st, msg, payload)
 
 
 # ---------------------------------------------------------------------------
@@ -487,10 +494,12 @@ class Contract:
 
     def price_american(self, model, exercise_dates: Sequence[float], n_paths: int = 100_000, seed: int = 42,
                        n_basis: int = 3, *, precision: str = "fp32", shared_draws: bool = False,
-                       basis: str = "monomial") -> PriceResult:
+                       basis: str = "monomial", per_path: bool = False):
         """Longstaff-Schwartz American pricing (lsm.rs:80-124); `self` is the
         exercised payoff, e.g. (K - S).clip(0) * one(USD). basis: "monomial"
-        (the reference's) or "laguerre" (weighted Laguerre functions of S/s0)."""
+        (the reference's) or "laguerre" (weighted Laguerre functions of S/s0).
+        per_path=True also returns every path's discounted realised value
+        (a numpy array)."""
         if basis not in ("monomial", "laguerre"):
             raise ValueError("basis must be 'monomial' or 'laguerre'")
         if not isinstance(model, (GBM, Model)):
@@ -499,11 +508,18 @@ class Contract:
         cfg = _cfg(n_paths, seed, 50, model.rate, precision, shared_draws)
         d = (C.c_double * max(1, len(exercise_dates)))(*[float(x) for x in exercise_dates])
         out = _abi.KxPriceResult()
+        pp = None
+        if per_path:
+            import numpy as np
+            pp = np.zeros(max(1, int(n_paths)))
         with _lock:
-            _check(_lib().kx_price_american_lsm_basis(self._handle().h, C.byref(cm), C.byref(cfg), d,
+            _check(_lib().kx_price_american_lsm_paths(self._handle().h, C.byref(cm), C.byref(cfg), d,
                                                       len(exercise_dates), int(n_basis),
                                                       _abi.KX_LSM_LAGUERRE if basis == "laguerre" else _abi.KX_LSM_MONOMIAL,
-                                                      C.byref(out)))
+                                                      C.byref(out),
+                                                      pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
+        if per_path:
+            return PriceResult(out), pp[: int(n_paths)]
         return PriceResult(out)
 
 

@@ -159,6 +159,7 @@ _P = C.c_void_p
 SIGNATURES = {
     "kx_abi_version": (C.c_int32, []),
     "kx_last_error_message": (C.c_char_p, []),
+    "kx_last_error_payload": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "kx_compile": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "kx_program_free": (None, [_P]),
     "kx_program_plan": (C.c_int, [_P, C.POINTER(KxPlanInfo), C.POINTER(C.c_double), C.c_size_t,
@@ -202,6 +203,9 @@ SIGNATURES = {
     "kx_price_american_lsm_basis": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                               C.POINTER(C.c_double), C.c_size_t, C.c_int32, C.c_int32,
                                               C.POINTER(KxPriceResult)]),
+    "kx_price_american_lsm_paths": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig),
+                                              C.POINTER(C.c_double), C.c_size_t, C.c_int32, C.c_int32,
+                                              C.POINTER(KxPriceResult), C.POINTER(C.c_double)]),
     "kx_price_american_lsm_batch": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
                                               C.POINTER(KxMcConfig), C.POINTER(C.POINTER(C.c_double)),
                                               C.POINTER(C.c_size_t), C.c_int32, C.c_int32,

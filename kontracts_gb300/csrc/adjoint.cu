@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;  // > 0 beyond the barrier
-                    surv[u] *= logistic(x);
+                    surv[u] *= smooth_weight(x);
                     const bool hit = pp.sgn[u] * y >= pp.hit[u];
                     if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
@@ -413,8 +413,8 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real s = logistic(x);
-                        const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy|
+                        const Real s = smooth_weight(x);
+                        const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy| (0 where s is exactly 1)
                         g -= Q[u] * pp.sgn[u] * dls;
                     }
                 // leaving an average window when walking below its first step
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
-                    surv[u] *= logistic(x);
+                    surv[u] *= smooth_weight(x);
                     if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
                 }
             if (k != nft) continue;
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real sv = logistic(x);
+                        const Real sv = smooth_weight(x);
                         g -= Q[u] * pp.sgn[u] * (Real(1) - sv) * inv_w;
                     }
                 lam += g;

@@ -12,9 +12,13 @@ struct kx_program {
 
 namespace kx {
 thread_local std::string g_last_error;
+thread_local double g_last_error_time = __builtin_nan("");
+thread_local uint64_t g_last_error_step = UINT64_MAX;
 
 kx_status fail_status(const Error &e) {
     g_last_error = e.msg;
+    g_last_error_time = e.time;
+    g_last_error_step = e.step;
     return e.code;
 }
 const Program &program_of(const kx_program *h, bool need_lowered) {
@@ -31,6 +35,12 @@ extern "C" {
 int32_t kx_abi_version(void) { return KX_ABI_VERSION; }
 
 const char *kx_last_error_message(void) { return g_last_error.c_str(); }
+
+kx_status kx_last_error_payload(double *time, uint64_t *step) {
+    if (time) *time = g_last_error_time;
+    if (step) *step = g_last_error_step;
+    return KX_OK;
+}
 
 kx_status kx_compile(const char *contract_json, kx_program **out) {
     return guarded([&] {

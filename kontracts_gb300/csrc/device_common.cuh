@@ -115,6 +115,19 @@ __device__ __forceinline__ double next_down(double t) { return ::nextafter(t, -(
 __device__ __forceinline__ float logistic(float x) { return __fdividef(1.0f, 1.0f + __expf(x)); }
 __device__ __forceinline__ double logistic(double x) { return 1.0 / (1.0 + exp(x)); }
 
+// The weight of one step under a smoothed barrier, logistic(x) with x the
+// signed distance past the barrier in widths. Where 1 + e^x rounds to 1 in
+// the arithmetic's precision (e^x below half an ulp of 1: x <= -17 in FP32,
+// x <= -38 in FP64) the weight is exactly 1, so a kernel may skip those steps
+// and still agree bit for bit with one that evaluates them.
+template <class Real> __device__ __forceinline__ Real smooth_cut();
+template <> __device__ __forceinline__ float smooth_cut<float>() { return -17.0f; }
+template <> __device__ __forceinline__ double smooth_cut<double>() { return -38.0; }
+template <class Real>
+__device__ __forceinline__ Real smooth_weight(Real x) {
+    return x <= smooth_cut<Real>() ? Real(1) : logistic(x);
+}
+
 // Separately rounded arithmetic in either precision (never fused into an FMA).
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }

@@ -318,10 +318,13 @@ template void pack_steps<double>(const StepTables &, std::vector<unsigned char> 
 // Launch the fused path kernel over `jobs` (all of one model kind, one
 // precision and one scenario count). Per-path values land in c.pv:
 // scenario s of job j, path i at s * stride + jobs[j].dev.pv_off + i.
-const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat, bool acc) {
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat, bool acc, bool sm) {
     if (model == KX_MODEL_MULTI_GBM) return paths_kernel_multi(f64, minb);  // general handler
-    if (lean)
-        return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc) : lean_kernel_heston(f64, minb, stat, acc);
+    if (lean) {
+        if (sm && model != KX_MODEL_GBM) return nullptr;
+        return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc, sm)
+                                     : lean_kernel_heston(f64, minb, stat, acc);
+    }
     if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
     if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
     return paths_kernel_heston(f64, minb);
@@ -338,12 +341,31 @@ static bool lean_average(const KxProgram &P) {
     return P.n_acc == 1 && P.acc[0].inner == IK_SPOT && !P.acc[0].static_err;
 }
 
+// until(Spot cmp Const) slots that a smoothed job weighs instead of knocking.
+static int smoothed_untils(const Job &j) {
+    if (!j.dev.smooth) return 0;
+    int n = 0;
+    for (int i = 0; i < j.prog.n_trig; ++i)
+        n += j.prog.trig[i].kind == TK_UNTIL && j.prog.trig[i].cond_kind == CK_SPOT_CMP;
+    return n;
+}
+
+bool lean_smoothed(const std::vector<Job> &jobs) {
+    for (auto &j : jobs)
+        if (smoothed_untils(j)) return true;
+    return false;
+}
+
 static bool lean_applies(const std::vector<Job> &jobs, int ns) {
     if (ns != 1) return false;
     bool avg = false;
+    const bool sm = lean_smoothed(jobs);
     for (auto &j : jobs) {
         if (j.model.kind == KX_MODEL_MULTI_GBM) return false;
-        if (j.dev.smooth) return false;
+        if (sm) {  // smoothed barriers: GBM on static schedules (survival weights in registers)
+            StaticDev T;
+            if (j.model.kind != KX_MODEL_GBM || j.prog.n_acc || !build_static(j, T)) return false;
+        }
         if (j.prog.n_acc && !lean_average(j.prog)) return false;
         // the spot each step: for the average (kept by k_lean) or a general condition (not served)
         if (j.prog.spot_each_step && !j.prog.n_acc) return false;
@@ -368,8 +390,8 @@ bool lean_has_average(const std::vector<Job> &jobs) {
 bool use_lean(const std::vector<Job> &jobs, int ns) {
     const char *env = getenv("KX_PATH_KERNEL");
     if (env && strcmp(env, "general") == 0) return false;
-    // "lean" forces the general event handler, which keeps no averages
-    if (env && strcmp(env, "lean") == 0 && lean_has_average(jobs)) return false;
+    // "lean" forces the general event handler, which keeps no averages and weighs no barrier
+    if (env && strcmp(env, "lean") == 0 && (lean_has_average(jobs) || lean_smoothed(jobs))) return false;
     return lean_applies(jobs, ns);
 }
 
@@ -396,12 +418,30 @@ bool build_static(const Job &j, StaticDev &T) {
         for (int i = 0; i < P.n_trig; ++i)
             if ((f.price_untils >> i) & 1u) T.kill[i] |= 1u << f.leaf;
     }
+    const bool smooth = j.dev.smooth != 0;
+    int sm_spot[KX_MAX_SM] = {-1, -1};
     for (int i = 0; i < P.n_trig; ++i) {
         const KxTrig &Tr = P.trig[i];
         if (Tr.cond_kind == CK_GENERAL) return false;
         if (Tr.cond_kind != CK_SPOT_CMP) continue;
         if (Tr.kind != TK_UNTIL) return false;
         if (S.arm[i] == StaticSchedule::NEVER || T.kill[i] == 0u) continue;  // never tested, or drops nothing
+        if (smooth) {  // weighs instead of knocking: no arming event, not a live barrier
+            if (P.n_acc || T.n_sm >= KX_MAX_SM) return false;
+            for (int q = 0; q < T.n_sm; ++q)
+                if (sm_spot[q] == Tr.spot_slot) return false;  // one weight per condition slot (as on_event)
+            const int q = T.n_sm++;
+            sm_spot[q] = Tr.spot_slot;
+            const double t = j.thr[Tr.spot_slot];
+            const bool down = Tr.cmp == CMP_LE || Tr.cmp == CMP_LT;
+            T.sm_arm[q] = S.arm[i];
+            T.sm_flows[q] = T.kill[i];
+            T.sm_thr64[q] = t;
+            T.sm_thr32[q] = (float)t;
+            T.sm_mul64[q] = down ? -j.dev.inv_w : j.dev.inv_w;  // (y - t) * -m is exactly -((y - t) * m)
+            T.sm_mul32[q] = down ? -j.dev.inv_wf : j.dev.inv_wf;
+            continue;
+        }
         at[S.arm[i]].first |= 1u << i;
         const double t = j.thr[Tr.spot_slot];
         const float tf = (float)t;
@@ -552,7 +592,9 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.lean = lean;
     P.stat = lean && stat;
     P.acc = P.stat && lean_has_average(jobs);
+    P.sm = P.stat && lean_smoothed(jobs);
     if (lean && !P.stat && lean_has_average(jobs)) raise(KX_CUDA_ERROR, "averages need the static family");
+    if (lean && !P.stat && lean_smoothed(jobs)) raise(KX_CUDA_ERROR, "smoothed barriers need the static family");
     if (P.stat) {
         P.statics.resize(jobs.size());
         for (size_t q = 0; q < jobs.size(); ++q)
@@ -602,7 +644,7 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.surv_base = 2u * (uint32_t)max_acc;
     P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
     P.smem = lean ? 0 : (size_t)ns * P.slots * block * (f64 ? 8 : 4);  // k_lean keeps its average in registers
-    P.kfn = pair ? paths_kernel_pair(P.model, f64) : select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc);
+    P.kfn = pair ? paths_kernel_pair(P.model, f64) : select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc, P.sm);
     if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (P.smem > 48 * 1024)
         KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
@@ -1289,7 +1331,8 @@ static void greek_stats(uint64_t begin, uint64_t n, const double h[3], StatsJob 
 // therefore the same normals. The lean kernels value each job at the speed
 // of a plain price; the seven values of a path sit n_paths apart.
 static void append_reprices(std::vector<Job> &jobs, const Program &p, const Model &base, const kx_mc_config &cfg,
-                            const std::vector<double> &grid, const std::vector<Scenario> &sc) {
+                            const std::vector<double> &grid, const std::vector<Scenario> &sc, int smooth = 0,
+                            double smooth_w = 0.0) {
     for (const Scenario &s : sc) {
         Model m = base;
         m.s0 = s.s0;
@@ -1297,7 +1340,7 @@ static void append_reprices(std::vector<Job> &jobs, const Program &p, const Mode
         m.sigma = s.sigma;
         kx_mc_config c2 = cfg;
         c2.rate = s.rate;
-        jobs.push_back(make_job(p, m, c2, grid, {}, 0, 0.0));
+        jobs.push_back(make_job(p, m, c2, grid, {}, smooth, smooth_w));
     }
 }
 
@@ -1527,15 +1570,12 @@ kx_status kx_greeks_bump(const kx_program *prog, const kx_model *model, const kx
         std::vector<Job> jobs;
         std::vector<StatsJob> sj(5);
         uint64_t stride = 0;
-        if (b.smooth) {  // the smoothed payoff: one job whose seven scenarios share each path's draws
-            const double w = b.smoothing_width;
-            jobs.push_back(make_job(p, mb, *cfg, grid, sc, 1, w > 0 ? w : 1.0));
-            run_paths(c, jobs, *cfg, KX_MAX_NS, stride);
-        } else {
-            append_reprices(jobs, p, mb, *cfg, grid, sc);
-            run_paths(c, jobs, *cfg, 1, stride);
-            stride = cfg->n_paths;
-        }
+        // the seven reprices as plain jobs of one launch (the smoothed payoff: each job
+        // weighs its barriers with the logistic of the stated width instead of knocking)
+        const double w = b.smoothing_width;
+        append_reprices(jobs, p, mb, *cfg, grid, sc, b.smooth ? 1 : 0, w > 0 ? w : 1.0);
+        run_paths(c, jobs, *cfg, 1, stride);
+        stride = cfg->n_paths;
         greek_stats(0, cfg->n_paths, h, sj.data());
         auto st = device_stats(c, c.pv.as<double>(), stride, sj);
         fill_greeks(st.data(), out);

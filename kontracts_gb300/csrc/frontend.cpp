@@ -12,6 +12,17 @@
 namespace kx {
 
 void raise(kx_status code, const std::string &msg) { throw Error{code, msg}; }
+// the reference's messages (src/error.rs:11-15), with the payload kept apart
+void raise_time_out_of_range(double t) {
+    Error e{KX_TIME_OUT_OF_RANGE, "date d'observation hors de la timeline : " + std::to_string(t)};
+    e.time = t;
+    throw e;
+}
+void raise_step_out_of_range(uint64_t step) {
+    Error e{KX_STEP_OUT_OF_RANGE, "pas de temps hors de la trajectoire : index " + std::to_string(step)};
+    e.step = step;
+    throw e;
+}
 
 // ============================================================================
 // serde_json reader for the externally tagged enums of src/ast.rs.

@@ -11,12 +11,18 @@
 
 namespace kx {
 
-// Thrown by host code; converted to kx_status at the C boundary.
+// Thrown by host code; converted to kx_status at the C boundary. `time` and
+// `step` carry the payloads of KontractError::TimeOutOfRange(f64) and
+// StepOutOfRange(usize) (src/error.rs:11-15); NaN / UINT64_MAX otherwise.
 struct Error {
     kx_status code;
     std::string msg;
+    double time = __builtin_nan("");
+    uint64_t step = UINT64_MAX;
 };
 [[noreturn]] void raise(kx_status code, const std::string &msg);
+[[noreturn]] void raise_time_out_of_range(double t);
+[[noreturn]] void raise_step_out_of_range(uint64_t step);
 
 // ---- AST (src/ast.rs:34-206) ------------------------------------------------
 enum class NK {

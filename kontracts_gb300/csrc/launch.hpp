@@ -35,12 +35,15 @@ template <class Real>
 void pack_steps(const StepTables &t, std::vector<unsigned char> &out);
 
 // Path kernel for a model, precision, scenario count and register budget.
-const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat = false, bool acc = false);
+const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool stat = false, bool acc = false,
+                          bool sm = false);
 
 // Whether the lean kernel serves these jobs (KX_PATH_KERNEL may force the general one).
 bool use_lean(const std::vector<Job> &jobs, int ns);
 // Whether some job keeps a running average (the lean kernel's ACC variant).
 bool lean_has_average(const std::vector<Job> &jobs);
+// Whether some job weighs smoothed barriers (the lean kernel's SM variant).
+bool lean_smoothed(const std::vector<Job> &jobs);
 
 // Compiles the static schedule of a job; false when it has none.
 bool build_static(const Job &j, StaticDev &T);
@@ -54,7 +57,7 @@ const int *variants(int model, bool f64, int ns, bool lean, int &n);
 
 // Host-side tables and geometry of one path-kernel launch over `jobs`.
 struct PathPlan {
-    bool f64 = false, lean = false, stat = false, acc = false;
+    bool f64 = false, lean = false, stat = false, acc = false, sm = false;
     int model = 0, ns = 1, minb = 0;
     std::vector<KxProgram> progs;
     std::vector<unsigned char> steps, thr;

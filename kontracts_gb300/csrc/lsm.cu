@@ -19,6 +19,7 @@
 //     through the same deterministic statistics as every price.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "device_common.cuh"
@@ -490,7 +491,8 @@ __device__ void solve_gauss_warp_ff(const ff *red, int NA, ff (&x)[LSM_MAXM]) {
 constexpr int LSM_PPT = 32;
 constexpr unsigned LSM_TILE = LSM_BLOCK * LSM_PPT;
 constexpr int LSM_NSUM = 32;                    // stride of a partial (>= m(m+1)/2 + m + 1 for m <= 6)
-constexpr unsigned LSM_SPIN_LIMIT = 1u << 22;   // polls of a wait (32 ns apart at least) before giving up
+constexpr unsigned LSM_SPIN_LIMIT = 1u << 22;   // polls of a wait (32 ns apart at least) before giving up;
+                                                // KX_LSM_SPIN_LIMIT in the environment overrides it (tests)
 constexpr int LSM_MAX_CASES = 1024;             // cases of one backward launch
 constexpr int LSM_MAX_COORD = 16;               // coordinator blocks of one backward launch
 
@@ -555,13 +557,14 @@ __device__ __forceinline__ void lsm_sum_rows_ff(const float2 *src, unsigned n, f
 // Waits until the published iteration count of a case reaches `want`
 // (thread 0 polls, bounded); false when the wait gave up or another block
 // reported an error. Called by the whole block.
-__device__ __forceinline__ bool lsm_wait(const unsigned *ready, unsigned want, unsigned *err, int &flag) {
+__device__ __forceinline__ bool lsm_wait(const unsigned *ready, unsigned want, unsigned *err, int &flag,
+                                         unsigned spin_limit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         bool ok = true;
         unsigned n = 0;
         while (*(volatile const unsigned *)ready < want) {
-            if (++n > LSM_SPIN_LIMIT || *(volatile unsigned *)err != 0u) {
+            if (++n > spin_limit || *(volatile unsigned *)err != 0u) {
                 ok = false;
                 break;
             }
@@ -970,11 +973,11 @@ __device__ void lsm_solve_case(const LsmArgs &A, int it, double *red) {
 // k + n_coord, ... (one thread per case, so one round trip covers them) and
 // runs lsm_solve_case for every case whose iteration is complete, the lowest
 // case first. Each case has n_ex - 1 regressions (iterations 0 .. n_ex - 2).
-// A poll that sees no progress for LSM_SPIN_LIMIT rounds gives up and sets the
+// A poll that sees no progress for spin_limit rounds gives up and sets the
 // error word.
 template <class Real, int M>
 __device__ void lsm_coordinator(const LsmArgs *cases, int n_cases, int k, int n_coord, unsigned *err, double *red,
-                                int *next, int &ready_c) {
+                                int *next, int &ready_c, unsigned spin_limit) {
     for (int c = threadIdx.x; c < n_cases; c += blockDim.x) next[c] = 0;
     __syncthreads();
     unsigned idle = 0;
@@ -998,7 +1001,7 @@ __device__ void lsm_coordinator(const LsmArgs *cases, int n_cases, int k, int n_
             if (threadIdx.x == 0) ++next[c];
             __syncthreads();
         } else {
-            if (++idle > LSM_SPIN_LIMIT || *(volatile unsigned *)err != 0u) {
+            if (++idle > spin_limit || *(volatile unsigned *)err != 0u) {
                 if (threadIdx.x == 0) atomicOr(err, 1u);
                 return;
             }
@@ -1016,13 +1019,15 @@ __device__ void lsm_coordinator(const LsmArgs *cases, int n_cases, int k, int n_
 // no launch ends between dates.
 template <class Real, int M, int B, bool GEN>
 __global__ void __launch_bounds__(LSM_BLOCK, sizeof(Real) == 4 ? 4 : 2)
-    k_lsm_backward(const LsmArgs *__restrict__ cases, int n_cases, int max_ex, int n_coord, unsigned *err) {
+    k_lsm_backward(const LsmArgs *__restrict__ cases, int n_cases, int max_ex, int n_coord, unsigned *err,
+                   unsigned spin_limit) {
     __shared__ double red[LSM_RED_OUT + 32];
     __shared__ int flag;
     const unsigned n_tile_blocks = gridDim.x - (unsigned)n_coord;
     if (blockIdx.x >= n_tile_blocks) {  // the coordinators: the regression solves
         __shared__ int next[LSM_MAX_CASES];
-        lsm_coordinator<Real, M>(cases, n_cases, (int)(blockIdx.x - n_tile_blocks), n_coord, err, red, next, flag);
+        lsm_coordinator<Real, M>(cases, n_cases, (int)(blockIdx.x - n_tile_blocks), n_coord, err, red, next, flag,
+                                 spin_limit);
         return;
     }
     extern __shared__ __align__(16) float4 lsm_ring[];  // FP32: [LSM_NSTAGE][3][LSM_BLOCK]
@@ -1032,7 +1037,7 @@ __global__ void __launch_bounds__(LSM_BLOCK, sizeof(Real) == 4 ? 4 : 2)
     while (more) {
         const LsmArgs &A = cases[cur.c];
         if (cur.it > 0 && (cur.c != seen_c || cur.it != seen_it)) {
-            if (!lsm_wait(A.sync, (unsigned)cur.it, err, flag)) break;
+            if (!lsm_wait(A.sync, (unsigned)cur.it, err, flag, spin_limit)) break;
             seen_c = cur.c;
             seen_it = cur.it;
         }
@@ -1156,7 +1161,8 @@ static size_t lsm_case_bytes(const LsmCase &L, size_t rs) {
 
 // Prices the cases (all of one precision): uploads, forward simulations, the
 // cooperative backward launch, per-path statistics.
-static void lsm_run(Ctx &c, std::vector<LsmCase> &cs, bool f64, int n_basis, int basis, kx_price_result *out) {
+static void lsm_run(Ctx &c, std::vector<LsmCase> &cs, bool f64, int n_basis, int basis, kx_price_result *out,
+                    double *const *per_path = nullptr) {
     const size_t n = cs.size();
     const size_t rs = f64 ? 8 : 4;
     std::vector<size_t> off(n + 1, 0);
@@ -1244,7 +1250,12 @@ static void lsm_run(Ctx &c, std::vector<LsmCase> &cs, bool f64, int n_basis, int
         if (cap < (uint64_t)n_coord + 1) n_coord = (int)std::max<uint64_t>(1, cap / 2);
         const unsigned grid = (unsigned)std::min<uint64_t>(cap, tot_tiles + n_coord);
         int n_cases = (int)n;
-        void *kargs[] = {(void *)&cases_dev, (void *)&n_cases, (void *)&max_ex, (void *)&n_coord, (void *)&err};
+        // every wait of the launch gives up after spin_limit polls; a test sets a tiny limit through
+        // KX_LSM_SPIN_LIMIT to make a wait run out (the call then fails with KX_DEVICE_TIMEOUT)
+        unsigned spin_limit = LSM_SPIN_LIMIT;
+        if (const char *e = getenv("KX_LSM_SPIN_LIMIT")) spin_limit = (unsigned)strtoul(e, nullptr, 10);
+        void *kargs[] = {(void *)&cases_dev, (void *)&n_cases, (void *)&max_ex, (void *)&n_coord, (void *)&err,
+                         (void *)&spin_limit};
         KX_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(LSM_BLOCK), kargs, dyn, c.stream));
         c.last.kernel_launches++;
         KX_CUDA(cudaEventRecord(c.ev1, c.stream));
@@ -1258,15 +1269,22 @@ static void lsm_run(Ctx &c, std::vector<LsmCase> &cs, bool f64, int n_basis, int
     }
     auto st = device_stats(c, reinterpret_cast<const double *>(base), 0, sj);
     for (size_t i = 0; i < n; ++i) out[i] = finish(st[i]);
+    if (per_path)
+        for (size_t i = 0; i < n; ++i)
+            if (per_path[i] && cs[i].np) {
+                KX_CUDA(cudaMemcpy(per_path[i], cs[i].a.pv, cs[i].np * sizeof(double), cudaMemcpyDeviceToHost));
+                c.last.d2h_bytes += cs[i].np * sizeof(double);
+            }
 }
 
 }  // namespace kx
 
 using namespace kx;
 
-extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *model,
+extern "C" kx_status kx_price_american_lsm_paths(const kx_program *prog, const kx_model *model,
                                                  const kx_mc_config *cfg, const double *dates, size_t n_dates,
-                                                 int32_t n_basis, int32_t basis, kx_price_result *out) {
+                                                 int32_t n_basis, int32_t basis, kx_price_result *out,
+                                                 double *per_path_pv) {
     return guarded([&] {
         if (!out) raise(KX_INVALID_ARGUMENT, "NULL argument");
         std::vector<LsmCase> cs;
@@ -1285,9 +1303,15 @@ extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const k
             L.a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
             L.a.z_dpp = ds.dpp;
         }
-        lsm_run(c, cs, cfg->precision == KX_PREC_FP64, n_basis, basis, out);
+        lsm_run(c, cs, cfg->precision == KX_PREC_FP64, n_basis, basis, out, &per_path_pv);
         c.last.total_ms += now_ms();
     });
+}
+
+extern "C" kx_status kx_price_american_lsm_basis(const kx_program *prog, const kx_model *model,
+                                                 const kx_mc_config *cfg, const double *dates, size_t n_dates,
+                                                 int32_t n_basis, int32_t basis, kx_price_result *out) {
+    return kx_price_american_lsm_paths(prog, model, cfg, dates, n_dates, n_basis, basis, out, nullptr);
 }
 
 extern "C" kx_status kx_price_american_lsm(const kx_program *prog, const kx_model *model, const kx_mc_config *cfg,

@@ -223,12 +223,13 @@ __device__ __forceinline__ bool cmp_y(uint8_t cmp, Real y, Real thr) {
 }
 
 // Survival weight of one step under a smoothed until(S cmp B): the breach
-// indicator 1{y cmp b} is replaced by the logistic sigma(+-(y - b) / w).
+// indicator 1{y cmp b} is replaced by the logistic sigma(+-(y - b) / w)
+// (smooth_weight: exactly 1 far inside the barrier).
 template <class Real>
 __device__ __forceinline__ Real smooth_survival(uint8_t cmp, Real y, Real thr, Real inv_w) {
     Real x = (y - thr) * inv_w;  // > 0 beyond the barrier for >=, >
     if (cmp == CMP_LE || cmp == CMP_LT) x = -x;
-    return logistic(x);
+    return smooth_weight(x);
 }
 
 // Full condition evaluation of the slots in `mask` at step k: time bits from

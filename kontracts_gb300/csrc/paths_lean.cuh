@@ -143,6 +143,7 @@ __device__ __forceinline__ Trig lean_event(const KxProgram *Pp, const ContractDe
 // order as on_event and is the same bit for bit.
 // ---------------------------------------------------------------------------
 constexpr int KX_MAX_SEV = 64;
+constexpr int KX_MAX_SM = 2;  // smoothed barriers a static schedule carries in registers
 
 struct StaticDev {
     int32_t n_ev;
@@ -162,6 +163,16 @@ struct StaticDev {
     uint8_t f_fast[KX_MAX_LEAF];  // KxFastAmount of the flow slot (FA_NONE: constant amount)
     double f_k[KX_MAX_LEAF];      // its constant K
     double f_sign[KX_MAX_LEAF];   // its sign (the constant amount itself for FA_NONE)
+    // Smoothed barriers (a bump of the smoothed payoff): until(Spot cmp Const)
+    // slots that never knock; from their arming step on, every step multiplies
+    // the slot's weight by smooth_weight(x), x = (y - thr) * mul (mul = +-1/w,
+    // negative for a downward barrier), and a paid flow is multiplied by the
+    // weights of the slots above it, in slot order (on_event's arithmetic).
+    int32_t n_sm;
+    int32_t sm_arm[KX_MAX_SM];     // first weighed step
+    uint32_t sm_flows[KX_MAX_SM];  // flow slots under the barrier
+    float sm_thr32[KX_MAX_SM], sm_mul32[KX_MAX_SM];
+    double sm_thr64[KX_MAX_SM], sm_mul64[KX_MAX_SM];
 };
 
 struct SLane {
@@ -202,9 +213,48 @@ __device__ __forceinline__ void acc_add(int kind, Real &v, Real &c, Real x) {
 // once, flows paid), as on_event orders them (pricer.rs:374-433). ACC: flows
 // in gen_flows read the running average (av, ac: its sum and compensation),
 // evaluated by the interpreter as on_event evaluates them.
-template <class Real, bool ACC = false>
+// Smoothed barriers of one contract (warp-uniform, from StaticDev) and the
+// weight update of one step: slot q (live in `sml`, armed at or before step
+// k) multiplies its weight by smooth_weight((y - t_q) m_q), skipping the
+// steps where that weight is exactly 1.
+template <class Real>
+struct SmoothPar {
+    int n;
+    int a0, a1;
+    Real t0, t1, m0, m1;
+};
+
+template <class Real>
+__device__ __forceinline__ SmoothPar<Real> smooth_par(const StaticDev &T) {
+    const bool f = sizeof(Real) == 4;
+    return SmoothPar<Real>{T.n_sm, T.sm_arm[0], T.sm_arm[1],
+                           f ? (Real)T.sm_thr32[0] : (Real)T.sm_thr64[0], f ? (Real)T.sm_thr32[1] : (Real)T.sm_thr64[1],
+                           f ? (Real)T.sm_mul32[0] : (Real)T.sm_mul64[0], f ? (Real)T.sm_mul32[1] : (Real)T.sm_mul64[1]};
+}
+
+template <class Real>
+__device__ __forceinline__ void smooth_step(const SmoothPar<Real> &sp, Real y, int k, uint32_t sml, Real &w0,
+                                            Real &w1) {
+    if ((sml & 1u) && k >= sp.a0) {
+        const Real x = (y - sp.t0) * sp.m0;
+        if (x > smooth_cut<Real>()) w0 *= logistic(x);
+    }
+    if ((sml & 2u) && k >= sp.a1) {
+        const Real x = (y - sp.t1) * sp.m1;
+        if (x > smooth_cut<Real>()) w1 *= logistic(x);
+    }
+}
+
+// A live smoothed weight reached exactly 0: its flows can add nothing more.
+template <class Real>
+__device__ __forceinline__ bool smooth_zero(uint32_t sml, Real w0, Real w1) {
+    return ((sml & 1u) && w0 == Real(0)) || ((sml & 2u) && w1 == Real(0));
+}
+
+template <class Real, bool ACC = false, bool SM = false>
 __device__ __forceinline__ void static_event(const StaticDev &T, const double *D, Real s0, Real y, int k, SLane &L,
-                                             const KxProgram *P = nullptr, Real av = Real(0), Real ac = Real(0)) {
+                                             const KxProgram *P = nullptr, Real av = Real(0), Real ac = Real(0),
+                                             Real w0 = Real(1), Real w1 = Real(1), uint32_t *sml = nullptr) {
     uint32_t m = L.live;
     while (m) {
         const int i = __ffs(m) - 1;
@@ -247,11 +297,25 @@ __device__ __forceinline__ void static_event(const StaticDev &T, const double *D
                     }
                     amt = (double)(T.f_sign[j] < 0.0 ? -r : r);
                 }
+                if (SM) {  // the weights of the smoothed barriers above the flow, in slot order
+                    if (T.n_sm > 0 && ((T.sm_flows[0] >> j) & 1u) && k >= T.sm_arm[0]) amt *= (double)w0;
+                    if (T.n_sm > 1 && ((T.sm_flows[1] >> j) & 1u) && k >= T.sm_arm[1]) amt *= (double)w1;
+                }
                 L.pv = __dadd_rn(L.pv, __dmul_rn(amt, D[k]));
             }
         }
         L.rem &= ~T.ev_pay[L.e];
         ++L.e;
+    }
+    if (SM) {  // a weight that reached 0 zeroes its flows: drop them (they would add +-0)
+        if ((*sml & 1u) && w0 == Real(0)) {
+            L.rem &= ~T.sm_flows[0];
+            *sml &= ~1u;
+        }
+        if ((*sml & 2u) && w1 == Real(0)) {
+            L.rem &= ~T.sm_flows[1];
+            *sml &= ~2u;
+        }
     }
 }
 
@@ -282,10 +346,12 @@ struct HestonPar {
 // the same bit for bit whichever way the block is walked. ACC: the spot of
 // every step in af .. at is added to the accumulator of kind AK (av, ac;
 // AK < 0: none).
-template <class Real, int MODEL, bool UNI, int AK>
+template <class Real, int MODEL, bool UNI, int AK, bool SM = false>
 __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Real uc1, const HestonPar<Real> &hp,
                                            const Real (&zz)[4], int off, Real hi, Real lo, int lim, Real &y, Real &v,
-                                           int &k, Real s0, int af, int at, Real &av, Real &ac) {
+                                           int &k, Real s0, int af, int at, Real &av, Real &ac,
+                                           const SmoothPar<Real> *sp = nullptr, uint32_t sml = 0u,
+                                           Real *w0 = nullptr, Real *w1 = nullptr) {
     constexpr bool ACC = AK >= 0;
     constexpr int SPB = MODEL == M_GBM ? 4 : 2;
     // GBM: a whole block is stepped first and tested once (min and max of its
@@ -295,6 +361,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
     if (MODEL == M_GBM && off == 0) {
         Real yy = y, vv = v, mx = Real(-INFINITY), mn = Real(INFINITY);
         Real av2 = av, ac2 = ac;
+        Real w0c = SM ? *w0 : Real(1), w1c = SM ? *w1 : Real(1);
 #pragma unroll
         for (int j = 0; j < SPB; ++j) {
             Real c0 = uc0, c1 = uc1;
@@ -310,15 +377,21 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                                   zz[2 * j], zz[2 * j + 1], yy, vv);
             }
             if (ACC && k + j >= af && k + j <= at) acc_add<Real, AK>(AK, av2, ac2, spot_of<Real>(s0, yy));
+            if (SM) smooth_step<Real>(*sp, yy, k + j, sml, w0c, w1c);
             mx = fmax(mx, yy);
             mn = fmin(mn, yy);
         }
-        if (mx < hi && mn > lo && k + SPB - 1 < lim) {  // nothing fires inside the block
+        if (mx < hi && mn > lo && k + SPB - 1 < lim && !(SM && smooth_zero<Real>(sml, w0c, w1c))) {
+            // nothing fires inside the block
             y = yy;
             v = vv;
             if (ACC) {
                 av = av2;
                 ac = ac2;
+            }
+            if (SM) {
+                *w0 = w0c;
+                *w1 = w1c;
             }
             k += SPB;
             return false;
@@ -341,7 +414,8 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                                   zz[2 * j], zz[2 * j + 1], y, v);
             }
             if (ACC && k >= af && k <= at) acc_add<Real, AK>(AK, av, ac, spot_of<Real>(s0, y));
-            if (y >= hi || y <= lo || k >= lim) ev = true;
+            if (SM) smooth_step<Real>(*sp, y, k, sml, *w0, *w1);
+            if (y >= hi || y <= lo || k >= lim || (SM && smooth_zero<Real>(sml, *w0, *w1))) ev = true;
             else ++k;
         }
     }
@@ -349,10 +423,13 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
 }
 
 // ACC (static schedules only): the contracts may keep one accumulator of the
-// spot (slot 0: an average, a running max or min), in registers.
-template <class Real, int MODEL, int MINB, bool STATIC, bool ACC = false>
+// spot (slot 0: an average, a running max or min), in registers. SM (static
+// schedules only, no accumulator): the contracts' barriers are smoothed
+// (survival weights in registers instead of knock-outs).
+template <class Real, int MODEL, int MINB, bool STATIC, bool ACC = false, bool SM = false>
 __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     static_assert(!ACC || STATIC, "averages need a static schedule");
+    static_assert(!SM || (STATIC && !ACC), "smoothed barriers need a static schedule without an accumulator");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -397,6 +474,9 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     Real av = 0, ac = 0;      // accumulator: value (sum, max or min) and compensation
     int acc_f = 1, acc_t = 0; // warp-uniform: the contract's accumulator window (empty: none)
     int acc_k = ACC_SUM;      // and its kind
+    SmoothPar<Real> sp{0, 0, 0, Real(0), Real(0), Real(0), Real(0)};  // warp-uniform: smoothed barriers
+    Real sw0 = 1, sw1 = 1;    // lane: their survival weights
+    uint32_t sml = 0u;        // lane: the smoothed barriers whose weight is not yet 0
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
 
@@ -451,6 +531,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         acc_t = T.acc_on ? T.acc_to : 0;
                         acc_k = T.acc_kind;
                     }
+                    if (SM) sp = smooth_par<Real>(static_cast<const StaticDev *>(A.statics)[cur]);
                 }
                 pend = -1;
                 nx = (uint32_t)w.first;
@@ -471,6 +552,11 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 av = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
                 ac = Real(0);
                 if (STATIC) sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
+                if (SM) {
+                    sw0 = Real(1);
+                    sw1 = Real(1);
+                    sml = (1u << sp.n) - 1u;
+                }
                 else st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
                 k = 0;
             }
@@ -506,7 +592,14 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 }
                 const int k_in = k;
                 const HestonPar<Real> hp{hr, hk, hth, hsv, hrho, hrp, scheme};
-                if (!ACC) {
+                if (SM) {
+                    if (uniform)
+                        ev = lean_steps<Real, MODEL, true, -1, true>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0,
+                                                                     0, -1, av, ac, &sp, sml, &sw0, &sw1);
+                    else
+                        ev = lean_steps<Real, MODEL, false, -1, true>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k,
+                                                                      s0, 0, -1, av, ac, &sp, sml, &sw0, &sw1);
+                } else if (!ACC) {
                     if (uniform)
                         ev = lean_steps<Real, MODEL, true, -1>(R, uc0, uc1, hp, zz, off, hi, lo, lim, y, v, k, s0, 0, -1,
                                                                av, ac);
@@ -547,7 +640,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
                         if (ACC && k == 0 && acc_f <= 0 && 0 <= acc_t)  // the spot at t = 0 (steps >= 1: lean_steps)
                             acc_add<Real>(acc_k, av, ac, spot_of<Real>(s0, y));
-                        static_event<Real, ACC>(T, D, s0, y, k, sl, P, av, ac);
+                        if (SM && k == 0) smooth_step<Real>(sp, y, 0, sml, sw0, sw1);  // t = 0 (steps >= 1: lean_steps)
+                        static_event<Real, ACC, SM>(T, D, s0, y, k, sl, P, av, ac, sw0, sw1, &sml);
                         static_window<Real>(T, sl.live, hi, lo);
                         lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;
                         done = sl.rem == 0u;
@@ -583,7 +677,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
 
 // which: fp64 0/1; returns nullptr for a missing register budget.
 // acc: the static family with a running average (stat must be set).
-const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc);
+const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc, bool sm = false);
 const void *lean_kernel_heston(int fp64, int minb, bool stat, bool acc);
 
 }  // namespace kx

@@ -119,6 +119,8 @@ class Oracle:
         L.ko_price_multi.argtypes = [C.c_char_p, P(_abi.KxMultiGbm), P(_abi.KxMcConfig), P(_abi.KxPriceResult), P(D)]
         L.ko_price_american.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                         C.c_int, P(_abi.KxPriceResult), P(D)]
+        L.ko_price_american_detail.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
+                                               C.c_int, C.c_int, P(_abi.KxPriceResult), P(D), P(C.c_int32), P(D)]
         L.ko_price_american_basis.argtypes = [C.c_char_p, P(_abi.KxModel), P(_abi.KxMcConfig), P(D), C.c_size_t,
                                               C.c_int, C.c_int, P(_abi.KxPriceResult), P(D)]
         for f, n in [("ko_bs_call", 5), ("ko_bs_put", 5), ("ko_down_and_out_call", 6), ("ko_up_and_out_call", 6),
@@ -327,6 +329,25 @@ class Oracle:
                                                  1 if basis == "laguerre" else 0, C.byref(r),
                                                  pp.ctypes.data_as(C.POINTER(C.c_double)) if per_path else None))
         return (Result(r), pp[:n_paths]) if per_path else Result(r)
+
+    def price_american_detail(self, js: str, model, dates, n_paths=100_000, seed=42, n_basis=3, shared=False,
+                              basis="monomial"):
+        """price_american_lsm with per-path detail: (result, realised values,
+        exercise date index per path (-1: never exercised), decision margin
+        per path: the smallest |exercise - continuation| over its regression
+        decisions)."""
+        cm = _model_c(model)
+        cfg = self.cfg(n_paths, seed, 50, _rate(model, None), shared)
+        d = (C.c_double * len(dates))(*dates)
+        r = _abi.KxPriceResult()
+        n = max(1, n_paths)
+        pv, ex, mg = np.zeros(n), np.zeros(n, dtype=np.int32), np.zeros(n)
+        self._chk(self.L.ko_price_american_detail(js.encode(), C.byref(cm), C.byref(cfg), d, len(dates), n_basis,
+                                                  1 if basis == "laguerre" else 0, C.byref(r),
+                                                  pv.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  ex.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  mg.ctypes.data_as(C.POINTER(C.c_double))))
+        return Result(r), pv[:n_paths], ex[:n_paths], mg[:n_paths]
 
     def value_on_path(self, js: str, times, values, asset: str = "S", rate: float = 0.0) -> float:
         t = np.ascontiguousarray(times, dtype=np.float64)

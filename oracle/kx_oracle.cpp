@@ -32,6 +32,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <memory>
 #include <set>
 #include <stdexcept>
@@ -1583,8 +1584,17 @@ int ko_price_multi(const char *json, const kx_multi_gbm *mm, const kx_mc_config 
     });
 }
 
-int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
-                            size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
+// price_american_lsm (lsm.rs:80-229) with, per path (each array nullable, n
+// entries): the discounted realised value (lsm.rs:226), the exercise date of
+// the path (index into dates; -1 when the path is never exercised, i.e. its
+// payoff is 0 at the last date and it was continued at every earlier one),
+// and the decision margin: the smallest |exercise value - continuation| over
+// the dates where the path was in the money and a regression decided
+// (+inf when there was none). A decision can only differ between two
+// implementations whose fitted continuations differ by more than its margin.
+int ko_price_american_detail(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
+                             size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path,
+                             int32_t *ex_index, double *margin) {
     return run([&] {
         ConP c = parse_contract(json);
         Model m = to_model(model);
@@ -1634,6 +1644,9 @@ int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc
         if (err) fail(err, emsg);
         // backward induction (lsm.rs:129-229)
         std::vector<double> value = payoff[n_ex - 1];
+        std::vector<int32_t> exi(np);
+        std::vector<double> mrg(np, std::numeric_limits<double>::infinity());
+        for (size_t i = 0; i < np; ++i) exi[i] = payoff[n_ex - 1][i] > 0.0 ? (int32_t)(n_ex - 1) : -1;
         for (size_t d = n_ex - 1; d-- > 0;) {
             double t_now = grid[d + 1], t_next = grid[d + 2];
             double disc = std::exp(-mc.rate * (t_next - t_now));
@@ -1649,6 +1662,8 @@ int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc
                     double cont = !have ? discounted
                                   : basis == 1 ? laguerre_eval(coef, spots[d][i], m.s0) : poly_eval(coef, spots[d][i]);
                     value[i] = payoff[d][i] > cont ? payoff[d][i] : discounted;
+                    if (payoff[d][i] > cont) exi[i] = (int32_t)d;
+                    if (have) mrg[i] = std::min(mrg[i], std::fabs(payoff[d][i] - cont));
                 } else {
                     value[i] = discounted;
                 }
@@ -1658,7 +1673,14 @@ int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc
         for (auto &v : value) v *= disc0;
         *out = summarize(value);
         if (per_path) memcpy(per_path, value.data(), value.size() * sizeof(double));
+        if (ex_index) memcpy(ex_index, exi.data(), exi.size() * sizeof(int32_t));
+        if (margin) memcpy(margin, mrg.data(), mrg.size() * sizeof(double));
     });
+}
+
+int ko_price_american_basis(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
+                            size_t n_dates, int n_basis, int basis, kx_price_result *out, double *per_path) {
+    return ko_price_american_detail(json, model, cfg, dates, n_dates, n_basis, basis, out, per_path, nullptr, nullptr);
 }
 
 int ko_price_american(const char *json, const kx_model *model, const kx_mc_config *cfg, const double *dates,
