@@ -78,7 +78,13 @@ typedef struct kx_model {
  * rate. The remaining fields select engine options the reference does not
  * have. */
 enum { KX_RNG_PHILOX = 0, KX_RNG_SHARED_DRAWS = 1 };
-enum { KX_PREC_FP32 = 0, KX_PREC_FP64 = 1 };
+/* Path arithmetic. FP32: paths in FP32, payoffs and their sums in FP64.
+ * FP64: everything in FP64. FP32_KAHAN (kx_price; elsewhere it is FP32):
+ * paths in FP32, and the sum over paths accumulated in Kahan-compensated FP32
+ * (each path's value rounded to FP32 once, compensated sums per thread,
+ * float-float across threads), FP64 only for the final merge of the chunk
+ * statistics. */
+enum { KX_PREC_FP32 = 0, KX_PREC_FP64 = 1, KX_PREC_FP32_KAHAN = 2 };
 
 typedef struct kx_mc_config {
     uint64_t n_paths;        /* number of paths (0 gives a zero result) */
@@ -86,8 +92,7 @@ typedef struct kx_mc_config {
     uint32_t steps_per_year; /* fine-grid resolution (compiler.rs:54-65) */
     int32_t rng;             /* KX_RNG_*: Philox in registers, or the host normals
                                 registered with kx_set_shared_draws */
-    int32_t precision;       /* KX_PREC_*: path arithmetic type; payoff sums are
-                                always FP64 */
+    int32_t precision;       /* KX_PREC_*: path arithmetic type and payoff sums */
     int32_t flags;           /* KX_VR_* bits (kx_price only), else 0 */
     double rate;             /* deterministic discount rate */
 } kx_mc_config;

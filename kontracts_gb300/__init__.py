@@ -331,7 +331,7 @@ def heston(spot: float, v0: float, kappa: float, theta: float, sigma_v: float, r
                                        rho=rho, r=r, asset=asset, scheme=scheme))
 
 
-_PREC = {"fp32": _abi.KX_PREC_FP32, "fp64": _abi.KX_PREC_FP64}
+_PREC = {"fp32": _abi.KX_PREC_FP32, "fp64": _abi.KX_PREC_FP64, "fp32_kahan": _abi.KX_PREC_FP32_KAHAN}
 
 
 def _cfg(n_paths: int, seed: int, spy: int, rate: float, precision: str, shared_draws: bool) -> _abi.KxMcConfig:

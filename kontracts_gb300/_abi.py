@@ -39,6 +39,7 @@ KX_RNG_PHILOX = 0
 KX_RNG_SHARED_DRAWS = 1
 KX_PREC_FP32 = 0
 KX_PREC_FP64 = 1
+KX_PREC_FP32_KAHAN = 2
 
 
 class KxModel(C.Structure):

@@ -538,12 +538,22 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
 // lives in registers, the segment loops are unrolled, and the GBM step's
 // Jacobian (d y_{k+1} / d y_k = 1) leaves the adjoint unchanged across a
 // step. Same quantities as k_adjoint.
+//
+// The checkpoints and the per-flow records of a path live in shared memory,
+// one column per thread (ck[c * ADJ_BLOCK + t], the flows' values after the
+// checkpoints), so that registers hold only the state of the step loops and
+// eight blocks (FP32; four in FP64) fit an SM: n_ck checkpoint rows are
+// allocated at launch.
 template <class Real, int K, int NSU>
-__global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__restrict__ all,
-                                                           const uint64_t *__restrict__ off, int n_contracts,
-                                                           uint64_t total, double *__restrict__ out,
-                                                           const PhiloxKeys keys) {
+__global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoint_gbm(const AdjArgs *__restrict__ all,
+                                                              const uint64_t *__restrict__ off, int n_contracts,
+                                                              uint64_t total, double *__restrict__ out,
+                                                              const PhiloxKeys keys, int n_ck) {
     static_assert(K % 4 == 0 && (K & (K - 1)) == 0 && K <= ADJ_KMAX, "K: a power of two, multiple of 4");
+    extern __shared__ __align__(16) unsigned char adj_smem[];
+    double *const fP = reinterpret_cast<double *>(adj_smem) + threadIdx.x;                  // [ADJ_MAXF][ADJ_BLOCK]
+    Real *const fcs = reinterpret_cast<Real *>(adj_smem + ADJ_MAXF * ADJ_BLOCK * sizeof(double)) + threadIdx.x;
+    Real *const ck_y = fcs + ADJ_MAXF * ADJ_BLOCK;                                          // [n_ck][ADJ_BLOCK]
     for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
          gp += (uint64_t)gridDim.x * blockDim.x) {
         int lo = 0, hi = n_contracts - 1;  // contract of global path gp
@@ -565,7 +575,6 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
 #pragma unroll
         for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
         // ------------------------------ forward ------------------------------
-        Real ck_y[ADJ_MAXCK];
         Real y = Real(0);
         Real surv[ADJ_MAXU];
         int knock[ADJ_MAXU];
@@ -574,8 +583,6 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
             knock[u] = INT_MAX;
         }
         double pv_hard = 0.0, pv = 0.0, pv_t = 0.0;
-        double fP[ADJ_MAXF];
-        Real fcs[ADJ_MAXF];
         int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
         Real z[4];
         for (int k = 0; k <= N; ++k) {
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                 if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
                 y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
             }
-            if (k % K == 0) ck_y[k / K] = y;  // K is a power of two: a mask, not a division
+            if (k % K == 0) ck_y[(k / K) * ADJ_BLOCK] = y;  // K is a power of two: a mask, not a division
 #pragma unroll
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
@@ -610,10 +617,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                 for (int u = 0; u < nsu; ++u)
                     if ((F.su_mask >> u) & 1u) w *= surv[u];
                 const double df = A.disc[k];
-                fP[f] = (double)amt.v * (double)w * df;
-                fcs[f] = (Real)((double)(amt.d[0] * w) * df);
-                pv += fP[f];
-                pv_t += A.times[k] * fP[f];
+                const double fpv = (double)amt.v * (double)w * df;
+                fP[f * ADJ_BLOCK] = fpv;
+                fcs[f * ADJ_BLOCK] = (Real)((double)(amt.d[0] * w) * df);
+                pv += fpv;
+                pv_t += A.times[k] * fpv;
                 bool alive = true;
 #pragma unroll
                 for (int u = 0; u < nsu; ++u)
@@ -632,7 +640,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
             const int k0 = c * K;
             const int k1 = min(k0 + K, N);
             Real sy[K + 1], sz[K + 2];
-            sy[0] = ck_y[c];
+            sy[0] = ck_y[c * ADJ_BLOCK];
             sz[K + 1] = Real(0);
 #pragma unroll
             for (int q = 0; q < K / 4; ++q) {  // the draws of steps k0 + 1 .. k0 + K
@@ -664,10 +672,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint_gbm(const AdjArgs *__rest
                     int f0 = pf;
                     while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
                     for (int f = f0; f <= pf; ++f) {
-                        g += fcs[f] * Sk;
+                        g += fcs[f * ADJ_BLOCK] * Sk;
 #pragma unroll
                         for (int u = 0; u < nsu; ++u)
-                            if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f];
+                            if ((A.flow[f].su_mask >> u) & 1u) Q[u] += (Real)fP[f * ADJ_BLOCK];
                     }
                     pf = f0 - 1;
                     pft = pf >= 0 ? A.flow[pf].t : -1;
@@ -839,6 +847,7 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     // checkpoint interval (results do not depend on it: the recomputation
     // repeats the forward pass's operations)
     std::vector<std::pair<int, const void *>> cands;
+    int kck = 0;  // checkpoint interval of the chosen GBM kernel (0: the generic kernel)
     if (model == KX_MODEL_GBM && !acc && same_nsu) {
         if (max_n / 8 + 1 <= ADJ_MAXCK)
             cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>(nsu) : adj_gbm_kernel<float, 8>(nsu)});
@@ -853,12 +862,22 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
         bool one_seed = true;
         for (int i = 0; i < nc; ++i) one_seed = one_seed && args[i].seed == args[0].seed;
         if (one_seed) keys = philox_keys(args[0].seed);
-        void *kargs[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys};
-        auto launch = [&](const void *fn) {
-            const int full = persistent_blocks(fn, ADJ_BLOCK, 0);
+        int n_ck = 0;  // checkpoint rows of the GBM kernels (set per candidate)
+        void *kargs_g[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys};
+        void *kargs_r[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys, (void *)&n_ck};
+        auto launch = [&](const void *fn, int ck_every) {
+            // the register-resident GBM kernels keep checkpoints and flow records in shared memory
+            size_t smem = 0;
+            if (ck_every > 0) {
+                n_ck = max_n / ck_every + 1;
+                smem = (size_t)ADJ_BLOCK * (ADJ_MAXF * sizeof(double) + (ADJ_MAXF + n_ck) * (f64 ? 8 : 4));
+                KX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            }
+            const int full = persistent_blocks(fn, ADJ_BLOCK, smem);
             const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
             KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-            KX_CUDA(cudaLaunchKernel(fn, dim3(blocks), dim3(ADJ_BLOCK), kargs, 0, c.stream));
+            KX_CUDA(cudaLaunchKernel(fn, dim3(blocks), dim3(ADJ_BLOCK), ck_every > 0 ? kargs_r : kargs_g, smem,
+                                     c.stream));
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
@@ -874,15 +893,19 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             if (tune && tk == 0 && cands.size() > 1) {
                 float best = 1e30f;
                 for (auto &cd : cands) {
-                    const float ms = launch(cd.second);  // this call's own work: every candidate computes it
+                    const float ms = launch(cd.second, cd.first);  // this call's own work: every candidate computes it
                     if (ms < best) { best = ms; tk = cd.first; }
                 }
             }
             kfn = cands[0].second;
+            kck = cands[0].first;
             for (auto &cd : cands)
-                if (cd.first == (tk ? tk : 8)) kfn = cd.second;
+                if (cd.first == (tk ? tk : 16)) {
+                    kfn = cd.second;
+                    kck = cd.first;
+                }
         }
-        const float ms = launch(kfn);
+        const float ms = launch(kfn, kck);
         c.last.kernel_ms += ms;
         c.last.kernel_launches++;
         c.last.block_threads = ADJ_BLOCK;

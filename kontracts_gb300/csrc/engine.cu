@@ -26,6 +26,7 @@
 
 #include "device_common.cuh"
 #include "engine.hpp"
+#include "ffloat.cuh"
 #include "launch.hpp"
 #include "stats.cuh"
 
@@ -121,6 +122,59 @@ __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ 
     if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
 }
 
+// The same statistics in compensated FP32 (KX_PREC_FP32_KAHAN): each path's
+// value is rounded to FP32 once; every thread adds its values with Kahan's
+// compensated summation (the sum and its running correction), the threads'
+// (sum, correction) pairs are added in float-float in a fixed tree, and the
+// chunk's mean and M2 leave as doubles for the final cross-chunk merge, the
+// only FP64 arithmetic of the call's reduction.
+__device__ __forceinline__ ff ff_block_sum(ff v, ff *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    ff t = ff{0.0f, 0.0f};
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : ff{0.0f, 0.0f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff{__shfl_xor_sync(0xffffffffu, t.hi, o), __shfl_xor_sync(0xffffffffu, t.lo, o)});
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    t = red[0];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(256) k_chunk_stats_kahan(const double *__restrict__ vals,
+                                                           const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
+    __shared__ ff red[32];
+    const ChunkDesc c = ch[blockIdx.x];
+    float s = 0.0f, e = 0.0f;  // Kahan: running sum and the correction of its lost low part
+    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) {
+        const float x = __fsub_rn((float)vals[c.begin + i], e);
+        const float t = __fadd_rn(s, x);
+        e = __fsub_rn(__fsub_rn(t, s), x);
+        s = t;
+    }
+    const ff sum = ff_block_sum(ff{s, -e}, red);
+    const ff mean = ff_div(sum, ff_make((float)c.count));
+    float q = 0.0f, f = 0.0f;
+    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) {
+        const ff dv = ff_sub(ff_make((float)vals[c.begin + i]), mean);
+        const ff d2 = ff_mul(dv, dv);
+        const float x = __fsub_rn(d2.hi, f);
+        const float t = __fadd_rn(q, x);
+        f = __fsub_rn(__fsub_rn(t, q), x);
+        q = t;
+    }
+    const ff m2 = ff_block_sum(ff{q, -f}, red);
+    if (threadIdx.x == 0)
+        out[blockIdx.x] = ChunkOut{(double)c.count, (double)mean.hi + (double)mean.lo, (double)m2.hi + (double)m2.lo};
+}
+
 std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, const std::vector<StatsJob> &jobs) {
     const uint32_t CH = KX_STATS_CHUNK;
     std::vector<ChunkDesc> chunks;
@@ -148,7 +202,13 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
         size_t e = j + 1;
         while (e < jobs.size() && jobs[e].ns == jobs[j].ns && !memcmp(jobs[e].w, jobs[j].w, sizeof jobs[j].w)) ++e;
         const size_t nc = first[e] - first[j];
-        if (nc) {
+        const bool plain = jobs[j].ns == 1 && jobs[j].w[0] == 1.0;
+        if (nc && c.kahan_stats && plain) {  // KX_PREC_FP32_KAHAN: compensated FP32 sums
+            k_chunk_stats_kahan<<<(unsigned)nc, 256, 0, c.stream>>>(values, c.chunks.as<ChunkDesc>() + first[j],
+                                                                    c.chunk_out.as<ChunkOut>() + first[j]);
+            KX_CUDA(cudaGetLastError());
+            c.last.kernel_launches++;
+        } else if (nc) {
             k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, c.weights.as<double>() + j * 8,
                                                               c.chunks.as<ChunkDesc>() + first[j],
                                                               c.chunk_out.as<ChunkOut>() + first[j]);
@@ -209,7 +269,8 @@ kx_price_result finish(const Stats &s) {  // pricer.rs:303-328
 void check_cfg(const kx_mc_config *cfg) {
     if (!cfg) raise(KX_INVALID_ARGUMENT, "config is NULL");
     if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
-    if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
+    if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64 && cfg->precision != KX_PREC_FP32_KAHAN)
+        raise(KX_INVALID_ARGUMENT, "unknown precision");
     if (cfg->flags != 0) raise(KX_INVALID_ARGUMENT, "flags must be 0");
     if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
 }
@@ -809,6 +870,7 @@ std::vector<Stats> batch_paths(Ctx &c, const std::vector<const Program *> &progs
 void begin_call(Ctx &c) {
     memset(&c.last, 0, sizeof c.last);
     c.last.total_ms = -now_ms();
+    c.kahan_stats = false;
 }
 void end_call(Ctx &c) { c.last.total_ms += now_ms(); }
 
@@ -1168,6 +1230,7 @@ kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_co
         std::vector<StatsJob> sj(1);
         sj[0].begin = 0;
         sj[0].n = cfg->n_paths;
+        c.kahan_stats = cfg->precision == KX_PREC_FP32_KAHAN;
         *out = finish(device_stats(c, c.pv.as<double>(), stride, sj)[0]);
         if (per_path_pv && cfg->n_paths) {
             KX_CUDA(cudaMemcpyAsync(per_path_pv, c.pv.p, cfg->n_paths * sizeof(double), cudaMemcpyDeviceToHost, c.stream));

@@ -44,6 +44,7 @@ struct Ctx {
         lsm_stats, statics, mlmc;
     DrawStore draws;
     kx_launch_stats last{};
+    bool kahan_stats = false;  // this call's plain statistics in compensated FP32 (KX_PREC_FP32_KAHAN)
     std::mutex mu;
 };
 

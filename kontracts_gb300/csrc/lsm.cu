@@ -214,6 +214,70 @@ __global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward(const LsmArgs A) {
     }
 }
 
+// k_lsm_forward for FP32 paths: thread t simulates the four consecutive paths
+// 4t .. 4t + 3 side by side (four independent Philox chains per thread) and
+// stores their spots at each date with one 16-byte store: rows of S are
+// padded to 64 elements (256 bytes), so S + d * ld + 4t is 16-byte aligned,
+// and a row's padding past n_paths absorbs the last group's extra lanes.
+// Every path's spots are those of k_lsm_forward<float> bit for bit (the same
+// operations on the same draws).
+template <int MODEL>
+__global__ void __launch_bounds__(LSM_BLOCK) k_lsm_forward4(const LsmArgs A) {
+    constexpr int DRAWS = MODEL == KX_MODEL_GBM ? 1 : 2;
+    const StepRec<float> *R = reinterpret_cast<const StepRec<float> *>(A.steps);
+    float *S = reinterpret_cast<float *>(A.S);
+    const float s0 = A.s0_f, r = A.r_f, kap = A.kappa_f, th = A.theta_f, sv = A.sigma_v_f, rho = A.rho_f,
+                rp = A.rho_perp_f;
+    const float v_init = A.v0_f;  // max(v0, 0) in FP32
+    const uint64_t n_groups = (A.n_paths + 3) / 4;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n_groups;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i0 = 4 * g;
+        float y[4] = {0.f, 0.f, 0.f, 0.f}, v[4] = {v_init, v_init, v_init, v_init};
+        constexpr int SPB = 4 / DRAWS;  // steps per Philox block
+        const int n_steps = A.n_times - 1;
+        for (int kb = 0; kb < n_steps; kb += SPB) {  // steps kb + 1 .. kb + SPB
+            const uint64_t d = (uint64_t)kb * DRAWS;  // the block's first draw (a multiple of 4)
+            float z[4][4];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const uint64_t i = i0 + p;
+                if (A.z64 == nullptr && A.z32 == nullptr) {
+                    const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)i, (uint32_t)(i >> 32), 0u),
+                                                  (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+                    box_muller(w.x, w.y, z[p][0], z[p][1]);
+                    box_muller(w.z, w.w, z[p][2], z[p][3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        z[p][j] = i < A.n_paths && d + j < A.z_dpp
+                                      ? (A.z64 ? (float)A.z64[i * A.z_dpp + d + j] : A.z32[i * A.z_dpp + d + j])
+                                      : 0.f;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < SPB; ++j) {
+                const int k = kb + 1 + j;
+                if (k > n_steps) break;
+                const StepRec<float> rec = R[k];
+                float4 out;
+                float *o = &out.x;
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    if (MODEL == KX_MODEL_GBM) {
+                        y[p] = gbm_step(y[p], rec.c0, rec.c1, z[p][j]);
+                    } else {
+                        heston_step<float>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[p][2 * j],
+                                           z[p][2 * j + 1], y[p], v[p]);
+                    }
+                    o[p] = s0 * fast_exp<float>(y[p]);
+                }
+                *reinterpret_cast<float4 *>(S + (uint64_t)(k - 1) * A.ld + i0) = out;
+            }
+        }
+    }
+}
+
 // Block-wide sum of `n` <= 32 doubles per thread into red[LSM_RED_OUT + q]
 // (fixed order).
 __device__ void block_sums(double *vals, int n, double *red) {
@@ -1225,9 +1289,12 @@ static void lsm_run(Ctx &c, std::vector<LsmCase> &cs, bool f64, int n_basis, int
             if (f64) {
                 if (L.m.kind == KX_MODEL_GBM) k_lsm_forward<double, KX_MODEL_GBM><<<fblocks, LSM_BLOCK, 0, c.stream>>>(L.a);
                 else k_lsm_forward<double, KX_MODEL_HESTON><<<fblocks, LSM_BLOCK, 0, c.stream>>>(L.a);
-            } else {
-                if (L.m.kind == KX_MODEL_GBM) k_lsm_forward<float, KX_MODEL_GBM><<<fblocks, LSM_BLOCK, 0, c.stream>>>(L.a);
-                else k_lsm_forward<float, KX_MODEL_HESTON><<<fblocks, LSM_BLOCK, 0, c.stream>>>(L.a);
+            } else {  // four paths per thread, one 16-byte store per date; one group per thread
+                const uint64_t groups = (L.np + 3) / 4;
+                const unsigned gb = (unsigned)std::min<uint64_t>((groups + LSM_BLOCK - 1) / LSM_BLOCK,
+                                                                 (uint64_t)c.sm_count * 64);
+                if (L.m.kind == KX_MODEL_GBM) k_lsm_forward4<KX_MODEL_GBM><<<gb, LSM_BLOCK, 0, c.stream>>>(L.a);
+                else k_lsm_forward4<KX_MODEL_HESTON><<<gb, LSM_BLOCK, 0, c.stream>>>(L.a);
             }
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;

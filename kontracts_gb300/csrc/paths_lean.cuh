@@ -479,6 +479,44 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     uint32_t sml = 0u;        // lane: the smoothed barriers whose weight is not yet 0
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
+    // a new path on this lane: S = s0, step 0 next
+    auto start_path = [&](uint32_t p) {
+        path = p;
+        busy = true;
+        y = Real(0);
+        v = fmax(hv0, Real(0));
+        // as k_paths starts an accumulator
+        av = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
+        ac = Real(0);
+        if (STATIC) {
+            sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
+        } else {
+            st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
+        }
+        if (SM) {
+            sw0 = Real(1);
+            sw1 = Real(1);
+            sml = (1u << sp.n) - 1u;
+        }
+        k = 0;
+    };
+    // static schedules: the contract at step k of this lane's path (knock-outs,
+    // the static event of step k), then the next event step; the path's value
+    // is stored when nothing more can be paid
+    auto static_lane_event = [&]() {
+        const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
+        if (ACC && k == 0 && acc_f <= 0 && 0 <= acc_t)  // the spot at t = 0 (steps >= 1: lean_steps)
+            acc_add<Real>(acc_k, av, ac, spot_of<Real>(s0, y));
+        if (SM && k == 0) smooth_step<Real>(sp, y, 0, sml, sw0, sw1);  // t = 0 (steps >= 1: lean_steps)
+        static_event<Real, ACC, SM>(T, D, s0, y, k, sl, P, av, ac, sw0, sw1, &sml);
+        static_window<Real>(T, sl.live, hi, lo);
+        lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;
+        ++k;
+        if (sl.rem == 0u || k >= nt) {
+            A.pv[pv_off + path] = sl.pv;
+            busy = false;
+        }
+    };
 
     while (true) {
         // ---- hand paths to idle lanes (warp-uniform control) ----
@@ -543,22 +581,10 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
             const int take = avail < (uint32_t)nidle ? (int)avail : nidle;
             const int rank = __popc(idle & lt);
             if (!busy && rank < take) {
-                // new path: S = s0; the contract at step 0 runs as this lane's first event
-                path = nx + (uint32_t)rank;
-                busy = true;
-                y = Real(0);
-                v = fmax(hv0, Real(0));
-                // as k_paths starts an accumulator
-                av = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
-                ac = Real(0);
-                if (STATIC) sl = SLane{0u, static_cast<const StaticDev *>(A.statics)[cur].all_flows, 0, 0.0};
-                if (SM) {
-                    sw0 = Real(1);
-                    sw1 = Real(1);
-                    sml = (1u << sp.n) - 1u;
-                }
-                else st = Trig{P->root_arm, 0u, 0u, 0u, 0u, st.err, 0, 0, 0.0};
-                k = 0;
+                // new path: the contract at step 0 runs as this lane's first event (at once
+                // for static schedules; a path that ends at step 0 leaves the lane idle)
+                start_path(nx + (uint32_t)rank);
+                if (STATIC) static_lane_event();
             }
             nx += (uint32_t)take;
             if (take == 0) break;
@@ -634,29 +660,17 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                 wait = 0;
                 if (evp) {
                     evp = false;
-                    bool done;
-                    double pv;
                     if (STATIC) {
-                        const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
-                        if (ACC && k == 0 && acc_f <= 0 && 0 <= acc_t)  // the spot at t = 0 (steps >= 1: lean_steps)
-                            acc_add<Real>(acc_k, av, ac, spot_of<Real>(s0, y));
-                        if (SM && k == 0) smooth_step<Real>(sp, y, 0, sml, sw0, sw1);  // t = 0 (steps >= 1: lean_steps)
-                        static_event<Real, ACC, SM>(T, D, s0, y, k, sl, P, av, ac, sw0, sw1, &sml);
-                        static_window<Real>(T, sl.live, hi, lo);
-                        lim = sl.e < T.n_ev ? min(T.ev_step[sl.e], nt - 1) : nt - 1;
-                        done = sl.rem == 0u;
-                        pv = sl.pv;
+                        static_lane_event();
                     } else {
                         st = lean_event<Real>(P, C, R, thr, D, s0, y, k, st);
                         lean_window<Real>(*P, thr, st.armed & ~st.resolved, hi, lo);
                         lim = min(st.nte, nt - 1);
-                        done = st.done != 0;
-                        pv = st.pv;
-                    }
-                    ++k;
-                    if (done || k >= nt) {
-                        A.pv[pv_off + path] = pv;
-                        busy = false;
+                        ++k;
+                        if (st.done != 0 || k >= nt) {
+                            A.pv[pv_off + path] = st.pv;
+                            busy = false;
+                        }
                     }
                 }
             }

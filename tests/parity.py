@@ -31,9 +31,12 @@ def perturbed_oracle(orc, js, model, rel=REL, **kw):
     """The oracle's per-path values of the contract started from s0 (1 - rel)
     and s0 (1 + rel), on the same draws."""
     out = []
+    src = model._c()
     for f in (1.0 - rel, 1.0 + rel):
-        cm = model._c()
-        cm.s0 = cm.s0 * f
+        cm = type(src)()  # a copy: some models hand out their own structure
+        for name, _ in src._fields_:
+            setattr(cm, name, getattr(src, name))
+        cm.s0 = src.s0 * f
         _, pv = orc.price(js, cm, rate=model.rate, per_path=True, **kw)
         out.append(np.asarray(pv))
     return out

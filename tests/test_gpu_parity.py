@@ -199,3 +199,22 @@ def test_bump_greeks_match_oracle_shared_normals(orc):
     ref = orc.greeks(c.to_json(), model, n_paths=20000, seed=5, steps_per_year=1)
     for k in ("price", "delta", "gamma", "vega", "rho"):
         assert abs(getattr(g, k) - ref[k]) <= 1e-9 * max(1.0, abs(ref[k])), (k, getattr(g, k), ref[k])
+
+
+def test_fp32_kahan_sums_equal_fp64_sums_of_the_same_paths():
+    """KX_PREC_FP32_KAHAN: the same FP32 paths as "fp32", the sum over paths
+    accumulated in Kahan-compensated FP32 (FP64 only for the final merge of
+    the chunk statistics). It must give the FP64-accumulated price and
+    standard error of the same per-path values to 1e-7 and 1e-6, where a plain
+    FP32 running sum of the same values, chunk by chunk, is measurably worse."""
+    c = kx.up_and_out_call("X", 100.0, 200.0, 1.0)
+    m = kx.GBM(s0=180.0, sigma=0.25, r=0.05, asset="X")
+    n = 1 << 20
+    a, pv = c.price(m, n_paths=n, seed=5, steps_per_year=365, precision="fp32", per_path=True)
+    b = c.price(m, n_paths=n, seed=5, steps_per_year=365, precision="fp32_kahan")
+    err_kahan = abs(b.price - a.price) / abs(a.price)
+    assert err_kahan <= 1e-7, err_kahan
+    assert abs(b.std_error - a.std_error) <= 1e-6 * a.std_error
+    pv32 = np.asarray(pv, dtype=np.float32).reshape(-1, 16384)
+    naive = np.cumsum(pv32, axis=1, dtype=np.float32)[:, -1].astype(np.float64).sum() / n
+    assert abs(naive - a.price) / abs(a.price) > err_kahan
