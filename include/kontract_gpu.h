@@ -171,7 +171,9 @@ typedef struct kx_launch_stats {
     uint32_t path_kernel;      /* last path kernel: 0 none, 1 k_paths (every
                                   contract), 2 k_lean (barrier/time contracts),
                                   3 k_lean on compiled static schedules, 4 the
-                                  same with a running average of the spot */
+                                  same with a running average of the spot,
+                                  5 k_multi_lean (correlated factors, affine
+                                  conditions and amounts) */
     uint64_t h2d_bytes, d2h_bytes;
 } kx_launch_stats;
 

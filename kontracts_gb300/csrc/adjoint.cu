@@ -265,14 +265,16 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 next_ck += K;
             }
             const bool pays = k == nft;
-            const Real S = (ACC || pays) ? s0 * fast_exp<Real>(y) : Real(0);
+            // the spot and the sums rounded once each (no contraction into FMAs), so that
+            // k_adjoint_gbm_acc, which repeats these operations, gives the same values
+            const Real S = (ACC || pays) ? spot_of<Real>(s0, y) : Real(0);
             if (ACC)
                 for (int a = 0; a < A.n_acc; ++a) {
                     const AdjAcc &Ac = A.acc[a];
                     if (k < Ac.i_from || k > Ac.i_to) continue;
                     if (Ac.kind == ACC_MAX) { if (S > accraw[a]) { accraw[a] = S; argx[a] = k; } }
                     else if (Ac.kind == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
-                    else accraw[a] += S;
+                    else accraw[a] = add_rn(accraw[a], S);
                 }
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
@@ -381,7 +383,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 const Real yk = sy[j];
                 Real g = Real(0);
                 if (ACC) {
-                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    const Real Sk = spot_of<Real>(s0, yk);
                     for (int f = 0; f < nflows; ++f) {
                         // an average read at t_f covers [i_from, min(t_f, i_to)]: its coefficient
                         // joins when the sweep reaches the window's last step
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                     for (int a = 0; a < A.n_acc; ++a)  // averages: inside the window
                         if (A.acc[a].kind == ACC_SUM && k >= A.acc[a].i_from) g += G[a] * Sk;
                 } else if (k == pft) {  // the flows paid at step k, in slot order
-                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    const Real Sk = spot_of<Real>(s0, yk);
                     int f0 = pf;
                     while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
                     for (int f = f0; f <= pf; ++f) {
@@ -700,6 +702,259 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
     }
 }
 
+// GBM contracts with averages or running extrema (Asians, lookbacks, their
+// barrier versions), checkpoint interval K fixed at compile time: the
+// accumulators and the recomputed segment live in registers, the checkpoints
+// and the per-flow records (values, spot and accumulator coefficients, the
+// steps of the running extrema) in shared memory, one column per thread.
+// Every quantity is computed with k_adjoint's operations in k_adjoint's
+// order, so the two kernels give the same outputs; what changes is the
+// bookkeeping of the reverse sweep: an average's coefficient joins at a step
+// the host schedule fixes (min(t_f, window end)), and a running extremum's
+// coefficient at the path's arg-extremum, so the sweep looks for the next of
+// each instead of scanning every flow at every step.
+template <class Real, int K>
+__global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
+    k_adjoint_gbm_acc(const AdjArgs *__restrict__ all, const uint64_t *__restrict__ off, int n_contracts,
+                      uint64_t total, double *__restrict__ out, const PhiloxKeys keys, int n_ck) {
+    static_assert(K % 4 == 0 && (K & (K - 1)) == 0 && K <= ADJ_KMAX, "K: a power of two, multiple of 4");
+    extern __shared__ __align__(16) unsigned char adj_smem[];
+    constexpr size_t B = ADJ_BLOCK;
+    constexpr size_t O_FCS = ADJ_MAXF * B * sizeof(double);
+    constexpr size_t O_FCA = O_FCS + ADJ_MAXF * B * sizeof(Real);
+    constexpr size_t O_FARG = O_FCA + ADJ_MAXF * ADJ_MAXA * B * sizeof(Real);
+    constexpr size_t O_CK = O_FARG + ADJ_MAXF * ADJ_MAXA * B * sizeof(int);
+    double *const fP = reinterpret_cast<double *>(adj_smem) + threadIdx.x;           // [f * B]
+    Real *const fcs = reinterpret_cast<Real *>(adj_smem + O_FCS) + threadIdx.x;      // [f * B]
+    Real *const fca = reinterpret_cast<Real *>(adj_smem + O_FCA) + threadIdx.x;      // [(f * ADJ_MAXA + a) * B]
+    int *const farg = reinterpret_cast<int *>(adj_smem + O_FARG) + threadIdx.x;      // [(f * ADJ_MAXA + a) * B]
+    Real *const ck_y = reinterpret_cast<Real *>(adj_smem + O_CK) + threadIdx.x;      // [c * B], c < n_ck
+    for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
+         gp += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_contracts - 1;  // contract of global path gp
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= gp) lo = mid;
+            else hi = mid - 1;
+        }
+        const AdjArgs &A = all[lo];
+        const uint64_t path = gp - off[lo];
+        const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+        const KxProgram &P = *A.P;
+        const int N = A.n_times - 1;
+        const AdjPar<Real> pp = adj_par<Real>(A);
+        const Real s0 = pp.s0, inv_w = pp.inv_w;
+        const int nflows = A.n_flows, nsu = A.n_su, nacc = A.n_acc;
+        int su_arm[ADJ_MAXU], a_kind[ADJ_MAXA], a_from[ADJ_MAXA], a_to[ADJ_MAXA];
+#pragma unroll
+        for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
+#pragma unroll
+        for (int a = 0; a < ADJ_MAXA; ++a) {
+            a_kind[a] = a < nacc ? A.acc[a].kind : ACC_SUM;
+            a_from[a] = a < nacc ? A.acc[a].i_from : INT_MAX;
+            a_to[a] = a < nacc ? A.acc[a].i_to : -1;
+        }
+        // ------------------------------ forward ------------------------------
+        Real y = Real(0);
+        Real accraw[ADJ_MAXA];
+        int argx[ADJ_MAXA];
+#pragma unroll
+        for (int a = 0; a < ADJ_MAXA; ++a) {
+            accraw[a] = a < nacc ? (a_kind[a] == ACC_MAX ? Real(-INFINITY) : a_kind[a] == ACC_MIN ? Real(INFINITY) : Real(0))
+                                 : Real(0);
+            argx[a] = 0;
+        }
+        Real surv[ADJ_MAXU];
+        int knock[ADJ_MAXU];
+#pragma unroll
+        for (int u = 0; u < ADJ_MAXU; ++u) {
+            surv[u] = Real(1);
+            knock[u] = INT_MAX;
+        }
+        double pv_hard = 0.0, pv = 0.0, pv_t = 0.0;
+        int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
+        Real z[4];
+        for (int k = 0; k <= N; ++k) {
+            if (k > 0) {
+                const uint64_t d = (uint64_t)(k - 1);
+                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
+                y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
+            }
+            if (k % K == 0) ck_y[(k / K) * B] = y;
+            const Real S = spot_of<Real>(s0, y);
+#pragma unroll
+            for (int a = 0; a < ADJ_MAXA; ++a) {
+                if (a >= nacc || k < a_from[a] || k > a_to[a]) continue;
+                if (a_kind[a] == ACC_MAX) { if (S > accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                else if (a_kind[a] == ACC_MIN) { if (S < accraw[a]) { accraw[a] = S; argx[a] = k; } }
+                else accraw[a] = add_rn(accraw[a], S);
+            }
+#pragma unroll
+            for (int u = 0; u < ADJ_MAXU; ++u)
+                if (u < nsu && k >= su_arm[u]) {
+                    const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
+                    surv[u] *= smooth_weight(x);
+                    if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
+                }
+            if (k != nft) continue;
+            Real accv[ADJ_MAXA];
+#pragma unroll
+            for (int a = 0; a < ADJ_MAXA; ++a)
+                accv[a] = a < nacc && a_kind[a] == ACC_SUM ? accraw[a] / (Real)(min(k, a_to[a]) - a_from[a] + 1)
+                          : a < nacc ? accraw[a] : Real(0);
+            for (int f = nf; f < nflows && A.flow[f].t == k; ++f) {
+                const AdjFlow &F = A.flow[f];
+                nf = f + 1;
+                Dual<Real> amt;
+                if (F.kind == AK_CONST) {
+                    amt.v = (Real)F.sign;
+                    for (int q = 0; q < 1 + ADJ_MAXA; ++q) amt.d[q] = Real(0);
+                } else {
+                    amt = eval_dual<Real>(P, F.code_off, F.code_len, S, accv);
+                }
+                Real w = Real(1);
+#pragma unroll
+                for (int u = 0; u < ADJ_MAXU; ++u)
+                    if (u < nsu && ((F.su_mask >> u) & 1u)) w *= surv[u];
+                const double df = A.disc[k];
+                const double fpv = (double)amt.v * (double)w * df;
+                fP[f * B] = fpv;
+                fcs[f * B] = (Real)((double)(amt.d[0] * w) * df);
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a) {
+                    Real c = (Real)((double)(amt.d[1 + a] * w) * df);
+                    if (a < nacc && a_kind[a] == ACC_SUM) c /= (Real)(min(k, a_to[a]) - a_from[a] + 1);
+                    fca[(f * ADJ_MAXA + a) * B] = c;
+                    farg[(f * ADJ_MAXA + a) * B] = argx[a];
+                }
+                pv += fpv;
+                pv_t += A.times[k] * fpv;
+                bool alive = true;
+#pragma unroll
+                for (int u = 0; u < ADJ_MAXU; ++u)
+                    if (u < nsu && ((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
+                if (alive) pv_hard += (double)amt.v * df;
+            }
+            nft = nf < nflows ? A.flow[nf].t : INT_MAX;
+        }
+        // ------------------------------ reverse ------------------------------
+        // the next step (below lim) at which an average's coefficient joins, or
+        // at which a running extremum of some flow was taken
+        auto next_join = [&](int lim) {
+            int m = -1;
+            for (int f = 0; f < nflows; ++f)
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a)
+                    if (a < nacc && a_kind[a] == ACC_SUM) {
+                        const int s = min(A.flow[f].t, a_to[a]);
+                        if (s < lim && s > m) m = s;
+                    }
+            return m;
+        };
+        auto next_ext = [&](int lim) {
+            int m = -1;
+            for (int f = 0; f < nflows; ++f)
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a)
+                    if (a < nacc && a_kind[a] != ACC_SUM) {
+                        const int s = farg[(f * ADJ_MAXA + a) * B];
+                        if (s < lim && s > m) m = s;
+                    }
+            return m;
+        };
+        int kj = next_join(INT_MAX), ke = next_ext(INT_MAX);
+        Real lam = Real(0);
+        Real Q[ADJ_MAXU] = {};
+        Real G[ADJ_MAXA] = {};
+        Real g_sig = Real(0), g_r = Real(0);
+        int pf = nflows - 1, pft = pf >= 0 ? A.flow[pf].t : -1;
+        const int nseg = (N + K - 1) / K;
+        for (int c = nseg - 1; c >= 0; --c) {
+            const int k0 = c * K;
+            const int k1 = min(k0 + K, N);
+            Real sy[K + 1], sz[K + 2];
+            sy[0] = ck_y[c * B];
+            sz[K + 1] = Real(0);
+#pragma unroll
+            for (int q = 0; q < K / 4; ++q) {  // the draws of steps k0 + 1 .. k0 + K
+                Real w4[4];
+                draws4<Real>(A, keys, path, (uint64_t)(k0 + 4 * q), w4);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) sz[1 + 4 * q + j] = w4[j];
+            }
+#pragma unroll
+            for (int j = 1; j <= K; ++j) {
+                const StepRec<Real> rec = R[min(k0 + j, N)];  // past N: harmless states never read
+                sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
+            }
+            const int jtop = (c == nseg - 1) ? k1 - k0 : k1 - k0 - 1;
+#pragma unroll
+            for (int j = K; j >= 0; --j) {
+                if (j > jtop) continue;
+                const int k = k0 + j;
+                if (k < N) {
+                    const StepRec<Real> rec = R[k + 1];
+                    const Real dt = rec.c0, sq = rec.c1;
+                    g_sig += lam * (-pp.sigma * dt + sq * sz[j + 1]);
+                    g_r += lam * dt;
+                }
+                const Real Sk = spot_of<Real>(s0, sy[j]);
+                Real g = Real(0);
+                if (k == kj) {  // average coefficients whose window ends here, flows in slot order
+                    for (int f = 0; f < nflows; ++f)
+#pragma unroll
+                        for (int a = 0; a < ADJ_MAXA; ++a)
+                            if (a < nacc && a_kind[a] == ACC_SUM && k == min(A.flow[f].t, a_to[a]))
+                                G[a] += fca[(f * ADJ_MAXA + a) * B];
+                    kj = next_join(k);
+                }
+                if (k == pft) {  // the flows paid at step k, in slot order
+                    int f0 = pf;
+                    while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
+                    for (int f = f0; f <= pf; ++f) {
+                        g += fcs[f * B] * Sk;
+#pragma unroll
+                        for (int u = 0; u < ADJ_MAXU; ++u)
+                            if (u < nsu && ((A.flow[f].su_mask >> u) & 1u)) Q[u] += (Real)fP[f * B];
+                    }
+                    pf = f0 - 1;
+                    pft = pf >= 0 ? A.flow[pf].t : -1;
+                }
+                if (k == ke) {  // running max / min: at the arg-extremum
+                    for (int f = 0; f < nflows; ++f)
+#pragma unroll
+                        for (int a = 0; a < ADJ_MAXA; ++a)
+                            if (a < nacc && a_kind[a] != ACC_SUM && farg[(f * ADJ_MAXA + a) * B] == k)
+                                g += fca[(f * ADJ_MAXA + a) * B] * Sk;
+                    ke = next_ext(k);
+                }
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a)  // averages: inside the window
+                    if (a < nacc && a_kind[a] == ACC_SUM && k >= a_from[a]) g += G[a] * Sk;
+#pragma unroll
+                for (int u = 0; u < ADJ_MAXU; ++u)
+                    if (u < nsu && k >= su_arm[u] && Q[u] != Real(0)) {
+                        const Real x = pp.sgn[u] * (sy[j] - pp.thr[u]) * inv_w;
+                        const Real sv = smooth_weight(x);
+                        const Real dls = (Real(1) - sv) * inv_w;
+                        g -= Q[u] * pp.sgn[u] * dls;
+                    }
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a)
+                    if (a < nacc && a_kind[a] == ACC_SUM && k == a_from[a]) G[a] = Real(0);
+                lam += g;
+            }
+        }
+        double *o = out + A.out_off + path;
+        const uint64_t n = total;
+        o[8 * n] = pv_hard;
+        o[0 * n] = pv;
+        o[1 * n] = (double)lam / A.s0;
+        o[2 * n] = (double)g_sig;
+        o[3 * n] = (double)g_r - pv_t;
+    }
+}
+
 template <class Real, int K>
 static const void *adj_gbm_kernel(int nsu) {
     switch (nsu) {
@@ -846,13 +1101,24 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     // GBM without accumulators: the register-resident kernel at a tuned
     // checkpoint interval (results do not depend on it: the recomputation
     // repeats the forward pass's operations)
+    // (with accumulators: the kernel that keeps them in registers). KX_ADJOINT_KERNEL
+    // = "general" keeps the generic kernel.
     std::vector<std::pair<int, const void *>> cands;
     int kck = 0;  // checkpoint interval of the chosen GBM kernel (0: the generic kernel)
-    if (model == KX_MODEL_GBM && !acc && same_nsu) {
+    const char *kenv = getenv("KX_ADJOINT_KERNEL");
+    const bool generic_only = kenv && strcmp(kenv, "general") == 0;
+    if (model == KX_MODEL_GBM && !acc && same_nsu && !generic_only) {
         if (max_n / 8 + 1 <= ADJ_MAXCK)
             cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>(nsu) : adj_gbm_kernel<float, 8>(nsu)});
         if (max_n / 16 + 1 <= ADJ_MAXCK)
             cands.push_back({16, f64 ? adj_gbm_kernel<double, 16>(nsu) : adj_gbm_kernel<float, 16>(nsu)});
+    }
+    if (model == KX_MODEL_GBM && acc && !generic_only) {
+        if (max_n / 8 + 1 <= ADJ_MAXCK)
+            cands.push_back({8, f64 ? (const void *)&k_adjoint_gbm_acc<double, 8> : (const void *)&k_adjoint_gbm_acc<float, 8>});
+        if (max_n / 16 + 1 <= ADJ_MAXCK)
+            cands.push_back(
+                {16, f64 ? (const void *)&k_adjoint_gbm_acc<double, 16> : (const void *)&k_adjoint_gbm_acc<float, 16>});
     }
     if (total > 0) {
         const AdjArgs *ap = c.cons.as<AdjArgs>();
@@ -870,7 +1136,9 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             size_t smem = 0;
             if (ck_every > 0) {
                 n_ck = max_n / ck_every + 1;
-                smem = (size_t)ADJ_BLOCK * (ADJ_MAXF * sizeof(double) + (ADJ_MAXF + n_ck) * (f64 ? 8 : 4));
+                const size_t real = f64 ? 8 : 4;
+                smem = (size_t)ADJ_BLOCK * (ADJ_MAXF * sizeof(double) + (ADJ_MAXF + n_ck) * real);
+                if (acc) smem += (size_t)ADJ_BLOCK * ADJ_MAXF * ADJ_MAXA * (real + sizeof(int));  // fca, farg
                 KX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             }
             const int full = persistent_blocks(fn, ADJ_BLOCK, smem);
@@ -886,10 +1154,11 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             return ms;
         };
         if (!cands.empty()) {
-            static int tuned_k[2][ADJ_MAXU + 1] = {};  // per precision and barrier count; 0: not tuned yet
+            // per precision, accumulators present and barrier count (ADJ_MAXU + 1: mixed); 0: not tuned yet
+            static int tuned_k[2][2][ADJ_MAXU + 2] = {};
             const char *env = getenv("KX_TUNE");
             const bool tune = !(env && env[0] == '0');
-            int &tk = tuned_k[f64 ? 1 : 0][std::min(std::max(nsu, 0), ADJ_MAXU)];
+            int &tk = tuned_k[f64 ? 1 : 0][acc ? 1 : 0][same_nsu ? std::min(std::max(nsu, 0), ADJ_MAXU) : ADJ_MAXU + 1];
             if (tune && tk == 0 && cands.size() > 1) {
                 float best = 1e30f;
                 for (auto &cd : cands) {

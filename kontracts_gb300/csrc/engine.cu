@@ -705,7 +705,10 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     P.surv_base = 2u * (uint32_t)max_acc;
     P.slots = P.surv_base + (smooth ? (uint32_t)max_spot : 0u);
     P.smem = lean ? 0 : (size_t)ns * P.slots * block * (f64 ? 8 : 4);  // k_lean keeps its average in registers
-    P.kfn = pair ? paths_kernel_pair(P.model, f64) : select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc, P.sm);
+    if (pair && P.sm) raise(KX_UNSUPPORTED, "smoothed barriers on multilevel pairs");
+    P.kfn = !pair ? select_kernel(P.model, f64, ns, minb, lean, P.stat, P.acc, P.sm)
+            : lean ? lean_kernel_pair(P.model, f64, P.stat, P.acc)
+                   : paths_kernel_pair(P.model, f64);
     if (!P.kfn) raise(KX_CUDA_ERROR, "missing kernel variant");
     if (P.smem > 48 * 1024)
         KX_CUDA(cudaFuncSetAttribute(P.kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
@@ -1225,8 +1228,8 @@ kx_status kx_price(const kx_program *prog, const kx_model *model, const kx_mc_co
         }
         std::vector<Job> jobs;
         jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
-        uint64_t stride = 0;
-        run_paths(c, jobs, *cfg, 1, stride);
+        uint64_t stride = cfg->n_paths;
+        if (!multi_lean_run(c, jobs[0], *cfg)) run_paths(c, jobs, *cfg, 1, stride);
         std::vector<StatsJob> sj(1);
         sj[0].begin = 0;
         sj[0].n = cfg->n_paths;
@@ -1538,7 +1541,7 @@ static std::vector<Stats> mlmc_level_stats(Ctx &c, const Program &p, const Model
     if (nfine)
         KX_CUDA(cudaMemcpyAsync(c.mlmc.p, c.pv.p, nfine * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
     if (!coarse.empty()) {
-        run_paths_v(c, coarse, cfg, 1, ncoarse, 2, false, true);
+        run_paths_v(c, coarse, cfg, 1, ncoarse, 2, use_lean(coarse, 1), true);
         KX_CUDA(cudaMemcpyAsync(c.mlmc.as<double>() + nfine, c.pv.p, ncoarse * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c.stream));
     }
@@ -1928,8 +1931,8 @@ kx_status kx_price_multi(const kx_program *prog, const kx_multi_gbm *model, cons
         begin_call(c);
         std::vector<Job> jobs;
         jobs.push_back(make_job(p, m, *cfg, grid, {}, 0, 0.0));
-        uint64_t stride = 0;
-        run_paths(c, jobs, *cfg, 1, stride);
+        uint64_t stride = cfg->n_paths;
+        if (!multi_lean_run(c, jobs[0], *cfg)) run_paths(c, jobs, *cfg, 1, stride);
         std::vector<StatsJob> sj(1);
         sj[0].n = cfg->n_paths;
         *out = finish(device_stats(c, c.pv.as<double>(), stride, sj)[0]);

@@ -90,6 +90,11 @@ PathArgs path_args(const PathPlan &P, const PathBuffers &B);
 void upload_plan(const PathPlan &P, const PathBuffers &B, cudaStream_t s);
 size_t plan_upload_bytes(const PathPlan &P);
 
+// Prices a correlated multi-factor job with k_multi_lean when its contract
+// has affine conditions and amounts on a static schedule (per-path values at
+// c.pv[0 .. n_paths)); false, with nothing launched, otherwise.
+bool multi_lean_run(Ctx &c, Job &j, const kx_mc_config &cfg);
+
 // Raises the error the device error word of a path launch reports.
 void check_err_word(uint32_t err);
 

@@ -339,6 +339,35 @@ struct HestonPar {
     int scheme;
 };
 
+// Grid steps per Philox block (four normals) and normals per grid step of a
+// path model. The _PAIR models are the coarse paths of multilevel pairs: a
+// coarse GBM step adds the normals of its two fine steps (simulator.rs:373-377),
+// a coarse Heston step sums the two fine (z1, z2) pairs over sqrt 2 (:656-661).
+template <int MODEL>
+constexpr int lean_spb() { return MODEL == M_GBM ? 4 : MODEL == M_HESTON_PAIR ? 1 : 2; }
+template <int MODEL>
+constexpr int lean_draws() { return MODEL == M_GBM ? 1 : MODEL == M_HESTON_PAIR ? 4 : 2; }
+template <int MODEL>
+constexpr bool lean_gbmlike() { return MODEL == M_GBM || MODEL == M_GBM_PAIR; }
+
+// Grid step j of a Philox block, as k_paths steps it.
+template <class Real, int MODEL>
+__device__ __forceinline__ void lean_model_step(const HestonPar<Real> &hp, Real c0, Real c1, const Real (&zz)[4], int j,
+                                                Real &y, Real &v) {
+    if (MODEL == M_GBM) {
+        y = gbm_step(y, c0, c1, zz[j]);  // log-space exact GBM step (simulator.rs:238-245)
+    } else if (MODEL == M_GBM_PAIR) {
+        y = gbm_step(y, c0, c1, zz[2 * j] + zz[2 * j + 1]);
+    } else if (MODEL == M_HESTON) {
+        heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1, zz[2 * j],
+                          zz[2 * j + 1], y, v);
+    } else {
+        const Real inv_sqrt2 = Real(0.70710678118654752440);
+        heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
+                          (zz[0] + zz[2]) * inv_sqrt2, (zz[1] + zz[3]) * inv_sqrt2, y, v);
+    }
+}
+
 // The steps of one Philox block from offset `off` on, up to the first step at
 // which the barrier window or the step limit fires (returns true; k is that
 // step) or to the end of the block (k is the next step). UNI: every step has
@@ -353,12 +382,12 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                                            const SmoothPar<Real> *sp = nullptr, uint32_t sml = 0u,
                                            Real *w0 = nullptr, Real *w1 = nullptr) {
     constexpr bool ACC = AK >= 0;
-    constexpr int SPB = MODEL == M_GBM ? 4 : 2;
+    constexpr int SPB = lean_spb<MODEL>();
     // GBM: a whole block is stepped first and tested once (min and max of its
     // states against the window, its last step against the limit); only a
     // block in which something fires is walked again step by step. A Heston
     // step is long enough that redoing it costs more than the test saves.
-    if (MODEL == M_GBM && off == 0) {
+    if (lean_gbmlike<MODEL>() && off == 0) {
         Real yy = y, vv = v, mx = Real(-INFINITY), mn = Real(INFINITY);
         Real av2 = av, ac2 = ac;
         Real w0c = SM ? *w0 : Real(1), w1c = SM ? *w1 : Real(1);
@@ -370,12 +399,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 c0 = rec.c0;
                 c1 = rec.c1;
             }
-            if (MODEL == M_GBM) {
-                yy = gbm_step(yy, c0, c1, zz[j]);
-            } else {
-                heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
-                                  zz[2 * j], zz[2 * j + 1], yy, vv);
-            }
+            lean_model_step<Real, MODEL>(hp, c0, c1, zz, j, yy, vv);
             if (ACC && k + j >= af && k + j <= at) acc_add<Real, AK>(AK, av2, ac2, spot_of<Real>(s0, yy));
             if (SM) smooth_step<Real>(*sp, yy, k + j, sml, w0c, w1c);
             mx = fmax(mx, yy);
@@ -407,12 +431,7 @@ __device__ __forceinline__ bool lean_steps(const StepRec<Real> *R, Real uc0, Rea
                 c0 = rec.c0;
                 c1 = rec.c1;
             }
-            if (MODEL == M_GBM) {
-                y = gbm_step(y, c0, c1, zz[j]);  // log-space exact GBM step (simulator.rs:238-245)
-            } else {
-                heston_step<Real>(hp.r, hp.kappa, hp.theta, hp.sigma_v, hp.rho, hp.rho_perp, hp.scheme, c0, c1,
-                                  zz[2 * j], zz[2 * j + 1], y, v);
-            }
+            lean_model_step<Real, MODEL>(hp, c0, c1, zz, j, y, v);
             if (ACC && k >= af && k <= at) acc_add<Real, AK>(AK, av, ac, spot_of<Real>(s0, y));
             if (SM) smooth_step<Real>(*sp, y, k, sml, *w0, *w1);
             if (y >= hi || y <= lo || k >= lim || (SM && smooth_zero<Real>(sml, *w0, *w1))) ev = true;
@@ -433,18 +452,22 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    constexpr int SPB = MODEL == M_GBM ? 4 : 2;  // grid steps per Philox block
-    constexpr int DRAWS = MODEL == M_GBM ? 1 : 2;
+    constexpr int SPB = lean_spb<MODEL>();  // grid steps per Philox block
+    constexpr int DRAWS = lean_draws<MODEL>();
+    constexpr bool GBMLIKE = lean_gbmlike<MODEL>();
+    constexpr bool HESTON = !GBMLIKE;
     // Event batching: a lane whose path reached an event waits (up to
     // EV_WAIT blocks) until EV_BATCH lanes of its warp have one, so the
     // handler runs once for many lanes instead of once per lane. Worth it
     // for GBM, whose blocks are short next to the handler; a Heston block is
     // long enough that waiting costs more than it saves.
-    constexpr int EV_BATCH = MODEL == M_GBM ? 8 : 1;
-    constexpr int EV_WAIT = MODEL == M_GBM ? 4 : 8;  // rounds of BPI blocks
-    // Philox blocks a lane steps through per round of the warp loop: four for
-    // GBM (16 steps) cut the per-round hand-out and event ballots per step.
-    constexpr int BPI = MODEL == M_GBM ? 4 : 1;
+    // (GBM: batches of 6 with waits of 3 rounds of 8 blocks took 1.341 ms on
+    // the 4M-path up-and-out call, 8 / 4 rounds of 4 blocks 1.362 ms.)
+    constexpr int EV_BATCH = GBMLIKE ? 6 : 1;
+    constexpr int EV_WAIT = GBMLIKE ? 3 : 8;  // rounds of BPI blocks
+    // Philox blocks a lane steps through per round of the warp loop: eight for
+    // GBM (32 steps) cut the per-round hand-out and event ballots per step.
+    constexpr int BPI = GBMLIKE ? 8 : 1;
 
     // warp-uniform work state (path indices are per contract, < 2^32)
     int cur = -1, pend = -1;
@@ -553,7 +576,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                     s0 = pick<Real>(C->s0[0], C->s0f[0]);
                     uc0 = pick<Real>(C->uc0, C->uc0f);
                     uc1 = pick<Real>(C->uc1, C->uc1f);
-                    if (MODEL == M_HESTON) {
+                    if (HESTON) {
                         hr = pick<Real>(C->r, C->rf);
                         hk = pick<Real>(C->kappa, C->kappaf);
                         hth = pick<Real>(C->theta, C->thetaf);
@@ -693,5 +716,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
 // acc: the static family with a running average (stat must be set).
 const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc, bool sm = false);
 const void *lean_kernel_heston(int fp64, int minb, bool stat, bool acc);
+// The coarse paths of multilevel pairs (model: KX_MODEL_GBM or KX_MODEL_HESTON).
+const void *lean_kernel_pair(int model, int fp64, bool stat, bool acc);
 
 }  // namespace kx

@@ -201,3 +201,32 @@ def test_smoothed_bump_on_lean_kernel_equals_general_kernel(monkeypatch, prec, n
     assert kx.last_launch_stats()["path_kernel"] == 1
     for f in ("price", "delta", "gamma", "vega", "rho", "price_se", "delta_se", "gamma_se", "vega_se", "rho_se"):
         assert getattr(lean, f) == getattr(gen, f), (f, getattr(lean, f), getattr(gen, f))
+
+
+ACC_CASES = {
+    "asian": lambda: kx.scale((kx.average(kx.S("X")) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "lookback_max": lambda: kx.scale((kx.running_max(kx.S("X")) - 95.0).clip(0.0), kx.one()) @ kx.at(1.0),
+    "lookback_min_put": lambda: kx.scale((105.0 - kx.running_min(kx.S("X"))).clip(0.0), kx.one()) @ kx.at(1.0),
+    "asian_up_and_out": lambda: kx.until(kx.S("X") >= 140.0,
+                                         kx.scale((kx.average(kx.S("X")) - 100.0).clip(0.0), kx.one()) @ kx.at(1.0)),
+    "window_and_strip": lambda: (kx.scale((kx.average_over(kx.S("X"), 0.25, 0.75) - 100.0).clip(0.0), kx.one())
+                                 @ kx.at(0.75))
+    + (kx.scale((kx.running_max(kx.S("X")) - 110.0).clip(0.0), kx.one()) @ kx.at(1.0)),
+}
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", sorted(ACC_CASES))
+def test_accumulator_adjoint_kernel_equals_generic_kernel(monkeypatch, prec, name):
+    """GBM contracts with averages or running extrema take the adjoint kernel
+    that keeps its accumulators in registers and its flow records in shared
+    memory; it performs the generic kernel's operations in the same order, so
+    every output equals the generic kernel's (KX_ADJOINT_KERNEL=general) bit
+    for bit."""
+    c, m = ACC_CASES[name](), kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
+    kw = dict(n_paths=20_000, seed=9, steps_per_year=252, precision=prec)
+    a = c.adjoint(m, **kw)
+    monkeypatch.setenv("KX_ADJOINT_KERNEL", "general")
+    g = c.adjoint(m, **kw)
+    for f in ("price", "d_s0", "d_sigma", "d_r", "se_s0", "se_sigma", "se_r"):
+        assert getattr(a, f) == getattr(g, f), (name, f, getattr(a, f), getattr(g, f))

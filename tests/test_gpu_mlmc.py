@@ -104,3 +104,17 @@ def test_no_pilot_allocates_one_path_per_level(orc):
     o = orc.price_mlmc(c.to_json(), m, n_levels=3, pilot_paths=0, target_variance=1e-4, seed=2)
     assert g.level_paths == o["level_paths"] == [1, 1, 1, 1]
     assert abs(g.price.price - o["price"].price) <= 1e-10 * max(1.0, abs(o["price"].price))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("model", sorted(MODELS))
+@pytest.mark.parametrize("name", sorted(CONTRACTS))
+def test_lean_level_pairs_equal_general_kernel(monkeypatch, precision, model, name):
+    """The coarse paths of a level pair on k_lean (static schedules, the running
+    average in registers) and on k_paths (KX_PATH_KERNEL=general) are the same
+    arithmetic on the same normals: the level variances agree exactly."""
+    c, m = CONTRACTS[name](), MODELS[model]()
+    got = [kx.estimate_variance_at_level(c, m, level, 20_000, seed=3, precision=precision) for level in (1, 3, 6)]
+    monkeypatch.setenv("KX_PATH_KERNEL", "general")
+    ref = [kx.estimate_variance_at_level(c, m, level, 20_000, seed=3, precision=precision) for level in (1, 3, 6)]
+    assert got == ref, (name, model, precision, got, ref)

@@ -95,3 +95,97 @@ def test_seven_factors_equal_oracle_and_eight_rejected(orc):
     assert np.allclose(np.asarray(pp), op, rtol=1e-11, atol=1e-11)
     with pytest.raises(ValueError):
         kx.CorrelatedGbmN(fac + [("A7", 100.0, 0.0, 0.2)], [[1.0] * 8] * 8)
+
+
+# ---------------------------------------------------------------------------
+# k_multi_lean: contracts whose price conditions and amounts are affine in the
+# factor spots, on a static schedule of time events (path_kernel 5); the
+# others (an average, a min of two spots) stay on the general kernel (1).
+# ---------------------------------------------------------------------------
+def _basket3():
+    return (S("S1") + S("S2") + S("S3")) / 3.0
+
+
+LEAN = {
+    "basket_knock_out": lambda: kx.until(_basket3() >= 125.0,
+                                         kx.scale((_basket3() - 100.0).clip(0.0), kx.one()) @ kx.at(1.0)),
+    "spread_down_and_out": lambda: kx.until(S("S2") - S("S1") <= -30.0,
+                                            kx.scale((S("S1") - S("S2")).clip(0.0), kx.one()) @ kx.at(0.75)),
+    "bermudan_strip": lambda: (kx.scale((_basket3() - 100.0).clip(0.0), kx.one()) @ kx.at(0.5))
+    + (kx.scale((_basket3() - 105.0).clip(0.0), kx.one()) @ kx.at(1.0)),
+    "short_basket_put": lambda: -(kx.scale((100.0 - _basket3()).clip(0.0), kx.one()) @ kx.at(1.0)),
+    "digital_double_knock_out": lambda: kx.until(_basket3() >= 125.0,
+                                                 kx.until(S("S1") <= 80.0, kx.one() @ kx.at(1.0))),
+    "capped_basket": lambda: kx.scale(_basket3().min(110.0), kx.one()) @ kx.at(1.0),
+    "forward_on_difference": lambda: kx.scale(2.0 * S("S1") - S("S3"), kx.one()) @ kx.at(1.0),
+    "knock_in_window": lambda: kx.until(S("S3") <= 90.0, kx.scale((S("S2") - 95.0).clip(0.0), kx.one()) @ kx.at(1.0))
+    @ kx.at(0.25),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LEAN))
+def test_affine_kernel_fp64_paths_equal_oracle(orc, name):
+    c, m = LEAN[name](), M3()
+    r, pp = c.price(m, n_paths=4000, seed=5, steps_per_year=52, precision="fp64", per_path=True)
+    assert kx.last_launch_stats()["path_kernel"] == 5, name
+    o, op = orc.price_multi(c.to_json(), m, n_paths=4000, seed=5, steps_per_year=52, per_path=True)
+    assert np.allclose(np.asarray(pp), op, rtol=1e-11, atol=1e-11), name
+    assert abs(r.price - o.price) <= 1e-11 * max(1.0, abs(o.price))
+
+
+@pytest.mark.parametrize("name", ["asian_on_s3", "worst_of"])
+def test_non_affine_contracts_stay_on_the_general_kernel(name):
+    CONTRACTS[name]().price(M3(), n_paths=1000, seed=5, steps_per_year=52)
+    assert kx.last_launch_stats()["path_kernel"] == 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", sorted(LEAN))
+def test_affine_kernel_equals_general_kernel(monkeypatch, name, precision):
+    """The same paths through the general kernel (KX_PATH_KERNEL=general): FP64
+    to 1e-12; FP32 to the rounding of the affine forms, which add their terms
+    in another order than the interpreter (a few FP32 ulps of the spot level,
+    1e-6 of max(|pv|, 100))."""
+    c, m = LEAN[name](), M3()
+    kw = dict(n_paths=50_000, seed=13, steps_per_year=252, precision=precision, per_path=True)
+    r, pp = c.price(m, **kw)
+    assert kx.last_launch_stats()["path_kernel"] == 5
+    monkeypatch.setenv("KX_PATH_KERNEL", "general")
+    g, gp = c.price(m, **kw)
+    assert kx.last_launch_stats()["path_kernel"] == 1
+    pp, gp = np.asarray(pp), np.asarray(gp)
+    if precision == "fp64":
+        assert np.allclose(pp, gp, rtol=1e-12, atol=1e-12), name
+    else:
+        d = np.abs(pp - gp)
+        assert np.all(d <= 1e-6 * np.maximum(np.abs(gp), 100.0)), (name, float(d.max()))
+    assert abs(r.price - g.price) <= 1e-3 * r.std_error + 1e-12
+
+
+def _scaled(m, f):
+    return kx.CorrelatedGbmN([(n, s0 * f, mu, sg) for n, s0, mu, sg in m.factors], m.corr, rate=m.rate)
+
+
+def test_affine_kernel_fp32_per_path_at_benchmark_shape(orc):
+    """The 5-factor knock-out basket of the benchmark (252 steps a year) in
+    FP32 against the FP64 oracle, path by path: forward error 1e-5, or the
+    oracle's value for every spot scaled by 1 +- 1e-5 (the factor log-spots
+    do not depend on s0, so the whole path scales). The backward form serves
+    the paths whose basket ends near the strike: the FP32 basket carries the
+    rounding of five spots and of the Cholesky mix (measured: 1.9 % of
+    paths)."""
+    from parity import REL, fp32_check
+    n_f = 5
+    m = kx.CorrelatedGbmN([(f"S{i}", 100.0, 0.03, 0.15 + 0.05 * i) for i in range(n_f)],
+                          [[1.0 if i == j else 0.4 for j in range(n_f)] for i in range(n_f)], rate=0.03)
+    basket = (S("S0") + S("S1") + S("S2") + S("S3") + S("S4")) / 5.0
+    c = kx.until(basket >= 130.0, kx.scale((basket - 100.0).clip(0.0), kx.one()) @ kx.at(1.0))
+    n, kw = 20_000, dict(seed=42, steps_per_year=252)
+    r, pp = c.price(m, n_paths=n, precision="fp32", per_path=True, **kw)
+    assert kx.last_launch_stats()["path_kernel"] == 5
+    _, ref = orc.price_multi(c.to_json(), m, n_paths=n, per_path=True, **kw)
+    _, dn = orc.price_multi(c.to_json(), _scaled(m, 1.0 - REL), n_paths=n, per_path=True, **kw)
+    _, up = orc.price_multi(c.to_json(), _scaled(m, 1.0 + REL), n_paths=n, per_path=True, **kw)
+    ok, fwd = fp32_check(pp, ref, dn, up)
+    assert ok.all(), (int((~ok).sum()), np.flatnonzero(~ok)[:5])
+    assert fwd.mean() > 0.95, float(fwd.mean())
