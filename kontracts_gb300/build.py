@@ -23,7 +23,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXX_SOURCES = ["frontend.cpp", "capi.cpp"]
-CU_SOURCES = ["engine.cu", "paths_gbm.cu", "paths_heston.cu", "paths_bump.cu", "batch.cu", "lsm.cu", "adjoint.cu",
+CU_SOURCES = ["engine.cu", "paths_gbm.cu", "paths_heston.cu", "batch.cu", "lsm.cu", "adjoint.cu",
               "fixed_scratch.cu", "book.cu", "paths_pair.cu", "paths_multi.cu",
               "paths_multi_lean.cu"]
 

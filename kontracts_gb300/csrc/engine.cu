@@ -386,9 +386,8 @@ const void *select_kernel(int model, bool f64, int ns, int minb, bool lean, bool
         return model == KX_MODEL_GBM ? lean_kernel_gbm(f64, minb, stat, acc, sm)
                                      : lean_kernel_heston(f64, minb, stat, acc);
     }
-    if (model == KX_MODEL_GBM) return ns == 1 ? paths_kernel_gbm(f64, minb) : paths_kernel_bump(f64, minb);
-    if (ns != 1) raise(KX_UNSUPPORTED, "scenario launches need a GBM model");
-    return paths_kernel_heston(f64, minb);
+    if (ns != 1) raise(KX_CUDA_ERROR, "path launches carry one scenario");
+    return model == KX_MODEL_GBM ? paths_kernel_gbm(f64, minb) : paths_kernel_heston(f64, minb);
 }
 
 // k_lean serves launches whose contracts test the price only through
@@ -587,7 +586,6 @@ const int *variants(int model, bool f64, int ns, bool lean, int &n) {
         return f64 ? vm64 : vm32;
     }
     static const int v1[] = {4, 3, 2};
-    static const int v7[] = {2, 1};
     static const int l32[] = {4, 5, 6};
     static const int lg64[] = {4, 3};
     static const int lh64[] = {3};
@@ -597,9 +595,9 @@ const int *variants(int model, bool f64, int ns, bool lean, int &n) {
         n = 1;
         return lh64;
     }
-    if (ns == 1) { n = 3; return v1; }
-    n = 2;
-    return v7;
+    (void)ns;
+    n = 3;
+    return v1;
 }
 
 static uint64_t run_paths(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, uint64_t &stride_out) {

@@ -720,10 +720,8 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_paths(const PathArgs A) {
 const void *paths_kernel_pair(int model, int fp64);
 // paths_kernel_multi: correlated multi-factor GBM (M_MULTI) at a register budget.
 const void *paths_kernel_multi(int fp64, int minb);
-// which: 0 GBM FP32, 1 GBM FP64, 2 Heston FP32, 3 Heston FP64, 4 GBM FP32 x7
-// scenarios, 5 GBM FP64 x7 scenarios. Returns nullptr for a missing variant.
+// paths_kernel_gbm / _heston: one scenario at a register budget (MINB).
 const void *paths_kernel_gbm(int fp64, int minb);
 const void *paths_kernel_heston(int fp64, int minb);
-const void *paths_kernel_bump(int fp64, int minb);
 
 }  // namespace kx
