@@ -173,7 +173,8 @@ typedef struct kx_launch_stats {
                                   3 k_lean on compiled static schedules, 4 the
                                   same with a running average of the spot,
                                   5 k_multi_lean (correlated factors, affine
-                                  conditions and amounts) */
+                                  conditions and amounts), 6 k_mlmc_pairs
+                                  (fine and coarse multilevel paths at once) */
     uint64_t h2d_bytes, d2h_bytes;
 } kx_launch_stats;
 

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXX_SOURCES = ["frontend.cpp", "capi.cpp"]
 CU_SOURCES = ["engine.cu", "paths_gbm.cu", "paths_heston.cu", "batch.cu", "lsm.cu", "adjoint.cu",
               "fixed_scratch.cu", "book.cu", "paths_pair.cu", "paths_multi.cu",
-              "paths_multi_lean.cu"]
+              "paths_multi_lean.cu", "paths_mlmc.cu"]
 
 
 def _nvcc() -> str:

@@ -1534,14 +1534,16 @@ static std::vector<Stats> mlmc_level_stats(Ctx &c, const Program &p, const Model
         coarse.push_back(std::move(jc));
     }
     uint64_t nfine = 0, ncoarse = 0;
-    run_paths(c, fine, cfg, 1, nfine);
-    c.mlmc.ensure(std::max<uint64_t>(1, 2 * nfine) * sizeof(double));
-    if (nfine)
-        KX_CUDA(cudaMemcpyAsync(c.mlmc.p, c.pv.p, nfine * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
-    if (!coarse.empty()) {
-        run_paths_v(c, coarse, cfg, 1, ncoarse, 2, use_lean(coarse, 1), true);
-        KX_CUDA(cudaMemcpyAsync(c.mlmc.as<double>() + nfine, c.pv.p, ncoarse * sizeof(double),
-                                cudaMemcpyDeviceToDevice, c.stream));
+    if (!mlmc_pairs_run(c, fine, coarse, cfg, nfine)) {
+        run_paths(c, fine, cfg, 1, nfine);
+        c.mlmc.ensure(std::max<uint64_t>(1, 2 * nfine) * sizeof(double));
+        if (nfine)
+            KX_CUDA(cudaMemcpyAsync(c.mlmc.p, c.pv.p, nfine * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+        if (!coarse.empty()) {
+            run_paths_v(c, coarse, cfg, 1, ncoarse, 2, use_lean(coarse, 1), true);
+            KX_CUDA(cudaMemcpyAsync(c.mlmc.as<double>() + nfine, c.pv.p, ncoarse * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, c.stream));
+        }
     }
     // run q >= 1 (level >= 1): fine at f_q, coarse at nfine + f_q - n0, i.e. (nfine - n0) further on
     std::vector<StatsJob> sj(runs.size());

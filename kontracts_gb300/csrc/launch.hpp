@@ -95,6 +95,14 @@ size_t plan_upload_bytes(const PathPlan &P);
 // c.pv[0 .. n_paths)); false, with nothing launched, otherwise.
 bool multi_lean_run(Ctx &c, Job &j, const kx_mc_config &cfg);
 
+// The fine and coarse paths of multilevel runs in one k_mlmc_pairs launch when
+// every job has a static schedule (fine[q] is run q; coarse[] the runs of
+// level >= 1 in order). Per-path values go to c.mlmc: the fine paths of all
+// runs from 0 (nfine in total), the coarse ones from nfine; the jobs' pv_off
+// are set to those offsets. False, with nothing launched, otherwise.
+bool mlmc_pairs_run(Ctx &c, std::vector<Job> &fine, std::vector<Job> &coarse, const kx_mc_config &cfg,
+                    uint64_t &nfine);
+
 // Raises the error the device error word of a path launch reports.
 void check_err_word(uint32_t err);
 

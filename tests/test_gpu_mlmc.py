@@ -110,11 +110,14 @@ def test_no_pilot_allocates_one_path_per_level(orc):
 @pytest.mark.parametrize("model", sorted(MODELS))
 @pytest.mark.parametrize("name", sorted(CONTRACTS))
 def test_lean_level_pairs_equal_general_kernel(monkeypatch, precision, model, name):
-    """The coarse paths of a level pair on k_lean (static schedules, the running
-    average in registers) and on k_paths (KX_PATH_KERNEL=general) are the same
-    arithmetic on the same normals: the level variances agree exactly."""
+    """The paths of a level pair in one k_mlmc_pairs launch (fine and coarse
+    paths on the same Philox blocks; contracts on static schedules without
+    averages), or on k_lean (the Asian: the running average in registers),
+    and on k_paths (KX_PATH_KERNEL=general) are the same arithmetic on the
+    same normals: the level variances agree exactly."""
     c, m = CONTRACTS[name](), MODELS[model]()
     got = [kx.estimate_variance_at_level(c, m, level, 20_000, seed=3, precision=precision) for level in (1, 3, 6)]
+    assert (kx.last_launch_stats()["path_kernel"] == 6) == (name != "asian")
     monkeypatch.setenv("KX_PATH_KERNEL", "general")
     ref = [kx.estimate_variance_at_level(c, m, level, 20_000, seed=3, precision=precision) for level in (1, 3, 6)]
     assert got == ref, (name, model, precision, got, ref)
