@@ -215,26 +215,31 @@ def price_greeks(c, m, n_paths, seed, spy) -> dict:
     """Price + delta/vega/rho of the workload: the pathwise adjoint (one reverse
     sweep per path, checkpoints every 16 steps, logistic barrier of the
     default width) against GPU CRN bump-and-reprice of the same smoothed
-    payoff (seven scenarios sharing each path's normals, h = 1e-3 relative).
+    payoff (seven reprices on the seed's normals as plain jobs of one lean
+    launch, h = 1e-3 relative) and of the raw payoff.
     Equal standard error: the bump cost is scaled by the worst
     (SE_bump / SE_adjoint)^2 over the three Greeks (MC time ~ paths ~ SE^-2)."""
     import kontracts_gb300 as kx
 
-    def timed(fn, reps=3):
+    sim = {}
+
+    def timed(fn, reps=3, key=None):
         best = None
         for _ in range(reps):
             out = fn()
             st = kx.last_launch_stats()
             t = (st["kernel_ms"] + st["reduce_ms"]) * 1e-3
             best = t if best is None or t < best else best
+            if key:
+                sim[key] = st["steps_simulated"]
         return out, best
 
     adj, t_adj = timed(lambda: c.adjoint(m, n_paths=n_paths, seed=seed, steps_per_year=spy, checkpoint_every=16))
     w = adj.smoothing_width
     bump, t_bump = timed(lambda: c.greeks(m, n_paths=n_paths, seed=seed, steps_per_year=spy,
-                                          bumps=(1e-3, 1e-3, 1e-3), relative=True, smooth_width=w))
+                                          bumps=(1e-3, 1e-3, 1e-3), relative=True, smooth_width=w), key="smoothed")
     raw, t_raw = timed(lambda: c.greeks(m, n_paths=n_paths, seed=seed, steps_per_year=spy,
-                                        bumps=(1e-3, 1e-3, 1e-3), relative=True), reps=1)
+                                        bumps=(1e-3, 1e-3, 1e-3), relative=True), reps=1, key="raw")
     pairs = {"delta": (adj.d_s0, adj.se_s0, bump.delta, bump.delta_se, raw.delta, raw.delta_se),
              "vega": (adj.d_sigma, adj.se_sigma, bump.vega, bump.vega_se, raw.vega, raw.vega_se),
              "rho": (adj.d_r, adj.se_r, bump.rho, bump.rho_se, raw.rho, raw.rho_se)}
@@ -251,6 +256,11 @@ def price_greeks(c, m, n_paths, seed, spy) -> dict:
                             **{k + "_se": v[5] for k, v in pairs.items()}},
         "rel_diff_adjoint_vs_bump": {k: abs(v[0] - v[2]) / max(abs(v[2]), 1e-12) for k, v in pairs.items()},
         "smoothed_over_raw_bump_time": t_bump / t_raw,
+        # the smoothed payoff keeps paths alive past the barrier (their weight reaches exactly 0 only
+        # far beyond it), so it simulates more steps; per simulated step the two bumps run alike
+        "steps_simulated": {"bump_smoothed": sim.get("smoothed"), "bump_raw_payoff": sim.get("raw")},
+        "smoothed_over_raw_time_per_simulated_step": (t_bump / sim["smoothed"]) / (t_raw / sim["raw"])
+        if sim.get("smoothed") and sim.get("raw") else None,
         "equal_se_speedup_vs_bump_smoothed": t_bump * se_scale / t_adj,
         "equal_se_speedup_vs_bump_raw": t_raw * se_scale_raw / t_adj,
         "price_greeks_per_s_equal_se": {"adjoint": 1.0 / t_adj, "bump_smoothed": 1.0 / (t_bump * se_scale),
@@ -584,6 +594,20 @@ def heston_book(reps=3) -> dict:
         ta = _dev_seconds(kx)
         adj = (a, ta) if adj is None or ta < adj[1] else adj
     a, ta = adj
+    # the whole book: price and the seven Heston sensitivities of every contract by one portfolio
+    # adjoint launch, each contract on its own 1M paths
+    nb = 1_000_000
+    tb = None
+    for _ in range(2):
+        _, sens = kx.price_portfolio(book, [h] * len(book), [nb] * len(book), list(range(len(book))),
+                                     steps_per_year=252, greeks=True)
+        t = _dev_seconds(kx)
+        tb = t if tb is None or t < tb else tb
+    book_adj = {"workload": "price + (s0, v0, kappa, theta, sigma_v, rho, r) sensitivities of all 96 calls, "
+                            "one portfolio adjoint launch, 1M paths per contract, FP32",
+                "seconds": tb, "contracts_per_s": len(book) / tb,
+                "path_steps_per_s": sum(nb * (len(c.time_grid(252)) - 1) for c in book) / tb,
+                "d_s0_T1_K100": sens[32 + 15].d_s0, "d_v0_T1_K100": sens[32 + 15].d_v0}
     return {"workload": "96 Heston calls (32 strikes x 3 maturities) on one 2M-path simulation, full truncation, "
                         "252 steps/yr, FP32", "seconds": best, "path_steps_per_s": steps / best,
             "contracts_per_s": len(book) / best, "price_T1_K100": res[32 + 15].price,
@@ -594,7 +618,8 @@ def heston_book(reps=3) -> dict:
                          "note": "time includes the 96 payoffs on the shared simulation"},
             "adjoint_T1_K100": {"seconds": ta, "price": a.price, "d_s0": a.d_s0, "d_v0": a.d_v0,
                                 "d_kappa": a.d_kappa, "d_theta": a.d_theta, "d_sigma_v": a.d_sigma_v,
-                                "d_rho": a.d_rho, "se_v0": a.se_v0, "checkpoint_every": 16}}
+                                "d_rho": a.d_rho, "se_v0": a.se_v0, "checkpoint_every": 16},
+            "adjoint_book_96": book_adj}
 
 
 def book_256(reps=5) -> dict:

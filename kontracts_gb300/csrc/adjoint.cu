@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 
 #include "device_common.cuh"
@@ -65,6 +66,8 @@ struct AdjArgs {
     AdjUntil su[ADJ_MAXU];
     AdjAcc acc[ADJ_MAXA];
     int K;                // checkpoint interval (multiple of 4)
+    int uniform;          // every step k >= 1 has the coefficients (uc0, uc1): dt, sqrt(dt)
+    double uc0, uc1;
     int model, scheme;
     uint64_t n_paths, seed;
     double s0, mu, sigma;                         // GBM (mu = drift)
@@ -84,7 +87,7 @@ struct Dual {
 };
 
 template <class Real>
-__device__ Dual<Real> eval_dual(const KxProgram &P, int off, int len, Real S, const Real *accv) {
+__device__ __noinline__ Dual<Real> eval_dual(const KxProgram &P, int off, int len, Real S, const Real *accv) {
     Dual<Real> st[KX_MAX_STACK];
     int sp = 0;
     for (int pc = off; pc < off + len; ++pc) {
@@ -546,8 +549,8 @@ static void schedule(const Lowered &low, const KxProgram &P, const StepTables &t
 // checkpoints), so that registers hold only the state of the step loops and
 // eight blocks (FP32; four in FP64) fit an SM: n_ck checkpoint rows are
 // allocated at launch.
-template <class Real, int K, int NSU>
-__global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoint_gbm(const AdjArgs *__restrict__ all,
+template <class Real, int K, int NSU, int MINB>
+__global__ void __launch_bounds__(ADJ_BLOCK, MINB) k_adjoint_gbm(const AdjArgs *__restrict__ all,
                                                               const uint64_t *__restrict__ off, int n_contracts,
                                                               uint64_t total, double *__restrict__ out,
                                                               const PhiloxKeys keys, int n_ck) {
@@ -573,6 +576,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
         const Real s0 = pp.s0, inv_w = pp.inv_w;
         const int nflows = A.n_flows;
         constexpr int nsu = NSU;
+        const bool uni = A.uniform != 0;
+        const Real udt = (Real)A.uc0, usq = (Real)A.uc1;
+        const Real ua = mul_rn(pp.drift, udt), ub = mul_rn(pp.sigma, usq);  // uniform grids: the step's terms
         int su_arm[ADJ_MAXU];
 #pragma unroll
         for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
@@ -586,12 +592,18 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
         }
         double pv_hard = 0.0, pv = 0.0, pv_t = 0.0;
         int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
-        Real z[4];
+        Real z0 = 0, z1 = 0, z2 = 0, z3 = 0;
         for (int k = 0; k <= N; ++k) {
             if (k > 0) {
-                const uint64_t d = (uint64_t)(k - 1);
-                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
-                y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
+                const int q = (k - 1) & 3;
+                if (q == 0) {
+                    Real z[4];
+                    draws4<Real>(A, keys, path, (uint64_t)(k - 1), z);
+                    z0 = z[0]; z1 = z[1]; z2 = z[2]; z3 = z[3];
+                }
+                const Real zk = q == 0 ? z0 : q == 1 ? z1 : q == 2 ? z2 : z3;
+                y = uni ? gbm_step(y, ua, ub, zk)
+                        : gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), zk);
             }
             if (k % K == 0) ck_y[(k / K) * ADJ_BLOCK] = y;  // K is a power of two: a mask, not a division
 #pragma unroll
@@ -602,7 +614,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
                     if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
                 }
             if (k != nft) continue;
-            const Real S = s0 * fast_exp<Real>(y);
+            const Real S = spot_of<Real>(s0, y);
             for (int f = nf; f < nflows && A.flow[f].t == k; ++f) {
                 const AdjFlow &F = A.flow[f];
                 nf = f + 1;
@@ -653,9 +665,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
             }
 #pragma unroll
             for (int j = 1; j <= K; ++j) {
-                const int k = k0 + j;
-                const StepRec<Real> rec = R[min(k, N)];  // past N: harmless states never read
-                sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
+                if (uni) {
+                    sy[j] = gbm_step(sy[j - 1], ua, ub, sz[j]);
+                } else {
+                    const StepRec<Real> rec = R[min(k0 + j, N)];  // past N: harmless states never read
+                    sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
+                }
             }
             const int jtop = (c == nseg - 1) ? k1 - k0 : k1 - k0 - 1;
 #pragma unroll
@@ -663,14 +678,19 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
                 if (j > jtop) continue;
                 const int k = k0 + j;
                 if (k < N) {  // step k -> k + 1: d y_{k+1} / d y_k = 1, so lam carries over
-                    const StepRec<Real> rn = R[k + 1];
-                    g_sig += lam * (-pp.sigma * rn.c0 + rn.c1 * sz[j + 1]);
-                    g_r += lam * rn.c0;
+                    Real dt = udt, sq = usq;
+                    if (!uni) {
+                        const StepRec<Real> rn = R[k + 1];
+                        dt = rn.c0;
+                        sq = rn.c1;
+                    }
+                    g_sig += lam * (-pp.sigma * dt + sq * sz[j + 1]);
+                    g_r += lam * dt;
                 }
                 const Real yk = sy[j];
                 Real g = Real(0);
                 if (k == pft) {  // the flows paid at step k, in slot order
-                    const Real Sk = s0 * fast_exp<Real>(yk);
+                    const Real Sk = spot_of<Real>(s0, yk);
                     int f0 = pf;
                     while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
                     for (int f = f0; f <= pf; ++f) {
@@ -687,7 +707,8 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
                         const Real sv = smooth_weight(x);
-                        g -= Q[u] * pp.sgn[u] * (Real(1) - sv) * inv_w;
+                        const Real dls = (Real(1) - sv) * inv_w;
+                        g -= Q[u] * pp.sgn[u] * dls;
                     }
                 lam += g;
             }
@@ -702,33 +723,51 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4) k_adjoin
     }
 }
 
+// Per-thread records of the GBM adjoint kernels in shared memory, one column
+// per thread (entry e of thread t at e * ADJ_BLOCK + t), sized per launch:
+// nf flow values (double), nf spot coefficients, nf * na accumulator
+// coefficients and arg-extremum steps, n_ck checkpoints, and the K + 1
+// states and normals of the segment being swept.
+struct AdjSmem {
+    int nf, na, n_ck, K;
+};
+template <class Real>
+__host__ __device__ inline size_t adj_smem_bytes(const AdjSmem &L) {
+    return (size_t)ADJ_BLOCK * (L.nf * sizeof(double) +
+                                (L.nf + L.nf * L.na + L.n_ck + 2 * (L.K + 1)) * sizeof(Real) + L.nf * L.na * sizeof(int));
+}
+
 // GBM contracts with averages or running extrema (Asians, lookbacks, their
-// barrier versions), checkpoint interval K fixed at compile time: the
-// accumulators and the recomputed segment live in registers, the checkpoints
-// and the per-flow records (values, spot and accumulator coefficients, the
-// steps of the running extrema) in shared memory, one column per thread.
-// Every quantity is computed with k_adjoint's operations in k_adjoint's
-// order, so the two kernels give the same outputs; what changes is the
-// bookkeeping of the reverse sweep: an average's coefficient joins at a step
-// the host schedule fixes (min(t_f, window end)), and a running extremum's
-// coefficient at the path's arg-extremum, so the sweep looks for the next of
-// each instead of scanning every flow at every step.
-template <class Real, int K>
-__global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
+// barrier versions) and, with none, barrier and European contracts: the
+// checkpoint interval K is a launch parameter, the accumulators live in
+// registers, everything indexed by step in shared memory (AdjSmem), so the
+// step loops are short and not unrolled. Every quantity is computed with
+// k_adjoint's operations in k_adjoint's order, so the two kernels give the
+// same outputs; what changes is the bookkeeping:
+//  * on a uniform grid the step coefficients are formed once per path (the
+//    products k_adjoint forms at every step, same roundings);
+//  * the reverse sweep knows the next step at which something other than the
+//    step-by-step terms happens (a flow paid, an average's coefficient joining
+//    at min(t_f, window end), a running extremum's arg-extremum) and tests
+//    one step number per step.
+// NAC, AK0, NS: the launch's accumulator count, the kind of its first
+// accumulator and its smoothed-barrier count when every contract of the
+// launch shares them (-1: read per contract), so that the checks they decide
+// leave the step loops.
+template <class Real, int MINB, int NAC = -1, int AK0 = -1, int NS = -1>
+__global__ void __launch_bounds__(ADJ_BLOCK, MINB)
     k_adjoint_gbm_acc(const AdjArgs *__restrict__ all, const uint64_t *__restrict__ off, int n_contracts,
-                      uint64_t total, double *__restrict__ out, const PhiloxKeys keys, int n_ck) {
-    static_assert(K % 4 == 0 && (K & (K - 1)) == 0 && K <= ADJ_KMAX, "K: a power of two, multiple of 4");
+                      uint64_t total, double *__restrict__ out, const PhiloxKeys keys, const AdjSmem L) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
-    constexpr size_t B = ADJ_BLOCK;
-    constexpr size_t O_FCS = ADJ_MAXF * B * sizeof(double);
-    constexpr size_t O_FCA = O_FCS + ADJ_MAXF * B * sizeof(Real);
-    constexpr size_t O_FARG = O_FCA + ADJ_MAXF * ADJ_MAXA * B * sizeof(Real);
-    constexpr size_t O_CK = O_FARG + ADJ_MAXF * ADJ_MAXA * B * sizeof(int);
-    double *const fP = reinterpret_cast<double *>(adj_smem) + threadIdx.x;           // [f * B]
-    Real *const fcs = reinterpret_cast<Real *>(adj_smem + O_FCS) + threadIdx.x;      // [f * B]
-    Real *const fca = reinterpret_cast<Real *>(adj_smem + O_FCA) + threadIdx.x;      // [(f * ADJ_MAXA + a) * B]
-    int *const farg = reinterpret_cast<int *>(adj_smem + O_FARG) + threadIdx.x;      // [(f * ADJ_MAXA + a) * B]
-    Real *const ck_y = reinterpret_cast<Real *>(adj_smem + O_CK) + threadIdx.x;      // [c * B], c < n_ck
+    constexpr int B = ADJ_BLOCK;
+    const int K = L.K, NA = L.na;
+    double *const fP = reinterpret_cast<double *>(adj_smem) + threadIdx.x;                    // [f]
+    Real *const fcs = reinterpret_cast<Real *>(adj_smem + (size_t)B * L.nf * sizeof(double)) + threadIdx.x;  // [f]
+    Real *const fca = fcs + (size_t)B * L.nf;                                                 // [f * NA + a]
+    Real *const ck_y = fca + (size_t)B * L.nf * NA;                                           // [c]
+    Real *const sy = ck_y + (size_t)B * L.n_ck;                                               // [j], j <= K
+    Real *const sz = sy + (size_t)B * (K + 1);                                                // [j - 1], 1 <= j <= K
+    int *const farg = reinterpret_cast<int *>(sz + (size_t)B * (K + 1) - threadIdx.x) + threadIdx.x;  // [f * NA + a]
     for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
          gp += (uint64_t)gridDim.x * blockDim.x) {
         int lo = 0, hi = n_contracts - 1;  // contract of global path gp
@@ -744,13 +783,17 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
         const int N = A.n_times - 1;
         const AdjPar<Real> pp = adj_par<Real>(A);
         const Real s0 = pp.s0, inv_w = pp.inv_w;
-        const int nflows = A.n_flows, nsu = A.n_su, nacc = A.n_acc;
+        const int nflows = A.n_flows;
+        const int nsu = NS >= 0 ? NS : A.n_su, nacc = NAC >= 0 ? NAC : A.n_acc;
+        const bool uni = A.uniform != 0;
+        const Real udt = (Real)A.uc0, usq = (Real)A.uc1;
+        const Real ua = mul_rn(pp.drift, udt), ub = mul_rn(pp.sigma, usq);  // uniform grids: the step's terms
         int su_arm[ADJ_MAXU], a_kind[ADJ_MAXA], a_from[ADJ_MAXA], a_to[ADJ_MAXA];
 #pragma unroll
         for (int u = 0; u < ADJ_MAXU; ++u) su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
 #pragma unroll
         for (int a = 0; a < ADJ_MAXA; ++a) {
-            a_kind[a] = a < nacc ? A.acc[a].kind : ACC_SUM;
+            a_kind[a] = a == 0 && AK0 >= 0 ? AK0 : a < nacc ? A.acc[a].kind : ACC_SUM;
             a_from[a] = a < nacc ? A.acc[a].i_from : INT_MAX;
             a_to[a] = a < nacc ? A.acc[a].i_to : -1;
         }
@@ -773,12 +816,19 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
         }
         double pv_hard = 0.0, pv = 0.0, pv_t = 0.0;
         int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
-        Real z[4];
+        Real z0 = 0, z1 = 0, z2 = 0, z3 = 0;
+#pragma unroll 1
         for (int k = 0; k <= N; ++k) {
             if (k > 0) {
-                const uint64_t d = (uint64_t)(k - 1);
-                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
-                y = gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), z[d & 3u]);
+                const int q = (k - 1) & 3;
+                if (q == 0) {
+                    Real z[4];
+                    draws4<Real>(A, keys, path, (uint64_t)(k - 1), z);
+                    z0 = z[0]; z1 = z[1]; z2 = z[2]; z3 = z[3];
+                }
+                const Real zk = q == 0 ? z0 : q == 1 ? z1 : q == 2 ? z2 : z3;
+                y = uni ? gbm_step(y, ua, ub, zk)
+                        : gbm_step(y, mul_rn(pp.drift, R[k].c0), mul_rn(pp.sigma, R[k].c1), zk);
             }
             if (k % K == 0) ck_y[(k / K) * B] = y;
             const Real S = spot_of<Real>(s0, y);
@@ -822,10 +872,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
                 fcs[f * B] = (Real)((double)(amt.d[0] * w) * df);
 #pragma unroll
                 for (int a = 0; a < ADJ_MAXA; ++a) {
+                    if (a >= NA) continue;
                     Real c = (Real)((double)(amt.d[1 + a] * w) * df);
                     if (a < nacc && a_kind[a] == ACC_SUM) c /= (Real)(min(k, a_to[a]) - a_from[a] + 1);
-                    fca[(f * ADJ_MAXA + a) * B] = c;
-                    farg[(f * ADJ_MAXA + a) * B] = argx[a];
+                    fca[(f * NA + a) * B] = c;
+                    farg[(f * NA + a) * B] = argx[a];
                 }
                 pv += fpv;
                 pv_t += A.times[k] * fpv;
@@ -857,7 +908,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
 #pragma unroll
                 for (int a = 0; a < ADJ_MAXA; ++a)
                     if (a < nacc && a_kind[a] != ACC_SUM) {
-                        const int s = farg[(f * ADJ_MAXA + a) * B];
+                        const int s = farg[(f * NA + a) * B];
                         if (s < lim && s > m) m = s;
                     }
             return m;
@@ -869,64 +920,77 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
         Real g_sig = Real(0), g_r = Real(0);
         int pf = nflows - 1, pft = pf >= 0 ? A.flow[pf].t : -1;
         const int nseg = (N + K - 1) / K;
+#pragma unroll 1
         for (int c = nseg - 1; c >= 0; --c) {
             const int k0 = c * K;
             const int k1 = min(k0 + K, N);
-            Real sy[K + 1], sz[K + 2];
-            sy[0] = ck_y[c * B];
-            sz[K + 1] = Real(0);
-#pragma unroll
-            for (int q = 0; q < K / 4; ++q) {  // the draws of steps k0 + 1 .. k0 + K
+            // recompute states k0 .. k0 + K and the draws of steps k0 + 1 .. k0 + K
+            Real yy = ck_y[c * B];
+            sy[0] = yy;
+#pragma unroll 1
+            for (int j = 1; j <= K; j += 4) {
                 Real w4[4];
-                draws4<Real>(A, keys, path, (uint64_t)(k0 + 4 * q), w4);
+                draws4<Real>(A, keys, path, (uint64_t)(k0 + j - 1), w4);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) sz[1 + 4 * q + j] = w4[j];
-            }
-#pragma unroll
-            for (int j = 1; j <= K; ++j) {
-                const StepRec<Real> rec = R[min(k0 + j, N)];  // past N: harmless states never read
-                sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
+                for (int i = 0; i < 4; ++i) {
+                    if (uni) {
+                        yy = gbm_step(yy, ua, ub, w4[i]);
+                    } else {
+                        const StepRec<Real> rec = R[min(k0 + j + i, N)];  // past N: harmless states never read
+                        yy = gbm_step(yy, mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), w4[i]);
+                    }
+                    sy[(j + i) * B] = yy;
+                    sz[(j + i - 1) * B] = w4[i];
+                }
             }
             const int jtop = (c == nseg - 1) ? k1 - k0 : k1 - k0 - 1;
-#pragma unroll
-            for (int j = K; j >= 0; --j) {
-                if (j > jtop) continue;
+            int nxt = max(max(kj, pft), ke);  // the next special step
+#pragma unroll 1
+            for (int j = jtop; j >= 0; --j) {
                 const int k = k0 + j;
                 if (k < N) {
-                    const StepRec<Real> rec = R[k + 1];
-                    const Real dt = rec.c0, sq = rec.c1;
-                    g_sig += lam * (-pp.sigma * dt + sq * sz[j + 1]);
+                    Real dt = udt, sq = usq;
+                    if (!uni) {
+                        const StepRec<Real> rec = R[k + 1];
+                        dt = rec.c0;
+                        sq = rec.c1;
+                    }
+                    g_sig += lam * (-pp.sigma * dt + sq * sz[j * B]);
                     g_r += lam * dt;
                 }
-                const Real Sk = spot_of<Real>(s0, sy[j]);
+                const Real yk = sy[j * B];
+                const Real Sk = spot_of<Real>(s0, yk);
                 Real g = Real(0);
-                if (k == kj) {  // average coefficients whose window ends here, flows in slot order
-                    for (int f = 0; f < nflows; ++f)
+                if (k == nxt) {
+                    if (k == kj) {  // average coefficients whose window ends here, flows in slot order
+                        for (int f = 0; f < nflows; ++f)
 #pragma unroll
-                        for (int a = 0; a < ADJ_MAXA; ++a)
-                            if (a < nacc && a_kind[a] == ACC_SUM && k == min(A.flow[f].t, a_to[a]))
-                                G[a] += fca[(f * ADJ_MAXA + a) * B];
-                    kj = next_join(k);
-                }
-                if (k == pft) {  // the flows paid at step k, in slot order
-                    int f0 = pf;
-                    while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
-                    for (int f = f0; f <= pf; ++f) {
-                        g += fcs[f * B] * Sk;
-#pragma unroll
-                        for (int u = 0; u < ADJ_MAXU; ++u)
-                            if (u < nsu && ((A.flow[f].su_mask >> u) & 1u)) Q[u] += (Real)fP[f * B];
+                            for (int a = 0; a < ADJ_MAXA; ++a)
+                                if (a < nacc && a_kind[a] == ACC_SUM && k == min(A.flow[f].t, a_to[a]))
+                                    G[a] += fca[(f * NA + a) * B];
+                        kj = next_join(k);
                     }
-                    pf = f0 - 1;
-                    pft = pf >= 0 ? A.flow[pf].t : -1;
-                }
-                if (k == ke) {  // running max / min: at the arg-extremum
-                    for (int f = 0; f < nflows; ++f)
+                    if (k == pft) {  // the flows paid at step k, in slot order
+                        int f0 = pf;
+                        while (f0 > 0 && A.flow[f0 - 1].t == k) --f0;
+                        for (int f = f0; f <= pf; ++f) {
+                            g += fcs[f * B] * Sk;
 #pragma unroll
-                        for (int a = 0; a < ADJ_MAXA; ++a)
-                            if (a < nacc && a_kind[a] != ACC_SUM && farg[(f * ADJ_MAXA + a) * B] == k)
-                                g += fca[(f * ADJ_MAXA + a) * B] * Sk;
-                    ke = next_ext(k);
+                            for (int u = 0; u < ADJ_MAXU; ++u)
+                                if (u < nsu && ((A.flow[f].su_mask >> u) & 1u)) Q[u] += (Real)fP[f * B];
+                        }
+                        pf = f0 - 1;
+                        pft = pf >= 0 ? A.flow[pf].t : -1;
+                    }
+                    if (k == ke) {  // running max / min: at the arg-extremum
+                        for (int f = 0; f < nflows; ++f)
+#pragma unroll
+                            for (int a = 0; a < ADJ_MAXA; ++a)
+                                if (a < nacc && a_kind[a] != ACC_SUM && farg[(f * NA + a) * B] == k)
+                                    g += fca[(f * NA + a) * B] * Sk;
+                        ke = next_ext(k);
+                    }
+                    nxt = max(max(kj, pft), ke);
                 }
 #pragma unroll
                 for (int a = 0; a < ADJ_MAXA; ++a)  // averages: inside the window
@@ -934,7 +998,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
 #pragma unroll
                 for (int u = 0; u < ADJ_MAXU; ++u)
                     if (u < nsu && k >= su_arm[u] && Q[u] != Real(0)) {
-                        const Real x = pp.sgn[u] * (sy[j] - pp.thr[u]) * inv_w;
+                        const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
                         const Real sv = smooth_weight(x);
                         const Real dls = (Real(1) - sv) * inv_w;
                         g -= Q[u] * pp.sgn[u] * dls;
@@ -955,12 +1019,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK, sizeof(Real) == 4 ? 8 : 4)
     }
 }
 
-template <class Real, int K>
+template <class Real, int K, int MINB>
 static const void *adj_gbm_kernel(int nsu) {
     switch (nsu) {
-    case 0: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 0>);
-    case 1: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 1>);
-    default: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 2>);
+    case 0: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 0, MINB>);
+    case 1: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 1, MINB>);
+    default: return reinterpret_cast<const void *>(&k_adjoint_gbm<Real, K, 2, MINB>);
     }
 }
 
@@ -1023,6 +1087,16 @@ static AdjJob make_adj_job(const Program &p, const Model &m, const kx_mc_config 
     a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
     a.r = m.r;
     const bool f64 = cfg.precision == KX_PREC_FP64;
+    // uniform grid: every step's (dt, sqrt dt) equal in the launch precision
+    const bool f64p = cfg.precision == KX_PREC_FP64;
+    a.uniform = N >= 1 ? 1 : 0;
+    a.uc0 = N >= 1 ? grid[1] - grid[0] : 0.0;
+    a.uc1 = std::sqrt(a.uc0);
+    for (int k = 2; k <= N && a.uniform; ++k) {
+        const double dt = grid[k] - grid[k - 1], sq = std::sqrt(dt);
+        if (f64p ? (dt != a.uc0 || sq != a.uc1) : ((float)dt != (float)a.uc0 || (float)sq != (float)a.uc1))
+            a.uniform = 0;
+    }
     J.steps.resize(n * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
     for (int k = 0; k < n; ++k) {
         const double dt = k == 0 ? 0.0 : grid[k] - grid[k - 1];
@@ -1098,28 +1172,57 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     const void *kfn = model == KX_MODEL_GBM
                           ? (f64 ? adj_kernel<double, KX_MODEL_GBM>(acc) : adj_kernel<float, KX_MODEL_GBM>(acc))
                           : (f64 ? adj_kernel<double, KX_MODEL_HESTON>(acc) : adj_kernel<float, KX_MODEL_HESTON>(acc));
-    // GBM without accumulators: the register-resident kernel at a tuned
-    // checkpoint interval (results do not depend on it: the recomputation
-    // repeats the forward pass's operations)
-    // (with accumulators: the kernel that keeps them in registers). KX_ADJOINT_KERNEL
-    // = "general" keeps the generic kernel.
+    // GBM: the specialised kernels, tuned over checkpoint interval and register
+    // budget on the call's own work (results do not depend on the choice: every
+    // GBM kernel repeats k_adjoint's operations in its order, and the
+    // recomputation repeats the forward pass's). KX_ADJOINT_KERNEL = "general"
+    // keeps the generic kernel.
     std::vector<std::pair<int, const void *>> cands;
     int kck = 0;  // checkpoint interval of the chosen GBM kernel (0: the generic kernel)
     const char *kenv = getenv("KX_ADJOINT_KERNEL");
     const bool generic_only = kenv && strcmp(kenv, "general") == 0;
     if (model == KX_MODEL_GBM && !acc && same_nsu && !generic_only) {
-        if (max_n / 8 + 1 <= ADJ_MAXCK)
-            cands.push_back({8, f64 ? adj_gbm_kernel<double, 8>(nsu) : adj_gbm_kernel<float, 8>(nsu)});
-        if (max_n / 16 + 1 <= ADJ_MAXCK)
-            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16>(nsu) : adj_gbm_kernel<float, 16>(nsu)});
+        // the register-resident kernel at two register budgets (resident blocks per SM)
+        if (max_n / 8 + 1 <= ADJ_MAXCK) {
+            cands.push_back({8, f64 ? adj_gbm_kernel<double, 8, 4>(nsu) : adj_gbm_kernel<float, 8, 8>(nsu)});
+            cands.push_back({8, f64 ? adj_gbm_kernel<double, 8, 2>(nsu) : adj_gbm_kernel<float, 8, 5>(nsu)});
+        }
+        if (max_n / 16 + 1 <= ADJ_MAXCK) {
+            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16, 4>(nsu) : adj_gbm_kernel<float, 16, 8>(nsu)});
+            cands.push_back({16, f64 ? adj_gbm_kernel<double, 16, 2>(nsu) : adj_gbm_kernel<float, 16, 5>(nsu)});
+        }
     }
-    if (model == KX_MODEL_GBM && acc && !generic_only) {
-        if (max_n / 8 + 1 <= ADJ_MAXCK)
-            cands.push_back({8, f64 ? (const void *)&k_adjoint_gbm_acc<double, 8> : (const void *)&k_adjoint_gbm_acc<float, 8>});
-        if (max_n / 16 + 1 <= ADJ_MAXCK)
-            cands.push_back(
-                {16, f64 ? (const void *)&k_adjoint_gbm_acc<double, 16> : (const void *)&k_adjoint_gbm_acc<float, 16>});
+    // the accumulator kernel at two register budgets (resident blocks per SM), specialised where
+    // every contract of the launch has one accumulator of one kind and no smoothed barrier
+    int one_kind = -1;
+    if (model == KX_MODEL_GBM) {
+        one_kind = jobs[0].a.n_acc == 1 && jobs[0].a.n_su == 0 ? jobs[0].a.acc[0].kind : -1;
+        for (auto &j : jobs)
+            if (j.a.n_acc != 1 || j.a.n_su != 0 || j.a.acc[0].kind != one_kind) one_kind = -1;
     }
+    const void *acc_fns[2];
+    if (one_kind == ACC_SUM) {
+        acc_fns[0] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 3, 1, ACC_SUM, 0>
+                         : (const void *)&k_adjoint_gbm_acc<float, 6, 1, ACC_SUM, 0>;
+        acc_fns[1] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 2, 1, ACC_SUM, 0>
+                         : (const void *)&k_adjoint_gbm_acc<float, 8, 1, ACC_SUM, 0>;
+    } else if (one_kind == ACC_MAX || one_kind == ACC_MIN) {
+        const bool mx = one_kind == ACC_MAX;
+        acc_fns[0] = f64 ? (mx ? (const void *)&k_adjoint_gbm_acc<double, 3, 1, ACC_MAX, 0>
+                               : (const void *)&k_adjoint_gbm_acc<double, 3, 1, ACC_MIN, 0>)
+                         : (mx ? (const void *)&k_adjoint_gbm_acc<float, 6, 1, ACC_MAX, 0>
+                               : (const void *)&k_adjoint_gbm_acc<float, 6, 1, ACC_MIN, 0>);
+        acc_fns[1] = f64 ? (mx ? (const void *)&k_adjoint_gbm_acc<double, 2, 1, ACC_MAX, 0>
+                               : (const void *)&k_adjoint_gbm_acc<double, 2, 1, ACC_MIN, 0>)
+                         : (mx ? (const void *)&k_adjoint_gbm_acc<float, 8, 1, ACC_MAX, 0>
+                               : (const void *)&k_adjoint_gbm_acc<float, 8, 1, ACC_MIN, 0>);
+    } else {
+        acc_fns[0] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 3> : (const void *)&k_adjoint_gbm_acc<float, 6>;
+        acc_fns[1] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 2> : (const void *)&k_adjoint_gbm_acc<float, 4>;
+    }
+    if (model == KX_MODEL_GBM && !generic_only)
+        for (const void *fn : acc_fns)
+            for (int kc : {8, 16, 32}) cands.push_back({kc, fn});
     if (total > 0) {
         const AdjArgs *ap = c.cons.as<AdjArgs>();
         const uint64_t *op = c.items.as<uint64_t>();
@@ -1129,23 +1232,34 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
         for (int i = 0; i < nc; ++i) one_seed = one_seed && args[i].seed == args[0].seed;
         if (one_seed) keys = philox_keys(args[0].seed);
         int n_ck = 0;  // checkpoint rows of the GBM kernels (set per candidate)
+        AdjSmem lay{0, 0, 0, 0};  // shared-memory records of the accumulator kernel (set per candidate)
+        for (auto &j : jobs) {
+            lay.nf = std::max(lay.nf, j.a.n_flows);
+            lay.na = std::max(lay.na, j.a.n_acc);
+        }
         void *kargs_g[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys};
         void *kargs_r[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys, (void *)&n_ck};
+        void *kargs_a[] = {&ap, &op, (void *)&nc, (void *)&total, &outp, &keys, (void *)&lay};
         auto launch = [&](const void *fn, int ck_every) {
-            // the register-resident GBM kernels keep checkpoints and flow records in shared memory
+            // the GBM kernels keep checkpoints and flow records in shared memory
             size_t smem = 0;
-            if (ck_every > 0) {
+            const bool is_acc = ck_every > 0 && (fn == acc_fns[0] || fn == acc_fns[1]);
+            if (is_acc) {
+                lay.K = ck_every;
+                lay.n_ck = max_n / ck_every + 1;
+                smem = f64 ? adj_smem_bytes<double>(lay) : adj_smem_bytes<float>(lay);
+                KX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            } else if (ck_every > 0) {
                 n_ck = max_n / ck_every + 1;
                 const size_t real = f64 ? 8 : 4;
                 smem = (size_t)ADJ_BLOCK * (ADJ_MAXF * sizeof(double) + (ADJ_MAXF + n_ck) * real);
-                if (acc) smem += (size_t)ADJ_BLOCK * ADJ_MAXF * ADJ_MAXA * (real + sizeof(int));  // fca, farg
                 KX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             }
             const int full = persistent_blocks(fn, ADJ_BLOCK, smem);
             const int blocks = (int)std::min<uint64_t>((uint64_t)full, (total + ADJ_BLOCK - 1) / ADJ_BLOCK);
             KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-            KX_CUDA(cudaLaunchKernel(fn, dim3(blocks), dim3(ADJ_BLOCK), ck_every > 0 ? kargs_r : kargs_g, smem,
-                                     c.stream));
+            KX_CUDA(cudaLaunchKernel(fn, dim3(blocks), dim3(ADJ_BLOCK), is_acc ? kargs_a : ck_every > 0 ? kargs_r : kargs_g,
+                                     smem, c.stream));
             KX_CUDA(cudaEventRecord(c.ev1, c.stream));
             KX_CUDA(cudaEventSynchronize(c.ev1));
             float ms = 0.f;
@@ -1154,25 +1268,32 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             return ms;
         };
         if (!cands.empty()) {
-            // per precision, accumulators present and barrier count (ADJ_MAXU + 1: mixed); 0: not tuned yet
-            static int tuned_k[2][2][ADJ_MAXU + 2] = {};
+            // the chosen candidate (index + 1) per precision, accumulators present and barrier
+            // count (ADJ_MAXU + 1: mixed); 0: not tuned yet (default: the first with K = 16)
+            static int tuned[2][2][ADJ_MAXU + 2] = {};
             const char *env = getenv("KX_TUNE");
             const bool tune = !(env && env[0] == '0');
-            int &tk = tuned_k[f64 ? 1 : 0][acc ? 1 : 0][same_nsu ? std::min(std::max(nsu, 0), ADJ_MAXU) : ADJ_MAXU + 1];
+            int &tk = tuned[f64 ? 1 : 0][acc ? 1 : 0][same_nsu ? std::min(std::max(nsu, 0), ADJ_MAXU) : ADJ_MAXU + 1];
             if (tune && tk == 0 && cands.size() > 1) {
                 float best = 1e30f;
-                for (auto &cd : cands) {
-                    const float ms = launch(cd.second, cd.first);  // this call's own work: every candidate computes it
-                    if (ms < best) { best = ms; tk = cd.first; }
+                const char *vb = getenv("KX_TUNE_VERBOSE");
+                for (size_t q = 0; q < cands.size(); ++q) {
+                    // this call's own work: every candidate computes it
+                    const float ms = launch(cands[q].second, cands[q].first);
+                    if (ms < best) { best = ms; tk = (int)q + 1; }
+                    if (vb && vb[0] == '1')
+                        fprintf(stderr, "[kx adjoint tune] candidate %zu (K %d): %.3f ms\n", q, cands[q].first, ms);
                 }
             }
-            kfn = cands[0].second;
-            kck = cands[0].first;
-            for (auto &cd : cands)
-                if (cd.first == (tk ? tk : 16)) {
-                    kfn = cd.second;
-                    kck = cd.first;
-                }
+            size_t pick = 0;
+            if (tk > 0 && (size_t)tk <= cands.size()) pick = (size_t)tk - 1;
+            else
+                for (size_t q = cands.size(); q-- > 0;)
+                    if (cands[q].first == 16) pick = q;
+            const char *ce = getenv("KX_ADJOINT_CANDIDATE");  // a given candidate (tests: each gives the same values)
+            if (ce && ce[0]) pick = (size_t)atoi(ce) % cands.size();
+            kfn = cands[pick].second;
+            kck = cands[pick].first;
         }
         const float ms = launch(kfn, kck);
         c.last.kernel_ms += ms;

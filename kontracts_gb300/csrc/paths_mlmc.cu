@@ -72,7 +72,7 @@ __device__ __forceinline__ void pair_event(const StaticDev &T, const double *D, 
 }
 
 template <class Real, bool HESTON>
-__global__ void __launch_bounds__(MP_BLOCK) k_mlmc_pairs(const __grid_constant__ MlmcArgs A) {
+__global__ void __launch_bounds__(MP_BLOCK, sizeof(Real) == 4 ? 4 : 2) k_mlmc_pairs(const __grid_constant__ MlmcArgs A) {
     constexpr int FM = HESTON ? M_HESTON : M_GBM;            // fine steps
     constexpr int CM = HESTON ? M_HESTON_PAIR : M_GBM_PAIR;  // coarse steps
     constexpr int SPF = lean_spb<FM>();                      // fine steps per Philox block

@@ -215,18 +215,32 @@ ACC_CASES = {
 }
 
 
+ACC_CASES.update({
+    "european": lambda: kx.european_call("X", 100.0, 1.0),
+    "up_and_out": lambda: kx.up_and_out_call("X", 100.0, 140.0, 1.0),
+    "double_barrier_put": lambda: kx.until(kx.S("X") >= 130.0,
+                                           kx.until(kx.S("X") <= 80.0, kx.european_put("X", 100.0, 1.0))),
+})
+
+
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 @pytest.mark.parametrize("name", sorted(ACC_CASES))
-def test_accumulator_adjoint_kernel_equals_generic_kernel(monkeypatch, prec, name):
-    """GBM contracts with averages or running extrema take the adjoint kernel
-    that keeps its accumulators in registers and its flow records in shared
-    memory; it performs the generic kernel's operations in the same order, so
-    every output equals the generic kernel's (KX_ADJOINT_KERNEL=general) bit
-    for bit."""
+def test_gbm_adjoint_kernels_equal_generic_kernel(monkeypatch, prec, name):
+    """The GBM adjoint kernels (the register-resident barrier kernel and the
+    kernel that keeps accumulators in registers and its records in shared
+    memory, tuned over checkpoint interval and register budget) perform the
+    generic kernel's operations in the same order, so every output equals the
+    generic kernel's (KX_ADJOINT_KERNEL=general) bit for bit, whichever
+    candidate the tuner keeps."""
     c, m = ACC_CASES[name](), kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
     kw = dict(n_paths=20_000, seed=9, steps_per_year=252, precision=prec)
-    a = c.adjoint(m, **kw)
+    outs = [c.adjoint(m, **kw)]
+    for q in range(10):  # every candidate (KX_ADJOINT_CANDIDATE is taken modulo their number)
+        monkeypatch.setenv("KX_ADJOINT_CANDIDATE", str(q))
+        outs.append(c.adjoint(m, **kw))
+    monkeypatch.delenv("KX_ADJOINT_CANDIDATE")
     monkeypatch.setenv("KX_ADJOINT_KERNEL", "general")
     g = c.adjoint(m, **kw)
-    for f in ("price", "d_s0", "d_sigma", "d_r", "se_s0", "se_sigma", "se_r"):
-        assert getattr(a, f) == getattr(g, f), (name, f, getattr(a, f), getattr(g, f))
+    for q, a in enumerate(outs):
+        for f in ("price", "d_s0", "d_sigma", "d_r", "se_s0", "se_sigma", "se_r"):
+            assert getattr(a, f) == getattr(g, f), (name, q, f, getattr(a, f), getattr(g, f))
