@@ -476,8 +476,8 @@ def mlmc_heston() -> dict:
     """price_mlmc_detailed (mlmc.rs:107-215) on a European call under Heston
     (s0 100, v0 0.04, kappa 1.5, theta 0.04, sigma_v 0.3, rho -0.7, r 0.05,
     T 1): 9 levels (2^0 .. 2^8 steps), 2,000 pilot paths, target standard
-    error 0.005, seed 11; per phase one fine and one coarse path launch for
-    all levels. Against the oracle (the reference's level loop restated, all
+    error 0.005, seed 11; per phase one k_mlmc_pairs launch for the fine and
+    coarse paths of all levels. Against the oracle (the reference's level loop restated, all
     host threads) on the same configuration, and against plain Monte Carlo on
     the GPU at the finest grid and the same standard error (the reference's
     mlmc_cheaper_than_standard_mc comparison)."""
@@ -654,9 +654,17 @@ def book_256(reps=5) -> dict:
            "graph_seconds": best, "path_steps_per_s": info["path_steps"] / best, "contracts_per_s": 256 / best,
            "e2e_seconds": e2e, "e2e_contracts_per_s": 256 / e2e}
     book.close()
+    # steps the price simulates (knocked-out paths stop) against the adjoint's (every step of every
+    # path twice: the forward pass and the recomputation of the reverse sweep; smoothed barriers
+    # never knock out)
+    kx.price_portfolio(cs, ms, ns, seeds, steps_per_year=252)
+    sim_price = kx.last_launch_stats()["steps_simulated"]
     # price + delta + vega: adjoint (one launch per kernel group) vs CRN bump per contract
     _, sens = kx.price_portfolio(cs, ms, ns, seeds, steps_per_year=252, greeks=True)
     t_adj = _dev_seconds(kx)
+    sim_adj = kx.last_launch_stats()["steps_simulated"]
+    out["steps_simulated"] = {"price": sim_price, "adjoint_forward_and_recompute": sim_adj}
+    out["adjoint_over_graph_time_per_simulated_step"] = (t_adj / sim_adj) / (best / sim_price)
     by_kind = {}
     for kind in sorted({c["kind"] for c in fx}):
         ix = [i for i, c in enumerate(fx) if c["kind"] == kind]

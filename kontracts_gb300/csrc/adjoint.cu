@@ -1193,7 +1193,8 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
         }
     }
     // the accumulator kernel at two register budgets (resident blocks per SM), specialised where
-    // every contract of the launch has one accumulator of one kind and no smoothed barrier
+    // every contract of the launch has one accumulator of one kind and no smoothed barrier, or
+    // none and the same number (0 or 1) of smoothed barriers
     int one_kind = -1;
     if (model == KX_MODEL_GBM) {
         one_kind = jobs[0].a.n_acc == 1 && jobs[0].a.n_su == 0 ? jobs[0].a.acc[0].kind : -1;
@@ -1201,7 +1202,16 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             if (j.a.n_acc != 1 || j.a.n_su != 0 || j.a.acc[0].kind != one_kind) one_kind = -1;
     }
     const void *acc_fns[2];
-    if (one_kind == ACC_SUM) {
+    if (!acc && same_nsu && nsu >= 0 && nsu <= 1) {  // no accumulators, 0 or 1 smoothed barriers
+        acc_fns[0] = f64 ? (nsu ? (const void *)&k_adjoint_gbm_acc<double, 3, 0, -1, 1>
+                                : (const void *)&k_adjoint_gbm_acc<double, 3, 0, -1, 0>)
+                         : (nsu ? (const void *)&k_adjoint_gbm_acc<float, 6, 0, -1, 1>
+                                : (const void *)&k_adjoint_gbm_acc<float, 6, 0, -1, 0>);
+        acc_fns[1] = f64 ? (nsu ? (const void *)&k_adjoint_gbm_acc<double, 2, 0, -1, 1>
+                                : (const void *)&k_adjoint_gbm_acc<double, 2, 0, -1, 0>)
+                         : (nsu ? (const void *)&k_adjoint_gbm_acc<float, 8, 0, -1, 1>
+                                : (const void *)&k_adjoint_gbm_acc<float, 8, 0, -1, 0>);
+    } else if (one_kind == ACC_SUM) {
         acc_fns[0] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 3, 1, ACC_SUM, 0>
                          : (const void *)&k_adjoint_gbm_acc<float, 6, 1, ACC_SUM, 0>;
         acc_fns[1] = f64 ? (const void *)&k_adjoint_gbm_acc<double, 2, 1, ACC_SUM, 0>
