@@ -36,7 +36,12 @@ struct MlmcRun {
     int32_t nt_f, nt_c;    // grid points of the fine and coarse paths (nt_c = 0: level 0, no coarse path)
     int32_t st_f, st_c;    // StaticDev of the fine and coarse jobs
     int32_t d_f, d_c;      // first discount factor of each
-    double c0f, c1f, c0c, c1c;  // step coefficients (uniform grids)
+    // step coefficients of the uniform grids (fine c0, c1, coarse c0, c1) in the launch
+    // precision: doubles, or floats in the first 16 bytes (no FP64 conversion per path)
+    union {
+        double d[4];
+        float f[4];
+    } coef;
     uint32_t stream, pad;
     uint32_t rk[20];       // Philox round keys of the run's seed
 };
@@ -91,7 +96,9 @@ __global__ void __launch_bounds__(MP_BLOCK, sizeof(Real) == 4 ? 4 : 2) k_mlmc_pa
         uint32_t rk[20];
 #pragma unroll
         for (int i = 0; i < 20; ++i) rk[i] = U.rk[i];
-        const Real c0f = (Real)U.c0f, c1f = (Real)U.c1f, c0c = (Real)U.c0c, c1c = (Real)U.c1c;
+        constexpr bool F32 = sizeof(Real) == 4;
+        const Real c0f = F32 ? (Real)U.coef.f[0] : (Real)U.coef.d[0], c1f = F32 ? (Real)U.coef.f[1] : (Real)U.coef.d[1];
+        const Real c0c = F32 ? (Real)U.coef.f[2] : (Real)U.coef.d[2], c1c = F32 ? (Real)U.coef.f[3] : (Real)U.coef.d[3];
         const StaticDev &Tf = A.statics[U.st_f];
         const StaticDev &Tc = A.statics[U.nt_c > 0 ? U.st_c : U.st_f];
         const double *Df = A.disc + U.d_f;
@@ -156,6 +163,7 @@ bool mlmc_pairs_run(Ctx &c, std::vector<Job> &fine, std::vector<Job> &coarse, co
     };
     MlmcArgs A;
     memset(&A, 0, sizeof A);
+    const bool f64 = cfg.precision == KX_PREC_FP64;
     std::vector<double> disc;
     size_t qc = 0;
     std::vector<uint64_t> off_f(fine.size()), off_c(fine.size());
@@ -180,8 +188,7 @@ bool mlmc_pairs_run(Ctx &c, std::vector<Job> &fine, std::vector<Job> &coarse, co
         if ((U.st_f = add(jf)) < 0) return false;
         U.d_f = (int32_t)disc.size();
         disc.insert(disc.end(), jf.tab.disc.begin(), jf.tab.disc.end());
-        U.c0f = jf.dev.uc0;
-        U.c1f = jf.dev.uc1;
+        double cf[4] = {jf.dev.uc0, jf.dev.uc1, 0.0, 0.0};
         U.stream = jf.dev.stream;
         const PhiloxKeys K = philox_keys(jf.dev.seed);
         memcpy(U.rk, K.rk, sizeof U.rk);
@@ -193,8 +200,12 @@ bool mlmc_pairs_run(Ctx &c, std::vector<Job> &fine, std::vector<Job> &coarse, co
             if ((U.st_c = add(*jc)) < 0) return false;
             U.d_c = (int32_t)disc.size();
             disc.insert(disc.end(), jc->tab.disc.begin(), jc->tab.disc.end());
-            U.c0c = jc->dev.uc0;
-            U.c1c = jc->dev.uc1;
+            cf[2] = jc->dev.uc0;
+            cf[3] = jc->dev.uc1;
+        }
+        for (int i = 0; i < 4; ++i) {
+            if (f64) U.coef.d[i] = cf[i];
+            else U.coef.f[i] = (float)cf[i];
         }
     }
     if (qc != coarse.size()) return false;
@@ -252,7 +263,6 @@ bool mlmc_pairs_run(Ctx &c, std::vector<Job> &fine, std::vector<Job> &coarse, co
     B.disc = c.disc.as<double>();
     B.out = c.mlmc.as<double>();
     B.steps_done = c.counters.as<unsigned long long>();
-    const bool f64 = cfg.precision == KX_PREC_FP64;
     const void *kfn = f64 ? (B.heston ? (const void *)&k_mlmc_pairs<double, true> : (const void *)&k_mlmc_pairs<double, false>)
                           : (B.heston ? (const void *)&k_mlmc_pairs<float, true> : (const void *)&k_mlmc_pairs<float, false>);
     const int full = persistent_blocks(kfn, MP_BLOCK, 0);
