@@ -526,6 +526,7 @@ bool build_static(const Job &j, StaticDev &T) {
         T.f_fast[q] = F.kind == AK_CONST || !simple ? (uint8_t)FA_NONE : F.fast;
         T.f_k[q] = F.kind == AK_CONST || !simple ? 0.0 : P.cpool[F.fast_k];
         T.f_sign[q] = F.sign;
+        if (F.sign < 0.0) T.f_neg |= 1u << q;
         if (F.kind != AK_CONST && !simple) T.gen_flows |= 1u << q;
     }
     if (P.n_acc) {

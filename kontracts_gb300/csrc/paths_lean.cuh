@@ -163,6 +163,7 @@ struct StaticDev {
     uint8_t f_fast[KX_MAX_LEAF];  // KxFastAmount of the flow slot (FA_NONE: constant amount)
     double f_k[KX_MAX_LEAF];      // its constant K
     double f_sign[KX_MAX_LEAF];   // its sign (the constant amount itself for FA_NONE)
+    uint32_t f_neg;               // flow slots whose sign is negative (tested without FP64)
     // Smoothed barriers (a bump of the smoothed payoff): until(Spot cmp Const)
     // slots that never knock; from their arming step on, every step multiplies
     // the slot's weight by smooth_weight(x), x = (y - thr) * mul (mul = +-1/w,
@@ -295,7 +296,7 @@ __device__ __forceinline__ void static_event(const StaticDev &T, const double *D
                     case FA_SPOT: r = S; break;
                     default: r = K; break;
                     }
-                    amt = (double)(T.f_sign[j] < 0.0 ? -r : r);
+                    amt = (double)(((T.f_neg >> j) & 1u) ? -r : r);
                 }
                 if (SM) {  // the weights of the smoothed barriers above the flow, in slot order
                     if (T.n_sm > 0 && ((T.sm_flows[0] >> j) & 1u) && k >= T.sm_arm[0]) amt *= (double)w0;

@@ -66,7 +66,8 @@ struct MultiLeanArgs {
     uint8_t kill[ML_MAXB];               // flows dropped when the barrier knocks
     uint8_t b_cmp[ML_MAXB];              // KxCmp of "form cmp 0"
     uint8_t f_form[ML_MAXF];
-    uint8_t pad[4];
+    uint8_t f_neg;                       // flows whose sign is negative
+    uint8_t pad[3];
     double b_c[ML_MAXB][KX_MAX_NS + 1];  // [0] constant, [1 + i] coefficient of S_i
     float b_cf[ML_MAXB][KX_MAX_NS + 1];
     double f_c[ML_MAXF][KX_MAX_NS + 1];
@@ -130,7 +131,7 @@ __device__ __forceinline__ void multi_event(const MultiLeanArgs &A, const Real (
                     const Real K = pick<Real>(A.f_k[f], A.f_kf[f]);
                     if (A.f_form[f] == MF_MAX) v = fmax(v, K);
                     else if (A.f_form[f] == MF_MIN) v = fmin(v, K);
-                    amt = (double)(A.f_sign[f] < 0.0 ? -v : v);
+                    amt = (double)(((A.f_neg >> f) & 1u) ? -v : v);
                 }
                 pv = __dadd_rn(pv, __dmul_rn(amt, D));
             }
@@ -445,6 +446,7 @@ static bool multi_lean_args(const Job &j, MultiLeanArgs &A) {
             return false;
         }
         A.f_sign[f] = neg ? -1.0 : 1.0;
+        if (neg) A.f_neg |= (uint8_t)(1u << f);
         put_row(fm, na, A.f_c[f], A.f_cf[f]);
     }
     // barriers: untils on prices that are armed and drop some flow
