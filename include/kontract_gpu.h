@@ -351,9 +351,12 @@ typedef struct kx_multi_gbm {
 /* price_gbm (src/pricer.rs:97) under a CorrelatedGbmN: every Spot(name) of the
  * contract reads its factor; each grid step draws n_assets normals, correlates
  * them with the lower Cholesky factor (numerics.rs:158-183) and steps every
- * factor exactly in log space (multi_asset.rs:85-170). The general path kernel
- * (M_MULTI). Fewer than 2 factors or a negative volatility is
- * KX_MALFORMED_CONTRACT, a spot of no factor KX_UNKNOWN_ASSET. */
+ * factor exactly in log space (multi_asset.rs:85-170). Contracts whose price
+ * conditions and amounts are affine in the spots (baskets, spreads) on a
+ * time-only schedule run on the compiled kernel (path_kernel 5; Philox only),
+ * the others on the general path kernel (M_MULTI). Fewer than 2 factors or a
+ * negative volatility is KX_MALFORMED_CONTRACT, a spot of no factor
+ * KX_UNKNOWN_ASSET. */
 kx_status kx_price_multi(const kx_program *prog, const kx_multi_gbm *model, const kx_mc_config *cfg,
                          kx_price_result *out, double *per_path_pv);
 

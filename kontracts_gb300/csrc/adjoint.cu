@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;  // > 0 beyond the barrier
-                    surv[u] *= smooth_weight(x);
+                    if (x > smooth_cut<Real>()) surv[u] *= logistic(x);  // weight 1 below the cut
                     const bool hit = pp.sgn[u] * y >= pp.hit[u];
                     if (hit && knock[u] == INT_MAX) knock[u] = k;
                 }
@@ -418,9 +418,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_adjoint(const AdjArgs *__restrict
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real s = smooth_weight(x);
-                        const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy| (0 where s is exactly 1)
-                        g -= Q[u] * pp.sgn[u] * dls;
+                        if (x > smooth_cut<Real>()) {  // below the cut the weight is 1: no term
+                            const Real s = logistic(x);
+                            const Real dls = (Real(1) - s) * inv_w;  // |d log s / dy|
+                            g -= Q[u] * pp.sgn[u] * dls;
+                        }
                     }
                 // leaving an average window when walking below its first step
                 if (ACC)
@@ -610,7 +612,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, MINB) k_adjoint_gbm(const AdjArgs *
             for (int u = 0; u < nsu; ++u)
                 if (k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
-                    surv[u] *= smooth_weight(x);
+                    if (x > smooth_cut<Real>()) surv[u] *= logistic(x);  // weight 1 below the cut
                     if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
                 }
             if (k != nft) continue;
@@ -706,9 +708,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK, MINB) k_adjoint_gbm(const AdjArgs *
                 for (int u = 0; u < nsu; ++u)
                     if (k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real sv = smooth_weight(x);
-                        const Real dls = (Real(1) - sv) * inv_w;
-                        g -= Q[u] * pp.sgn[u] * dls;
+                        if (x > smooth_cut<Real>()) {  // below the cut the weight is 1: no term
+                            const Real sv = logistic(x);
+                            const Real dls = (Real(1) - sv) * inv_w;
+                            g -= Q[u] * pp.sgn[u] * dls;
+                        }
                     }
                 lam += g;
             }
@@ -843,7 +847,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, MINB)
             for (int u = 0; u < ADJ_MAXU; ++u)
                 if (u < nsu && k >= su_arm[u]) {
                     const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
-                    surv[u] *= smooth_weight(x);
+                    if (x > smooth_cut<Real>()) surv[u] *= logistic(x);  // weight 1 below the cut
                     if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
                 }
             if (k != nft) continue;
@@ -999,9 +1003,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK, MINB)
                 for (int u = 0; u < ADJ_MAXU; ++u)
                     if (u < nsu && k >= su_arm[u] && Q[u] != Real(0)) {
                         const Real x = pp.sgn[u] * (yk - pp.thr[u]) * inv_w;
-                        const Real sv = smooth_weight(x);
-                        const Real dls = (Real(1) - sv) * inv_w;
-                        g -= Q[u] * pp.sgn[u] * dls;
+                        if (x > smooth_cut<Real>()) {  // below the cut the weight is 1: no term
+                            const Real sv = logistic(x);
+                            const Real dls = (Real(1) - sv) * inv_w;
+                            g -= Q[u] * pp.sgn[u] * dls;
+                        }
                     }
 #pragma unroll
                 for (int a = 0; a < ADJ_MAXA; ++a)
