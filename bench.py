@@ -828,10 +828,10 @@ def run_ours(args, ws, rank, local) -> None:
     achieved = sim_steps / (ker_ms * 1e-3) / 1e9
     peak = peaks.get("bare_path_steps", float("nan")) / 1e9
     # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum of the path kernel
-    # on the 1M-path case (profiles/k_lean_static_up_and_out.md: 19,968 + 0 bytes), scaled by the
+    # on the 1M-path case (profiles/k_lean_static_up_and_out.md: 23,296 + 0 bytes), scaled by the
     # number of paths; the per-path values (8 B/path) stay in L2 during the launch.
     rank_paths = rank_steps // max(1, steps_per_path * args.steps)  # paths of one launch on this rank
-    traffic = 19968.0 / 1_000_000 * rank_paths
+    traffic = 23296.0 / 1_000_000 * rank_paths
     kname = {1: "k_paths<float,GBM>", 2: "k_lean<float,GBM>", 3: "k_lean<float,GBM,static schedule>"}.get(
         kx.last_launch_stats()["path_kernel"], "?")
     roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gsteps/s",
@@ -843,6 +843,19 @@ def run_ours(args, ws, rank, local) -> None:
                 "steps_simulated_fraction": sim_steps / max(1, rank_steps),
                 "mufu_results_per_s_share": 2.0 * sim_steps / (ker_ms * 1e-3) / peaks.get("mufu", float("nan")),
                 "measured_peaks_per_s": dict(peaks)}
+    # the per-pipe form of the same roofline: frozen algorithmic ops per simulated step (2 MUFU
+    # results, 5 32x32 high multiplies of Philox, 7 FP32 operations) over each pipe's peak measured
+    # in this run; the binding pipe's share is the fraction
+    rate = sim_steps / (ker_ms * 1e-3)
+    shares = {"xu": 2.0 * rate / peaks.get("mufu", float("nan")),
+              "imad_hi": 5.0 * rate / peaks.get("imad_hi", float("nan")),
+              "fp32": 7.0 * rate / peaks.get("fp32_fma", float("nan"))}
+    roofline["pipe_shares"] = shares
+    roofline["pipe_bound"] = max(shares, key=lambda k: shares[k] if shares[k] == shares[k] else -1.0)
+    roofline["bare_loop_pipe_shares"] = {
+        "xu": 2.0 * peaks.get("bare_path_steps", float("nan")) / peaks.get("mufu", float("nan")),
+        "imad_hi": 5.0 * peaks.get("bare_path_steps", float("nan")) / peaks.get("imad_hi", float("nan")),
+        "fp32": 7.0 * peaks.get("bare_path_steps", float("nan")) / peaks.get("fp32_fma", float("nan"))}
     greeks = None if args.no_greeks else price_greeks(c, m, n_paths, seed, w["steps_per_year"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

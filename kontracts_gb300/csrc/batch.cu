@@ -50,10 +50,6 @@ struct FlowArgs {
     const float *z32;
     uint64_t z_dpp;
     double *pv;            // [n_contracts][n_paths], zeroed before the launch
-    PhiloxKeys keys;       // the seed's round keys (constant-bank operands of every draw)
-    int uniform;           // every step k >= 1 has the coefficients (uc0, uc1)
-    double uc0, uc1;
-    float uc0f, uc1f;
 };
 
 template <class Real>
@@ -100,8 +96,8 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
             const uint64_t d = (uint64_t)(k - 1) * DRAWS;
             Real z[4];
             if (A.z64 == nullptr && A.z32 == nullptr) {
-                const uint4 w =
-                    philox4x32_10_rk(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u), A.keys.rk);
+                const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
+                                              (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
                 box_muller(w.x, w.y, z[0], z[1]);
                 box_muller(w.z, w.w, z[2], z[3]);
             } else {
@@ -114,14 +110,9 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
             for (int j = 0; j < SPB; ++j) {
                 const int kk = k + j;
                 if (kk >= A.n_times) break;
-                Real c0 = pick<Real>(A.uc0, A.uc0f), c1 = pick<Real>(A.uc1, A.uc1f);
-                if (!A.uniform) {
-                    const StepRec<Real> rec = R[kk];
-                    c0 = rec.c0;
-                    c1 = rec.c1;
-                }
-                if (MODEL == KX_MODEL_GBM) y = gbm_step(y, c0, c1, z[j]);
-                else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, c0, c1, z[2 * j], z[2 * j + 1], y, v);
+                const StepRec<Real> rec = R[kk];
+                if (MODEL == KX_MODEL_GBM) y = gbm_step(y, rec.c0, rec.c1, z[j]);
+                else heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, rec.c0, rec.c1, z[2 * j], z[2 * j + 1], y, v);
                 if (kk == nf) {
                     pay_flows<Real>(A, kk, spot_of<Real>(s0, y), path);
                     nf = A.next[kk + 1];
@@ -293,19 +284,6 @@ extern "C" kx_status kx_price_batch_shared(size_t n, const kx_program *const *pr
                 a.z_dpp = ds.dpp;
             }
             a.pv = c.pv.as<double>();
-            a.keys = philox_keys(cfg->seed);
-            // uniform grid: every step's coefficients equal in the launch precision
-            const StepTables &t0 = tabs[stat[0]];
-            a.uniform = nt > 1 ? 1 : 0;
-            for (int k = 2; k < nt && a.uniform; ++k)
-                a.uniform = f64 ? (t0.c0[k] == t0.c0[1] && t0.c1[k] == t0.c1[1])
-                                : ((float)t0.c0[k] == (float)t0.c0[1] && (float)t0.c1[k] == (float)t0.c1[1]);
-            if (nt > 1) {
-                a.uc0 = t0.c0[1];
-                a.uc1 = t0.c1[1];
-                a.uc0f = (float)a.uc0;
-                a.uc1f = (float)a.uc1;
-            }
             const void *kfn = m.kind == KX_MODEL_GBM ? (f64 ? flows_kernel<double, KX_MODEL_GBM>() : flows_kernel<float, KX_MODEL_GBM>())
                                                      : (f64 ? flows_kernel<double, KX_MODEL_HESTON>() : flows_kernel<float, KX_MODEL_HESTON>());
             if (np > 0) {
