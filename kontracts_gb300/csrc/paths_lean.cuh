@@ -503,6 +503,18 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     uint32_t sml = 0u;        // lane: the smoothed barriers whose weight is not yet 0
     bool evp = false;  // this lane waits with an event at step k
     int wait = 0;      // warp-uniform: blocks since the last handler round
+    // static schedules: every path of a contract is at S = s0 at t = 0, so its state after
+    // step 0 (barriers armed and tested, flows of t = 0 paid, the window, the next event) is
+    // the same for all of them: computed once per contract and warp, copied at each hand-out
+    struct Start0 {
+        SLane sl;
+        Real hi, lo, av, ac, w0, w1;
+        int lim;
+        uint32_t sml;
+        int done;
+    };
+    __shared__ Start0 start0[KX_BLOCK / 32];
+    Start0 &T0 = start0[threadIdx.x >> 5];
     // a new path on this lane: S = s0, step 0 next
     auto start_path = [&](uint32_t p) {
         path = p;
@@ -594,6 +606,22 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         acc_k = T.acc_kind;
                     }
                     if (SM) sp = smooth_par<Real>(static_cast<const StaticDev *>(A.statics)[cur]);
+                    if (STATIC) {  // every lane is idle here: the warp computes the contract's step 0
+                        const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
+                        SLane t{0u, T.all_flows, 0, 0.0};
+                        Real tav = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
+                        Real tac = Real(0), tw0 = Real(1), tw1 = Real(1);
+                        uint32_t tsml = SM ? (1u << sp.n) - 1u : 0u;
+                        if (ACC && acc_f <= 0 && 0 <= acc_t) acc_add<Real>(acc_k, tav, tac, spot_of<Real>(s0, Real(0)));
+                        if (SM) smooth_step<Real>(sp, Real(0), 0, tsml, tw0, tw1);
+                        static_event<Real, ACC, SM>(T, D, s0, Real(0), 0, t, P, tav, tac, tw0, tw1, &tsml);
+                        Real thi, tlo;
+                        static_window<Real>(T, t.live, thi, tlo);
+                        const int tlim = t.e < T.n_ev ? min(T.ev_step[t.e], nt - 1) : nt - 1;
+                        if (lane == 0)
+                            T0 = Start0{t, thi, tlo, tav, tac, tw0, tw1, tlim, tsml, (t.rem == 0u || nt <= 1) ? 1 : 0};
+                        __syncwarp();
+                    }
                 }
                 pend = -1;
                 nx = (uint32_t)w.first;
@@ -605,10 +633,33 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
             const int take = avail < (uint32_t)nidle ? (int)avail : nidle;
             const int rank = __popc(idle & lt);
             if (!busy && rank < take) {
-                // new path: the contract at step 0 runs as this lane's first event (at once
-                // for static schedules; a path that ends at step 0 leaves the lane idle)
-                start_path(nx + (uint32_t)rank);
-                if (STATIC) static_lane_event();
+                // new path: the contract at step 0 runs as this lane's first event (for static
+                // schedules its outcome is the contract's Start0; a path that ends at step 0
+                // leaves the lane idle)
+                if (STATIC) {
+                    path = nx + (uint32_t)rank;
+                    busy = true;
+                    y = Real(0);
+                    v = fmax(hv0, Real(0));
+                    sl = T0.sl;
+                    hi = T0.hi;
+                    lo = T0.lo;
+                    lim = T0.lim;
+                    av = T0.av;
+                    ac = T0.ac;
+                    if (SM) {
+                        sw0 = T0.w0;
+                        sw1 = T0.w1;
+                        sml = T0.sml;
+                    }
+                    k = 1;
+                    if (T0.done) {
+                        A.pv[pv_off + path] = sl.pv;
+                        busy = false;
+                    }
+                } else {
+                    start_path(nx + (uint32_t)rank);
+                }
             }
             nx += (uint32_t)take;
             if (take == 0) break;
