@@ -665,11 +665,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK, MINB) k_adjoint_gbm(const AdjArgs *
 #pragma unroll
                 for (int j = 0; j < 4; ++j) sz[1 + 4 * q + j] = w4[j];
             }
+            if (uni) {  // one branch per segment, none per step
 #pragma unroll
-            for (int j = 1; j <= K; ++j) {
-                if (uni) {
-                    sy[j] = gbm_step(sy[j - 1], ua, ub, sz[j]);
-                } else {
+                for (int j = 1; j <= K; ++j) sy[j] = gbm_step(sy[j - 1], ua, ub, sz[j]);
+            } else {
+#pragma unroll
+                for (int j = 1; j <= K; ++j) {
                     const StepRec<Real> rec = R[min(k0 + j, N)];  // past N: harmless states never read
                     sy[j] = gbm_step(sy[j - 1], mul_rn(pp.drift, rec.c0), mul_rn(pp.sigma, rec.c1), sz[j]);
                 }
