@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
     // static schedules: every path of a contract is at S = s0 at t = 0, so its state after
     // step 0 (barriers armed and tested, flows of t = 0 paid, the window, the next event) is
     // the same for all of them: computed once per contract and warp, copied at each hand-out
+    // (not in the accumulator and smoothed families, whose registers the copy would strain)
     struct Start0 {
         SLane sl;
         Real hi, lo, av, ac, w0, w1;
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
                         acc_k = T.acc_kind;
                     }
                     if (SM) sp = smooth_par<Real>(static_cast<const StaticDev *>(A.statics)[cur]);
-                    if (STATIC) {  // every lane is idle here: the warp computes the contract's step 0
+                    if (STATIC && !ACC && !SM) {  // every lane is idle here: the warp computes the contract's step 0
                         const StaticDev &T = static_cast<const StaticDev *>(A.statics)[cur];
                         SLane t{0u, T.all_flows, 0, 0.0};
                         Real tav = acc_k == ACC_MAX ? Real(-INFINITY) : acc_k == ACC_MIN ? Real(INFINITY) : Real(0);
@@ -634,9 +635,13 @@ __global__ void __launch_bounds__(KX_BLOCK, MINB) k_lean(const PathArgs A) {
             const int rank = __popc(idle & lt);
             if (!busy && rank < take) {
                 // new path: the contract at step 0 runs as this lane's first event (for static
-                // schedules its outcome is the contract's Start0; a path that ends at step 0
+                // schedules its outcome is the contract's Start0, copied; the accumulator and
+                // smoothed families, tighter on registers, run it; a path that ends at step 0
                 // leaves the lane idle)
-                if (STATIC) {
+                if (STATIC && (ACC || SM)) {
+                    start_path(nx + (uint32_t)rank);
+                    static_lane_event();
+                } else if (STATIC) {
                     path = nx + (uint32_t)rank;
                     busy = true;
                     y = Real(0);
