@@ -101,24 +101,24 @@ __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ 
                                                      ChunkOut *__restrict__ out) {
     __shared__ double red[32];
     const ChunkDesc c = ch[blockIdx.x];
-    double ww[8];
+    double mean = 0.0, m2 = 0.0;
+    const double *v = vals + c.begin;
+    if (ns == 1 && w[0] == 1.0) {  // a plain price: the value itself
+        chunk_moments([&](uint32_t i) { return v[i]; }, c.count, red, mean, m2);
+    } else if (ns == 2 && w[0] == 1.0 && w[1] == -1.0) {  // a difference (multilevel pairs)
+        chunk_moments([&](uint32_t i) { return v[i] - v[stride + i]; }, c.count, red, mean, m2);
+    } else {  // weighted scenarios (Greek estimators, variance-reduction corrections)
+        double ww[8];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
-    auto val = [&](uint64_t i) {
-        double x = 0.0;
-        for (int s = 0; s < ns; ++s) x += ww[s] * vals[(uint64_t)s * stride + c.begin + i];
-        return x;
-    };
-    double a = 0.0;
-    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) a += val(i);
-    const double sum = block_sum(a, red);
-    const double mean = sum / (double)c.count;
-    double b = 0.0;
-    for (uint32_t i = threadIdx.x; i < c.count; i += blockDim.x) {
-        const double d = val(i) - mean;
-        b += d * d;
+        for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
+        chunk_moments(
+            [&](uint32_t i) {
+                double x = ww[0] * v[i];
+                for (int s = 1; s < ns; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
+                return x;
+            },
+            c.count, red, mean, m2);
     }
-    const double m2 = block_sum(b, red);
     if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
 }
 

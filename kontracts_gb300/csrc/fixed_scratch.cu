@@ -86,24 +86,17 @@ static unsigned char *scratch(Ctx &c) {
     return g_scratch_ptr;
 }
 
-// The chunk statistics of k_chunk_stats for one scenario with unit weight,
-// the chunk bounds taken from the block index instead of a descriptor table.
+// The chunk statistics of k_chunk_stats for one scenario with unit weight
+// (chunk_moments), the chunk bounds taken from the block index instead of a
+// descriptor table.
 __global__ void __launch_bounds__(256) k_fixed_stats(const double *__restrict__ vals, uint64_t n,
                                                      ChunkOut *__restrict__ out) {
     __shared__ double red[32];
     const uint64_t begin = (uint64_t)blockIdx.x * KX_STATS_CHUNK;
     const uint32_t count = (uint32_t)std::min<uint64_t>(KX_STATS_CHUNK, n - begin);
-    auto val = [&](uint64_t i) { return 0.0 + 1.0 * vals[begin + i]; };  // weight 1, as k_chunk_stats
-    double a = 0.0;
-    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) a += val(i);
-    const double sum = block_sum(a, red);
-    const double mean = sum / (double)count;
-    double b = 0.0;
-    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
-        const double d = val(i) - mean;
-        b += d * d;
-    }
-    const double m2 = block_sum(b, red);
+    const double *v = vals + begin;
+    double mean = 0.0, m2 = 0.0;
+    chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);  // as k_chunk_stats, one scenario
     if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)count, mean, m2};
 }
 

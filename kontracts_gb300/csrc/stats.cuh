@@ -41,4 +41,40 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
     return t;
 }
 
+// The two passes over one chunk: its mean, then the sum of squared deviations
+// from it (pricer.rs:303-328 also takes two passes). GB300's FP64 units are
+// few and the values are FP64, so the loops spend one FP64 operation per
+// value in the first pass and two in the second, and every thread keeps four
+// accumulators (values i, i + B, i + 2B, i + 3B of its stride, B the block
+// size) so that their adds overlap; the order of every sum is fixed.
+template <class Val>
+__device__ __forceinline__ void chunk_moments(const Val &val, uint32_t count, double *red, double &mean, double &m2) {
+    const uint32_t B = blockDim.x;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    uint32_t i = threadIdx.x;
+    for (; i + 3 * B < count; i += 4 * B) {
+        a0 += val(i);
+        a1 += val(i + B);
+        a2 += val(i + 2 * B);
+        a3 += val(i + 3 * B);
+    }
+    for (; i < count; i += B) a0 += val(i);
+    mean = block_sum((a0 + a1) + (a2 + a3), red) / (double)count;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0;
+    i = threadIdx.x;
+    for (; i + 3 * B < count; i += 4 * B) {
+        const double d0 = val(i) - mean, d1 = val(i + B) - mean, d2 = val(i + 2 * B) - mean,
+                     d3 = val(i + 3 * B) - mean;
+        b0 = fma(d0, d0, b0);
+        b1 = fma(d1, d1, b1);
+        b2 = fma(d2, d2, b2);
+        b3 = fma(d3, d3, b3);
+    }
+    for (; i < count; i += B) {
+        const double d = val(i) - mean;
+        b0 = fma(d, d, b0);
+    }
+    m2 = block_sum((b0 + b1) + (b2 + b3), red);
+}
+
 }  // namespace kx
