@@ -52,6 +52,17 @@ void DevBuf::ensure(size_t bytes) {
     cap = want;
 }
 
+void PinnedBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) cudaFreeHost(p);  // the previous call's copies completed before it returned
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, 4096);
+    want = std::max(want, cap * 2);
+    KX_CUDA(cudaHostAlloc(&p, want, cudaHostAllocDefault));
+    cap = want;
+}
+
 Ctx &ctx() {
     static Ctx c;
     static std::mutex setup_mu;
@@ -187,15 +198,21 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
     first[jobs.size()] = chunks.size();
     std::vector<Stats> res(jobs.size());
     if (chunks.empty()) return res;
-    // jobs with different weights run as separate launches
-    c.chunks.ensure(chunks.size() * sizeof(ChunkDesc));
-    c.chunk_out.ensure(chunks.size() * sizeof(ChunkOut));
-    c.weights.ensure(jobs.size() * 8 * sizeof(double));
-    std::vector<double> wts(jobs.size() * 8);
+    // jobs with different weights run as separate launches; the chunk table and the weights go
+    // up in one copy from pinned memory, the chunks' statistics come back the same way
+    const size_t b_chunks = chunks.size() * sizeof(ChunkDesc), b_w = jobs.size() * 8 * sizeof(double);
+    const size_t b_out = chunks.size() * sizeof(ChunkOut);
+    c.stats_in.ensure(b_chunks + b_w);
+    c.chunk_out.ensure(b_out);
+    c.stats_stage.ensure(std::max(b_chunks + b_w, b_out));
+    unsigned char *stage = c.stats_stage.as<unsigned char>();
+    memcpy(stage, chunks.data(), b_chunks);
+    double *wts = reinterpret_cast<double *>(stage + b_chunks);
     for (size_t j = 0; j < jobs.size(); ++j)
         for (int s = 0; s < 8; ++s) wts[j * 8 + s] = jobs[j].w[s];
-    KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice, c.stream));
-    KX_CUDA(cudaMemcpyAsync(c.weights.p, wts.data(), wts.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.stats_in.p, stage, b_chunks + b_w, cudaMemcpyHostToDevice, c.stream));
+    const ChunkDesc *d_chunks = c.stats_in.as<ChunkDesc>();
+    const double *d_w = reinterpret_cast<const double *>(c.stats_in.as<unsigned char>() + b_chunks);
     KX_CUDA(cudaEventRecord(c.ev0, c.stream));
     // one launch per run of consecutive jobs with the same weights
     for (size_t j = 0; j < jobs.size();) {
@@ -204,13 +221,13 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
         const size_t nc = first[e] - first[j];
         const bool plain = jobs[j].ns == 1 && jobs[j].w[0] == 1.0;
         if (nc && c.kahan_stats && plain) {  // KX_PREC_FP32_KAHAN: compensated FP32 sums
-            k_chunk_stats_kahan<<<(unsigned)nc, 256, 0, c.stream>>>(values, c.chunks.as<ChunkDesc>() + first[j],
+            k_chunk_stats_kahan<<<(unsigned)nc, 256, 0, c.stream>>>(values, d_chunks + first[j],
                                                                     c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         } else if (nc) {
-            k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, c.weights.as<double>() + j * 8,
-                                                              c.chunks.as<ChunkDesc>() + first[j],
+            k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, d_w + j * 8,
+                                                              d_chunks + first[j],
                                                               c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
@@ -218,14 +235,14 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
         j = e;
     }
     KX_CUDA(cudaEventRecord(c.ev1, c.stream));
-    std::vector<ChunkOut> h(chunks.size());
-    KX_CUDA(cudaMemcpyAsync(h.data(), c.chunk_out.p, h.size() * sizeof(ChunkOut), cudaMemcpyDeviceToHost, c.stream));
+    const ChunkOut *h = c.stats_stage.as<ChunkOut>();  // the staged uploads were consumed in stream order
+    KX_CUDA(cudaMemcpyAsync(c.stats_stage.p, c.chunk_out.p, b_out, cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));
     float rms = 0.f;
     KX_CUDA(cudaEventElapsedTime(&rms, c.ev0, c.ev1));
     c.last.reduce_ms += rms;
-    c.last.d2h_bytes += h.size() * sizeof(ChunkOut);
-    for (size_t j = 0; j < jobs.size(); ++j) res[j] = merge_chunks(h.data() + first[j], first[j + 1] - first[j]);
+    c.last.d2h_bytes += b_out;
+    for (size_t j = 0; j < jobs.size(); ++j) res[j] = merge_chunks(h + first[j], first[j + 1] - first[j]);
     return res;
 }
 
@@ -798,20 +815,31 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.last.path_steps += P.path_steps;
     stride_out = P.total;
     if (P.n_items == 0) return P.total;
-    c.progs.ensure(P.progs.size() * sizeof(KxProgram));
-    c.steps.ensure(P.steps.size());
-    c.disc.ensure(P.disc.size() * sizeof(double));
-    c.cons.ensure(P.cons.size() * sizeof(ContractDev));
-    c.thr.ensure(P.thr.size());
-    c.items.ensure(P.item_idx.size() * sizeof(uint32_t));
-    c.counters.ensure(64);
+    // the plan's tables and the zeroed counters in one device region, staged in pinned memory
+    // and uploaded by one copy (each table 256-byte aligned)
+    const size_t sz[8] = {P.progs.size() * sizeof(KxProgram), P.steps.size(), P.disc.size() * sizeof(double),
+                          P.cons.size() * sizeof(ContractDev), P.thr.size(), P.item_idx.size() * sizeof(uint32_t),
+                          P.statics.size() * sizeof(StaticDev), 64};
+    const void *src[8] = {P.progs.data(), P.steps.data(), P.disc.data(), P.cons.data(), P.thr.data(),
+                          P.item_idx.data(), P.statics.data(), nullptr};
+    size_t off[8], total = 0;
+    for (int q = 0; q < 8; ++q) {
+        off[q] = total;
+        total += (sz[q] + 255) & ~size_t(255);
+    }
+    c.plan.ensure(total);
+    c.plan_stage.ensure(total + 64);  // + the counters read back after the launch
+    unsigned char *stage = c.plan_stage.as<unsigned char>();
+    for (int q = 0; q < 8; ++q) {
+        if (src[q] && sz[q]) memcpy(stage + off[q], src[q], sz[q]);
+        else if (sz[q]) memset(stage + off[q], 0, sz[q]);
+    }
+    KX_CUDA(cudaMemcpyAsync(c.plan.p, stage, total, cudaMemcpyHostToDevice, c.stream));
     c.pv.ensure(std::max<uint64_t>(1, P.total * ns) * sizeof(double));
-    c.statics.ensure(std::max<size_t>(1, P.statics.size()) * sizeof(StaticDev));
-    const PathBuffers B{c.progs.p, c.steps.p, c.disc.p,  c.cons.p, c.thr.p, c.items.p, c.counters.as<uint32_t>(),
-                        c.pv.as<double>(), c.statics.p};
-    upload_plan(P, B, c.stream);
-    KX_CUDA(cudaMemsetAsync(c.counters.p, 0, 64, c.stream));
-    c.last.h2d_bytes += plan_upload_bytes(P);
+    unsigned char *dp = c.plan.as<unsigned char>();
+    const PathBuffers B{dp + off[0], dp + off[1], dp + off[2], dp + off[3], dp + off[4], dp + off[5],
+                        reinterpret_cast<uint32_t *>(dp + off[7]), c.pv.as<double>(), dp + off[6]};
+    c.last.h2d_bytes += total;
     PathArgs a = path_args(P, B);
     if (cfg.rng == KX_RNG_SHARED_DRAWS) {
         DrawStore &ds = c.draws;
@@ -834,8 +862,8 @@ static uint64_t run_paths_v(Ctx &c, std::vector<Job> &jobs, const kx_mc_config &
     c.last.grid_blocks = (uint32_t)P.grid_blocks;
     c.last.block_threads = (uint32_t)KX_BLOCK;
     c.last.path_kernel = P.acc ? 4u : P.stat ? 3u : lean ? 2u : 1u;
-    uint32_t hc[4] = {0, 0, 0, 0};
-    KX_CUDA(cudaMemcpyAsync(hc, c.counters.p, sizeof hc, cudaMemcpyDeviceToHost, c.stream));
+    uint32_t *hc = reinterpret_cast<uint32_t *>(stage + total);  // pinned: the counters come back by DMA
+    KX_CUDA(cudaMemcpyAsync(hc, B.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
     KX_CUDA(cudaStreamSynchronize(c.stream));
     float ms = 0.f;
     KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));

@@ -24,6 +24,16 @@ struct DevBuf {
     T *as() const { return static_cast<T *>(p); }
 };
 
+// Growable page-locked host buffer: copies from and to it are true
+// asynchronous DMA (a pageable source costs a staging copy per call).
+struct PinnedBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    void ensure(size_t bytes);
+    template <class T>
+    T *as() const { return static_cast<T *>(p); }
+};
+
 struct DrawStore {  // host normals for KX_RNG_SHARED_DRAWS
     DevBuf z64, z32;
     bool is64 = false;
@@ -41,7 +51,9 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scratch owned by the context
     DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, weights, misc, vr, lsm_paths, lsm_value,
-        lsm_stats, statics, mlmc;
+        lsm_stats, statics, mlmc, plan, stats_in;
+    // host staging of a call's uploads and downloads (path plan, statistics)
+    PinnedBuf plan_stage, stats_stage;
     DrawStore draws;
     kx_launch_stats last{};
     bool kahan_stats = false;  // this call's plain statistics in compensated FP32 (KX_PREC_FP32_KAHAN)
