@@ -1744,7 +1744,7 @@ kx_status kx_calib_gbm_prices(const kx_program *prog, const char *asset, const d
         const Program &p = program_of(prog);
         check_cfg(cfg);
         if (cfg->rng != KX_RNG_PHILOX) raise(KX_UNSUPPORTED, "calibration pricing uses Philox normals");
-        if ((n_quotes && !spots) || (n_sigmas && !sigmas) || (n_quotes * n_sigmas && !out))
+        if ((n_quotes && !spots) || (n_sigmas && !sigmas) || (n_quotes != 0 && n_sigmas != 0 && !out))
             raise(KX_INVALID_ARGUMENT, "NULL argument");
         // Gbm::new(asset, spot, rate, sigma) per quote and volatility (calibration.rs:83)
         std::vector<Model> models;
