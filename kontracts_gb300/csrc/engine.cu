@@ -54,11 +54,10 @@ void DevBuf::ensure(size_t bytes) {
 
 void PinnedBuf::ensure(size_t bytes) {
     if (bytes <= cap) return;
+    const size_t want = std::max<size_t>(std::max<size_t>(bytes, 4096), 2 * cap);  // grow geometrically
     if (p) cudaFreeHost(p);  // the previous call's copies completed before it returned
     p = nullptr;
     cap = 0;
-    size_t want = std::max<size_t>(bytes, 4096);
-    want = std::max(want, cap * 2);
     KX_CUDA(cudaHostAlloc(&p, want, cudaHostAllocDefault));
     cap = want;
 }
