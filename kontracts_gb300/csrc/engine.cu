@@ -604,9 +604,11 @@ const int *variants(int model, bool f64, int ns, bool lean, int &n) {
     }
     static const int v1[] = {4, 3, 2};
     static const int l32[] = {4, 5, 6};
+    static const int lg32[] = {4, 5, 6, 3};  // GBM: 3 blocks per SM keeps the accumulator family unspilled
     static const int lg64[] = {4, 3};
     static const int lh64[] = {3};
     if (lean) {
+        if (!f64 && model == KX_MODEL_GBM) { n = 4; return lg32; }
         if (!f64) { n = 3; return l32; }
         if (model == KX_MODEL_GBM) { n = 2; return lg64; }
         n = 1;

@@ -13,6 +13,9 @@ template __global__ void k_lean<float, M_GBM, 6, true, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, false>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, true, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 3, false>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 3, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 3, true, true>(const PathArgs);  // the accumulator family: no spills at 80
 template __global__ void k_lean<float, M_GBM, 4, false>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 4, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 4, true, true>(const PathArgs);
@@ -24,6 +27,7 @@ template __global__ void k_lean<double, M_GBM, 3, true>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 3, true, true>(const PathArgs);
 // smoothed barriers (bumps of the smoothed payoff)
 template __global__ void k_lean<float, M_GBM, 6, true, false, true>(const PathArgs);
+template __global__ void k_lean<float, M_GBM, 3, true, false, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 5, true, false, true>(const PathArgs);
 template __global__ void k_lean<float, M_GBM, 4, true, false, true>(const PathArgs);
 template __global__ void k_lean<double, M_GBM, 4, true, false, true>(const PathArgs);
@@ -50,6 +54,7 @@ const void *lean_kernel_gbm(int fp64, int minb, bool stat, bool acc, bool sm) {
     switch (minb) {
     case 6: return lean_pick<float, 6>(stat, acc, sm);
     case 5: return lean_pick<float, 5>(stat, acc, sm);
+    case 3: return lean_pick<float, 3>(stat, acc, sm);
     default: return lean_pick<float, 4>(stat, acc, sm);
     }
 }
