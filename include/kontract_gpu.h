@@ -256,6 +256,13 @@ kx_status kx_price_chunks(const kx_program *prog, const kx_model *model,
                           kx_chunk_stats *out, size_t cap, size_t *n_out);
 kx_status kx_merge_chunks(const kx_chunk_stats *chunks, size_t n,
                           kx_price_result *out);
+/* The statistics of one chunk of n <= KX_STATS_CHUNK values (values[i], or
+ * values[i] - subtrahend[i] when subtrahend is not NULL), on the host, bit for
+ * bit as the device reduction computes them for finite values: exact integer
+ * sums of the values in units of 2^-2 of the last mantissa bit of the chunk's
+ * largest value, one rounding for the mean and at most two for M2. */
+kx_status kx_chunk_moments(const double *values, const double *subtrahend,
+                           uint32_t n, kx_chunk_stats *out);
 
 /* kx_price for callers that must not allocate device memory while pricing
  * (no counterpart in the reference). Same arguments and same result as

@@ -215,6 +215,8 @@ SIGNATURES = {
     "kx_price_chunks": (C.c_int, [_P, C.POINTER(KxModel), C.POINTER(KxMcConfig), C.c_uint64,
                                   C.POINTER(KxChunkStats), C.c_size_t, C.POINTER(C.c_size_t)]),
     "kx_merge_chunks": (C.c_int, [C.POINTER(KxChunkStats), C.c_size_t, C.POINTER(KxPriceResult)]),
+    "kx_chunk_moments": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint32,
+                                   C.POINTER(KxChunkStats)]),
     "kx_book_create": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel), C.POINTER(KxMcConfig),
                                  C.c_uint32, C.POINTER(_P)]),
     "kx_book_price": (C.c_int, [_P, C.POINTER(KxPriceResult)]),

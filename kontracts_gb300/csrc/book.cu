@@ -48,7 +48,6 @@ struct kx_book {
     void *arena = nullptr;
     kx::ChunkDesc *d_chunks = nullptr;
     kx::ChunkOut *d_out = nullptr;
-    double *d_w = nullptr;
     double *d_pv = nullptr;
     uint32_t *d_counters = nullptr;  // 16 u32 per group
     kx::ChunkOut *h_out = nullptr;   // pinned
@@ -119,7 +118,7 @@ void capture(Ctx &c, kx_book &b) {
     }
     if (err == cudaSuccess && b.n_chunks) {
         // one launch over every contract's chunks (unit weight, one scenario)
-        launch_chunk_stats(c.stream, b.d_pv, 0, 1, b.d_w, b.d_chunks, b.d_out, (unsigned)b.n_chunks);
+        launch_chunk_stats(c.stream, b.d_pv, b.d_chunks, b.d_out, (unsigned)b.n_chunks);
         err = cudaMemcpyAsync(b.h_out, b.d_out, b.n_chunks * sizeof(ChunkOut), cudaMemcpyDeviceToHost, c.stream);
     }
     if (err == cudaSuccess)
@@ -235,8 +234,7 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
         const size_t off_cnt = A256(off_pv + std::max<uint64_t>(1, b->n_paths) * sizeof(double));
         const size_t off_ch = A256(off_cnt + b->groups.size() * 64);
         const size_t off_out = A256(off_ch + std::max<size_t>(1, b->n_chunks) * sizeof(ChunkDesc));
-        const size_t off_w = A256(off_out + std::max<size_t>(1, b->n_chunks) * sizeof(ChunkOut));
-        const size_t total = A256(off_w + 8 * sizeof(double));
+        const size_t total = A256(off_out + std::max<size_t>(1, b->n_chunks) * sizeof(ChunkOut));
         KX_CUDA(cudaMalloc(&b->arena, total));
         KX_CUDA(cudaMallocHost((void **)&b->h_out, std::max<size_t>(1, b->n_chunks) * sizeof(ChunkOut)));
         KX_CUDA(cudaMallocHost((void **)&b->h_counters, b->groups.size() * 64));
@@ -245,7 +243,6 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
         b->d_counters = reinterpret_cast<uint32_t *>(base + off_cnt);
         b->d_chunks = reinterpret_cast<ChunkDesc *>(base + off_ch);
         b->d_out = reinterpret_cast<ChunkOut *>(base + off_out);
-        b->d_w = reinterpret_cast<double *>(base + off_w);
         size_t o = 0;
         for (size_t q = 0; q < b->groups.size(); ++q) {
             auto &g = b->groups[q];
@@ -260,8 +257,6 @@ kx_status kx_book_create(size_t n, const kx_program *const *progs, const kx_mode
             g.B.counters = b->d_counters + 16 * q;
             g.B.pv = b->d_pv + g.pv_base;
         }
-        const double w[8] = {1, 0, 0, 0, 0, 0, 0, 0};
-        KX_CUDA(cudaMemcpyAsync(b->d_w, w, sizeof w, cudaMemcpyHostToDevice, c.stream));
         if (b->n_chunks)
             KX_CUDA(cudaMemcpyAsync(b->d_chunks, chunks.data(), chunks.size() * sizeof(ChunkDesc),
                                     cudaMemcpyHostToDevice, c.stream));

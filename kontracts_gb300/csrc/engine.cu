@@ -104,8 +104,36 @@ double now_ms() {
 
 // ---------------------------------------------------------------------------
 // Deterministic chunk statistics: each block takes one fixed chunk of values
-// and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes).
+// and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes):
+// exact integer sums for prices (k_chunk_stats_exact, the chunk in registers
+// of 1024 threads) and multilevel differences values[i] - values[stride + i]
+// (k_chunk_stats_diff); FP64 passes for weighted scenarios (k_chunk_stats).
 // ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024, 1) k_chunk_stats_exact(const double *__restrict__ vals,
+                                                              const ChunkDesc *__restrict__ ch,
+                                                              ChunkOut *__restrict__ out) {
+    __shared__ uint32_t emax[33];
+    __shared__ uint64_t part[4 * 32];
+    __shared__ double red[32];
+    const ChunkDesc c = ch[blockIdx.x];
+    double mean = 0.0, m2 = 0.0;
+    chunk_moments_exact_regs<1024>(vals + c.begin, c.count, emax, part, red, mean, m2);
+    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
+}
+
+__global__ void __launch_bounds__(256) k_chunk_stats_diff(const double *__restrict__ vals, uint64_t stride,
+                                                          const ChunkDesc *__restrict__ ch,
+                                                          ChunkOut *__restrict__ out) {
+    __shared__ double red[32];
+    const ChunkDesc c = ch[blockIdx.x];
+    double mean = 0.0, m2 = 0.0;
+    const double *v = vals + c.begin;
+    chunk_moments_exact<2>(v, v + stride, c.count, red, mean, m2);
+    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
+}
+
+// Weighted scenarios (Greek estimators, variance-reduction corrections):
+// values sum_s w[s] * vals[s * stride + i] in FP64.
 __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns,
                                                      const double *__restrict__ w, const ChunkDesc *__restrict__ ch,
                                                      ChunkOut *__restrict__ out) {
@@ -113,22 +141,16 @@ __global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ 
     const ChunkDesc c = ch[blockIdx.x];
     double mean = 0.0, m2 = 0.0;
     const double *v = vals + c.begin;
-    if (ns == 1 && w[0] == 1.0) {  // a plain price: the value itself
-        chunk_moments([&](uint32_t i) { return v[i]; }, c.count, red, mean, m2);
-    } else if (ns == 2 && w[0] == 1.0 && w[1] == -1.0) {  // a difference (multilevel pairs)
-        chunk_moments([&](uint32_t i) { return v[i] - v[stride + i]; }, c.count, red, mean, m2);
-    } else {  // weighted scenarios (Greek estimators, variance-reduction corrections)
-        double ww[8];
+    double ww[8];
 #pragma unroll
-        for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
-        chunk_moments(
-            [&](uint32_t i) {
-                double x = ww[0] * v[i];
-                for (int s = 1; s < ns; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
-                return x;
-            },
-            c.count, red, mean, m2);
-    }
+    for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
+    chunk_moments(
+        [&](uint32_t i) {
+            double x = ww[0] * v[i];
+            for (int s = 1; s < ns; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
+            return x;
+        },
+        c.count, red, mean, m2);
     if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
 }
 
@@ -224,6 +246,16 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
                                                                     c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
+        } else if (nc && plain) {
+            k_chunk_stats_exact<<<(unsigned)nc, 1024, 0, c.stream>>>(values, d_chunks + first[j],
+                                                                     c.chunk_out.as<ChunkOut>() + first[j]);
+            KX_CUDA(cudaGetLastError());
+            c.last.kernel_launches++;
+        } else if (nc && jobs[j].ns == 2 && jobs[j].w[0] == 1.0 && jobs[j].w[1] == -1.0) {  // multilevel pairs
+            k_chunk_stats_diff<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, d_chunks + first[j],
+                                                                   c.chunk_out.as<ChunkOut>() + first[j]);
+            KX_CUDA(cudaGetLastError());
+            c.last.kernel_launches++;
         } else if (nc) {
             k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, d_w + j * 8,
                                                               d_chunks + first[j],
@@ -259,10 +291,10 @@ Stats merge_chunks(const ChunkOut *h, size_t n) {
     return s;
 }
 
-void launch_chunk_stats(cudaStream_t s, const double *values, uint64_t stride, int ns, const double *w,
-                        const ChunkDesc *chunks, ChunkOut *out, unsigned n_chunks) {
+void launch_chunk_stats(cudaStream_t s, const double *values, const ChunkDesc *chunks, ChunkOut *out,
+                        unsigned n_chunks) {
     if (!n_chunks) return;
-    k_chunk_stats<<<n_chunks, 256, 0, s>>>(values, stride, ns, w, chunks, out);
+    k_chunk_stats_exact<<<n_chunks, 1024, 0, s>>>(values, chunks, out);
     KX_CUDA(cudaGetLastError());
 }
 
@@ -1303,13 +1335,10 @@ kx_status kx_price_chunks(const kx_program *prog, const kx_model *model, const k
         if (!chunks.empty()) {
             c.chunks.ensure(chunks.size() * sizeof(ChunkDesc));
             c.chunk_out.ensure(chunks.size() * sizeof(ChunkOut));
-            c.weights.ensure(8 * sizeof(double));
-            const double w[8] = {1, 0, 0, 0, 0, 0, 0, 0};
             KX_CUDA(cudaMemcpyAsync(c.chunks.p, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice,
                                     c.stream));
-            KX_CUDA(cudaMemcpyAsync(c.weights.p, w, sizeof w, cudaMemcpyHostToDevice, c.stream));
-            launch_chunk_stats(c.stream, c.pv.as<double>(), stride, 1, c.weights.as<double>(),
-                               c.chunks.as<ChunkDesc>(), c.chunk_out.as<ChunkOut>(), (unsigned)chunks.size());
+            launch_chunk_stats(c.stream, c.pv.as<double>(), c.chunks.as<ChunkDesc>(), c.chunk_out.as<ChunkOut>(),
+                               (unsigned)chunks.size());
             c.last.kernel_launches++;
             std::vector<ChunkOut> h(chunks.size());
             KX_CUDA(cudaMemcpyAsync(h.data(), c.chunk_out.p, h.size() * sizeof(ChunkOut), cudaMemcpyDeviceToHost,
@@ -1319,6 +1348,16 @@ kx_status kx_price_chunks(const kx_program *prog, const kx_model *model, const k
         }
         *n_out = chunks.size();
         end_call(c);
+    });
+}
+
+kx_status kx_chunk_moments(const double *values, const double *subtrahend, uint32_t n, kx_chunk_stats *out) {
+    return guarded([&] {
+        if (!out || (n && !values)) raise(KX_INVALID_ARGUMENT, "NULL argument");
+        if (n > KX_STATS_CHUNK) raise(KX_INVALID_ARGUMENT, "a chunk holds at most KX_STATS_CHUNK values");
+        double mean = 0.0, m2 = 0.0;
+        chunk_moments_exact_host(values, subtrahend, n, mean, m2);
+        *out = kx_chunk_stats{(double)n, mean, m2};
     });
 }
 

@@ -50,7 +50,7 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scratch owned by the context
-    DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, weights, misc, vr, lsm_paths, lsm_value,
+    DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, misc, vr, lsm_paths, lsm_value,
         lsm_stats, statics, mlmc, plan, stats_in;
     // host staging of a call's uploads and downloads (path plan, statistics)
     PinnedBuf plan_stage, stats_stage;

@@ -86,17 +86,18 @@ static unsigned char *scratch(Ctx &c) {
     return g_scratch_ptr;
 }
 
-// The chunk statistics of k_chunk_stats for one scenario with unit weight
-// (chunk_moments), the chunk bounds taken from the block index instead of a
+// The chunk statistics of k_chunk_stats_exact (chunk_moments_exact_regs, 1024
+// threads), the chunk bounds taken from the block index instead of a
 // descriptor table.
-__global__ void __launch_bounds__(256) k_fixed_stats(const double *__restrict__ vals, uint64_t n,
-                                                     ChunkOut *__restrict__ out) {
+__global__ void __launch_bounds__(1024, 1) k_fixed_stats(const double *__restrict__ vals, uint64_t n,
+                                                        ChunkOut *__restrict__ out) {
+    __shared__ uint32_t emax[33];
+    __shared__ uint64_t part[4 * 32];
     __shared__ double red[32];
     const uint64_t begin = (uint64_t)blockIdx.x * KX_STATS_CHUNK;
     const uint32_t count = (uint32_t)std::min<uint64_t>(KX_STATS_CHUNK, n - begin);
-    const double *v = vals + begin;
     double mean = 0.0, m2 = 0.0;
-    chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);  // as k_chunk_stats, one scenario
+    chunk_moments_exact_regs<1024>(vals + begin, count, emax, part, red, mean, m2);
     if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)count, mean, m2};
 }
 
@@ -209,7 +210,7 @@ extern "C" kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_mod
         }
         const uint64_t nc = (n + KX_STATS_CHUNK - 1) / KX_STATS_CHUNK;
         if (nc) {
-            k_fixed_stats<<<(unsigned)nc, 256, 0, c.stream>>>(pv, n, chunks);
+            k_fixed_stats<<<(unsigned)nc, 1024, 0, c.stream>>>(pv, n, chunks);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         }

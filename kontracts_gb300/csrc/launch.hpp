@@ -108,10 +108,10 @@ void check_err_word(uint32_t err);
 
 // Merge of consecutive chunk statistics in chunk order (Chan et al.).
 Stats merge_chunks(const ChunkOut *h, size_t n);
-// One launch of the chunk-statistics kernel: chunk q of `chunks` reduces
-// values[s * stride + begin + i] weighted by w[s], s < ns, into out[q].
-void launch_chunk_stats(cudaStream_t s, const double *values, uint64_t stride, int ns, const double *w,
-                        const ChunkDesc *chunks, ChunkOut *out, unsigned n_chunks);
+// One launch of the chunk statistics of prices: chunk q of `chunks` reduces
+// values[begin + i] into out[q] (exact integer sums, chunk_moments_exact).
+void launch_chunk_stats(cudaStream_t s, const double *values, const ChunkDesc *chunks, ChunkOut *out,
+                        unsigned n_chunks);
 
 // Per-call bookkeeping of the launch statistics.
 void begin_call(Ctx &c);

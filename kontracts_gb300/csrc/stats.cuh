@@ -2,7 +2,9 @@
 // reduction kernels: a chunk's (n, mean, M2) and the block-wide sum whose
 // summation order every reduction kernel follows.
 #pragma once
+#include <algorithm>
 #include <cstdint>
+#include <cstring>
 
 #include "../../include/kontract_gpu.h"
 
@@ -75,6 +77,298 @@ __device__ __forceinline__ void chunk_moments(const Val &val, uint32_t count, do
         b0 = fma(d, d, b0);
     }
     m2 = block_sum((b0 + b1) + (b2 + b3), red);
+}
+
+// ---------------------------------------------------------------------------
+// Exact chunk statistics in integers. GB300 runs FP64 at about 1/64 of its
+// FP32 rate, so the FP64 passes above cost about two SM cycles per value and
+// bound the reduction. Here each value becomes a signed integer X, a multiple
+// of one unit 2^(E - 1075 - FX_GUARD) where E is the largest exponent field
+// in the chunk: X = m << FX_GUARD >> (E - e) for the 53-bit mantissa m and
+// exponent field e of the value (truncated toward zero when e < E - FX_GUARD,
+// i.e. an error below 2^-54 of the chunk's largest value; exact otherwise).
+// Deviations d = X - C from the chunk's first value C are summed exactly,
+// S = sum d in 128 bits and Q = sum d^2 in unsigned 128 bits (|d| < 2^57 and
+// at most 2^14 values, so neither overflows), and one thread turns them into
+// the mean C + S/n and M2 = Q - S^2/n, each rounded once or twice. Integer
+// sums do not depend on their order, so the result depends only on the
+// chunk's values, on any launch shape, and the host mirror below gives the
+// same bits. About 35 integer instructions per value replace the 3 FP64 ones.
+// Chunks holding an infinity or a NaN take the FP64 passes.
+// ---------------------------------------------------------------------------
+#if defined(__CUDACC__)
+#define KX_HD __host__ __device__
+#else
+#define KX_HD
+#endif
+constexpr int FX_GUARD = 2;  // fraction bits kept below the largest value's last mantissa bit
+typedef __int128 fx_i128;
+typedef unsigned __int128 fx_u128;
+
+KX_HD inline uint64_t fx_bits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+KX_HD inline uint32_t fx_expo(double x) { return (uint32_t)(fx_bits(x) >> 52) & 0x7FFu; }
+
+// x in units of 2^(E - 1075 - FX_GUARD), E >= 1 and >= the exponent field of x.
+KX_HD inline int64_t fx_value(double x, uint32_t E) {
+    const uint64_t b = fx_bits(x);
+    const uint32_t ef = (uint32_t)(b >> 52) & 0x7FFu;
+    uint64_t m = b & 0x000FFFFFFFFFFFFFull;
+    if (ef) m |= 0x0010000000000000ull;  // the implicit bit (subnormals have none and e = 1)
+    const uint32_t t = E - (ef ? ef : 1u);
+    m = t < 64u ? (m << FX_GUARD) >> t : 0ull;
+    const int64_t s = (int64_t)b >> 63;  // 0 or -1: the sign
+    return ((int64_t)m ^ s) - s;
+}
+
+// d^2 for |d| < 2^57 from three 32 x 32 -> 64 products.
+KX_HD inline fx_u128 fx_square(int64_t d) {
+    const uint64_t a = d < 0 ? 0ull - (uint64_t)d : (uint64_t)d;
+    const uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
+    const uint64_t ll = (uint64_t)lo * lo, lh = (uint64_t)lo * hi, hh = (uint64_t)hi * hi;
+    return ((fx_u128)hh << 64) + ((fx_u128)(lh << 1) << 32) + ll;
+}
+
+KX_HD inline double fx_u128_to_double(fx_u128 v) {  // round-to-nearest of each half; hi * 2^64 is exact
+    return (double)(uint64_t)(v >> 64) * 18446744073709551616.0 + (double)(uint64_t)v;
+}
+KX_HD inline double fx_i128_to_double(fx_i128 v) {
+    return (double)(int64_t)(v >> 64) * 18446744073709551616.0 + (double)(uint64_t)v;
+}
+
+// 2^k for -1022 <= k <= 1023, from its bits.
+KX_HD inline double fx_pow2(int k) {
+    const uint64_t b = (uint64_t)(k + 1023) << 52;
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+
+// x * 2^k by exact power-of-two steps (one rounding at most, where the result
+// is subnormal).
+KX_HD inline double fx_scale(double x, int k) {
+    while (k > 1000) {
+        x *= 0x1p1000;
+        k -= 1000;
+    }
+    while (k < -1000) {
+        x *= 0x1p-1000;
+        k += 1000;
+    }
+    return x * fx_pow2(k);
+}
+
+// The chunk's mean and M2 from the exact sums (n values, first value C).
+KX_HD inline void fx_finish(int64_t C, fx_i128 S, fx_u128 Q, uint32_t n, uint32_t E, double &mean, double &m2) {
+    // S = q n + r with |r| < n: q from a rounded quotient, then corrected exactly
+    const int64_t q1 = (int64_t)(fx_i128_to_double(S) / (double)n);
+    const int64_t r1 = (int64_t)(S - (fx_i128)q1 * (fx_i128)n);
+    const int64_t q2 = r1 / (int64_t)n;
+    const int64_t q = q1 + q2, r = r1 - q2 * (int64_t)n;
+    // n M2 = n Q - S^2, so M2 = (Q - q^2 n - 2 q r) - r^2 / n; the bracket is an
+    // integer in [0, 2^128), exact in wrapping unsigned arithmetic
+    const fx_u128 T = Q - fx_square(q) * (fx_u128)n - (fx_u128)((fx_i128)(2 * q) * (fx_i128)r);
+    const double m2u = fx_u128_to_double(T) - (double)(r * r) / (double)n;
+    const double mu = (double)(C + q) + (double)r / (double)n;
+    const int k = (int)E - 1075 - FX_GUARD;
+    mean = fx_scale(mu, k);
+    m2 = fx_scale(m2u, 2 * k);
+}
+
+// The exact statistics of one chunk of values a[i] (OPS 1) or a[i] - b[i]
+// (OPS 2, the difference taken exactly), 1 <= count <= KX_STATS_CHUNK, by a
+// block of at most 256 threads (whole warps); `red` holds 32 doubles. Pass 1
+// finds E, pass 2 sums. mean and m2 are valid in thread 0.
+template <int OPS>
+__device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a, const double *__restrict__ b,
+                                                    uint32_t count, double *red, double &mean, double &m2) {
+    const uint32_t B = blockDim.x, nw = B >> 5;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    uint32_t e = 0;
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < count; i += B) {
+        e = max(e, fx_expo(a[i]));
+        if (OPS == 2) e = max(e, fx_expo(b[i]));
+    }
+    e = __reduce_max_sync(0xffffffffu, e);
+    uint32_t *const ured = reinterpret_cast<uint32_t *>(red);
+    if (l == 0) ured[w] = e;
+    __syncthreads();
+    uint32_t E = 0;
+    for (uint32_t q = 0; q < nw; ++q) E = max(E, ured[q]);
+    __syncthreads();
+    if (E == 0x7FFu) {  // an infinity or a NaN: the FP64 passes give the IEEE result
+        if (OPS == 1) chunk_moments([&](uint32_t i) { return a[i]; }, count, red, mean, m2);
+        else chunk_moments([&](uint32_t i) { return a[i] - b[i]; }, count, red, mean, m2);
+        return;
+    }
+    if (E == 0u) E = 1u;  // zeros and subnormals only
+    auto fx = [&](uint32_t i) -> int64_t {
+        return OPS == 1 ? fx_value(a[i], E) : fx_value(a[i], E) - fx_value(b[i], E);
+    };
+    const int64_t C = fx(0);
+    fx_i128 S = 0;
+    fx_u128 Q = 0;
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < count; i += B) {
+        const int64_t d = fx(i) - C;
+        S += d;
+        Q += fx_square(d);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)S, o);
+        const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(S >> 64), o);
+        const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Q, o);
+        const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Q >> 64), o);
+        S += (fx_i128)(((fx_u128)shi << 64) | slo);
+        Q += ((fx_u128)qhi << 64) | qlo;
+    }
+    uint64_t *const r64 = reinterpret_cast<uint64_t *>(red);  // 4 words per warp, 8 warps
+    if (l == 0) {
+        r64[4 * w] = (uint64_t)S;
+        r64[4 * w + 1] = (uint64_t)(S >> 64);
+        r64[4 * w + 2] = (uint64_t)Q;
+        r64[4 * w + 3] = (uint64_t)(Q >> 64);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        fx_i128 St = 0;
+        fx_u128 Qt = 0;
+        for (uint32_t q = 0; q < nw; ++q) {
+            St += (fx_i128)(((fx_u128)r64[4 * q + 1] << 64) | r64[4 * q]);
+            Qt += ((fx_u128)r64[4 * q + 3] << 64) | r64[4 * q + 2];
+        }
+        fx_finish(C, St, Qt, count, E, mean, m2);
+    }
+    __syncthreads();  // red is free again
+}
+
+// chunk_moments_exact for prices (OPS 1) by a block of NT threads that holds
+// the chunk in registers, KX_STATS_CHUNK / NT values a thread: the chunk is
+// read once, with all of a thread's loads in flight together, and both passes
+// run on the registers. The sums are the same integers, so the result is the
+// same bits. `emax` holds 33 words and `part` 4 * 32 (one row per warp);
+// `red` (32 doubles) serves the FP64 passes of a non-finite chunk. mean and
+// m2 are valid in thread 0.
+template <int NT>
+__device__ __forceinline__ void chunk_moments_exact_regs(const double *__restrict__ v, uint32_t count, uint32_t *emax,
+                                                         uint64_t *part, double *red, double &mean, double &m2) {
+    constexpr int VPT = (int)KX_STATS_CHUNK / NT;
+    static_assert(VPT * NT == (int)KX_STATS_CHUNK && NT % 32 == 0 && NT <= 1024, "block shape");
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    double x[VPT];
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) {
+        const uint32_t i = threadIdx.x + (uint32_t)(k * NT);
+        x[k] = i < count ? v[i] : 0.0;  // past the end: exponent field 0, excluded from the sums below
+    }
+    uint32_t e = 0;
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) e = max(e, fx_expo(x[k]));
+    e = __reduce_max_sync(0xffffffffu, e);
+    if (l == 0) emax[w] = e;
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t t = __reduce_max_sync(0xffffffffu, l < NT / 32 ? emax[l] : 0u);
+        if (l == 0) emax[32] = t;
+    }
+    __syncthreads();
+    uint32_t E = emax[32];
+    if (E == 0x7FFu) {  // an infinity or a NaN: the FP64 passes give the IEEE result
+        chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);
+        return;
+    }
+    if (E == 0u) E = 1u;
+    const int64_t C = fx_value(v[0], E);
+    int64_t S = 0;  // |S| < VPT * 2^56
+    fx_u128 Q = 0;
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) {
+        if (threadIdx.x + (uint32_t)(k * NT) < count) {
+            const int64_t d = fx_value(x[k], E) - C;
+            S += d;
+            Q += fx_square(d);
+        }
+    }
+    fx_i128 Sw = S;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Sw, o);
+        const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Sw >> 64), o);
+        const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Q, o);
+        const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Q >> 64), o);
+        Sw += (fx_i128)(((fx_u128)shi << 64) | slo);
+        Q += ((fx_u128)qhi << 64) | qlo;
+    }
+    if (l == 0) {
+        part[4 * w] = (uint64_t)Sw;
+        part[4 * w + 1] = (uint64_t)(Sw >> 64);
+        part[4 * w + 2] = (uint64_t)Q;
+        part[4 * w + 3] = (uint64_t)(Q >> 64);
+    }
+    __syncthreads();
+    if (w == 0) {
+        fx_i128 St = 0;
+        fx_u128 Qt = 0;
+        if (l < NT / 32) {
+            St = (fx_i128)(((fx_u128)part[4 * l + 1] << 64) | part[4 * l]);
+            Qt = ((fx_u128)part[4 * l + 3] << 64) | part[4 * l + 2];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)St, o);
+            const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(St >> 64), o);
+            const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Qt, o);
+            const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Qt >> 64), o);
+            St += (fx_i128)(((fx_u128)shi << 64) | slo);
+            Qt += ((fx_u128)qhi << 64) | qlo;
+        }
+        if (l == 0) fx_finish(C, St, Qt, count, E, mean, m2);
+    }
+}
+
+// Host mirror of chunk_moments_exact: the same bits for finite values. A
+// chunk with an infinity or a NaN gets the plain two-pass FP64 result, of the
+// same IEEE class as the device's.
+inline void chunk_moments_exact_host(const double *a, const double *b, uint32_t count, double &mean, double &m2) {
+    mean = m2 = 0.0;
+    if (count == 0) return;
+    uint32_t E = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        E = std::max(E, fx_expo(a[i]));
+        if (b) E = std::max(E, fx_expo(b[i]));
+    }
+    auto val = [&](uint32_t i) { return b ? a[i] - b[i] : a[i]; };
+    if (E == 0x7FFu) {
+        double s = 0.0;
+        for (uint32_t i = 0; i < count; ++i) s += val(i);
+        mean = s / (double)count;
+        for (uint32_t i = 0; i < count; ++i) m2 += (val(i) - mean) * (val(i) - mean);
+        return;
+    }
+    if (E == 0u) E = 1u;
+    auto fx = [&](uint32_t i) -> int64_t { return b ? fx_value(a[i], E) - fx_value(b[i], E) : fx_value(a[i], E); };
+    const int64_t C = fx(0);
+    fx_i128 S = 0;
+    fx_u128 Q = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const int64_t d = fx(i) - C;
+        S += d;
+        Q += fx_square(d);
+    }
+    fx_finish(C, S, Q, count, E, mean, m2);
 }
 
 }  // namespace kx

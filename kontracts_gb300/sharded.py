@@ -46,6 +46,24 @@ def price_chunks(contract, model, first_path: int, n_paths: int, seed: int = 42,
     return [(out[q].n, out[q].mean, out[q].m2) for q in range(n_out.value)]
 
 
+def chunk_moments(values, subtrahend=None) -> tuple[float, float, float]:
+    """(n, mean, M2) of one chunk of at most CHUNK values (values[i], or
+    values[i] - subtrahend[i]) on the host, bit for bit as the device's chunk
+    reduction computes them for finite values."""
+    import numpy as np
+    from . import _check, _lib
+    a = np.ascontiguousarray(values, dtype=np.float64)
+    pb = None
+    if subtrahend is not None:
+        b = np.ascontiguousarray(subtrahend, dtype=np.float64)
+        if b.shape != a.shape:
+            raise ValueError("values and subtrahend differ in length")
+        pb = b.ctypes.data_as(C.POINTER(C.c_double))
+    out = _abi.KxChunkStats()
+    _check(_lib().kx_chunk_moments(a.ctypes.data_as(C.POINTER(C.c_double)), pb, len(a), C.byref(out)))
+    return (out.n, out.mean, out.m2)
+
+
 def merge(chunks: Sequence[tuple[float, float, float]]):
     """The price of chunk statistics merged in the given order (the library's
     own merge, so the result equals kx_price's bit for bit)."""

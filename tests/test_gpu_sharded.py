@@ -29,6 +29,22 @@ def test_ranges_merge_to_the_whole_price(name, prec):
     assert r.price == full.price and r.std_error == full.std_error and r.n_paths == n
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", ["up_and_out", "short_put_spread"])
+def test_device_chunk_statistics_equal_the_host_mirror(name, prec):
+    """The device's exact integer chunk sums and the host's give the same bits
+    on the same per-path values (a ragged last chunk included)."""
+    S = kx.S("X")
+    c = {"up_and_out": kx.up_and_out_call("X", 100.0, 130.0, 1.0),
+         "short_put_spread": kx.scale((90.0 - S).clip(0.0) - (110.0 - S).clip(0.0), kx.one()) @ kx.at(1.0)}[name]
+    m = kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
+    n = 3 * C + 777
+    _, pv = c.price(m, n_paths=n, seed=9, steps_per_year=252, precision=prec, per_path=True)
+    dev = sharded.price_chunks(c, m, 0, n, seed=9, steps_per_year=252, precision=prec)
+    host = [sharded.chunk_moments(pv[q:q + C]) for q in range(0, n, C)]
+    assert dev == host
+
+
 def test_ranges_must_start_on_a_chunk():
     c = kx.european_call("X", 100.0, 1.0)
     m = kx.GBM(s0=100.0, sigma=0.25, r=0.03, asset="X")
