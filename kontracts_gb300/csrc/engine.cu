@@ -106,19 +106,20 @@ double now_ms() {
 // Deterministic chunk statistics: each block takes one fixed chunk of values
 // and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes):
 // exact integer sums for prices (k_chunk_stats_exact, the chunk in registers
-// of 1024 threads) and multilevel differences values[i] - values[stride + i]
+// of a cluster of 4 blocks) and multilevel differences values[i] - values[stride + i]
 // (k_chunk_stats_diff); FP64 passes for weighted scenarios (k_chunk_stats).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024, 1) k_chunk_stats_exact(const double *__restrict__ vals,
-                                                              const ChunkDesc *__restrict__ ch,
-                                                              ChunkOut *__restrict__ out) {
-    __shared__ uint32_t emax[33];
-    __shared__ uint64_t part[4 * 32];
+__global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 4)
+    k_chunk_stats_exact(const double *__restrict__ vals, const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
+    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + 1];
+    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + 1)];
     __shared__ double red[32];
-    const ChunkDesc c = ch[blockIdx.x];
+    const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;  // the chunk of this cluster
+    const ChunkDesc c = ch[q];
     double mean = 0.0, m2 = 0.0;
-    chunk_moments_exact_regs<1024>(vals + c.begin, c.count, emax, part, red, mean, m2);
-    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
+    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>(vals + c.begin, c.count, emax, part, red, mean,
+                                                                     m2);
+    if (blockIdx.x % KX_STATS_CLUSTER == 0 && threadIdx.x == 0) out[q] = ChunkOut{(double)c.count, mean, m2};
 }
 
 __global__ void __launch_bounds__(256) k_chunk_stats_diff(const double *__restrict__ vals, uint64_t stride,
@@ -247,8 +248,8 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         } else if (nc && plain) {
-            k_chunk_stats_exact<<<(unsigned)nc, 1024, 0, c.stream>>>(values, d_chunks + first[j],
-                                                                     c.chunk_out.as<ChunkOut>() + first[j]);
+            k_chunk_stats_exact<<<(unsigned)nc * KX_STATS_CLUSTER, KX_STATS_THREADS, 0, c.stream>>>(
+                values, d_chunks + first[j], c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         } else if (nc && jobs[j].ns == 2 && jobs[j].w[0] == 1.0 && jobs[j].w[1] == -1.0) {  // multilevel pairs
@@ -294,7 +295,7 @@ Stats merge_chunks(const ChunkOut *h, size_t n) {
 void launch_chunk_stats(cudaStream_t s, const double *values, const ChunkDesc *chunks, ChunkOut *out,
                         unsigned n_chunks) {
     if (!n_chunks) return;
-    k_chunk_stats_exact<<<n_chunks, 1024, 0, s>>>(values, chunks, out);
+    k_chunk_stats_exact<<<n_chunks * KX_STATS_CLUSTER, KX_STATS_THREADS, 0, s>>>(values, chunks, out);
     KX_CUDA(cudaGetLastError());
 }
 

@@ -86,19 +86,20 @@ static unsigned char *scratch(Ctx &c) {
     return g_scratch_ptr;
 }
 
-// The chunk statistics of k_chunk_stats_exact (chunk_moments_exact_regs, 1024
-// threads), the chunk bounds taken from the block index instead of a
-// descriptor table.
-__global__ void __launch_bounds__(1024, 1) k_fixed_stats(const double *__restrict__ vals, uint64_t n,
-                                                        ChunkOut *__restrict__ out) {
-    __shared__ uint32_t emax[33];
-    __shared__ uint64_t part[4 * 32];
+// The chunk statistics of k_chunk_stats_exact (a cluster of blocks a chunk,
+// chunk_moments_exact_cluster), the chunk bounds taken from the cluster index
+// instead of a descriptor table.
+__global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 3)
+    k_fixed_stats(const double *__restrict__ vals, uint64_t n, ChunkOut *__restrict__ out) {
+    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + 1];
+    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + 1)];
     __shared__ double red[32];
-    const uint64_t begin = (uint64_t)blockIdx.x * KX_STATS_CHUNK;
+    const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;
+    const uint64_t begin = (uint64_t)q * KX_STATS_CHUNK;
     const uint32_t count = (uint32_t)std::min<uint64_t>(KX_STATS_CHUNK, n - begin);
     double mean = 0.0, m2 = 0.0;
-    chunk_moments_exact_regs<1024>(vals + begin, count, emax, part, red, mean, m2);
-    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)count, mean, m2};
+    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>(vals + begin, count, emax, part, red, mean, m2);
+    if (blockIdx.x % KX_STATS_CLUSTER == 0 && threadIdx.x == 0) out[q] = ChunkOut{(double)count, mean, m2};
 }
 
 }  // namespace kx
@@ -210,7 +211,7 @@ extern "C" kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_mod
         }
         const uint64_t nc = (n + KX_STATS_CHUNK - 1) / KX_STATS_CHUNK;
         if (nc) {
-            k_fixed_stats<<<(unsigned)nc, 1024, 0, c.stream>>>(pv, n, chunks);
+            k_fixed_stats<<<(unsigned)nc * KX_STATS_CLUSTER, KX_STATS_THREADS, 0, c.stream>>>(pv, n, chunks);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         }

@@ -7,12 +7,20 @@
 #include <cstring>
 
 #include "../../include/kontract_gpu.h"
+#if defined(__CUDACC__)
+#include <cooperative_groups.h>
+#endif
 
 namespace kx {
 
 // Values per chunk: a chunk's statistics do not depend on how many chunks
 // or blocks a launch has, so every launch shape gives the same result.
 static_assert(KX_STATS_CHUNK == 16384u, "chunk size of the C ABI");
+
+// The exact reduction of a chunk of prices: a cluster of KX_STATS_CLUSTER
+// blocks of KX_STATS_THREADS threads, 16 values a thread.
+#define KX_STATS_CLUSTER 4
+#define KX_STATS_THREADS 256
 
 struct ChunkDesc {
     uint64_t begin;
@@ -123,7 +131,11 @@ KX_HD inline int64_t fx_value(double x, uint32_t E) {
     uint64_t m = b & 0x000FFFFFFFFFFFFFull;
     if (ef) m |= 0x0010000000000000ull;  // the implicit bit (subnormals have none and e = 1)
     const uint32_t t = E - (ef ? ef : 1u);
+#if defined(__CUDA_ARCH__)
+    asm("shr.b64 %0, %1, %2;" : "=l"(m) : "l"(m << FX_GUARD), "r"(t));  // PTX: a shift of 64 or more gives 0
+#else
     m = t < 64u ? (m << FX_GUARD) >> t : 0ull;
+#endif
     const int64_t s = (int64_t)b >> 63;  // 0 or -1: the sign
     return ((int64_t)m ^ s) - s;
 }
@@ -186,10 +198,25 @@ KX_HD inline void fx_finish(int64_t C, fx_i128 S, fx_u128 Q, uint32_t n, uint32_
     m2 = fx_scale(m2u, 2 * k);
 }
 
+// Sums of S (signed) and Q (unsigned) over a warp, 128 bits each.
+__device__ __forceinline__ void fx_warp_sum(fx_i128 &S, fx_u128 &Q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)S, o);
+        const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(S >> 64), o);
+        const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Q, o);
+        const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Q >> 64), o);
+        S += (fx_i128)(((fx_u128)shi << 64) | slo);
+        Q += ((fx_u128)qhi << 64) | qlo;
+    }
+}
+
 // The exact statistics of one chunk of values a[i] (OPS 1) or a[i] - b[i]
-// (OPS 2, the difference taken exactly), 1 <= count <= KX_STATS_CHUNK, by a
-// block of at most 256 threads (whole warps); `red` holds 32 doubles. Pass 1
-// finds E, pass 2 sums. mean and m2 are valid in thread 0.
+// (OPS 2, the difference taken exactly), 1 <= count <= KX_STATS_CHUNK, by one
+// block of at most 256 threads (whole warps), two passes over memory (the
+// multilevel differences; prices take chunk_moments_exact_cluster); `red`
+// holds 32 doubles. Pass 1 finds E, pass 2 sums. mean and m2 are valid in
+// thread 0.
 template <int OPS>
 __device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a, const double *__restrict__ b,
                                                     uint32_t count, double *red, double &mean, double &m2) {
@@ -226,15 +253,7 @@ __device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a
         S += d;
         Q += fx_square(d);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)S, o);
-        const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(S >> 64), o);
-        const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Q, o);
-        const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Q >> 64), o);
-        S += (fx_i128)(((fx_u128)shi << 64) | slo);
-        Q += ((fx_u128)qhi << 64) | qlo;
-    }
+    fx_warp_sum(S, Q);
     uint64_t *const r64 = reinterpret_cast<uint64_t *>(red);  // 4 words per warp, 8 warps
     if (l == 0) {
         r64[4 * w] = (uint64_t)S;
@@ -255,23 +274,30 @@ __device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a
     __syncthreads();  // red is free again
 }
 
-// chunk_moments_exact for prices (OPS 1) by a block of NT threads that holds
-// the chunk in registers, KX_STATS_CHUNK / NT values a thread: the chunk is
-// read once, with all of a thread's loads in flight together, and both passes
-// run on the registers. The sums are the same integers, so the result is the
-// same bits. `emax` holds 33 words and `part` 4 * 32 (one row per warp);
-// `red` (32 doubles) serves the FP64 passes of a non-finite chunk. mean and
-// m2 are valid in thread 0.
-template <int NT>
-__device__ __forceinline__ void chunk_moments_exact_regs(const double *__restrict__ v, uint32_t count, uint32_t *emax,
-                                                         uint64_t *part, double *red, double &mean, double &m2) {
-    constexpr int VPT = (int)KX_STATS_CHUNK / NT;
-    static_assert(VPT * NT == (int)KX_STATS_CHUNK && NT % 32 == 0 && NT <= 1024, "block shape");
+// chunk_moments_exact for prices by a cluster of CS blocks of NT threads:
+// block r of the cluster holds values r * NT * VPT .. (r + 1) * NT * VPT - 1
+// of the chunk in registers, VPT a thread, all loaded at once. The blocks
+// exchange their exponent maxima, then their sums, through distributed shared
+// memory (cluster barriers, no polling). A block of NT threads at 64
+// registers leaves room for 65536 / (64 NT) resident blocks a multiprocessor,
+// so one block's loads overlap another's integer work. Smem: `emax` NT/32 + 1
+// words, `part` 4 (NT/32 + 1) words, `red` 32 doubles (FP64 passes of a
+// non-finite chunk, run by block 0). mean and m2 are valid in thread 0 of
+// block 0 of the cluster.
+template <int CS, int NT>
+__device__ __forceinline__ void chunk_moments_exact_cluster(const double *__restrict__ v, uint32_t count,
+                                                            uint32_t *emax, uint64_t *part, double *red, double &mean,
+                                                            double &m2) {
+    constexpr int NW = NT / 32, VPT = (int)KX_STATS_CHUNK / (CS * NT);
+    static_assert(VPT * CS * NT == (int)KX_STATS_CHUNK && NT % 32 == 0, "cluster shape");
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t rank = cl.block_rank(), base = rank * (uint32_t)(NT * VPT);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     double x[VPT];
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
-        const uint32_t i = threadIdx.x + (uint32_t)(k * NT);
+        const uint32_t i = base + threadIdx.x + (uint32_t)(k * NT);
         x[k] = i < count ? v[i] : 0.0;  // past the end: exponent field 0, excluded from the sums below
     }
     uint32_t e = 0;
@@ -281,62 +307,65 @@ __device__ __forceinline__ void chunk_moments_exact_regs(const double *__restric
     if (l == 0) emax[w] = e;
     __syncthreads();
     if (w == 0) {
-        const uint32_t t = __reduce_max_sync(0xffffffffu, l < NT / 32 ? emax[l] : 0u);
-        if (l == 0) emax[32] = t;
+        const uint32_t t = __reduce_max_sync(0xffffffffu, l < NW ? emax[l] : 0u);
+        if (l == 0) emax[NW] = t;  // this block's maximum
     }
-    __syncthreads();
-    uint32_t E = emax[32];
-    if (E == 0x7FFu) {  // an infinity or a NaN: the FP64 passes give the IEEE result
-        chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);
+    cl.sync();  // every block's maximum is written
+    uint32_t E = 0;
+    for (int r = 0; r < CS; ++r) E = max(E, *cl.map_shared_rank(emax + NW, r));
+    if (E == 0x7FFu) {  // an infinity or a NaN: block 0 runs the FP64 passes over the chunk
+        if (rank == 0) chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);
+        cl.sync();  // no block leaves while another reads its maximum
         return;
     }
     if (E == 0u) E = 1u;
     const int64_t C = fx_value(v[0], E);
-    int64_t S = 0;  // |S| < VPT * 2^56
+    int64_t S1 = 0;  // |S1| < VPT * 2^56
     fx_u128 Q = 0;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
-        if (threadIdx.x + (uint32_t)(k * NT) < count) {
+        if (base + threadIdx.x + (uint32_t)(k * NT) < count) {
             const int64_t d = fx_value(x[k], E) - C;
-            S += d;
+            S1 += d;
             Q += fx_square(d);
         }
     }
-    fx_i128 Sw = S;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Sw, o);
-        const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Sw >> 64), o);
-        const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Q, o);
-        const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Q >> 64), o);
-        Sw += (fx_i128)(((fx_u128)shi << 64) | slo);
-        Q += ((fx_u128)qhi << 64) | qlo;
-    }
+    fx_i128 S = S1;
+    fx_warp_sum(S, Q);
     if (l == 0) {
-        part[4 * w] = (uint64_t)Sw;
-        part[4 * w + 1] = (uint64_t)(Sw >> 64);
+        part[4 * w] = (uint64_t)S;
+        part[4 * w + 1] = (uint64_t)(S >> 64);
         part[4 * w + 2] = (uint64_t)Q;
         part[4 * w + 3] = (uint64_t)(Q >> 64);
     }
     __syncthreads();
     if (w == 0) {
+        S = 0;
+        Q = 0;
+        if (l < NW) {
+            S = (fx_i128)(((fx_u128)part[4 * l + 1] << 64) | part[4 * l]);
+            Q = ((fx_u128)part[4 * l + 3] << 64) | part[4 * l + 2];
+        }
+        fx_warp_sum(S, Q);
+        if (l == 0) {  // this block's sums
+            part[4 * NW] = (uint64_t)S;
+            part[4 * NW + 1] = (uint64_t)(S >> 64);
+            part[4 * NW + 2] = (uint64_t)Q;
+            part[4 * NW + 3] = (uint64_t)(Q >> 64);
+        }
+    }
+    cl.sync();  // every block's sums are written (and every maximum read)
+    if (rank == 0 && threadIdx.x == 0) {
         fx_i128 St = 0;
         fx_u128 Qt = 0;
-        if (l < NT / 32) {
-            St = (fx_i128)(((fx_u128)part[4 * l + 1] << 64) | part[4 * l]);
-            Qt = ((fx_u128)part[4 * l + 3] << 64) | part[4 * l + 2];
+        for (int r = 0; r < CS; ++r) {
+            const uint64_t *p = cl.map_shared_rank(part + 4 * NW, r);
+            St += (fx_i128)(((fx_u128)p[1] << 64) | p[0]);
+            Qt += ((fx_u128)p[3] << 64) | p[2];
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint64_t slo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)St, o);
-            const uint64_t shi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(St >> 64), o);
-            const uint64_t qlo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)Qt, o);
-            const uint64_t qhi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(Qt >> 64), o);
-            St += (fx_i128)(((fx_u128)shi << 64) | slo);
-            Qt += ((fx_u128)qhi << 64) | qlo;
-        }
-        if (l == 0) fx_finish(C, St, Qt, count, E, mean, m2);
+        fx_finish(C, St, Qt, count, E, mean, m2);
     }
+    cl.sync();  // no block leaves while block 0 reads its sums
 }
 
 // Host mirror of chunk_moments_exact: the same bits for finite values. A
