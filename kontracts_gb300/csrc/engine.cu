@@ -111,8 +111,8 @@ double now_ms() {
 // ---------------------------------------------------------------------------
 __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 4)
     k_chunk_stats_exact(const double *__restrict__ vals, const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
-    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + 1];
-    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + 1)];
+    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + KX_STATS_CLUSTER];
+    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + KX_STATS_CLUSTER)];
     __shared__ double red[32];
     const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;  // the chunk of this cluster
     const ChunkDesc c = ch[q];

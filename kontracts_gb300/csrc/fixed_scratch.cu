@@ -91,8 +91,8 @@ static unsigned char *scratch(Ctx &c) {
 // instead of a descriptor table.
 __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 3)
     k_fixed_stats(const double *__restrict__ vals, uint64_t n, ChunkOut *__restrict__ out) {
-    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + 1];
-    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + 1)];
+    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + KX_STATS_CLUSTER];
+    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + KX_STATS_CLUSTER)];
     __shared__ double red[32];
     const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;
     const uint64_t begin = (uint64_t)q * KX_STATS_CHUNK;

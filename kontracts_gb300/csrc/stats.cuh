@@ -274,16 +274,28 @@ __device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a
     __syncthreads();  // red is free again
 }
 
+// Cluster barrier phases (PTX barrier.cluster): every thread of every block
+// of the cluster arrives, then waits for all of them. `release` / `acquire`
+// order the distributed shared memory writes before the barrier with the
+// reads after it.
+__device__ __forceinline__ void cluster_arrive_relaxed() { asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
 // chunk_moments_exact for prices by a cluster of CS blocks of NT threads:
 // block r of the cluster holds values r * NT * VPT .. (r + 1) * NT * VPT - 1
-// of the chunk in registers, VPT a thread, all loaded at once. The blocks
-// exchange their exponent maxima, then their sums, through distributed shared
-// memory (cluster barriers, no polling). A block of NT threads at 64
-// registers leaves room for 65536 / (64 NT) resident blocks a multiprocessor,
-// so one block's loads overlap another's integer work. Smem: `emax` NT/32 + 1
-// words, `part` 4 (NT/32 + 1) words, `red` 32 doubles (FP64 passes of a
-// non-finite chunk, run by block 0). mean and m2 are valid in thread 0 of
-// block 0 of the cluster.
+// of the chunk in registers, VPT a thread, all loaded at once. A block of NT
+// threads at 64 registers leaves room for 65536 / (64 NT) resident blocks a
+// multiprocessor, so one block's loads overlap another's integer work. The
+// blocks push their exponent maxima into every block's shared memory and
+// their sums into block 0's (distributed shared memory), so every read is
+// local and the other blocks leave while block 0 forms the result. Every
+// block passes the same three barrier phases: (A) all blocks have started
+// (arrived before the loads complete, waited on before the first remote
+// write), (B) every maximum is written, (C) every sum is written. Smem:
+// `emax` NW + CS words, `part` 4 (NW + CS) words, `red` 32 doubles (FP64
+// passes of a non-finite chunk, run by block 0). mean and m2 are valid in
+// thread 0 of block 0 of the cluster.
 template <int CS, int NT>
 __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__restrict__ v, uint32_t count,
                                                             uint32_t *emax, uint64_t *part, double *red, double &mean,
@@ -300,22 +312,27 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__rest
         const uint32_t i = base + threadIdx.x + (uint32_t)(k * NT);
         x[k] = i < count ? v[i] : 0.0;  // past the end: exponent field 0, excluded from the sums below
     }
+    cluster_arrive_relaxed();  // (A) this block has started
     uint32_t e = 0;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) e = max(e, fx_expo(x[k]));
     e = __reduce_max_sync(0xffffffffu, e);
     if (l == 0) emax[w] = e;
     __syncthreads();
+    cluster_wait_acquire();  // (A) every block has started: remote writes are safe
     if (w == 0) {
         const uint32_t t = __reduce_max_sync(0xffffffffu, l < NW ? emax[l] : 0u);
-        if (l == 0) emax[NW] = t;  // this block's maximum
+        if (l < CS) *cl.map_shared_rank(emax + NW + rank, l) = t;  // this block's maximum, to block l
     }
-    cl.sync();  // every block's maximum is written
+    cluster_arrive_release();
+    cluster_wait_acquire();  // (B) every maximum is in every block
     uint32_t E = 0;
-    for (int r = 0; r < CS; ++r) E = max(E, *cl.map_shared_rank(emax + NW, r));
+#pragma unroll
+    for (int r = 0; r < CS; ++r) E = max(E, emax[NW + r]);
     if (E == 0x7FFu) {  // an infinity or a NaN: block 0 runs the FP64 passes over the chunk
         if (rank == 0) chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);
-        cl.sync();  // no block leaves while another reads its maximum
+        cluster_arrive_relaxed();
+        cluster_wait_acquire();  // (C)
         return;
     }
     if (E == 0u) E = 1u;
@@ -347,25 +364,24 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__rest
             Q = ((fx_u128)part[4 * l + 3] << 64) | part[4 * l + 2];
         }
         fx_warp_sum(S, Q);
-        if (l == 0) {  // this block's sums
-            part[4 * NW] = (uint64_t)S;
-            part[4 * NW + 1] = (uint64_t)(S >> 64);
-            part[4 * NW + 2] = (uint64_t)Q;
-            part[4 * NW + 3] = (uint64_t)(Q >> 64);
+        if (l < 4) {  // this block's sums, to block 0
+            const uint64_t word = l == 0 ? (uint64_t)S : l == 1 ? (uint64_t)(S >> 64) : l == 2 ? (uint64_t)Q
+                                                                                                  : (uint64_t)(Q >> 64);
+            *cl.map_shared_rank(part + 4 * NW + 4 * rank + l, 0) = word;
         }
     }
-    cl.sync();  // every block's sums are written (and every maximum read)
+    cluster_arrive_release();
+    cluster_wait_acquire();  // (C) every block's sums are in block 0
     if (rank == 0 && threadIdx.x == 0) {
         fx_i128 St = 0;
         fx_u128 Qt = 0;
         for (int r = 0; r < CS; ++r) {
-            const uint64_t *p = cl.map_shared_rank(part + 4 * NW, r);
+            const uint64_t *p = part + 4 * NW + 4 * r;
             St += (fx_i128)(((fx_u128)p[1] << 64) | p[0]);
             Qt += ((fx_u128)p[3] << 64) | p[2];
         }
         fx_finish(C, St, Qt, count, E, mean, m2);
     }
-    cl.sync();  // no block leaves while block 0 reads its sums
 }
 
 // Host mirror of chunk_moments_exact: the same bits for finite values. A
