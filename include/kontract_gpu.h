@@ -257,10 +257,11 @@ kx_status kx_price_chunks(const kx_program *prog, const kx_model *model,
 kx_status kx_merge_chunks(const kx_chunk_stats *chunks, size_t n,
                           kx_price_result *out);
 /* The statistics of one chunk of n <= KX_STATS_CHUNK values (values[i], or
- * values[i] - subtrahend[i] when subtrahend is not NULL), on the host, bit for
- * bit as the device reduction computes them for finite values: exact integer
- * sums of the values in units of 2^-2 of the last mantissa bit of the chunk's
- * largest value, one rounding for the mean and at most two for M2. */
+ * values[i] - subtrahend[i] rounded to double when subtrahend is not NULL, as
+ * a multilevel difference), on the host, bit for bit as the device reduction
+ * computes them for finite values: exact integer sums of the values in units
+ * of 2^-2 of the last mantissa bit of the chunk's largest value, one or two
+ * roundings for the mean and for M2. */
 kx_status kx_chunk_moments(const double *values, const double *subtrahend,
                            uint32_t n, kx_chunk_stats *out);
 

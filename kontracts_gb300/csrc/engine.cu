@@ -103,11 +103,13 @@ double now_ms() {
 }
 
 // ---------------------------------------------------------------------------
-// Deterministic chunk statistics: each block takes one fixed chunk of values
-// and returns (n, mean, M2) by two passes (pricer.rs:303-328 uses two passes):
-// exact integer sums for prices (k_chunk_stats_exact, the chunk in registers
-// of a cluster of 4 blocks) and multilevel differences values[i] - values[stride + i]
-// (k_chunk_stats_diff); FP64 passes for weighted scenarios (k_chunk_stats).
+// Deterministic chunk statistics: each cluster of blocks takes one fixed chunk
+// of values and returns (n, mean, M2) from exact integer sums
+// (pricer.rs:303-328 takes two passes over the values; the integer sums give
+// its mean and M2 with one or two roundings): prices (k_chunk_stats_exact) and
+// estimators sum_s w[s] * vals[s * stride + i] formed per path in FP64
+// (k_chunk_stats: Greek estimators, variance-reduction corrections,
+// multilevel differences with w = {1, -1}).
 // ---------------------------------------------------------------------------
 __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 4)
     k_chunk_stats_exact(const double *__restrict__ vals, const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
@@ -116,43 +118,43 @@ __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_ST
     __shared__ double red[32];
     const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;  // the chunk of this cluster
     const ChunkDesc c = ch[q];
+    const double *v = vals + c.begin;
     double mean = 0.0, m2 = 0.0;
-    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>(vals + c.begin, c.count, emax, part, red, mean,
-                                                                     m2);
+    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>([&](uint32_t i) { return v[i]; }, c.count, emax,
+                                                                     part, red, mean, m2);
     if (blockIdx.x % KX_STATS_CLUSTER == 0 && threadIdx.x == 0) out[q] = ChunkOut{(double)c.count, mean, m2};
 }
 
-__global__ void __launch_bounds__(256) k_chunk_stats_diff(const double *__restrict__ vals, uint64_t stride,
-                                                          const ChunkDesc *__restrict__ ch,
-                                                          ChunkOut *__restrict__ out) {
+// NS: the scenario count when it is 2 (multilevel differences, two-point
+// estimators: the loads of a value unrolled and issued together), 0 for any
+// count ns <= 8.
+template <int NS>
+__global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 4)
+    k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns, const double *__restrict__ w,
+                  const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
+    __shared__ uint32_t emax[KX_STATS_THREADS / 32 + KX_STATS_CLUSTER];
+    __shared__ uint64_t part[4 * (KX_STATS_THREADS / 32 + KX_STATS_CLUSTER)];
     __shared__ double red[32];
-    const ChunkDesc c = ch[blockIdx.x];
-    double mean = 0.0, m2 = 0.0;
+    __shared__ double ww[8];
+    if (threadIdx.x < 8) ww[threadIdx.x] = (int)threadIdx.x < ns ? w[threadIdx.x] : 0.0;
+    __syncthreads();
+    const uint32_t q = blockIdx.x / KX_STATS_CLUSTER;
+    const ChunkDesc c = ch[q];
     const double *v = vals + c.begin;
-    chunk_moments_exact<2>(v, v + stride, c.count, red, mean, m2);
-    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
-}
-
-// Weighted scenarios (Greek estimators, variance-reduction corrections):
-// values sum_s w[s] * vals[s * stride + i] in FP64.
-__global__ void __launch_bounds__(256) k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns,
-                                                     const double *__restrict__ w, const ChunkDesc *__restrict__ ch,
-                                                     ChunkOut *__restrict__ out) {
-    __shared__ double red[32];
-    const ChunkDesc c = ch[blockIdx.x];
     double mean = 0.0, m2 = 0.0;
-    const double *v = vals + c.begin;
-    double ww[8];
-#pragma unroll
-    for (int s = 0; s < 8; ++s) ww[s] = s < ns ? w[s] : 0.0;
-    chunk_moments(
+    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>(
         [&](uint32_t i) {
             double x = ww[0] * v[i];
-            for (int s = 1; s < ns; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
+            if (NS > 0) {
+#pragma unroll
+                for (int s = 1; s < NS; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
+            } else {
+                for (int s = 1; s < ns; ++s) x = fma(ww[s], v[(uint64_t)s * stride + i], x);
+            }
             return x;
         },
-        c.count, red, mean, m2);
-    if (threadIdx.x == 0) out[blockIdx.x] = ChunkOut{(double)c.count, mean, m2};
+        c.count, emax, part, red, mean, m2);
+    if (blockIdx.x % KX_STATS_CLUSTER == 0 && threadIdx.x == 0) out[q] = ChunkOut{(double)c.count, mean, m2};
 }
 
 // The same statistics in compensated FP32 (KX_PREC_FP32_KAHAN): each path's
@@ -252,15 +254,11 @@ std::vector<Stats> device_stats(Ctx &c, const double *values, uint64_t stride, c
                 values, d_chunks + first[j], c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
-        } else if (nc && jobs[j].ns == 2 && jobs[j].w[0] == 1.0 && jobs[j].w[1] == -1.0) {  // multilevel pairs
-            k_chunk_stats_diff<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, d_chunks + first[j],
-                                                                   c.chunk_out.as<ChunkOut>() + first[j]);
-            KX_CUDA(cudaGetLastError());
-            c.last.kernel_launches++;
-        } else if (nc) {
-            k_chunk_stats<<<(unsigned)nc, 256, 0, c.stream>>>(values, stride, jobs[j].ns, d_w + j * 8,
-                                                              d_chunks + first[j],
-                                                              c.chunk_out.as<ChunkOut>() + first[j]);
+        } else if (nc) {  // weighted scenarios, multilevel differences
+            const int ns = jobs[j].ns;
+            auto kfn = ns == 2 ? k_chunk_stats<2> : k_chunk_stats<0>;
+            kfn<<<(unsigned)nc * KX_STATS_CLUSTER, KX_STATS_THREADS, 0, c.stream>>>(
+                values, stride, ns, d_w + j * 8, d_chunks + first[j], c.chunk_out.as<ChunkOut>() + first[j]);
             KX_CUDA(cudaGetLastError());
             c.last.kernel_launches++;
         }

@@ -98,7 +98,9 @@ __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_ST
     const uint64_t begin = (uint64_t)q * KX_STATS_CHUNK;
     const uint32_t count = (uint32_t)std::min<uint64_t>(KX_STATS_CHUNK, n - begin);
     double mean = 0.0, m2 = 0.0;
-    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>(vals + begin, count, emax, part, red, mean, m2);
+    const double *v = vals + begin;
+    chunk_moments_exact_cluster<KX_STATS_CLUSTER, KX_STATS_THREADS>([&](uint32_t i) { return v[i]; }, count, emax, part,
+                                                                     red, mean, m2);
     if (blockIdx.x % KX_STATS_CLUSTER == 0 && threadIdx.x == 0) out[q] = ChunkOut{(double)count, mean, m2};
 }
 

@@ -1,6 +1,7 @@
-// stats.cuh — pieces of the deterministic chunk statistics shared by the
-// reduction kernels: a chunk's (n, mean, M2) and the block-wide sum whose
-// summation order every reduction kernel follows.
+// stats.cuh — the deterministic chunk statistics shared by the reduction
+// kernels: a chunk's (n, mean, M2) from exact integer sums (device, by a
+// cluster of blocks, and its host mirror), and the FP64 passes kept for
+// chunks with non-finite values.
 #pragma once
 #include <algorithm>
 #include <cstdint>
@@ -51,12 +52,11 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
     return t;
 }
 
-// The two passes over one chunk: its mean, then the sum of squared deviations
-// from it (pricer.rs:303-328 also takes two passes). GB300's FP64 units are
-// few and the values are FP64, so the loops spend one FP64 operation per
-// value in the first pass and two in the second, and every thread keeps four
-// accumulators (values i, i + B, i + 2B, i + 3B of its stride, B the block
-// size) so that their adds overlap; the order of every sum is fixed.
+// The two FP64 passes over one chunk, by one block: its mean, then the sum of
+// squared deviations from it (pricer.rs:303-328 also takes two passes); four
+// accumulators a thread (values i, i + B, i + 2B, i + 3B of its stride, B the
+// block size), the order of every sum fixed. Used for chunks holding an
+// infinity or a NaN, where the integer sums below do not apply.
 template <class Val>
 __device__ __forceinline__ void chunk_moments(const Val &val, uint32_t count, double *red, double &mean, double &m2) {
     const uint32_t B = blockDim.x;
@@ -101,7 +101,7 @@ __device__ __forceinline__ void chunk_moments(const Val &val, uint32_t count, do
 // the mean C + S/n and M2 = Q - S^2/n, each rounded once or twice. Integer
 // sums do not depend on their order, so the result depends only on the
 // chunk's values, on any launch shape, and the host mirror below gives the
-// same bits. About 35 integer instructions per value replace the 3 FP64 ones.
+// same bits. About 35 integer instructions per value replace 3 FP64 ones.
 // Chunks holding an infinity or a NaN take the FP64 passes.
 // ---------------------------------------------------------------------------
 #if defined(__CUDACC__)
@@ -211,69 +211,6 @@ __device__ __forceinline__ void fx_warp_sum(fx_i128 &S, fx_u128 &Q) {
     }
 }
 
-// The exact statistics of one chunk of values a[i] (OPS 1) or a[i] - b[i]
-// (OPS 2, the difference taken exactly), 1 <= count <= KX_STATS_CHUNK, by one
-// block of at most 256 threads (whole warps), two passes over memory (the
-// multilevel differences; prices take chunk_moments_exact_cluster); `red`
-// holds 32 doubles. Pass 1 finds E, pass 2 sums. mean and m2 are valid in
-// thread 0.
-template <int OPS>
-__device__ __forceinline__ void chunk_moments_exact(const double *__restrict__ a, const double *__restrict__ b,
-                                                    uint32_t count, double *red, double &mean, double &m2) {
-    const uint32_t B = blockDim.x, nw = B >> 5;
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    uint32_t e = 0;
-#pragma unroll 4
-    for (uint32_t i = threadIdx.x; i < count; i += B) {
-        e = max(e, fx_expo(a[i]));
-        if (OPS == 2) e = max(e, fx_expo(b[i]));
-    }
-    e = __reduce_max_sync(0xffffffffu, e);
-    uint32_t *const ured = reinterpret_cast<uint32_t *>(red);
-    if (l == 0) ured[w] = e;
-    __syncthreads();
-    uint32_t E = 0;
-    for (uint32_t q = 0; q < nw; ++q) E = max(E, ured[q]);
-    __syncthreads();
-    if (E == 0x7FFu) {  // an infinity or a NaN: the FP64 passes give the IEEE result
-        if (OPS == 1) chunk_moments([&](uint32_t i) { return a[i]; }, count, red, mean, m2);
-        else chunk_moments([&](uint32_t i) { return a[i] - b[i]; }, count, red, mean, m2);
-        return;
-    }
-    if (E == 0u) E = 1u;  // zeros and subnormals only
-    auto fx = [&](uint32_t i) -> int64_t {
-        return OPS == 1 ? fx_value(a[i], E) : fx_value(a[i], E) - fx_value(b[i], E);
-    };
-    const int64_t C = fx(0);
-    fx_i128 S = 0;
-    fx_u128 Q = 0;
-#pragma unroll 4
-    for (uint32_t i = threadIdx.x; i < count; i += B) {
-        const int64_t d = fx(i) - C;
-        S += d;
-        Q += fx_square(d);
-    }
-    fx_warp_sum(S, Q);
-    uint64_t *const r64 = reinterpret_cast<uint64_t *>(red);  // 4 words per warp, 8 warps
-    if (l == 0) {
-        r64[4 * w] = (uint64_t)S;
-        r64[4 * w + 1] = (uint64_t)(S >> 64);
-        r64[4 * w + 2] = (uint64_t)Q;
-        r64[4 * w + 3] = (uint64_t)(Q >> 64);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        fx_i128 St = 0;
-        fx_u128 Qt = 0;
-        for (uint32_t q = 0; q < nw; ++q) {
-            St += (fx_i128)(((fx_u128)r64[4 * q + 1] << 64) | r64[4 * q]);
-            Qt += ((fx_u128)r64[4 * q + 3] << 64) | r64[4 * q + 2];
-        }
-        fx_finish(C, St, Qt, count, E, mean, m2);
-    }
-    __syncthreads();  // red is free again
-}
-
 // Cluster barrier phases (PTX barrier.cluster): every thread of every block
 // of the cluster arrives, then waits for all of them. `release` / `acquire`
 // order the distributed shared memory writes before the barrier with the
@@ -282,7 +219,9 @@ __device__ __forceinline__ void cluster_arrive_relaxed() { asm volatile("barrier
 __device__ __forceinline__ void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-// chunk_moments_exact for prices by a cluster of CS blocks of NT threads:
+// The exact statistics of one chunk of values val(i), 1 <= count <=
+// KX_STATS_CHUNK (a price, or an estimator formed per path in FP64 from
+// weighted scenarios), by a cluster of CS blocks of NT threads:
 // block r of the cluster holds values r * NT * VPT .. (r + 1) * NT * VPT - 1
 // of the chunk in registers, VPT a thread, all loaded at once. A block of NT
 // threads at 64 registers leaves room for 65536 / (64 NT) resident blocks a
@@ -296,10 +235,9 @@ __device__ __forceinline__ void cluster_wait_acquire() { asm volatile("barrier.c
 // `emax` NW + CS words, `part` 4 (NW + CS) words, `red` 32 doubles (FP64
 // passes of a non-finite chunk, run by block 0). mean and m2 are valid in
 // thread 0 of block 0 of the cluster.
-template <int CS, int NT>
-__device__ __forceinline__ void chunk_moments_exact_cluster(const double *__restrict__ v, uint32_t count,
-                                                            uint32_t *emax, uint64_t *part, double *red, double &mean,
-                                                            double &m2) {
+template <int CS, int NT, class Val>
+__device__ __forceinline__ void chunk_moments_exact_cluster(const Val &val, uint32_t count, uint32_t *emax,
+                                                            uint64_t *part, double *red, double &mean, double &m2) {
     constexpr int NW = NT / 32, VPT = (int)KX_STATS_CHUNK / (CS * NT);
     static_assert(VPT * CS * NT == (int)KX_STATS_CHUNK && NT % 32 == 0, "cluster shape");
     namespace cg = cooperative_groups;
@@ -310,7 +248,7 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__rest
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         const uint32_t i = base + threadIdx.x + (uint32_t)(k * NT);
-        x[k] = i < count ? v[i] : 0.0;  // past the end: exponent field 0, excluded from the sums below
+        x[k] = i < count ? val(i) : 0.0;  // past the end: exponent field 0, excluded from the sums below
     }
     cluster_arrive_relaxed();  // (A) this block has started
     uint32_t e = 0;
@@ -330,13 +268,13 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__rest
 #pragma unroll
     for (int r = 0; r < CS; ++r) E = max(E, emax[NW + r]);
     if (E == 0x7FFu) {  // an infinity or a NaN: block 0 runs the FP64 passes over the chunk
-        if (rank == 0) chunk_moments([&](uint32_t i) { return v[i]; }, count, red, mean, m2);
+        if (rank == 0) chunk_moments(val, count, red, mean, m2);
         cluster_arrive_relaxed();
         cluster_wait_acquire();  // (C)
         return;
     }
     if (E == 0u) E = 1u;
-    const int64_t C = fx_value(v[0], E);
+    const int64_t C = fx_value(val(0), E);  // value 0 of the chunk
     int64_t S1 = 0;  // |S1| < VPT * 2^56
     fx_u128 Q = 0;
 #pragma unroll
@@ -384,18 +322,16 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const double *__rest
     }
 }
 
-// Host mirror of chunk_moments_exact: the same bits for finite values. A
-// chunk with an infinity or a NaN gets the plain two-pass FP64 result, of the
-// same IEEE class as the device's.
+// Host mirror of chunk_moments_exact_cluster: the same bits for finite
+// values a[i], or a[i] - b[i] rounded to FP64 (as the device forms the
+// estimator of weights {1, -1}). A chunk with an infinity or a NaN gets the
+// plain two-pass FP64 result, of the same IEEE class as the device's.
 inline void chunk_moments_exact_host(const double *a, const double *b, uint32_t count, double &mean, double &m2) {
     mean = m2 = 0.0;
     if (count == 0) return;
-    uint32_t E = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-        E = std::max(E, fx_expo(a[i]));
-        if (b) E = std::max(E, fx_expo(b[i]));
-    }
     auto val = [&](uint32_t i) { return b ? a[i] - b[i] : a[i]; };
+    uint32_t E = 0;
+    for (uint32_t i = 0; i < count; ++i) E = std::max(E, fx_expo(val(i)));
     if (E == 0x7FFu) {
         double s = 0.0;
         for (uint32_t i = 0; i < count; ++i) s += val(i);
@@ -404,12 +340,11 @@ inline void chunk_moments_exact_host(const double *a, const double *b, uint32_t 
         return;
     }
     if (E == 0u) E = 1u;
-    auto fx = [&](uint32_t i) -> int64_t { return b ? fx_value(a[i], E) - fx_value(b[i], E) : fx_value(a[i], E); };
-    const int64_t C = fx(0);
+    const int64_t C = fx_value(val(0), E);
     fx_i128 S = 0;
     fx_u128 Q = 0;
     for (uint32_t i = 0; i < count; ++i) {
-        const int64_t d = fx(i) - C;
+        const int64_t d = fx_value(val(i), E) - C;
         S += d;
         Q += fx_square(d);
     }

@@ -91,17 +91,16 @@ def test_single_value_and_empty_chunk(lib):
     assert (out.n, out.mean, out.m2) == (0.0, 0.0, 0.0)
 
 
-def test_difference_mode_sums_the_exact_differences(lib):
+def test_difference_mode_takes_the_fp64_differences(lib):
+    """values - subtrahend: each difference rounded to FP64 (the per-path
+    multilevel difference P_fine - P_coarse the oracle forms), then the exact
+    statistics of those differences."""
     r = np.random.default_rng(3)
     fine = r.normal(10.0, 4.0, CHUNK)
     coarse = fine + r.normal(0.0, 0.05, CHUNK)
     n, mean, m2 = _moments(lib, fine, coarse)
-    fr = [Fraction(float(x)) - Fraction(float(y)) for x, y in zip(fine, coarse)]
-    em = sum(fr) / len(fr)
-    e2 = sum((x - em) ** 2 for x in fr)
-    assert abs(Fraction(mean) - em) <= Fraction(3 * 2.0 ** -52 * abs(float(em))) + Fraction(_unit(fine) * 2)
-    assert abs(Fraction(m2) - e2) <= Fraction(4 * 2.0 ** -52 * float(e2)) + Fraction(
-        2 * math.sqrt(CHUNK * float(e2)) * _unit(fine) * 2)
+    assert (n, mean, m2) == _moments(lib, fine - coarse)
+    _check(fine - coarse, mean, m2)
 
 
 def test_result_does_not_depend_on_value_order(lib):
