@@ -127,9 +127,9 @@ __global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_ST
 
 // NS: the scenario count when it is 2 (multilevel differences, two-point
 // estimators: the loads of a value unrolled and issued together), 0 for any
-// count ns <= 8.
+// count ns <= 8. 3 blocks per SM: the scenario operands take registers.
 template <int NS>
-__global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 4)
+__global__ void __cluster_dims__(KX_STATS_CLUSTER, 1, 1) __launch_bounds__(KX_STATS_THREADS, 3)
     k_chunk_stats(const double *__restrict__ vals, uint64_t stride, int ns, const double *__restrict__ w,
                   const ChunkDesc *__restrict__ ch, ChunkOut *__restrict__ out) {
     __shared__ uint32_t emax[KX_STATS_THREADS / 32 + KX_STATS_CLUSTER];
@@ -282,9 +282,13 @@ Stats merge_chunks(const ChunkOut *h, size_t n) {
         const ChunkOut &o = h[q];
         if (s.n == 0) { s.n = o.n; s.mean = o.mean; s.m2 = o.m2; continue; }
         const double tn = s.n + o.n;
-        const double d = o.mean - s.mean;
-        s.mean = s.mean + d * (o.n / tn);
-        s.m2 = s.m2 + o.m2 + d * d * (s.n * o.n / tn);
+        if (o.mean == s.mean) {  // d = 0: the same result, and equal infinite means stay infinite
+            s.m2 = s.m2 + o.m2;  // (as the reference's one-pass mean, pricer.rs:303-328)
+        } else {
+            const double d = o.mean - s.mean;
+            s.mean = s.mean + d * (o.n / tn);
+            s.m2 = s.m2 + o.m2 + d * d * (s.n * o.n / tn);
+        }
         s.n = tn;
     }
     return s;

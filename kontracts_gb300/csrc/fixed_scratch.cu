@@ -239,17 +239,7 @@ extern "C" kx_status kx_price_fixed_scratch(const kx_program *prog, const kx_mod
         if (err & KX_ERR_LOOKAHEAD)
             raise(KX_UNSUPPORTED, "an average window is read before it closes (look-ahead average)");
         if (err & KX_ERR_MALFORMED) raise(KX_MALFORMED_CONTRACT, "average window inverted or empty at an evaluation date");
-        Stats s;
-        for (uint64_t q = 0; q < nc; ++q) {  // Chan et al. pairwise merge, chunk order (as kx_price)
-            const ChunkOut &o = h[q];
-            if (s.n == 0) { s.n = o.n; s.mean = o.mean; s.m2 = o.m2; continue; }
-            const double tn = s.n + o.n;
-            const double dd = o.mean - s.mean;
-            s.mean = s.mean + dd * (o.n / tn);
-            s.m2 = s.m2 + o.m2 + dd * dd * (s.n * o.n / tn);
-            s.n = tn;
-        }
-        *out = finish(s);
+        *out = finish(merge_chunks(h, nc));  // chunk order, as kx_price
         end_call(c);
     });
 }

@@ -275,16 +275,26 @@ __device__ __forceinline__ void chunk_moments_exact_cluster(const Val &val, uint
     }
     if (E == 0u) E = 1u;
     const int64_t C = fx_value(val(0), E);  // value 0 of the chunk
+    // d = dh 2^29 + dl (0 <= dl < 2^29, |dh| < 2^27 as |d| < 2^56): d^2 = dl^2 +
+    // 2^30 dl dh + 2^58 dh^2, each product a 32 x 32 -> 64 multiply-add into a
+    // 64-bit sum that VPT <= 16 values cannot overflow (< 2^62)
+    static_assert(VPT <= 16, "64-bit partial sums of the squares");
     int64_t S1 = 0;  // |S1| < VPT * 2^56
-    fx_u128 Q = 0;
+    uint64_t qll = 0;
+    int64_t qlh = 0, qhh = 0;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
         if (base + threadIdx.x + (uint32_t)(k * NT) < count) {
             const int64_t d = fx_value(x[k], E) - C;
             S1 += d;
-            Q += fx_square(d);
+            const uint32_t dl = (uint32_t)d & 0x1FFFFFFFu;
+            const int32_t dh = (int32_t)(d >> 29);
+            qll += (uint64_t)dl * dl;
+            qlh += (int64_t)dh * (int32_t)dl;
+            qhh += (int64_t)dh * dh;
         }
     }
+    fx_u128 Q = (fx_u128)((fx_i128)qll + ((fx_i128)qlh << 30) + ((fx_i128)qhh << 58));
     fx_i128 S = S1;
     fx_warp_sum(S, Q);
     if (l == 0) {

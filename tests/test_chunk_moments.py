@@ -136,3 +136,14 @@ def test_agrees_with_two_pass_fp64_on_prices(lib):
     m = vals.mean()
     assert abs(mean - m) <= 1e-14 * abs(m)
     assert abs(m2 - ((vals - m) ** 2).sum()) <= 1e-13 * m2
+
+
+def test_merge_of_equal_infinite_means_stays_infinite(lib):
+    """Chunks whose means are both +inf merge to +inf (the reference's one-pass
+    mean of infinite values), with a NaN spread; equal finite means merge as
+    the Chan update with d = 0."""
+    from kontracts_gb300 import sharded
+    r = sharded.merge([(16384.0, math.inf, math.nan), (16384.0, math.inf, math.nan)])
+    assert r.price == math.inf and math.isnan(r.std_error)
+    a = sharded.merge([(4.0, 2.5, 1.0), (4.0, 2.5, 3.0)])
+    assert a.price == 2.5 and a.std_error == math.sqrt(4.0 / 7.0) / math.sqrt(8.0)
