@@ -773,17 +773,27 @@ PathPlan plan_paths(std::vector<Job> &jobs, const kx_mc_config &cfg, int ns, int
     }
     item = (item + 31) / 32 * 32;
     P.item_paths = item;
-    // arithmetic items: per contract in launch order, its item count
+    // arithmetic items: per contract in launch order, its item count. The last
+    // contract's last paths go out in items of 32 (a path per lane), about one
+    // such item per resident warp: when the queue runs dry the warps hold at
+    // most a path a lane instead of a whole item, so they finish together.
+    const uint64_t small = 32, tail = warps_total * small;
     const size_t nc = jobs.size();
     P.item_idx.assign(2 * nc + 1, 0u);
     uint64_t n_items = 0;
     for (size_t q = 0; q < nc; ++q) {
         const int ci = order[q];
-        P.cons[ci].item_paths = (uint32_t)item;
-        P.cons[ci].path_base = jobs[ci].path_base;
+        ContractDev &C = P.cons[ci];
+        const uint64_t n = C.n_paths;
+        const uint64_t big = q + 1 < nc || n <= tail ? (n + item - 1) / item : (n - tail) / item;
+        C.item_paths = (uint32_t)item;
+        C.item_big = (uint32_t)big;
+        C.item_small = (uint32_t)small;
+        C.path_base = jobs[ci].path_base;
         P.item_idx[q] = (uint32_t)n_items;
         P.item_idx[nc + 1 + q] = (uint32_t)ci;
-        n_items += (P.cons[ci].n_paths + item - 1) / item;
+        const uint64_t rest = n > big * item ? n - big * item : 0;
+        n_items += big + (rest + small - 1) / small;
     }
     P.item_idx[nc] = (uint32_t)n_items;
     if (n_items >= (1ull << 31)) raise(KX_INVALID_ARGUMENT, "too many work items in one launch");

@@ -51,12 +51,13 @@ struct ContractDev {
     float s0f[KX_MAX_NS], driftf[KX_MAX_NS], sigmaf[KX_MAX_NS];
     double v0, kappa, theta, sigma_v, rho, rho_perp, r, inv_w;
     float v0f, kappaf, thetaf, sigma_vf, rhof, rho_perpf, rf, inv_wf;
-    uint32_t item_paths;  // paths per work item of this contract (arithmetic items)
+    uint32_t item_paths;  // paths per work item of this contract (arithmetic items) ...
+    uint32_t item_big;    // ... for its first item_big items; the rest of item_small paths
+    uint32_t item_small;  // (the launch's last contract ends in small items: a short tail)
     uint32_t path_base;   // index of its first path in the stream
     // M_MULTI: factors (s0 / drift / sigma above hold factor i at index i) and the
     // packed lower Cholesky factor of their correlation, row i at i (i + 1) / 2
     int32_t n_assets;
-    int32_t pad_assets;
     double chol[KX_MAX_NS * (KX_MAX_NS + 1) / 2];
     float cholf[KX_MAX_NS * (KX_MAX_NS + 1) / 2];
 };
@@ -90,7 +91,8 @@ struct PathArgs {
     const void *statics; // StaticDev per contract (static-schedule launches of k_lean)
     // Arithmetic work items (when `items` is null): the contracts in launch
     // order `item_order[0..n_order)`, contract item_order[q] owning items
-    // item_start[q] .. item_start[q + 1] - 1 of item_paths paths each.
+    // item_start[q] .. item_start[q + 1] - 1 (item_big of item_paths paths,
+    // then item_small paths each).
     const uint32_t *item_start;
     const int32_t *item_order;
     uint32_t n_order;
@@ -112,9 +114,17 @@ __device__ __forceinline__ WorkItem fetch_item(const PathArgs &A, int it) {
     }
     const int c = A.item_order[lo];
     const ContractDev &C = A.cons[c];
-    const uint64_t local = (uint64_t)((uint32_t)it - A.item_start[lo]) * C.item_paths;
+    const uint32_t j = (uint32_t)it - A.item_start[lo];
+    uint64_t local, cnt;
+    if (j < C.item_big) {
+        local = (uint64_t)j * C.item_paths;
+        cnt = C.item_paths;
+    } else {
+        local = (uint64_t)C.item_big * C.item_paths + (uint64_t)(j - C.item_big) * C.item_small;
+        cnt = C.item_small;
+    }
     const uint64_t left = C.n_paths - local;
-    return WorkItem{c, 0, (uint64_t)C.path_base + local, left < C.item_paths ? left : (uint64_t)C.item_paths};
+    return WorkItem{c, 0, (uint64_t)C.path_base + local, left < cnt ? left : cnt};
 }
 
 // Path models of k_paths. The _PAIR models are the coarse paths of a
