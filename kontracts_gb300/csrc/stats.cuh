@@ -96,13 +96,15 @@ __device__ __forceinline__ void chunk_moments(const Val &val, uint32_t count, do
 // exponent field e of the value (truncated toward zero when e < E - FX_GUARD,
 // i.e. an error below 2^-54 of the chunk's largest value; exact otherwise).
 // Deviations d = X - C from the chunk's first value C are summed exactly,
-// S = sum d in 128 bits and Q = sum d^2 in unsigned 128 bits (|d| < 2^57 and
-// at most 2^14 values, so neither overflows), and one thread turns them into
-// the mean C + S/n and M2 = Q - S^2/n, each rounded once or twice. Integer
-// sums do not depend on their order, so the result depends only on the
-// chunk's values, on any launch shape, and the host mirror below gives the
-// same bits. About 35 integer instructions per value replace 3 FP64 ones.
-// Chunks holding an infinity or a NaN take the FP64 passes.
+// S = sum d in 128 bits and Q = sum d^2 in unsigned 128 bits (|X| < 2^55, so
+// |d| < 2^56, and at most 2^14 values: neither overflows), and one thread
+// turns them into the mean C + S/n and M2 = Q - S^2/n, each rounded once or
+// twice. Integer sums do not depend on their order, so the result depends
+// only on the chunk's values, on any launch shape, and the host mirror below
+// gives the same bits. About 25 integer instructions per value (the squares'
+// products as multiply-adds on the FMA pipe, the rest on the ALU pipe)
+// replace 3 FP64 ones. Chunks holding an infinity or a NaN take the FP64
+// passes.
 // ---------------------------------------------------------------------------
 #if defined(__CUDACC__)
 #define KX_HD __host__ __device__
