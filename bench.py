@@ -570,7 +570,9 @@ def heston_book(reps=3) -> dict:
     {0.5, 1, 2}, full truncation, 252 steps a year, 2,000,000 paths, FP32, all
     96 contracts on one shared simulation (price_batch); plus the pathwise
     adjoint sensitivities (s0, v0, kappa, theta, sigma_v, rho) of the T = 1,
-    K = 100 call with a checkpoint every 16 steps."""
+    K = 100 call with a checkpoint every 16 steps, of all 96 calls each on its
+    own paths (portfolio adjoint), and of all 96 calls on the book's shared
+    simulation (tangent mode)."""
     import kontracts_gb300 as kx
     h = kx.heston(100.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.05, asset="S", scheme="full_truncation")
     ks = [80.0 + 40.0 * i / 31 for i in range(32)]
@@ -608,6 +610,19 @@ def heston_book(reps=3) -> dict:
                 "seconds": tb, "contracts_per_s": len(book) / tb,
                 "path_steps_per_s": sum(nb * (len(c.time_grid(252)) - 1) for c in book) / tb,
                 "d_s0_T1_K100": sens[32 + 15].d_s0, "d_v0_T1_K100": sens[32 + 15].d_v0}
+    # the same price + sensitivities of all 96 calls on the book's one shared 2M-path simulation
+    # (kx_price_batch_sens: the tangents of y and v carried forward, one pass for the whole book)
+    ts = None
+    for _ in range(reps):
+        res_s, sens_s = kx.price_batch(book, h, n_paths=n, seed=42, steps_per_year=252, greeks=True)
+        t = _dev_seconds(kx)
+        ts = t if ts is None or t < ts else ts
+    book_sens = {"workload": "price + (s0, v0, kappa, theta, sigma_v, rho, r) sensitivities of all 96 calls on the "
+                             "book's shared 2M-path simulation (kx_price_batch_sens, tangent mode), FP32",
+                 "seconds": ts, "contracts_per_s": len(book) / ts, "over_price_only": ts / best,
+                 "prices_equal_price_batch": all(a_.price == b_.price for a_, b_ in zip(res_s, res)),
+                 "d_s0_T1_K100": sens_s[32 + 15].d_s0, "d_v0_T1_K100": sens_s[32 + 15].d_v0,
+                 "d_kappa_T1_K100": sens_s[32 + 15].d_kappa, "se_v0_T1_K100": sens_s[32 + 15].se_v0}
     return {"workload": "96 Heston calls (32 strikes x 3 maturities) on one 2M-path simulation, full truncation, "
                         "252 steps/yr, FP32", "seconds": best, "path_steps_per_s": steps / best,
             "contracts_per_s": len(book) / best, "price_T1_K100": res[32 + 15].price,
@@ -619,7 +634,7 @@ def heston_book(reps=3) -> dict:
             "adjoint_T1_K100": {"seconds": ta, "price": a.price, "d_s0": a.d_s0, "d_v0": a.d_v0,
                                 "d_kappa": a.d_kappa, "d_theta": a.d_theta, "d_sigma_v": a.d_sigma_v,
                                 "d_rho": a.d_rho, "se_v0": a.se_v0, "checkpoint_every": 16},
-            "adjoint_book_96": book_adj}
+            "adjoint_book_96": book_adj, "sens_book_96_shared": book_sens}
 
 
 def book_256(reps=5) -> dict:

@@ -290,6 +290,23 @@ kx_status kx_price_batch_shared(size_t n, const kx_program *const *progs,
                                 const kx_model *model, const kx_mc_config *cfg,
                                 kx_price_result *out);
 
+/* kx_price_batch_shared with pathwise sensitivities (no reference
+ * counterpart; the adjoint of greeks.rs:60-98's quantities on the shared
+ * simulation): for a book whose contracts each pay one call, put or constant
+ * amount at a fixed date (Europeans), the derivatives of the log-spot and of
+ * the variance in every model parameter are carried forward along the shared
+ * paths, and each contract's sensitivities are its payoff's derivative times
+ * them at its date: d/ds0, d/dr (drift and discount together) and GBM
+ * d/dsigma or Heston d/dv0, d/dkappa, d/dtheta, d/dsigma_v, d/drho, each with
+ * its standard error; out[i] and sens[i].price are the prices of
+ * kx_price_batch_shared. The derivatives are the pathwise ones of
+ * kx_greeks_adjoint on the same paths (one forward pass for the whole book
+ * instead of a reverse sweep per contract). Other contracts: KX_UNSUPPORTED
+ * (kx_price_portfolio values any book with sensitivities). */
+kx_status kx_price_batch_sens(size_t n, const kx_program *const *progs,
+                              const kx_model *model, const kx_mc_config *cfg,
+                              kx_price_result *out, kx_sens *sens);
+
 /* Uneven portfolio in one persistent launch over a (contract, path-block)
  * work queue: each contract has its own model and config (its own grid,
  * n_paths and seed). Optional per-contract pathwise delta / vega (`sens`,

@@ -698,14 +698,22 @@ def fit_gbm_volatility(contract: Contract, maturities: Sequence[float], market_p
 
 
 def price_batch(contracts: Sequence[Contract], model, n_paths: int = 100_000, seed: int = 42,
-                steps_per_year: int = 50, *, precision: str = "fp32") -> list[PriceResult]:
-    """price_batch_gbm (src/pricer.rs:250-294): every contract on the same paths."""
+                steps_per_year: int = 50, *, precision: str = "fp32", greeks: bool = False):
+    """price_batch_gbm (src/pricer.rs:250-294): every contract on the same paths.
+    With greeks=True (a book of Europeans: each contract pays one call, put or
+    constant at a fixed date) also returns every contract's pathwise
+    Sensitivities, from one forward pass over the shared paths."""
     if not contracts:
-        return []
+        return ([], []) if greeks else []
     hs = (C.c_void_p * len(contracts))(*[c._handle().h.value for c in contracts])
     cm = model._c()
     cfg = _cfg(n_paths, seed, steps_per_year, model.rate, precision, False)
     out = (_abi.KxPriceResult * len(contracts))()
+    if greeks:
+        sens = (_abi.KxSens * len(contracts))()
+        with _lock:
+            _check(_lib().kx_price_batch_sens(len(contracts), hs, C.byref(cm), C.byref(cfg), out, sens))
+        return [PriceResult(r) for r in out], [Sensitivities(s) for s in sens]
     with _lock:
         _check(_lib().kx_price_batch_shared(len(contracts), hs, C.byref(cm), C.byref(cfg), out))
     return [PriceResult(r) for r in out]

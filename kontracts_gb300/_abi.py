@@ -176,6 +176,8 @@ SIGNATURES = {
                                          C.POINTER(KxPriceResult), C.POINTER(C.c_double)]),
     "kx_price_batch_shared": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
                                         C.POINTER(KxMcConfig), C.POINTER(KxPriceResult)]),
+    "kx_price_batch_sens": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel), C.POINTER(KxMcConfig),
+                                      C.POINTER(KxPriceResult), C.POINTER(KxSens)]),
     "kx_price_portfolio": (C.c_int, [C.c_size_t, C.POINTER(_P), C.POINTER(KxModel),
                                      C.POINTER(KxMcConfig), C.POINTER(KxPriceResult),
                                      C.POINTER(KxSens)]),

@@ -122,6 +122,143 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pathwise sensitivities of a book of European flows on the shared simulation
+// (kx_price_batch_sens). Every contract pays one closed-form amount A(S) at a
+// time-only date t, so its derivative in a parameter p is
+// df * A'(S) * S * dy_t/dp (y the log-spot): the derivatives of y and of the
+// variance v in each parameter are carried forward along the path (tangent
+// mode), and every contract paid at a step takes them from there. For many
+// contracts on one simulation this replaces one reverse sweep per contract
+// (kx_greeks_adjoint) by a single forward pass; the derivative is the same
+// pathwise one, term for term (the reverse sweep of adjoint.cu transposed):
+//   GBM:    dy/dsigma += -sigma dt + sqrt(dt) z;                 dy/dr = t
+//   Heston: vp = max(v, 0) (full truncation) or v, m = 0 where the truncation
+//           bites, sqv = sqrt(vp), mix = rho z1 + rho_perp z2:
+//           dy' = dy + (-dt/2 + z1 sq / (2 sqv)) m dv
+//           dv' = keep * ((1 + (-kappa dt + sigma_v mix sq / (2 sqv)) m) dv + c_p)
+//           c_v0 = 0, c_kappa = (theta - vp) dt, c_theta = kappa dt,
+//           c_sigma_v = sqv mix sq, c_rho = sigma_v sqv (z1 + drho_perp/drho z2) sq,
+//           keep = 0 where the reference scheme's floor bit (v' = 0), dv_0/dv0 = 1.
+// Outputs per contract and path, [q][contract][path]: q = 0 d/ds0 (dS/ds0 =
+// S/s0), 1 d/dr (drift dy/dr = t and the discount -t pv, as greeks.rs:70 moves
+// both), then GBM d/dsigma | Heston d/dv0, d/dkappa, d/dtheta, d/dsigma_v,
+// d/drho.
+// ---------------------------------------------------------------------------
+struct SensArgs {
+    FlowArgs F;              // the simulation and its flows; F.pv: the prices
+    const double *times;     // grid times
+    const void *dtq;         // StepRec<Real> {dt, sqrt(dt)} of every step (GBM's volatility tangent)
+    double *dv;              // the derivative outputs
+    double inv_s0, sigma, drp;
+};
+
+template <class Real, int NP>
+__device__ __forceinline__ void pay_flows_sens(const SensArgs &S, int k, Real Sk, const Real (&ty)[NP], uint64_t path,
+                                               Real inv_s0) {
+    const FlowArgs &A = S.F;
+    const double df = A.disc[k], tk = S.times[k];
+    const uint64_t np = A.n_paths, rows = (uint64_t)A.n_contracts * np;
+    for (int f = A.first[k]; f < A.first[k + 1]; ++f) {
+        const FlowRec &F = A.flows[f];
+        const Real sg = flow_sign<Real>(F), K = flow_a<Real>(F);
+        Real amt, damt;  // the amount and its derivative in the spot
+        if (F.kind == FK_CALL) {
+            amt = sg * fmax(Sk - K, Real(0));
+            damt = Sk > K ? sg : Real(0);
+        } else if (F.kind == FK_PUT) {
+            amt = sg * fmax(K - Sk, Real(0));
+            damt = K > Sk ? -sg : Real(0);
+        } else {
+            amt = sg;
+            damt = Real(0);
+        }
+        const double pv = (double)amt * df;
+        const uint64_t o = (uint64_t)F.contract * np + path;
+        A.pv[o] = pv;
+        const Real g = damt * Sk * (Real)df;  // d pv / d y
+        S.dv[o] = (double)(g * inv_s0);
+        S.dv[rows + o] = (double)(g * (Real)tk) - tk * pv;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) S.dv[(2 + p) * rows + o] = (double)(g * ty[p]);
+    }
+}
+
+template <class Real, int MODEL>
+__global__ void __launch_bounds__(256) k_flows_sens(const SensArgs S) {
+    const FlowArgs &A = S.F;
+    constexpr bool HESTON = MODEL == KX_MODEL_HESTON;
+    constexpr int DRAWS = HESTON ? 2 : 1, NP = HESTON ? 5 : 1;
+    const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+    const StepRec<Real> *Q = reinterpret_cast<const StepRec<Real> *>(S.dtq);
+    const Real s0 = (Real)A.s0, r = (Real)A.r, kap = (Real)A.kappa, th = (Real)A.theta, sv = (Real)A.sigma_v,
+               rho = (Real)A.rho, rp = (Real)A.rho_perp, drp = (Real)S.drp, sig = (Real)S.sigma,
+               inv_s0 = (Real)S.inv_s0;
+    const bool ft = A.scheme == KX_HESTON_FULL_TRUNCATION;
+    for (uint64_t path = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; path < A.n_paths;
+         path += (uint64_t)gridDim.x * blockDim.x) {
+        Real y = Real(0), v = (Real)fmax(A.v0, 0.0);
+        Real ty[NP], tv[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) ty[p] = tv[p] = Real(0);
+        if (HESTON) tv[0] = A.v0 > 0.0 ? Real(1) : Real(0);  // dv_0 / dv0
+        int nf = A.next[0];
+        if (nf == 0) {
+            pay_flows_sens<Real, NP>(S, 0, s0, ty, path, inv_s0);
+            nf = A.next[1];
+        }
+        constexpr int SPB = 4 / DRAWS;
+        for (int k = 1; k < A.n_times; k += SPB) {
+            const uint64_t d = (uint64_t)(k - 1) * DRAWS;
+            Real z[4];
+            if (A.z64 == nullptr && A.z32 == nullptr) {
+                const uint4 w = philox4x32_10(make_uint4((uint32_t)(d >> 2), (uint32_t)path, (uint32_t)(path >> 32), 0u),
+                                              (uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+                box_muller(w.x, w.y, z[0], z[1]);
+                box_muller(w.z, w.w, z[2], z[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    z[j] = d + j < A.z_dpp ? (A.z64 ? (Real)A.z64[path * A.z_dpp + d + j] : (Real)A.z32[path * A.z_dpp + d + j])
+                                           : Real(0);
+            }
+#pragma unroll
+            for (int j = 0; j < SPB; ++j) {
+                const int kk = k + j;
+                if (kk >= A.n_times) break;
+                const StepRec<Real> rec = R[kk];
+                if (!HESTON) {
+                    const StepRec<Real> q = Q[kk];
+                    ty[0] += -sig * q.c0 + q.c1 * z[j];
+                    y = gbm_step(y, rec.c0, rec.c1, z[j]);
+                } else {
+                    const Real z1 = z[2 * j], z2 = z[2 * j + 1], dt = rec.c0, sq = rec.c1;
+                    const Real vp = ft ? fmax(v, Real(0)) : v;
+                    const Real m = (ft && v <= Real(0)) ? Real(0) : Real(1);
+                    const Real sqv = sqrt(vp);
+                    const Real dsq = sqv > Real(0) ? Real(0.5) / sqv : Real(0);
+                    const Real mix = rho * z1 + rp * z2;
+                    const Real dx_dv = (Real(-0.5) * dt + z1 * sq * dsq) * m;
+                    const Real dvn_dv = Real(1) + (-kap * dt + sv * mix * sq * dsq) * m;
+                    const Real cp[5] = {Real(0), (th - vp) * dt, kap * dt, sqv * mix * sq,
+                                        sv * sqv * (z1 + drp * z2) * sq};
+                    heston_step<Real>(r, kap, th, sv, rho, rp, A.scheme, dt, sq, z1, z2, y, v);
+                    const Real keep = (ft || v > Real(0)) ? Real(1) : Real(0);
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        ty[p] += dx_dv * tv[p];
+                        tv[p] = keep * (dvn_dv * tv[p] + cp[p]);
+                    }
+                }
+                if (kk == nf) {
+                    pay_flows_sens<Real, NP>(S, kk, spot_of<Real>(s0, y), ty, path, inv_s0);
+                    nf = A.next[kk + 1];
+                }
+            }
+        }
+    }
+}
+
 // Amount kind of a flow slot from its lowered code (host).
 static FlowRec classify(const KxProgram &P, int leaf) {
     const KxLeaf &L = P.leaf[leaf];
@@ -137,6 +274,11 @@ static FlowRec classify(const KxProgram &P, int leaf) {
     f.code_len = L.code_len;
     const KxIns *c = P.code + L.code_off;
     int n = L.code_len;
+    if ((n == 1 || (n == 2 && c[1].op == OP_NEG)) && c[0].op == OP_CONST) {  // a constant amount as code
+        f.kind = FK_CONST;
+        f.sign = n == 2 ? -P.cpool[c[0].arg] : P.cpool[c[0].arg];
+        return f;
+    }
     double sign = 1.0;
     if (n == 6 && c[5].op == OP_NEG) {
         sign = -1.0;
@@ -161,6 +303,176 @@ static const void *flows_kernel() {
     return reinterpret_cast<const void *>(&k_flows<Real, MODEL>);
 }
 
+// A book on one shared simulation (price_batch_gbm, pricer.rs:250-294): the
+// merged grid, each contract bound to it, and the split into contracts with
+// static flow schedules (valued on the shared simulation by k_flows) and the
+// rest (the general path kernel on the same grid and seed).
+struct SharedBook {
+    Model m;
+    std::vector<double> grid;
+    std::vector<KxProgram> bound;
+    std::vector<StepTables> tabs;
+    std::vector<StaticSchedule> sched;
+    std::vector<size_t> stat, dyn;
+};
+
+static SharedBook shared_book(size_t n, const kx_program *const *progs, const kx_model *model,
+                              const kx_mc_config *cfg) {
+    SharedBook B;
+    B.m = model_from_c(model);
+    if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
+    if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
+    if (cfg->flags != 0) raise(KX_INVALID_ARGUMENT, "flags must be 0");
+    if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
+    validate_model(B.m);
+    // merged plan (pricer.rs:260-279)
+    Plan merged;
+    for (size_t i = 0; i < n; ++i) {
+        const Program &p = program_of(progs[i]);
+        merged.fixed_dates.insert(merged.fixed_dates.end(), p.plan.fixed_dates.begin(), p.plan.fixed_dates.end());
+        merged.horizon = std::max(merged.horizon, p.plan.horizon);
+        merged.needs_fine_grid = merged.needs_fine_grid || p.plan.needs_fine_grid;
+    }
+    B.grid = time_grid_forced(merged, cfg->steps_per_year, B.m.requires_fine_grid());
+    validate_grid(B.grid);
+    // split: static schedules share one simulation, the rest use the path kernel
+    B.bound.resize(n);
+    B.tabs.resize(n);
+    B.sched.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        const Program &p = program_of(progs[i]);
+        bind(p.low, B.grid, B.m, cfg->rate, B.bound[i], B.tabs[i]);
+        B.sched[i] = static_schedule(B.bound[i], B.tabs[i]);
+        bool ok = B.sched[i].static_ok && B.bound[i].n_acc == 0;
+        for (auto &f : B.sched[i].flows) ok = ok && f.price_untils == 0;
+        (ok ? B.stat : B.dyn).push_back(i);
+    }
+    return B;
+}
+
+// The flows of the static contracts by step: the flows paid at step k are
+// flows[first[k] .. first[k + 1]), next[k] the first step >= k with flows.
+struct FlowTable {
+    std::vector<KxProgram> progs;
+    std::vector<FlowRec> flows;
+    std::vector<int> first, next;
+    bool all_single = true;  // every contract has exactly one flow
+};
+
+static FlowTable flow_table(const SharedBook &B) {
+    const int nt = (int)B.grid.size();
+    FlowTable T;
+    std::vector<std::vector<FlowRec>> at(nt);
+    for (size_t q = 0; q < B.stat.size(); ++q) {
+        const size_t i = B.stat[q];
+        T.progs.push_back(B.bound[i]);
+        for (auto &f : B.sched[i].flows) {
+            FlowRec r = classify(B.bound[i], f.leaf);
+            r.contract = (int)q;
+            r.prog = (int)q;
+            r.only = B.sched[i].flows.size() == 1 ? 1 : 0;
+            r.af = (float)r.a;
+            r.signf = (float)r.sign;
+            at[f.step].push_back(r);
+        }
+        T.all_single = T.all_single && B.sched[i].flows.size() == 1;
+    }
+    T.first.resize(nt + 1);
+    T.next.resize(nt + 1);
+    for (int k = 0; k < nt; ++k) {
+        T.first[k] = (int)T.flows.size();
+        T.flows.insert(T.flows.end(), at[k].begin(), at[k].end());
+    }
+    T.first[nt] = (int)T.flows.size();
+    T.next[nt] = nt;
+    for (int k = nt - 1; k >= 0; --k) T.next[k] = T.first[k + 1] > T.first[k] ? k : T.next[k + 1];
+    return T;
+}
+
+// Uploads the flow table, the steps and the discount factors of the shared
+// simulation to the context's buffers and returns the kernel arguments
+// (prices of contract q at pv[q * n_paths + path], c.pv).
+static FlowArgs upload_flows(Ctx &c, const SharedBook &B, const FlowTable &T, const kx_mc_config &cfg) {
+    const int nt = (int)B.grid.size();
+    const uint64_t np = cfg.n_paths;
+    const bool f64 = cfg.precision == KX_PREC_FP64;
+    const Model &m = B.m;
+    const StepTables &tab = B.tabs[B.stat[0]];
+    std::vector<unsigned char> steps(nt * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+    for (int k = 0; k < nt; ++k) {
+        if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {tab.c0[k], tab.c1[k], 0u, 0u};
+        else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)tab.c0[k], (float)tab.c1[k], 0u, 0u};
+    }
+    const size_t ns = B.stat.size();
+    c.progs.ensure(T.progs.size() * sizeof(KxProgram));
+    c.items.ensure(std::max<size_t>(1, T.flows.size()) * sizeof(FlowRec));
+    c.misc.ensure(2 * (nt + 1) * sizeof(int));
+    c.steps.ensure(steps.size());
+    c.disc.ensure(nt * sizeof(double));
+    c.pv.ensure(std::max<uint64_t>(1, np * ns) * sizeof(double));
+    KX_CUDA(cudaMemcpyAsync(c.progs.p, T.progs.data(), T.progs.size() * sizeof(KxProgram), cudaMemcpyHostToDevice,
+                            c.stream));
+    if (!T.flows.empty())
+        KX_CUDA(cudaMemcpyAsync(c.items.p, T.flows.data(), T.flows.size() * sizeof(FlowRec), cudaMemcpyHostToDevice,
+                                c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.misc.p, T.first.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.misc.as<int>() + nt + 1, T.next.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                            c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
+    KX_CUDA(cudaMemcpyAsync(c.disc.p, tab.disc.data(), nt * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    // rows of contracts with several flows (or none) are added to: zero them; a contract
+    // with a single flow has it stored on every path (every path walks every step)
+    if (!T.all_single) KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np * ns) * sizeof(double), c.stream));
+    FlowArgs a{};
+    a.progs = c.progs.as<KxProgram>();
+    a.flows = c.items.as<FlowRec>();
+    a.first = c.misc.as<int>();
+    a.next = c.misc.as<int>() + nt + 1;
+    a.steps = c.steps.p;
+    a.disc = c.disc.as<double>();
+    a.n_times = nt;
+    a.n_contracts = (int)ns;
+    a.n_paths = np;
+    a.seed = cfg.seed;
+    a.model = m.kind;
+    a.scheme = m.scheme;
+    a.s0 = m.s0;
+    a.v0 = m.v0;
+    a.kappa = m.kappa;
+    a.theta = m.theta;
+    a.sigma_v = m.sigma_v;
+    a.rho = m.rho;
+    a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
+    a.r = m.r;
+    if (cfg.rng == KX_RNG_SHARED_DRAWS) {
+        DrawStore &ds = c.draws;
+        if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
+        if (ds.n_paths < np || ds.dpp < (uint64_t)(nt - 1) * m.draws_per_step())
+            raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
+        a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
+        a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
+        a.z_dpp = ds.dpp;
+    }
+    a.pv = c.pv.as<double>();
+    return a;
+}
+
+// One launch of a shared-simulation kernel over np paths, timed into c.last.
+static void launch_shared(Ctx &c, const void *kfn, void *arg, uint64_t np) {
+    if (np == 0) return;
+    const int full = persistent_blocks(kfn, 256, 0);
+    const int blocks = (int)std::min<uint64_t>((uint64_t)full, (np + 255) / 256);
+    void *args[] = {arg};
+    KX_CUDA(cudaEventRecord(c.ev0, c.stream));
+    KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(256), args, 0, c.stream));
+    KX_CUDA(cudaEventRecord(c.ev1, c.stream));
+    KX_CUDA(cudaEventSynchronize(c.ev1));
+    float ms = 0.f;
+    KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.last.kernel_ms += ms;
+    c.last.kernel_launches++;
+}
+
 }  // namespace kx
 
 using namespace kx;
@@ -170,135 +482,23 @@ extern "C" kx_status kx_price_batch_shared(size_t n, const kx_program *const *pr
     return guarded([&] {
         if (n == 0) return;  // pricer.rs:255-257
         if (!progs || !out || !cfg) raise(KX_INVALID_ARGUMENT, "NULL array");
-        Model m = model_from_c(model);
-        if (cfg->rng != KX_RNG_PHILOX && cfg->rng != KX_RNG_SHARED_DRAWS) raise(KX_INVALID_ARGUMENT, "unknown rng");
-        if (cfg->precision != KX_PREC_FP32 && cfg->precision != KX_PREC_FP64) raise(KX_INVALID_ARGUMENT, "unknown precision");
-        if (cfg->flags != 0) raise(KX_INVALID_ARGUMENT, "flags must be 0");
-        if (cfg->n_paths >= (1ull << 32)) raise(KX_INVALID_ARGUMENT, "n_paths must be below 2^32");
-        validate_model(m);
-        // merged plan (pricer.rs:260-279)
-        Plan merged;
-        for (size_t i = 0; i < n; ++i) {
-            const Program &p = program_of(progs[i]);
-            merged.fixed_dates.insert(merged.fixed_dates.end(), p.plan.fixed_dates.begin(), p.plan.fixed_dates.end());
-            merged.horizon = std::max(merged.horizon, p.plan.horizon);
-            merged.needs_fine_grid = merged.needs_fine_grid || p.plan.needs_fine_grid;
-        }
-        auto grid = time_grid_forced(merged, cfg->steps_per_year, m.requires_fine_grid());
-        validate_grid(grid);
-        const int nt = (int)grid.size();
+        const SharedBook B = shared_book(n, progs, model, cfg);
+        const Model &m = B.m;
+        const int nt = (int)B.grid.size();
         const uint64_t np = cfg->n_paths;
         const bool f64 = cfg->precision == KX_PREC_FP64;
-        // split: static schedules share one simulation, the rest use the path kernel
-        std::vector<KxProgram> bound(n);
-        std::vector<StepTables> tabs(n);
-        std::vector<size_t> stat, dyn;
-        std::vector<StaticSchedule> sched(n);
-        for (size_t i = 0; i < n; ++i) {
-            const Program &p = program_of(progs[i]);
-            bind(p.low, grid, m, cfg->rate, bound[i], tabs[i]);
-            sched[i] = static_schedule(bound[i], tabs[i]);
-            bool ok = sched[i].static_ok && bound[i].n_acc == 0;
-            for (auto &f : sched[i].flows) ok = ok && f.price_untils == 0;
-            (ok ? stat : dyn).push_back(i);
-        }
         Ctx &c = ctx();
         std::lock_guard<std::mutex> g(c.mu);
         memset(&c.last, 0, sizeof c.last);
         c.last.total_ms = -now_ms();
         std::vector<Stats> st_all(n);
-        if (!stat.empty()) {
-            std::vector<std::vector<FlowRec>> at(nt);
-            std::vector<KxProgram> progs_s;
-            for (size_t q = 0; q < stat.size(); ++q) {
-                const size_t i = stat[q];
-                progs_s.push_back(bound[i]);
-                for (auto &f : sched[i].flows) {
-                    FlowRec r = classify(bound[i], f.leaf);
-                    r.contract = (int)q;
-                    r.prog = (int)q;
-                    r.only = sched[i].flows.size() == 1 ? 1 : 0;
-                    r.af = (float)r.a;
-                    r.signf = (float)r.sign;
-                    at[f.step].push_back(r);
-                }
-            }
-            std::vector<FlowRec> flows;
-            std::vector<int> first(nt + 1), next(nt + 1);
-            for (int k = 0; k < nt; ++k) {
-                first[k] = (int)flows.size();
-                flows.insert(flows.end(), at[k].begin(), at[k].end());
-            }
-            first[nt] = (int)flows.size();
-            next[nt] = nt;
-            for (int k = nt - 1; k >= 0; --k) next[k] = first[k + 1] > first[k] ? k : next[k + 1];
-            std::vector<unsigned char> steps(nt * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
-            for (int k = 0; k < nt; ++k) {
-                if (f64) reinterpret_cast<StepRec<double> *>(steps.data())[k] = {tabs[stat[0]].c0[k], tabs[stat[0]].c1[k], 0u, 0u};
-                else reinterpret_cast<StepRec<float> *>(steps.data())[k] = {(float)tabs[stat[0]].c0[k], (float)tabs[stat[0]].c1[k], 0u, 0u};
-            }
-            const size_t ns = stat.size();
-            c.progs.ensure(progs_s.size() * sizeof(KxProgram));
-            c.items.ensure(std::max<size_t>(1, flows.size()) * sizeof(FlowRec));
-            c.misc.ensure(2 * (nt + 1) * sizeof(int));
-            c.steps.ensure(steps.size());
-            c.disc.ensure(nt * sizeof(double));
-            c.pv.ensure(std::max<uint64_t>(1, np * ns) * sizeof(double));
-            KX_CUDA(cudaMemcpyAsync(c.progs.p, progs_s.data(), progs_s.size() * sizeof(KxProgram), cudaMemcpyHostToDevice, c.stream));
-            if (!flows.empty())
-                KX_CUDA(cudaMemcpyAsync(c.items.p, flows.data(), flows.size() * sizeof(FlowRec), cudaMemcpyHostToDevice, c.stream));
-            KX_CUDA(cudaMemcpyAsync(c.misc.p, first.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
-            KX_CUDA(cudaMemcpyAsync(c.misc.as<int>() + nt + 1, next.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
-            KX_CUDA(cudaMemcpyAsync(c.steps.p, steps.data(), steps.size(), cudaMemcpyHostToDevice, c.stream));
-            KX_CUDA(cudaMemcpyAsync(c.disc.p, tabs[stat[0]].disc.data(), nt * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-            // rows of contracts with several flows (or none) are added to: zero them; a contract
-            // with a single flow has it stored on every path (every path walks every step)
-            bool all_single = true;
-            for (size_t q = 0; q < stat.size(); ++q) all_single = all_single && sched[stat[q]].flows.size() == 1;
-            if (!all_single)
-                KX_CUDA(cudaMemsetAsync(c.pv.p, 0, std::max<uint64_t>(1, np * ns) * sizeof(double), c.stream));
-            FlowArgs a{};
-            a.progs = c.progs.as<KxProgram>();
-            a.flows = c.items.as<FlowRec>();
-            a.first = c.misc.as<int>();
-            a.next = c.misc.as<int>() + nt + 1;
-            a.steps = c.steps.p;
-            a.disc = c.disc.as<double>();
-            a.n_times = nt;
-            a.n_contracts = (int)ns;
-            a.n_paths = np;
-            a.seed = cfg->seed;
-            a.model = m.kind;
-            a.scheme = m.scheme;
-            a.s0 = m.s0;
-            a.v0 = m.v0; a.kappa = m.kappa; a.theta = m.theta; a.sigma_v = m.sigma_v; a.rho = m.rho;
-            a.rho_perp = std::sqrt(std::max(1.0 - m.rho * m.rho, 0.0));
-            a.r = m.r;
-            if (cfg->rng == KX_RNG_SHARED_DRAWS) {
-                DrawStore &ds = c.draws;
-                if (!ds.set) raise(KX_INVALID_ARGUMENT, "no shared draws registered");
-                if (ds.n_paths < np || ds.dpp < (uint64_t)(nt - 1) * m.draws_per_step())
-                    raise(KX_INVALID_ARGUMENT, "shared draws too small for this simulation");
-                a.z64 = ds.is64 ? ds.z64.as<double>() : nullptr;
-                a.z32 = ds.is64 ? nullptr : ds.z32.as<float>();
-                a.z_dpp = ds.dpp;
-            }
-            a.pv = c.pv.as<double>();
+        if (!B.stat.empty()) {
+            const FlowTable T = flow_table(B);
+            FlowArgs a = upload_flows(c, B, T, *cfg);
+            const size_t ns = B.stat.size();
             const void *kfn = m.kind == KX_MODEL_GBM ? (f64 ? flows_kernel<double, KX_MODEL_GBM>() : flows_kernel<float, KX_MODEL_GBM>())
                                                      : (f64 ? flows_kernel<double, KX_MODEL_HESTON>() : flows_kernel<float, KX_MODEL_HESTON>());
-            if (np > 0) {
-                const int full = persistent_blocks(kfn, 256, 0);
-                const int blocks = (int)std::min<uint64_t>((uint64_t)full, (np + 255) / 256);
-                void *args[] = {&a};
-                KX_CUDA(cudaEventRecord(c.ev0, c.stream));
-                KX_CUDA(cudaLaunchKernel(kfn, dim3(blocks), dim3(256), args, 0, c.stream));
-                KX_CUDA(cudaEventRecord(c.ev1, c.stream));
-                KX_CUDA(cudaEventSynchronize(c.ev1));
-                float ms = 0.f;
-                KX_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
-                c.last.kernel_ms += ms;
-                c.last.kernel_launches++;
-            }
+            launch_shared(c, kfn, &a, np);
             c.last.path_steps += np * (uint64_t)(nt - 1);
             c.last.steps_simulated += np * (uint64_t)(nt - 1);
             std::vector<StatsJob> sj(ns);
@@ -307,15 +507,107 @@ extern "C" kx_status kx_price_batch_shared(size_t n, const kx_program *const *pr
                 sj[q].n = np;
             }
             auto st = device_stats(c, c.pv.as<double>(), 0, sj);
-            for (size_t q = 0; q < ns; ++q) st_all[stat[q]] = st[q];
+            for (size_t q = 0; q < ns; ++q) st_all[B.stat[q]] = st[q];
         }
-        if (!dyn.empty()) {  // same grid and seed: the same simulated paths
+        if (!B.dyn.empty()) {  // same grid and seed: the same simulated paths
             std::vector<const Program *> dp;
-            for (size_t i : dyn) dp.push_back(&program_of(progs[i]));
-            auto st = batch_paths(c, dp, m, *cfg, grid);
-            for (size_t q = 0; q < dyn.size(); ++q) st_all[dyn[q]] = st[q];
+            for (size_t i : B.dyn) dp.push_back(&program_of(progs[i]));
+            auto st = batch_paths(c, dp, m, *cfg, B.grid);
+            for (size_t q = 0; q < B.dyn.size(); ++q) st_all[B.dyn[q]] = st[q];
         }
         for (size_t i = 0; i < n; ++i) out[i] = finish(st_all[i]);
+        c.last.total_ms += now_ms();
+    });
+}
+
+extern "C" kx_status kx_price_batch_sens(size_t n, const kx_program *const *progs, const kx_model *model,
+                                         const kx_mc_config *cfg, kx_price_result *out, kx_sens *sens) {
+    return guarded([&] {
+        if (n == 0) return;
+        if (!progs || !out || !sens || !cfg) raise(KX_INVALID_ARGUMENT, "NULL array");
+        const SharedBook B = shared_book(n, progs, model, cfg);
+        const Model &m = B.m;
+        if (m.kind != KX_MODEL_GBM && m.kind != KX_MODEL_HESTON) raise(KX_UNSUPPORTED, "GBM and Heston books only");
+        const FlowTable T = flow_table(B);
+        bool ok = B.dyn.empty() && T.all_single;
+        for (auto &f : T.flows) ok = ok && f.kind != FK_GENERAL;
+        if (!ok)
+            raise(KX_UNSUPPORTED, "sensitivities on a shared simulation need contracts that each pay one call, put or "
+                                  "constant amount at a fixed date (kx_price_portfolio prices others with sensitivities)");
+        const int nt = (int)B.grid.size();
+        const uint64_t np = cfg->n_paths;
+        const bool f64 = cfg->precision == KX_PREC_FP64;
+        const bool heston = m.kind == KX_MODEL_HESTON;
+        const int nq = heston ? 7 : 3;  // derivative outputs per contract
+        Ctx &c = ctx();
+        std::lock_guard<std::mutex> g(c.mu);
+        memset(&c.last, 0, sizeof c.last);
+        c.last.total_ms = -now_ms();
+        SensArgs a{};
+        a.F = upload_flows(c, B, T, *cfg);
+        const size_t ns = B.stat.size();
+        std::vector<unsigned char> dtq(nt * (f64 ? sizeof(StepRec<double>) : sizeof(StepRec<float>)));
+        for (int k = 0; k < nt; ++k) {
+            const double dt = k == 0 ? 0.0 : B.grid[k] - B.grid[k - 1], sq = std::sqrt(dt);  // as the adjoint's tables
+            if (f64) reinterpret_cast<StepRec<double> *>(dtq.data())[k] = {dt, sq, 0u, 0u};
+            else reinterpret_cast<StepRec<float> *>(dtq.data())[k] = {(float)dt, (float)sq, 0u, 0u};
+        }
+        const size_t b_times = (size_t)nt * sizeof(double);
+        c.grid_tabs.ensure(b_times + dtq.size());
+        KX_CUDA(cudaMemcpyAsync(c.grid_tabs.p, B.grid.data(), b_times, cudaMemcpyHostToDevice, c.stream));
+        KX_CUDA(cudaMemcpyAsync(c.grid_tabs.as<unsigned char>() + b_times, dtq.data(), dtq.size(),
+                                cudaMemcpyHostToDevice, c.stream));
+        const uint64_t rows = (uint64_t)ns * np;
+        c.vr.ensure(std::max<uint64_t>(1, rows * nq) * sizeof(double));
+        a.times = c.grid_tabs.as<double>();
+        a.dtq = c.grid_tabs.as<unsigned char>() + b_times;
+        a.dv = c.vr.as<double>();
+        a.inv_s0 = 1.0 / m.s0;
+        a.sigma = m.sigma;
+        a.drp = a.F.rho_perp > 0.0 ? -m.rho / a.F.rho_perp : 0.0;
+        const void *kfn = heston ? (f64 ? (const void *)&k_flows_sens<double, KX_MODEL_HESTON>
+                                        : (const void *)&k_flows_sens<float, KX_MODEL_HESTON>)
+                                 : (f64 ? (const void *)&k_flows_sens<double, KX_MODEL_GBM>
+                                        : (const void *)&k_flows_sens<float, KX_MODEL_GBM>);
+        launch_shared(c, kfn, &a, np);
+        c.last.path_steps += np * (uint64_t)(nt - 1);
+        c.last.steps_simulated += np * (uint64_t)(nt - 1);
+        c.last.h2d_bytes += b_times + dtq.size();
+        std::vector<StatsJob> sj(ns), sd(ns * nq);
+        for (size_t q = 0; q < ns; ++q) {
+            sj[q].begin = (uint64_t)q * np;
+            sj[q].n = np;
+            for (int o = 0; o < nq; ++o) {
+                sd[o * ns + q].begin = (uint64_t)o * rows + (uint64_t)q * np;
+                sd[o * ns + q].n = np;
+            }
+        }
+        const auto sp = device_stats(c, c.pv.as<double>(), 0, sj);
+        const auto sv = device_stats(c, c.vr.as<double>(), 0, sd);
+        for (size_t q = 0; q < ns; ++q) {
+            const size_t i = B.stat[q];
+            out[i] = finish(sp[q]);
+            kx_sens &S = sens[i];
+            S = kx_sens{};
+            S.price = out[i].price;
+            S.price_se = out[i].std_error;
+            auto put = [&](int o, double &val, double &se) {
+                const kx_price_result r = finish(sv[o * ns + q]);
+                val = r.price;
+                se = r.std_error;
+            };
+            put(0, S.d_s0, S.se_s0);
+            put(1, S.d_r, S.se_r);
+            if (heston) {
+                put(2, S.d_v0, S.se_v0);
+                put(3, S.d_kappa, S.se_kappa);
+                put(4, S.d_theta, S.se_theta);
+                put(5, S.d_sigma_v, S.se_sigma_v);
+                put(6, S.d_rho, S.se_rho);
+            } else {
+                put(2, S.d_sigma, S.se_sigma);
+            }
+        }
         c.last.total_ms += now_ms();
     });
 }

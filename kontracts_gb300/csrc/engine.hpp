@@ -51,7 +51,7 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // scratch owned by the context
     DevBuf progs, steps, disc, thr, cons, items, counters, pv, chunks, chunk_out, misc, vr, lsm_paths, lsm_value,
-        lsm_stats, statics, mlmc, plan, stats_in;
+        grid_tabs, statics, mlmc, plan, stats_in;
     // host staging of a call's uploads and downloads (path plan, statistics)
     PinnedBuf plan_stage, stats_stage;
     DrawStore draws;
