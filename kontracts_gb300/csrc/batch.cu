@@ -140,24 +140,37 @@ __global__ void __launch_bounds__(256) k_flows(const FlowArgs A) {
 //           c_v0 = 0, c_kappa = (theta - vp) dt, c_theta = kappa dt,
 //           c_sigma_v = sqv mix sq, c_rho = sigma_v sqv (z1 + drho_perp/drho z2) sq,
 //           keep = 0 where the reference scheme's floor bit (v' = 0), dv_0/dv0 = 1.
-// Outputs per contract and path, [q][contract][path]: q = 0 d/ds0 (dS/ds0 =
-// S/s0), 1 d/dr (drift dy/dr = t and the discount -t pv, as greeks.rs:70 moves
-// both), then GBM d/dsigma | Heston d/dv0, d/dkappa, d/dtheta, d/dsigma_v,
-// d/drho.
+// Outputs per contract and path (doubles), [q][contract][path]: q = 0 d/ds0
+// (dS/ds0 = S/s0), 1 d/dr (drift dy/dr = t and the discount, t (g - A df), as
+// greeks.rs:70 moves both), then GBM d/dsigma | Heston d/dv0, d/dkappa,
+// d/dtheta, d/dsigma_v, d/drho, each formed in the path precision. The FP32
+// kernel reads FP32 copies of every parameter and table (GB300's FP64 pipe
+// is slow: no conversion per step); per flow only the price, as in k_flows,
+// and the outputs' conversions touch FP64.
 // ---------------------------------------------------------------------------
 struct SensArgs {
     FlowArgs F;              // the simulation and its flows; F.pv: the prices
     const double *times;     // grid times
     const void *dtq;         // StepRec<Real> {dt, sqrt(dt)} of every step (GBM's volatility tangent)
-    double *dv;              // the derivative outputs
+    const float *discf, *timesf;  // FP32 copies of the discount factors and the grid times
+    double *dv;              // [2 + NP][contract][path]
     double inv_s0, sigma, drp;
+    // FP32 copies: s0, r, kappa, theta, sigma_v, rho, rho_perp, drp, sigma, 1 / s0
+    float pf[10];
 };
+
+template <class Real>
+__device__ __forceinline__ Real sens_par(const SensArgs &S, double d, int i) {
+    return sizeof(Real) == 4 ? (Real)S.pf[i] : (Real)d;
+}
 
 template <class Real, int NP>
 __device__ __forceinline__ void pay_flows_sens(const SensArgs &S, int k, Real Sk, const Real (&ty)[NP], uint64_t path,
                                                Real inv_s0) {
     const FlowArgs &A = S.F;
-    const double df = A.disc[k], tk = S.times[k];
+    const double df = A.disc[k];
+    const Real dfr = sizeof(Real) == 4 ? (Real)S.discf[k] : (Real)df,
+               tk = sizeof(Real) == 4 ? (Real)S.timesf[k] : (Real)S.times[k];
     const uint64_t np = A.n_paths, rows = (uint64_t)A.n_contracts * np;
     for (int f = A.first[k]; f < A.first[k + 1]; ++f) {
         const FlowRec &F = A.flows[f];
@@ -176,24 +189,26 @@ __device__ __forceinline__ void pay_flows_sens(const SensArgs &S, int k, Real Sk
         const double pv = (double)amt * df;
         const uint64_t o = (uint64_t)F.contract * np + path;
         A.pv[o] = pv;
-        const Real g = damt * Sk * (Real)df;  // d pv / d y
+        const Real g = damt * Sk * dfr;  // d pv / d y
         S.dv[o] = (double)(g * inv_s0);
-        S.dv[rows + o] = (double)(g * (Real)tk) - tk * pv;
+        S.dv[rows + o] = (double)(tk * (g - amt * dfr));
 #pragma unroll
         for (int p = 0; p < NP; ++p) S.dv[(2 + p) * rows + o] = (double)(g * ty[p]);
     }
 }
 
 template <class Real, int MODEL>
-__global__ void __launch_bounds__(256) k_flows_sens(const SensArgs S) {
+__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 4 : 2) k_flows_sens(const SensArgs S) {
     const FlowArgs &A = S.F;
     constexpr bool HESTON = MODEL == KX_MODEL_HESTON;
     constexpr int DRAWS = HESTON ? 2 : 1, NP = HESTON ? 5 : 1;
     const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
     const StepRec<Real> *Q = reinterpret_cast<const StepRec<Real> *>(S.dtq);
-    const Real s0 = (Real)A.s0, r = (Real)A.r, kap = (Real)A.kappa, th = (Real)A.theta, sv = (Real)A.sigma_v,
-               rho = (Real)A.rho, rp = (Real)A.rho_perp, drp = (Real)S.drp, sig = (Real)S.sigma,
-               inv_s0 = (Real)S.inv_s0;
+    const Real s0 = sens_par<Real>(S, A.s0, 0), r = sens_par<Real>(S, A.r, 1), kap = sens_par<Real>(S, A.kappa, 2),
+               th = sens_par<Real>(S, A.theta, 3), sv = sens_par<Real>(S, A.sigma_v, 4),
+               rho = sens_par<Real>(S, A.rho, 5), rp = sens_par<Real>(S, A.rho_perp, 6),
+               drp = sens_par<Real>(S, S.drp, 7), sig = sens_par<Real>(S, S.sigma, 8),
+               inv_s0 = sens_par<Real>(S, S.inv_s0, 9);
     const bool ft = A.scheme == KX_HESTON_FULL_TRUNCATION;
     for (uint64_t path = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; path < A.n_paths;
          path += (uint64_t)gridDim.x * blockDim.x) {
@@ -552,19 +567,32 @@ extern "C" kx_status kx_price_batch_sens(size_t n, const kx_program *const *prog
             if (f64) reinterpret_cast<StepRec<double> *>(dtq.data())[k] = {dt, sq, 0u, 0u};
             else reinterpret_cast<StepRec<float> *>(dtq.data())[k] = {(float)dt, (float)sq, 0u, 0u};
         }
-        const size_t b_times = (size_t)nt * sizeof(double);
-        c.grid_tabs.ensure(b_times + dtq.size());
-        KX_CUDA(cudaMemcpyAsync(c.grid_tabs.p, B.grid.data(), b_times, cudaMemcpyHostToDevice, c.stream));
-        KX_CUDA(cudaMemcpyAsync(c.grid_tabs.as<unsigned char>() + b_times, dtq.data(), dtq.size(),
-                                cudaMemcpyHostToDevice, c.stream));
+        // one table upload: the grid times (double), the {dt, sqrt(dt)} records, FP32 copies of the
+        // discount factors and times
+        const size_t b_times = (size_t)nt * sizeof(double), b_f = (size_t)nt * sizeof(float);
+        std::vector<unsigned char> tabs(b_times + dtq.size() + 2 * b_f);
+        memcpy(tabs.data(), B.grid.data(), b_times);
+        memcpy(tabs.data() + b_times, dtq.data(), dtq.size());
+        float *ff = reinterpret_cast<float *>(tabs.data() + b_times + dtq.size());
+        const StepTables &tab0 = B.tabs[B.stat[0]];
+        for (int k = 0; k < nt; ++k) {
+            ff[k] = (float)tab0.disc[k];
+            ff[nt + k] = (float)B.grid[k];
+        }
+        c.grid_tabs.ensure(tabs.size());
+        KX_CUDA(cudaMemcpyAsync(c.grid_tabs.p, tabs.data(), tabs.size(), cudaMemcpyHostToDevice, c.stream));
         const uint64_t rows = (uint64_t)ns * np;
         c.vr.ensure(std::max<uint64_t>(1, rows * nq) * sizeof(double));
         a.times = c.grid_tabs.as<double>();
         a.dtq = c.grid_tabs.as<unsigned char>() + b_times;
+        a.discf = reinterpret_cast<const float *>(c.grid_tabs.as<unsigned char>() + b_times + dtq.size());
+        a.timesf = a.discf + nt;
         a.dv = c.vr.as<double>();
         a.inv_s0 = 1.0 / m.s0;
         a.sigma = m.sigma;
         a.drp = a.F.rho_perp > 0.0 ? -m.rho / a.F.rho_perp : 0.0;
+        const double pd[10] = {m.s0, a.F.r, m.kappa, m.theta, m.sigma_v, m.rho, a.F.rho_perp, a.drp, a.sigma, a.inv_s0};
+        for (int q = 0; q < 10; ++q) a.pf[q] = (float)pd[q];
         const void *kfn = heston ? (f64 ? (const void *)&k_flows_sens<double, KX_MODEL_HESTON>
                                         : (const void *)&k_flows_sens<float, KX_MODEL_HESTON>)
                                  : (f64 ? (const void *)&k_flows_sens<double, KX_MODEL_GBM>
@@ -572,18 +600,19 @@ extern "C" kx_status kx_price_batch_sens(size_t n, const kx_program *const *prog
         launch_shared(c, kfn, &a, np);
         c.last.path_steps += np * (uint64_t)(nt - 1);
         c.last.steps_simulated += np * (uint64_t)(nt - 1);
-        c.last.h2d_bytes += b_times + dtq.size();
-        std::vector<StatsJob> sj(ns), sd(ns * nq);
+        c.last.h2d_bytes += tabs.size();
+        // statistics: the prices, the derivatives
+        std::vector<StatsJob> sj(ns), sr(ns * nq);
         for (size_t q = 0; q < ns; ++q) {
             sj[q].begin = (uint64_t)q * np;
             sj[q].n = np;
             for (int o = 0; o < nq; ++o) {
-                sd[o * ns + q].begin = (uint64_t)o * rows + (uint64_t)q * np;
-                sd[o * ns + q].n = np;
+                sr[o * ns + q].begin = (uint64_t)o * rows + (uint64_t)q * np;
+                sr[o * ns + q].n = np;
             }
         }
         const auto sp = device_stats(c, c.pv.as<double>(), 0, sj);
-        const auto sv = device_stats(c, c.vr.as<double>(), 0, sd);
+        const auto sv = device_stats(c, a.dv, 0, sr);
         for (size_t q = 0; q < ns; ++q) {
             const size_t i = B.stat[q];
             out[i] = finish(sp[q]);
@@ -591,21 +620,21 @@ extern "C" kx_status kx_price_batch_sens(size_t n, const kx_program *const *prog
             S = kx_sens{};
             S.price = out[i].price;
             S.price_se = out[i].std_error;
-            auto put = [&](int o, double &val, double &se) {
-                const kx_price_result r = finish(sv[o * ns + q]);
+            auto put = [&](const Stats &st, double &val, double &se) {
+                const kx_price_result r = finish(st);
                 val = r.price;
                 se = r.std_error;
             };
-            put(0, S.d_s0, S.se_s0);
-            put(1, S.d_r, S.se_r);
+            put(sv[q], S.d_s0, S.se_s0);
+            put(sv[1 * ns + q], S.d_r, S.se_r);
             if (heston) {
-                put(2, S.d_v0, S.se_v0);
-                put(3, S.d_kappa, S.se_kappa);
-                put(4, S.d_theta, S.se_theta);
-                put(5, S.d_sigma_v, S.se_sigma_v);
-                put(6, S.d_rho, S.se_rho);
+                put(sv[2 * ns + q], S.d_v0, S.se_v0);
+                put(sv[3 * ns + q], S.d_kappa, S.se_kappa);
+                put(sv[4 * ns + q], S.d_theta, S.se_theta);
+                put(sv[5 * ns + q], S.d_sigma_v, S.se_sigma_v);
+                put(sv[6 * ns + q], S.d_rho, S.se_rho);
             } else {
-                put(2, S.d_sigma, S.se_sigma);
+                put(sv[2 * ns + q], S.d_sigma, S.se_sigma);
             }
         }
         c.last.total_ms += now_ms();
