@@ -119,3 +119,25 @@ def test_path_dependent_contracts_are_refused():
     with pytest.raises(kx.KontractError) as e:
         kx.price_batch([kx.european_call("X", 100.0, 1.0), c], _heston(), n_paths=1000, seed=1, greeks=True)
     assert e.value.status == "Unsupported"
+
+
+def test_autograd_book_prices():
+    """heston_book_price as a torch.autograd.Function: the forward values are
+    the shared-simulation prices, backward contracts the incoming gradient
+    with every contract's seven sensitivities."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+    from kontracts_gb300.autograd import heston_book_price
+    book = _book()
+    vals = [HP[k] for k in ("s0", "v0", "kappa", "theta", "sigma_v", "rho", "r")]
+    p = torch.tensor(vals, dtype=torch.float64, requires_grad=True)
+    prices = heston_book_price(book, p, asset="X", n_paths=20_000, seed=5, steps_per_year=252, precision="fp64",
+                               scheme="full_truncation")
+    w = torch.arange(1, len(book) + 1, dtype=torch.float64)
+    (w * prices).sum().backward()
+    res, sens = kx.price_batch(book, _heston(), n_paths=20_000, seed=5, steps_per_year=252, precision="fp64",
+                               greeks=True)
+    assert prices.tolist() == [r.price for r in res]
+    fields = ("d_s0", "d_v0", "d_kappa", "d_theta", "d_sigma_v", "d_rho", "d_r")
+    want = sum((i + 1) * np.array([getattr(s, f) for f in fields]) for i, s in enumerate(sens))
+    assert np.allclose(p.grad.numpy(), want, rtol=1e-12, atol=1e-12)
