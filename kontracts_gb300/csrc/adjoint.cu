@@ -1035,6 +1035,181 @@ static const void *adj_gbm_kernel(int nsu) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// GBM sensitivities in forward (tangent) mode: one pass along the path that
+// carries the derivative of the log-spot y_k in three directions D instead
+// of recomputing the path for a reverse sweep. With three parameters the
+// forward pass is cheaper than forward + recomputation + sweep, and it is
+// the same pathwise derivative, the sweep of k_adjoint transposed term for
+// term (values at rounding level apart):
+//   D = 0, a uniform shift of every y_k: d/ds0 = (d/dD0) / s0 (S = s0 e^y, and
+//          the barriers' log thresholds log(B / s0) move with it);
+//   D = 1, sigma: dy_k += -sigma dt + sqrt(dt) z per step;
+//   D = 2, r (the drift): dy_k += dt per step; the discount's -t P is added
+//          at the end (d/dr moves both, as greeks.rs:70);
+//   a smoothed until adds d log w / dD = sum over its weighing steps of
+//          -sgn (1 - s_k) / width * dy_k/dD (s_k the step's logistic weight);
+//   an average adds sum S_k dy_k/dD over its window / its count, a running
+//          extremum S_k dy_k/dD at its arg-extremum;
+//   a flow P = A(S, acc) w df adds df w (A_S S dy/dD + sum_a A_a dacc_a/dD +
+//          A d log w / dD).
+// Every primal quantity (path, spot, accumulators, weights, knock-outs, flow
+// values, the hard-barrier price) is computed with k_adjoint's operations, so
+// the price output is k_adjoint's bit for bit.
+// ---------------------------------------------------------------------------
+template <class Real, bool ACC>
+__global__ void __launch_bounds__(ADJ_BLOCK) k_tangent_gbm(const AdjArgs *__restrict__ all,
+                                                           const uint64_t *__restrict__ off, int n_contracts,
+                                                           uint64_t total, double *__restrict__ out,
+                                                           const PhiloxKeys keys) {
+    for (uint64_t gp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; gp < total;
+         gp += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_contracts - 1;  // contract of global path gp
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= gp) lo = mid;
+            else hi = mid - 1;
+        }
+        const AdjArgs &A = all[lo];
+        const uint64_t path = gp - off[lo];
+        const StepRec<Real> *R = reinterpret_cast<const StepRec<Real> *>(A.steps);
+        const KxProgram &P = *A.P;
+        const int N = A.n_times - 1;
+        const AdjPar<Real> pp = adj_par<Real>(A);
+        const Real s0 = pp.s0, inv_w = pp.inv_w;
+        const int nflows = A.n_flows, nsu = A.n_su, nacc = ACC ? A.n_acc : 0;
+        Real y = Real(0), ty = Real(0), tr = Real(0);  // y and dy/dsigma, dy/dr
+        Real accraw[ADJ_MAXA], dacc[ADJ_MAXA][3];
+#pragma unroll
+        for (int a = 0; a < ADJ_MAXA; ++a) {
+            accraw[a] = a < nacc ? (A.acc[a].kind == ACC_MAX ? Real(-INFINITY) : A.acc[a].kind == ACC_MIN ? Real(INFINITY) : Real(0)) : Real(0);
+            dacc[a][0] = dacc[a][1] = dacc[a][2] = Real(0);
+        }
+        Real surv[ADJ_MAXU], dlw[ADJ_MAXU][3];
+        int knock[ADJ_MAXU], su_arm[ADJ_MAXU];
+#pragma unroll
+        for (int u = 0; u < ADJ_MAXU; ++u) {
+            surv[u] = Real(1);
+            dlw[u][0] = dlw[u][1] = dlw[u][2] = Real(0);
+            knock[u] = INT_MAX;
+            su_arm[u] = u < nsu ? A.su[u].arm : INT_MAX;
+        }
+        double pv = 0.0, pv_t = 0.0, pv_hard = 0.0, dD[3] = {0.0, 0.0, 0.0};
+        int nf = 0, nft = nflows > 0 ? A.flow[0].t : INT_MAX;
+        Real z[4], vd = Real(0);  // vd: the variance slot of model_step (unused by GBM)
+        for (int k = 0; k <= N; ++k) {
+            if (k > 0) {
+                const uint64_t d = (uint64_t)(k - 1);
+                if ((d & 3u) == 0) draws4<Real>(A, keys, path, d, z);
+                const Real z1 = z[d & 3u];
+                const StepRec<Real> rec = R[k];
+                ty += -pp.sigma * rec.c0 + rec.c1 * z1;
+                tr += rec.c0;
+                model_step<Real, KX_MODEL_GBM>(pp, A.scheme, rec, z1, Real(0), y, vd);
+            }
+            const bool pays = k == nft;
+            const Real S = (ACC || pays) ? spot_of<Real>(s0, y) : Real(0);
+            if (ACC)
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a) {
+                    if (a >= nacc) continue;
+                    const AdjAcc &Ac = A.acc[a];
+                    if (k < Ac.i_from || k > Ac.i_to) continue;
+                    if (Ac.kind == ACC_MAX || Ac.kind == ACC_MIN) {
+                        if (Ac.kind == ACC_MAX ? S > accraw[a] : S < accraw[a]) {
+                            accraw[a] = S;
+                            dacc[a][0] = S;
+                            dacc[a][1] = S * ty;
+                            dacc[a][2] = S * tr;
+                        }
+                    } else {
+                        accraw[a] = add_rn(accraw[a], S);
+                        dacc[a][0] += S;
+                        dacc[a][1] += S * ty;
+                        dacc[a][2] += S * tr;
+                    }
+                }
+#pragma unroll
+            for (int u = 0; u < ADJ_MAXU; ++u)
+                if (u < nsu && k >= su_arm[u]) {
+                    const Real x = pp.sgn[u] * (y - pp.thr[u]) * inv_w;
+                    if (x > smooth_cut<Real>()) {
+                        const Real sv = logistic(x);
+                        surv[u] *= sv;
+                        const Real cdl = -pp.sgn[u] * (Real(1) - sv) * inv_w;  // d log(weight) / dy_k
+                        dlw[u][0] += cdl;
+                        dlw[u][1] += cdl * ty;
+                        dlw[u][2] += cdl * tr;
+                    }
+                    if (pp.sgn[u] * y >= pp.hit[u] && knock[u] == INT_MAX) knock[u] = k;
+                }
+            if (!pays) continue;
+            for (int f = nf; f < nflows && A.flow[f].t == k; ++f) {
+                const AdjFlow &F = A.flow[f];
+                nf = f + 1;
+                Real accv[ADJ_MAXA], cnt[ADJ_MAXA];
+#pragma unroll
+                for (int a = 0; a < ADJ_MAXA; ++a) {
+                    cnt[a] = Real(1);
+                    accv[a] = Real(0);
+                    if (a < nacc) {
+                        if (A.acc[a].kind == ACC_SUM) {
+                            cnt[a] = (Real)(min(k, A.acc[a].i_to) - A.acc[a].i_from + 1);
+                            accv[a] = accraw[a] / cnt[a];
+                        } else {
+                            accv[a] = accraw[a];
+                        }
+                    }
+                }
+                Dual<Real> amt;
+                if (F.kind == AK_CONST) {
+                    amt.v = (Real)F.sign;
+#pragma unroll
+                    for (int q = 0; q < 1 + ADJ_MAXA; ++q) amt.d[q] = Real(0);
+                } else {
+                    amt = eval_dual<Real>(P, F.code_off, F.code_len, S, accv);
+                }
+                Real w = Real(1);
+                Real lw[3] = {Real(0), Real(0), Real(0)};
+#pragma unroll
+                for (int u = 0; u < ADJ_MAXU; ++u)
+                    if (u < nsu && ((F.su_mask >> u) & 1u)) {
+                        w *= surv[u];
+                        lw[0] += dlw[u][0];
+                        lw[1] += dlw[u][1];
+                        lw[2] += dlw[u][2];
+                    }
+                const double df = A.disc[k];
+                const double fP = (double)amt.v * (double)w * df;
+                pv += fP;
+                pv_t += A.times[k] * fP;
+                bool alive = true;
+#pragma unroll
+                for (int u = 0; u < ADJ_MAXU; ++u)
+                    if (u < nsu && ((F.su_mask >> u) & 1u) && knock[u] <= k) alive = false;
+                if (alive) pv_hard += (double)amt.v * df;
+                const Real dy[3] = {Real(1), ty, tr};
+#pragma unroll
+                for (int D = 0; D < 3; ++D) {
+                    Real g = amt.d[0] * S * dy[D];
+#pragma unroll
+                    for (int a = 0; a < ADJ_MAXA; ++a)
+                        if (a < nacc) g += amt.d[1 + a] * (dacc[a][D] / cnt[a]);
+                    dD[D] += (double)((g + amt.v * lw[D]) * w) * df;
+                }
+            }
+            nft = nf < nflows ? A.flow[nf].t : INT_MAX;
+        }
+        double *o = out + A.out_off + path;
+        const uint64_t n = total;
+        o[8 * n] = pv_hard;
+        o[0 * n] = pv;
+        o[1 * n] = dD[0] / A.s0;
+        o[2 * n] = dD[1];
+        o[3 * n] = dD[2] - pv_t;
+    }
+}
+
 template <class Real, int MODEL>
 static const void *adj_kernel(bool acc) {
     return acc ? reinterpret_cast<const void *>(&k_adjoint<Real, MODEL, true>)
@@ -1188,6 +1363,15 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     int kck = 0;  // checkpoint interval of the chosen GBM kernel (0: the generic kernel)
     const char *kenv = getenv("KX_ADJOINT_KERNEL");
     const bool generic_only = kenv && strcmp(kenv, "general") == 0;
+    const bool tangent_only = kenv && strcmp(kenv, "tangent") == 0;
+    // GBM: the forward-mode kernel (one pass, no recomputation) is timed beside the reverse
+    // kernels; KX_ADJOINT_KERNEL = "tangent" keeps it, KX_ADJOINT_CANDIDATE picks among the
+    // reverse kernels only (those give k_adjoint's values bit for bit)
+    const void *tan_fn = nullptr;
+    if (model == KX_MODEL_GBM && !generic_only)
+        tan_fn = f64 ? (acc ? (const void *)&k_tangent_gbm<double, true> : (const void *)&k_tangent_gbm<double, false>)
+                     : (acc ? (const void *)&k_tangent_gbm<float, true> : (const void *)&k_tangent_gbm<float, false>);
+    bool use_tan = false;
     if (model == KX_MODEL_GBM && !acc && same_nsu && !generic_only) {
         // the register-resident kernel at two register budgets (resident blocks per SM)
         if (max_n / 8 + 1 <= ADJ_MAXCK) {
@@ -1285,21 +1469,24 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             return ms;
         };
         if (!cands.empty()) {
-            // the chosen candidate (index + 1) per precision, accumulators present and barrier
-            // count (ADJ_MAXU + 1: mixed); 0: not tuned yet (default: the first with K = 16)
+            // the chosen candidate (index + 1; cands.size() + 1: the tangent kernel) per
+            // precision, accumulators present and barrier count (ADJ_MAXU + 1: mixed); 0: not
+            // tuned yet (default: the first with K = 16)
             static int tuned[2][2][ADJ_MAXU + 2] = {};
             const char *env = getenv("KX_TUNE");
             const bool tune = !(env && env[0] == '0');
             int &tk = tuned[f64 ? 1 : 0][acc ? 1 : 0][same_nsu ? std::min(std::max(nsu, 0), ADJ_MAXU) : ADJ_MAXU + 1];
-            if (tune && tk == 0 && cands.size() > 1) {
+            if (tune && tk == 0 && cands.size() + (tan_fn ? 1 : 0) > 1) {
                 float best = 1e30f;
                 const char *vb = getenv("KX_TUNE_VERBOSE");
-                for (size_t q = 0; q < cands.size(); ++q) {
+                for (size_t q = 0; q < cands.size() + (tan_fn ? 1 : 0); ++q) {
                     // this call's own work: every candidate computes it
-                    const float ms = launch(cands[q].second, cands[q].first);
+                    const bool t = q == cands.size();
+                    const float ms = t ? launch(tan_fn, 0) : launch(cands[q].second, cands[q].first);
                     if (ms < best) { best = ms; tk = (int)q + 1; }
                     if (vb && vb[0] == '1')
-                        fprintf(stderr, "[kx adjoint tune] candidate %zu (K %d): %.3f ms\n", q, cands[q].first, ms);
+                        fprintf(stderr, "[kx adjoint tune] candidate %zu (%s K %d): %.3f ms\n", q,
+                                t ? "tangent" : "reverse", t ? 0 : cands[q].first, ms);
                 }
             }
             size_t pick = 0;
@@ -1307,10 +1494,28 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
             else
                 for (size_t q = cands.size(); q-- > 0;)
                     if (cands[q].first == 16) pick = q;
-            const char *ce = getenv("KX_ADJOINT_CANDIDATE");  // a given candidate (tests: each gives the same values)
-            if (ce && ce[0]) pick = (size_t)atoi(ce) % cands.size();
+            use_tan = tan_fn && tk == (int)cands.size() + 1;
+            const char *ce = getenv("KX_ADJOINT_CANDIDATE");  // a given reverse candidate (tests: each gives the same values)
+            if (ce && ce[0]) {
+                pick = (size_t)atoi(ce) % cands.size();
+                use_tan = false;
+            }
             kfn = cands[pick].second;
             kck = cands[pick].first;
+        } else if (tan_fn) {  // accumulators or mixed barrier counts: the generic kernel or the tangent one
+            static int tuned_g[2][2] = {};  // 1: generic, 2: tangent; 0: not tuned yet
+            const char *env = getenv("KX_TUNE");
+            int &tg = tuned_g[f64 ? 1 : 0][acc ? 1 : 0];
+            if (!(env && env[0] == '0') && tg == 0) {
+                const float mg = launch(kfn, 0), mt = launch(tan_fn, 0);
+                tg = mt < mg ? 2 : 1;
+            }
+            use_tan = tg == 2;
+        }
+        if (tangent_only && tan_fn) use_tan = true;
+        if (use_tan) {
+            kfn = tan_fn;
+            kck = 0;
         }
         const float ms = launch(kfn, kck);
         c.last.kernel_ms += ms;
@@ -1320,7 +1525,7 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     std::vector<StatsJob> sj;
     for (int i = 0; i < nc; ++i) {
         c.last.path_steps += jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);
-        c.last.steps_simulated += 2 * jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);  // forward + recompute
+        c.last.steps_simulated += (use_tan ? 1 : 2) * jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);  // forward (+ recompute)
         for (int q = 0; q < ADJ_OUT; ++q) {
             StatsJob j;
             j.begin = (uint64_t)q * total + off[i];

@@ -226,15 +226,16 @@ ACC_CASES.update({
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 @pytest.mark.parametrize("name", sorted(ACC_CASES))
 def test_gbm_adjoint_kernels_equal_generic_kernel(monkeypatch, prec, name):
-    """The GBM adjoint kernels (the register-resident barrier kernel and the
-    kernel that keeps accumulators in registers and its records in shared
+    """The GBM reverse-sweep kernels (the register-resident barrier kernel and
+    the kernel that keeps accumulators in registers and its records in shared
     memory, tuned over checkpoint interval and register budget) perform the
     generic kernel's operations in the same order, so every output equals the
-    generic kernel's (KX_ADJOINT_KERNEL=general) bit for bit, whichever
-    candidate the tuner keeps."""
+    generic kernel's (KX_ADJOINT_KERNEL=general) bit for bit, for each of
+    them. (The forward-mode kernel the tuner may also keep is checked against
+    the generic kernel to rounding below.)"""
     c, m = ACC_CASES[name](), kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
     kw = dict(n_paths=20_000, seed=9, steps_per_year=252, precision=prec)
-    outs = [c.adjoint(m, **kw)]
+    outs = []
     for q in range(10):  # every candidate (KX_ADJOINT_CANDIDATE is taken modulo their number)
         monkeypatch.setenv("KX_ADJOINT_CANDIDATE", str(q))
         outs.append(c.adjoint(m, **kw))
@@ -244,3 +245,26 @@ def test_gbm_adjoint_kernels_equal_generic_kernel(monkeypatch, prec, name):
     for q, a in enumerate(outs):
         for f in ("price", "d_s0", "d_sigma", "d_r", "se_s0", "se_sigma", "se_r"):
             assert getattr(a, f) == getattr(g, f), (name, q, f, getattr(a, f), getattr(g, f))
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("fp32", 2e-4)])
+@pytest.mark.parametrize("name", sorted(ACC_CASES))
+def test_gbm_tangent_kernel_equals_the_reverse_sweep(monkeypatch, prec, tol, name):
+    """The forward-mode GBM kernel (KX_ADJOINT_KERNEL=tangent: one pass
+    carrying dy/dsigma, dy/dr, the barriers' d log w and the accumulators'
+    derivatives) computes the same pathwise derivative as the reverse sweep:
+    the price bit for bit (the same primal operations), the sensitivities and
+    their standard errors to rounding (1e-9 relative in FP64; FP32: 2e-4 and a
+    fiftieth of a standard error)."""
+    c, m = ACC_CASES[name](), kx.GBM(s0=100.0, sigma=0.3, r=0.03, asset="X")
+    kw = dict(n_paths=20_000, seed=9, steps_per_year=252, precision=prec)
+    monkeypatch.setenv("KX_ADJOINT_KERNEL", "general")
+    g = c.adjoint(m, **kw)
+    monkeypatch.setenv("KX_ADJOINT_KERNEL", "tangent")
+    t = c.adjoint(m, **kw)
+    assert (t.price, t.price_se) == (g.price, g.price_se)
+    for f in ("d_s0", "d_sigma", "d_r"):
+        a, b = getattr(t, f), getattr(g, f)
+        se = getattr(g, "se" + f[1:])
+        assert abs(a - b) <= tol * max(abs(b), 1.0) + (0.02 * se if prec == "fp32" else 0.0), (name, f, a, b)
+        assert abs(getattr(t, "se" + f[1:]) - se) <= 10 * tol * max(se, 1e-6), (name, f)
