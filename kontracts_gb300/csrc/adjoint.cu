@@ -1522,11 +1522,16 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
         c.last.kernel_launches++;
         c.last.block_threads = ADJ_BLOCK;
     }
+    // the output rows a model fills: GBM price, d/ds0, d/dsigma, d/dr and the hard-barrier price
+    // (rows 4..7 are Heston's); the others stay empty statistics
+    std::vector<int> rows;
+    for (int q = 0; q < ADJ_OUT; ++q)
+        if (model != KX_MODEL_GBM || q <= 3 || q == 8) rows.push_back(q);
     std::vector<StatsJob> sj;
     for (int i = 0; i < nc; ++i) {
         c.last.path_steps += jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);
         c.last.steps_simulated += (use_tan ? 1 : 2) * jobs[i].a.n_paths * (uint64_t)(jobs[i].a.n_times - 1);  // forward (+ recompute)
-        for (int q = 0; q < ADJ_OUT; ++q) {
+        for (int q : rows) {
             StatsJob j;
             j.begin = (uint64_t)q * total + off[i];
             j.n = jobs[i].a.n_paths;
@@ -1535,7 +1540,10 @@ static std::vector<std::vector<Stats>> run_adjoint(Ctx &c, std::vector<AdjJob> &
     }
     auto st = device_stats(c, c.pv.as<double>(), 0, sj);
     std::vector<std::vector<Stats>> res(nc);
-    for (int i = 0; i < nc; ++i) res[i].assign(st.begin() + (size_t)i * ADJ_OUT, st.begin() + (size_t)(i + 1) * ADJ_OUT);
+    for (int i = 0; i < nc; ++i) {
+        res[i].assign(ADJ_OUT, Stats{});
+        for (size_t r = 0; r < rows.size(); ++r) res[i][rows[r]] = st[(size_t)i * rows.size() + r];
+    }
     return res;
 }
 
