@@ -1,7 +1,8 @@
 /* A plain C caller of the engine, compiled with gcc against
  * include/kontract_gpu.h only: what a Rust (or any FFI) binding does through
  * the same symbols. It compiles a contract, prices it, takes its pathwise
- * sensitivities and prices an American put, and prints one line per call:
+ * sensitivities, prices an American put and takes a chunk's statistics on the
+ * host, and prints one line per call:
  *   <call> <status> <values...>
  * Without a CUDA device the pricing calls return KX_NO_DEVICE; compilation,
  * plan and grid queries never need one. */
@@ -74,6 +75,13 @@ int main(void) {
     uint64_t k = 0;
     kx_last_error_payload(&t, &k);
     printf("unknown_asset %d %d %d\n", st, isnan(t) ? 1 : 0, k == UINT64_MAX ? 1 : 0);
+    /* statistics of a chunk of values on the host (no device): n, mean, M2 */
+    const double vals[4] = {1.0, 2.0, 3.0, 4.0};
+    kx_chunk_stats cs;
+    memset(&cs, 0, sizeof cs);
+    st = kx_chunk_moments(vals, NULL, 4u, &cs);
+    printf("chunk_moments %d %.17g %.17g %.17g\n", st, cs.n, cs.mean, cs.m2);
+
     kx_program_free(uo);
     kx_program_free(put);
     return 0;

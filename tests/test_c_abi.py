@@ -34,6 +34,7 @@ def test_c_caller_compiles_and_links(tmp_path):
     assert r["grid"] == ["0", "366"]
     for call in ("price", "adjoint", "lsm"):
         assert int(r[call][0]) in (_abi.KX_OK, _abi.KX_NO_DEVICE), (call, r[call])
+    assert r["chunk_moments"] == ["0", "4", "2.5", "5"]  # host code: no device needed
 
 
 @pytest.mark.gpu
