@@ -204,3 +204,24 @@ def test_measure_peak_rejects_unknown_loops():
     v = C.c_double()
     assert lib.kx_measure_peak(5, C.byref(v)) == _abi.KX_INVALID_ARGUMENT
     assert lib.kx_measure_peak(-1, C.byref(v)) == _abi.KX_INVALID_ARGUMENT
+
+
+def test_book_sensitivities_validate_the_book_on_the_host():
+    """kx_price_batch_sens checks its book before it needs a device: a
+    path-dependent contract is refused (Unsupported) wherever it runs, NULL
+    arrays are invalid, an empty book is a no-op; a book of Europeans then
+    needs the device (NoDevice here when there is none)."""
+    lib = _abi.load()
+    m = kx.heston(100.0, 0.04, 2.0, 0.04, 0.3, -0.5, 0.05, asset="X")
+    with pytest.raises(kx.KontractError) as e:
+        kx.price_batch([kx.european_call("X", 100.0, 1.0), kx.up_and_out_call("X", 100.0, 130.0, 1.0)], m,
+                       n_paths=100, greeks=True)
+    assert e.value.status == "Unsupported"
+    assert kx.price_batch([], m, greeks=True) == ([], [])
+    out, sens = _abi.KxPriceResult(), _abi.KxSens()
+    assert lib.kx_price_batch_sens(1, None, None, None, C.byref(out), C.byref(sens)) == _abi.KX_INVALID_ARGUMENT
+    n = C.c_int32()
+    if lib.kx_device_info(None, 0, C.byref(n), None, None) != _abi.KX_OK:
+        with pytest.raises(kx.KontractError) as e:
+            kx.price_batch([kx.european_call("X", 100.0, 1.0)], m, n_paths=100, greeks=True)
+        assert e.value.status == "NoDevice"
